@@ -1,0 +1,274 @@
+// K0 delay table and K4 brute-force dedispersion for sm_103a.
+//
+// out[d][t] = sum_{c=0..nchan-1} in[c][t + shift(c,d)]
+// (lib/DedispersionKernel.cu:15-50).  Each output is accumulated in one
+// register in channel order 0..nchan-1 with plain FP32 adds, the same order
+// as the reference kernel, so results are bit-identical to it.
+//
+// Tiling.  A CTA owns DMS consecutive trials (one warp each) and a time tile
+// of 32*R samples (lane l holds samples l, l+32, ...).  Channels are streamed
+// through shared memory CS at a time, double buffered with cp.async: for
+// channel c the CTA needs in[c][t0 + s(c,d0) .. t0 + s(c,d_last) + 32R),
+// whose length is 32R plus the delay spread of the tile's trials at c; that
+// spread is bounded on the host (delay_spread) and sizes the slot.  Every
+// shared-memory read of a warp is 32 consecutive words, so the loop has no
+// bank conflicts; the kernel is bounded by shared-memory bandwidth
+// (one 4-byte read per add).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "pv_common.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// K0: delay table
+// ---------------------------------------------------------------------------
+__global__ void delay_table_kernel(int* __restrict__ shifts, const float* __restrict__ dmshift,
+                                   int nchan, int tdms, float start, float step) {
+    const long long n = (long long)nchan * tdms;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int d = (int)(i / nchan), c = (int)(i % nchan);
+        shifts[i] = pv_shift(dmshift[c], pv_trial_value(d, start, step));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K4: dedispersion
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+struct DedispArgs {
+    float* out;
+    long long out_stride;
+    const float* in;
+    long long row_stride;
+    long long row_len;
+    const float* dmshift;
+    int nchan, nout, tdms;
+    float start, step;
+    int slot;  // floats per channel slot in shared memory
+};
+
+template <int DMS, int R, int CS>
+__global__ void __launch_bounds__(DMS * 32)
+dedisperse_kernel(const DedispArgs a) {
+    extern __shared__ float smem[];
+    constexpr int NT = DMS * 32;
+    constexpr int TT = 32 * R;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long t0 = (long long)blockIdx.x * TT;
+    const int d0 = blockIdx.y * DMS;
+    const int d_last = min(d0 + DMS, a.tdms) - 1;
+    const int d = d0 + warp;
+    const float dv0 = pv_trial_value(d0, a.start, a.step);
+    const float dv_last = pv_trial_value(d_last, a.start, a.step);
+    const float dv = pv_trial_value(d, a.start, a.step);
+
+    // Issues the copies of channels [c_begin, c_begin+CS) into buffer b.
+    auto load_stage = [&](int c_begin, float* buf) {
+        const int c_end = min(c_begin + CS, a.nchan);
+        for (int c = c_begin; c < c_end; ++c) {
+            const float k = a.dmshift[c];
+            const int s0 = pv_shift(k, dv0);
+            const int span = min(TT + pv_shift(k, dv_last) - s0, a.slot);
+            const long long g0 = t0 + s0;
+            const float* src = a.in + (long long)c * a.row_stride;
+            float* dst = buf + (c - c_begin) * a.slot;
+            // Contiguous rows (row_len == row_stride, the DedispersionBuffer
+            // layout) read on into the next row as the reference kernel does;
+            // only reads past the whole buffer become zeros.
+            const long long lim = a.row_len == a.row_stride
+                                      ? (long long)(a.nchan - c) * a.row_stride
+                                      : a.row_len;
+            for (int j = threadIdx.x; j < span; j += NT) {
+                const long long g = g0 + j;
+                if (g < lim) cp_async4(dst + j, src + g);
+                else dst[j] = 0.0f;
+            }
+        }
+    };
+
+    float acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = 0.0f;
+
+    const int nstages = (a.nchan + CS - 1) / CS;
+    load_stage(0, smem);
+    cp_async_commit();
+    for (int st = 0; st < nstages; ++st) {
+        if (st + 1 < nstages) {
+            load_stage((st + 1) * CS, smem + ((st + 1) & 1) * CS * a.slot);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const float* buf = smem + (st & 1) * CS * a.slot;
+        const int c_begin = st * CS;
+        const int c_end = min(c_begin + CS, a.nchan);
+        if (d <= d_last) {
+            for (int c = c_begin; c < c_end; ++c) {
+                const float k = a.dmshift[c];
+                const int off = pv_shift(k, dv) - pv_shift(k, dv0);
+                const float* row = buf + (c - c_begin) * a.slot + off + lane;
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
+            }
+        }
+        __syncthreads();
+    }
+    if (d <= d_last) {
+        float* o = a.out + (long long)d * a.out_stride;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const long long t = t0 + lane + 32 * r;
+            if (t < a.nout) o[t] = acc[r];
+        }
+    }
+}
+
+// Largest delay spread s(c, d0+DMS-1) - s(c, d0) over channels and DM tiles,
+// evaluated with the kernel's own float arithmetic on the host.
+int delay_spread(const std::vector<float>& dmshift, int tdms, int dms, float start, float step) {
+    int spread = 0;
+    for (int d0 = 0; d0 < tdms; d0 += dms) {
+        const int dl = std::min(d0 + dms, tdms) - 1;
+        const float v0 = std::fmaf((float)d0, step, start);
+        const float vl = std::fmaf((float)dl, step, start);
+        for (float k : dmshift) {
+            const float p0 = k * v0, pl = k * vl;
+            spread = std::max(spread, (int)pl - (int)p0);
+        }
+    }
+    return spread;
+}
+
+template <int DMS, int R, int CS>
+int launch_dedisperse(DedispArgs a, int spread, cudaStream_t s) {
+    constexpr int TT = 32 * R;
+    a.slot = TT + spread;
+    const size_t smem = (size_t)2 * CS * a.slot * sizeof(float);
+    if (smem > 227 * 1024) {
+        pv::set_error("dedispersion: delay spread %d per tile needs %zu bytes of shared memory",
+                      spread, smem);
+        return PV_ERR_ARG;
+    }
+    auto kern = dedisperse_kernel<DMS, R, CS>;
+    PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "cudaFuncSetAttribute(dedisperse)");
+    dim3 grid((unsigned)pv::ceil_div<long long>(a.nout, TT), (unsigned)pv::ceil_div(a.tdms, DMS));
+    if (grid.y > 65535u) {
+        pv::set_error("dedispersion: too many DM tiles");
+        return PV_ERR_ARG;
+    }
+    kern<<<grid, DMS * 32, smem, s>>>(a);
+    return pv::check_launch("dedisperse_kernel");
+}
+
+}  // namespace
+
+namespace pv {
+
+// Chooses the tile for the delay spread: the widest trial tile whose channel
+// slots fit in shared memory with two buffers of CS channels.
+int dedisperse_device(float* out, long long out_stride, const float* in, long long row_stride,
+                      long long row_len, int nchan, int nout, int tdms, const float* d_dmshift,
+                      const std::vector<float>& h_dmshift, float start, float step,
+                      cudaStream_t s) {
+    DedispArgs a{out, out_stride, in, row_stride, row_len, d_dmshift, nchan, nout, tdms,
+                 start, step, 0};
+    const int spread16 = delay_spread(h_dmshift, tdms, 16, start, step);
+    if ((size_t)2 * 4 * (1024 + spread16) * 4 <= 200 * 1024)
+        return launch_dedisperse<16, 32, 4>(a, spread16, s);
+    const int spread8 = delay_spread(h_dmshift, tdms, 8, start, step);
+    if ((size_t)2 * 4 * (1024 + spread8) * 4 <= 220 * 1024)
+        return launch_dedisperse<8, 32, 4>(a, spread8, s);
+    const int spread4 = delay_spread(h_dmshift, tdms, 4, start, step);
+    if ((size_t)2 * 2 * (512 + spread4) * 4 <= 220 * 1024)
+        return launch_dedisperse<4, 16, 2>(a, spread4, s);
+    const int spread1 = delay_spread(h_dmshift, tdms, 1, start, step);
+    return launch_dedisperse<1, 16, 1>(a, spread1, s);
+}
+
+}  // namespace pv
+
+extern "C" int pv_delay_table(int* d_shifts, const float* d_dmshift, int nchan, int tdms,
+                              float start_over_tsamp, float step_over_tsamp, void* stream) {
+    if (!d_shifts || !d_dmshift || nchan <= 0 || tdms <= 0) {
+        pv::set_error("pv_delay_table: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const long long n = (long long)nchan * tdms;
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(n, threads),
+                                                (long long)pv::sm_count() * 8);
+    delay_table_kernel<<<blocks, threads, 0, pv::as_stream(stream)>>>(
+        d_shifts, d_dmshift, nchan, tdms, start_over_tsamp, step_over_tsamp);
+    return pv::check_launch("delay_table_kernel");
+}
+
+extern "C" int pv_dedisperse_ex(float* d_out, long long out_stride, const float* d_in,
+                                long long row_stride, long long row_len, int nchans, int nout,
+                                int tdms, const float* d_dmshift, float start_over_tsamp,
+                                float step_over_tsamp, void* stream) {
+    if (!d_out || !d_in || !d_dmshift || nchans <= 0 || tdms < 0 || nout < 0 ||
+        out_stride < nout || row_stride <= 0 || row_len < 0) {
+        pv::set_error("pv_dedisperse_ex: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    if (tdms == 0 || nout == 0) return PV_OK;
+    std::vector<float> h(nchans);
+    cudaStream_t s = pv::as_stream(stream);
+    PV_CUDA(cudaMemcpyAsync(h.data(), d_dmshift, sizeof(float) * nchans, cudaMemcpyDeviceToHost, s),
+            "copy dmshift");
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+    // Every delay must be a finite, non-negative sample count: the tiles
+    // address shared memory and the input relative to the first trial's delay.
+    if (!(start_over_tsamp >= 0.0f) || !(step_over_tsamp >= 0.0f) ||
+        !std::isfinite(start_over_tsamp) || !std::isfinite(step_over_tsamp) || row_len > row_stride) {
+        pv::set_error("pv_dedisperse_ex: trial start/step must be finite and >= 0 and "
+                      "row_len <= row_stride");
+        return PV_ERR_ARG;
+    }
+    for (int c = 0; c < nchans; ++c) {
+        if (!(h[c] >= 0.0f) || !std::isfinite(h[c])) {
+            pv::set_error("pv_dedisperse_ex: dmshift[%d] = %g is not a finite value >= 0", c, h[c]);
+            return PV_ERR_ARG;
+        }
+    }
+    const float vmax = std::fmaf((float)(tdms - 1), step_over_tsamp, start_over_tsamp);
+    for (int c = 0; c < nchans; ++c) {
+        if ((double)h[c] * vmax > 2.0e9) {
+            pv::set_error("pv_dedisperse_ex: delay of channel %d exceeds the int range", c);
+            return PV_ERR_ARG;
+        }
+    }
+    return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, nchans, nout, tdms,
+                                 d_dmshift, h, start_over_tsamp, step_over_tsamp, s);
+}
+
+extern "C" int pv_dedisperse(float* d_out, long long out_bytes, const float* d_in,
+                             float start_over_tsamp, float step_over_tsamp, int tdms,
+                             int num_samples, const float* d_dmshift, int maxshift, int nchans,
+                             void* stream) {
+    const int nout = num_samples - maxshift;
+    if (nout < 0 || (long long)nout * tdms * (long long)sizeof(float) > out_bytes) {
+        pv::set_error("pv_dedisperse: output buffer of %lld bytes is smaller than %d trials x %d "
+                      "samples", out_bytes, tdms, nout);
+        return PV_ERR_ARG;
+    }
+    return pv_dedisperse_ex(d_out, nout, d_in, num_samples, num_samples, nchans, nout, tdms,
+                            d_dmshift, start_over_tsamp, step_over_tsamp, stream);
+}

@@ -1,0 +1,67 @@
+// Shared helpers of libpv: status codes, thread-local error text, launch
+// accounting and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "pv.h"
+
+namespace pv {
+
+// Thread-local last error message returned by pv_last_error().
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+// Kernels launched by this library since load (pv_kernel_launches()).
+extern std::atomic<long long> g_launches;
+inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+inline int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PV_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return PV_ERR_CUDA;
+}
+
+// Checks the launch that was just issued.
+inline int check_launch(const char* what) {
+    count_launch();
+    return cuda_status(cudaGetLastError(), what);
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+template <typename T>
+inline T ceil_div(T a, T b) { return (a + b - 1) / b; }
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Stream-ordered scratch allocation (cudaMallocAsync / cudaFreeAsync).
+int scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+void scratch_free(void* p, cudaStream_t s);
+
+}  // namespace pv
+
+#define PV_TRY(expr)                   \
+    do {                               \
+        int _rc = (expr);              \
+        if (_rc != PV_OK) return _rc;  \
+    } while (0)
+
+#define PV_CUDA(expr, what) PV_TRY(pv::cuda_status((expr), (what)))
+
+// The reference kernel's per-(channel, trial) integer delay
+// (DedispersionKernel.cu:29,36): trunc(dmshift[c] * (start + d*step)), the
+// trial value formed with one fused multiply-add as nvcc contracts it.
+__device__ __forceinline__ float pv_trial_value(int d, float start, float step) {
+    return fmaf((float)d, step, start);
+}
+__device__ __forceinline__ int pv_shift(float dmshift, float trial_value) {
+    return __float2int_rz(__fmul_rn(dmshift, trial_value));
+}

@@ -1,0 +1,169 @@
+"""ctypes binding of libpv.so, the GB300 beam-processing library.
+
+Device buffers are torch CUDA tensors (PyTorch provides device memory and
+streams only; all compute runs in libpv's own kernels).  Every call raises
+PvError with the library's message on a non-zero status.  The library must
+be built (``build.py``); nothing here falls back to a CPU path.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libpv.so")
+HEADER = os.path.join(ROOT, "include", "pv.h")
+
+EVENT_DTYPE = np.dtype([("dm", "<i4"), ("t", "<i4"), ("bin_factor", "<f4"), ("value", "<f4")])
+
+
+class PvError(RuntimeError):
+    pass
+
+
+class pv_event(C.Structure):
+    _fields_ = [("dm", C.c_int32), ("t", C.c_int32), ("bin_factor", C.c_float), ("value", C.c_float)]
+
+
+_lib = None
+
+
+def header_symbols():
+    """Function names declared in include/pv.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pv_[a-z0-9_]+)\s*\(", text)))
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise PvError("libpv.so is not built; run pelican-lofar_gb300/build.py")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp, i, f, d, ll = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_longlong
+    P = C.POINTER
+    sigs = {
+        "pv_last_error": (C.c_char_p, []),
+        "pv_version": (i, []),
+        "pv_kernel_launches": (ll, []),
+        "pv_dm_shifts": (i, [d, d, i, P(C.c_float), P(i)]),
+        "pv_maxshift": (i, [f, f, i, P(C.c_float), i, d, i, P(i), P(i)]),
+        "pv_delay_table": (i, [vp, vp, i, i, f, f, vp]),
+        "pv_dedisperse": (i, [vp, ll, vp, f, f, i, i, vp, i, i, vp]),
+        "pv_dedisperse_ex": (i, [vp, ll, vp, ll, ll, i, i, i, vp, f, f, vp]),
+        "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
+        "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
+    }
+    for name, (res, args) in sigs.items():
+        if hasattr(L, name):
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+
+
+def check(rc):
+    if rc != 0:
+        raise PvError("libpv error %d: %s" % (rc, load().pv_last_error().decode()))
+    return rc
+
+
+def launches():
+    return load().pv_kernel_launches()
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+# ---------------------------------------------------------------------------
+# host helpers
+# ---------------------------------------------------------------------------
+
+def dm_shifts(fch1, foff, nchan):
+    out = np.zeros(nchan, np.float32)
+    inv = C.c_int()
+    check(load().pv_dm_shifts(fch1, foff, nchan, out.ctypes.data_as(C.POINTER(C.c_float)),
+                              C.byref(inv)))
+    return out, bool(inv.value)
+
+
+def maxshift(dm_low, dm_step, tdms, dmshift, tsamp, buffer_samples):
+    dmshift = np.ascontiguousarray(dmshift, np.float32)
+    ms, rem = C.c_int(), C.c_int()
+    check(load().pv_maxshift(dm_low, dm_step, tdms, dmshift.ctypes.data_as(C.POINTER(C.c_float)),
+                             len(dmshift), tsamp, buffer_samples, C.byref(ms), C.byref(rem)))
+    return ms.value, rem.value
+
+
+def thresholds(threshold, rms, bin_pow2):
+    out = np.zeros(bin_pow2 + 1, np.float32)
+    check(load().pv_analyser_thresholds(threshold, rms, bin_pow2,
+                                        out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# device calls (torch CUDA tensors)
+# ---------------------------------------------------------------------------
+
+def delay_table(d_dmshift, tdms, start_over_tsamp, step_over_tsamp, stream=None):
+    import torch
+    nchan = d_dmshift.numel()
+    out = torch.empty((tdms, nchan), dtype=torch.int32, device=d_dmshift.device)
+    check(load().pv_delay_table(_ptr(out), _ptr(d_dmshift), nchan, tdms, start_over_tsamp,
+                                step_over_tsamp, _stream(stream)))
+    return out
+
+
+def dedisperse(d_in, nout, tdms, d_dmshift, start_over_tsamp, step_over_tsamp, out=None,
+               row_len=None, stream=None):
+    """d_in: float32 [nchan][row_stride] CUDA tensor -> [tdms][nout]."""
+    import torch
+    assert d_in.dtype == torch.float32 and d_in.is_contiguous()
+    nchan, stride = d_in.shape
+    if out is None:
+        out = torch.empty((tdms, nout), dtype=torch.float32, device=d_in.device)
+    check(load().pv_dedisperse_ex(_ptr(out), out.stride(0), _ptr(d_in), stride,
+                                  stride if row_len is None else row_len, nchan, nout, tdms,
+                                  _ptr(d_dmshift), start_over_tsamp, step_over_tsamp,
+                                  _stream(stream)))
+    return out
+
+
+def dedisperse_ref_api(d_out, d_in, start_over_tsamp, step_over_tsamp, tdms, num_samples,
+                       d_dmshift, maxshift_total, nchans, stream=None):
+    """The cacheDedisperseLoop-shaped entry point."""
+    check(load().pv_dedisperse(_ptr(d_out), d_out.numel() * 4, _ptr(d_in), start_over_tsamp,
+                               step_over_tsamp, tdms, num_samples, _ptr(d_dmshift),
+                               maxshift_total, nchans, _stream(stream)))
+    return d_out
+
+
+def analyse(d_data, threshold, rms, bin_pow2=6, cap=None, stream=None):
+    """Returns a numpy structured array of events (dummy first)."""
+    import torch
+    tdms, nsamp = d_data.shape
+    if cap is None:
+        cap = 1 + tdms * nsamp * 2
+    cap = max(int(cap), 1)
+    ev = torch.empty(cap * 4, dtype=torch.int32, device=d_data.device)
+    n = C.c_longlong()
+    check(load().pv_analyse(_ptr(d_data), d_data.stride(0), tdms, nsamp, threshold, rms, bin_pow2,
+                            _ptr(ev), cap, C.byref(n), _stream(stream)))
+    k = min(n.value, cap)
+    host = ev[: 4 * k].cpu().numpy().view(EVENT_DTYPE)
+    return host.copy(), n.value

@@ -1,0 +1,129 @@
+"""K0 delay table, K4 dedispersion and K5 analyser on the GPU against the
+oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from gen import GEN_FCH1, GEN_FOFF, GEN_NCHAN, GEN_NSUB, GEN_TSAMP, dm_index, generator_pulse
+
+pytestmark = pytest.mark.gpu
+
+# (fch1, foff, nchan, tdms, dm_low, dm_step, tsamp)
+DELAY_CASES = [
+    (150.0, -6.0 / 2048, 2048, 200, 0.0, 0.1, GEN_TSAMP),               # reference test fixture
+    (146.25, 0.01220703125, 512, 512, 0.0, 100.0 / 511, 327.68e-6),      # 32 subbands from 140 MHz
+    (110.0, 0.0122070312, 3904, 2048, 0.0, 500.0 / 2047, 327.68e-6),     # 244 subbands from 110 MHz
+    (150.0, -0.05, 97, 37, 1.5, 0.37, 1e-3),                              # ragged, dmLow > 0
+]
+
+
+@pytest.mark.parametrize("case", DELAY_CASES)
+def test_delay_table_bit_exact(pv, oracle, cuda, case):
+    import torch
+    fch1, foff, n, tdms, lo, step, tsamp = case
+    k, _ = pv.dm_shifts(fch1, foff, n)
+    start = np.float32(np.float32(lo) / np.float32(tsamp))
+    stp = np.float32(np.float32(step) / np.float32(tsamp))
+    got = pv.delay_table(torch.from_numpy(k).to(cuda), tdms, float(start), float(stp)).cpu().numpy()
+    want = oracle.shift_table(k, tdms, start, stp)
+    assert np.array_equal(got, want)
+    # FP64 delay table: report how many entries differ (documented deviation)
+    f64 = oracle.shift_table_f64(fch1, foff, n, tdms, lo, step, tsamp)
+    frac = np.mean(f64 != want)
+    assert frac < 0.05
+
+
+def _shift_bounds(oracle, k, tdms, start, step):
+    return int(oracle.shift_table(k, tdms, start, step).max())
+
+
+# (nchan, nout, tdms, fch1, foff, dm_step, tsamp)
+DD_CASES = [
+    (64, 300, 40, 150.0, -0.1, 0.5, 327.68e-6),
+    (512, 1024, 512, 146.25, -0.01220703125, 100.0 / 511, 327.68e-6),
+    (97, 777, 37, 150.0, -0.05, 0.37, 1e-3),
+    (3904, 256, 48, 157.6, -0.0122070312, 500.0 / 2047, 327.68e-6),
+    (16, 64, 1, 150.0, -1.0, 1.0, 1e-3),
+]
+
+
+@pytest.mark.parametrize("case", DD_CASES)
+def test_dedisperse_bit_exact(pv, oracle, cuda, case):
+    import torch
+    nchan, nout, tdms, fch1, foff, step, tsamp = case
+    rng = np.random.default_rng(nchan + tdms)
+    k, _ = pv.dm_shifts(fch1, foff, nchan)
+    start = np.float32(0.0)
+    stp = np.float32(np.float32(step) / np.float32(tsamp))
+    ms = _shift_bounds(oracle, k, tdms, start, stp)
+    buf = (rng.standard_normal((nchan, nout + ms + 3)) * 4).astype(np.float32)
+    want = oracle.dedisperse(buf, nout, tdms, k, start, stp)
+    d_buf = torch.from_numpy(buf).to(cuda)
+    got = pv.dedisperse(d_buf, nout, tdms, torch.from_numpy(k).to(cuda), float(start), float(stp))
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy(), want)
+    f64 = oracle.dedisperse(buf, nout, tdms, k, start, stp, f64=True)
+    scale = np.sqrt(nchan) * 4
+    assert np.max(np.abs(got.cpu().numpy() - f64)) / scale < 1e-5
+
+
+def test_reference_entry_point_known_answer(pv, oracle, cuda):
+    """cacheDedisperseLoop-shaped call on the DedispersionModuleTest fixture:
+    dmAmplitude(0, 10.0) == nSubbands*nChannels."""
+    import torch
+    B = 8192
+    blob = generator_pulse(B, 10.0)[0]
+    n = GEN_NSUB * GEN_NCHAN
+    k, inv = pv.dm_shifts(GEN_FCH1, GEN_FOFF, n)
+    ms, rem = pv.maxshift(0.0, 0.1, 200, k, GEN_TSAMP, B)
+    buf = np.ascontiguousarray(blob[:, :, 0, :].reshape(B, n).T)  # [chan][t]
+    start = np.float32(0.0) / np.float32(GEN_TSAMP)
+    stp = np.float32(0.1) / np.float32(GEN_TSAMP)
+    nout = B - ms - rem
+    out = torch.zeros((200, nout), dtype=torch.float32, device=cuda)
+    pv.dedisperse_ref_api(out, torch.from_numpy(buf).to(cuda), float(start), float(stp), 200, B,
+                          torch.from_numpy(k).to(cuda), ms + rem, n)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert got[dm_index(10.0, 0.0, 0.1), 0] == np.float32(n)
+    m = oracle.DedispersionModule(B, 200, 0.0, 0.1, GEN_FCH1, GEN_FOFF)
+    want, _ = m.add(blob, GEN_TSAMP)[0]
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("bin_pow2", [6, 3, 0, 8])
+def test_analyser_bit_exact(pv, oracle, cuda, bin_pow2):
+    import torch
+    rng = np.random.default_rng(bin_pow2)
+    tdms, nsamp = 33, 64 * 20 + 13
+    data = rng.standard_normal((tdms, nsamp)).astype(np.float32) * 3.0
+    data[5, 100:120] += 6
+    thr, rms = 2.5, 1.0
+    want = oracle.analyse(data, thr, rms, bin_pow2)
+    got, n = pv.analyse(torch.from_numpy(data).to(cuda), thr, rms, bin_pow2)
+    assert n == len(want)
+    assert np.array_equal(got, want.astype(got.dtype))
+
+
+def test_analyser_known_answer_and_empty(pv, oracle, cuda):
+    import torch
+    B = 8192
+    blob = generator_pulse(B, 10.0)[0]
+    m = oracle.DedispersionModule(B, 200, 0.0, 0.1, GEN_FCH1, GEN_FOFF)
+    data, _ = m.add(blob, GEN_TSAMP)[0]
+    rms = float(np.sqrt(np.float32(GEN_NCHAN) * np.float32(GEN_NSUB)))
+    got, n = pv.analyse(torch.from_numpy(data).to(cuda), 6.0, rms)
+    want = oracle.analyse(data, 6.0, rms)
+    assert n > 200 and np.array_equal(got, want.astype(got.dtype))
+    # empty and shorter-than-a-block inputs give only the dummy event
+    for shape in [(0, 0), (4, 63)]:
+        got, n = pv.analyse(torch.zeros(shape, dtype=torch.float32, device=cuda), 6.0, rms)
+        assert n == 1 and tuple(got[0]) == (0, 0, 1.0, 0.0)
+
+
+def test_analyser_capacity_truncates(pv, oracle, cuda):
+    import torch
+    data = np.full((2, 128), 10.0, np.float32)
+    want = oracle.analyse(data, 1.0, 1.0, 6)
+    got, n = pv.analyse(torch.from_numpy(data).to(cuda), 1.0, 1.0, 6, cap=50)
+    assert n == len(want) and len(got) == 50
+    assert np.array_equal(got, want[:50].astype(got.dtype))
