@@ -121,7 +121,9 @@ dedisperse_kernel(const DedispArgs a) {
         if (d <= d_last) {
             for (int c = c_begin; c < c_end; ++c) {
                 const float k = a.dmshift[c];
-                const int off = pv_shift(k, dv) - pv_shift(k, dv0);
+                // off <= slot - TT by the host's spread bound; the clamp keeps
+                // every read inside the slot regardless.
+                const int off = min(pv_shift(k, dv) - pv_shift(k, dv0), a.slot - TT);
                 const float* row = buf + (c - c_begin) * a.slot + off + lane;
 #pragma unroll
                 for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
