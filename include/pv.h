@@ -85,6 +85,33 @@ int pv_dedisperse_ex(float* d_out, long long out_stride, const float* d_in,
                      const float* d_dmshift, float start_over_tsamp, float step_over_tsamp,
                      void* stream);
 
+/* A dedispersion plan: the delay constants (host and device copies) and the
+ * tile choice for one channel set and trial grid, so that repeated launches
+ * need no host synchronisation.  h_dmshift is copied. */
+typedef struct pv_dedisp_plan pv_dedisp_plan;
+int pv_dedisp_plan_create(pv_dedisp_plan** plan, const float* h_dmshift, int nchans, int tdms,
+                          float start_over_tsamp, float step_over_tsamp);
+void pv_dedisp_plan_destroy(pv_dedisp_plan* plan);
+/* Largest integer delay of the plan (samples). */
+int pv_dedisp_plan_max_shift(const pv_dedisp_plan* plan);
+/* Dedisperses nout samples.  Linear mode (ring_len == 0): rows of row_stride
+ * floats, samples at or beyond row_len read as 0 (row_len == row_stride reads
+ * on into the next row, as the reference's contiguous buffer does).  Ring
+ * mode (ring_len > 0): each row is a ring of ring_len samples and output
+ * sample t reads physical column (t_base + t + shift) mod ring_len. */
+int pv_dedisp_plan_run(const pv_dedisp_plan* plan, float* d_out, long long out_stride,
+                       const float* d_in, long long row_stride, long long row_len,
+                       long long ring_len, long long t_base, int nout, void* stream);
+
+/* A8 DedispersionBuffer::addSamples (lib/src/DedispersionBuffer.cpp:98-180):
+ * writes nt Stokes samples [t][nsub][npol][nchan] (pol 0) into the rows of a
+ * per-channel ring at logical position pos (column (pos+t) mod ring_len; with
+ * ring_len == 0 the rows are linear).  Row r takes bin r, or bin
+ * nsub*nchan-1-r when inverted (DedispersionBuffer.cpp:131-156). */
+int pv_ring_write(float* d_ring, long long row_stride, long long ring_len, long long pos,
+                  const float* d_stokes, int nt, int nsub, int npol, int nchan, int inverted,
+                  void* stream);
+
 /* ------------------------------------------------------------------------
  * A11 analyser — DedispersionAnalyser::analyse (lib/src/DedispersionAnalyser.cpp:30-203)
  * ---------------------------------------------------------------------- */

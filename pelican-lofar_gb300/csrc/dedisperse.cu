@@ -52,7 +52,9 @@ struct DedispArgs {
     long long out_stride;
     const float* in;
     long long row_stride;
-    long long row_len;
+    long long row_len;   // linear mode: valid samples per row
+    long long ring_len;  // ring mode (> 0): rows are rings of ring_len samples
+    long long t_base;    // ring mode: physical position of output sample 0
     const float* dmshift;
     int nchan, nout, tdms;
     float start, step;
@@ -82,19 +84,29 @@ dedisperse_kernel(const DedispArgs a) {
             const float k = a.dmshift[c];
             const int s0 = pv_shift(k, dv0);
             const int span = min(TT + pv_shift(k, dv_last) - s0, a.slot);
-            const long long g0 = t0 + s0;
             const float* src = a.in + (long long)c * a.row_stride;
             float* dst = buf + (c - c_begin) * a.slot;
-            // Contiguous rows (row_len == row_stride, the DedispersionBuffer
-            // layout) read on into the next row as the reference kernel does;
-            // only reads past the whole buffer become zeros.
-            const long long lim = a.row_len == a.row_stride
-                                      ? (long long)(a.nchan - c) * a.row_stride
-                                      : a.row_len;
-            for (int j = threadIdx.x; j < span; j += NT) {
-                const long long g = g0 + j;
-                if (g < lim) cp_async4(dst + j, src + g);
-                else dst[j] = 0.0f;
+            if (a.ring_len > 0) {
+                // Ring rows: positions wrap modulo ring_len (span <= ring_len).
+                long long g0 = (a.t_base + t0 + s0) % a.ring_len;
+                for (int j = threadIdx.x; j < span; j += NT) {
+                    long long g = g0 + j;
+                    if (g >= a.ring_len) g -= a.ring_len;
+                    cp_async4(dst + j, src + g);
+                }
+            } else {
+                // Contiguous rows (row_len == row_stride, the DedispersionBuffer
+                // layout) read on into the next row as the reference kernel
+                // does; only reads past the whole buffer become zeros.
+                const long long g0 = t0 + s0;
+                const long long lim = a.row_len == a.row_stride
+                                          ? (long long)(a.nchan - c) * a.row_stride
+                                          : a.row_len;
+                for (int j = threadIdx.x; j < span; j += NT) {
+                    const long long g = g0 + j;
+                    if (g < lim) cp_async4(dst + j, src + g);
+                    else dst[j] = 0.0f;
+                }
             }
         }
     };
@@ -167,6 +179,11 @@ int launch_dedisperse(DedispArgs a, int spread, cudaStream_t s) {
                       spread, smem);
         return PV_ERR_ARG;
     }
+    if (a.ring_len > 0 && a.ring_len < a.slot) {
+        pv::set_error("dedispersion: ring of %lld samples is shorter than one tile span (%d)",
+                      a.ring_len, a.slot);
+        return PV_ERR_ARG;
+    }
     auto kern = dedisperse_kernel<DMS, R, CS>;
     PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
             "cudaFuncSetAttribute(dedisperse)");
@@ -186,11 +203,15 @@ namespace pv {
 // Chooses the tile for the delay spread: the widest trial tile whose channel
 // slots fit in shared memory with two buffers of CS channels.
 int dedisperse_device(float* out, long long out_stride, const float* in, long long row_stride,
-                      long long row_len, int nchan, int nout, int tdms, const float* d_dmshift,
-                      const std::vector<float>& h_dmshift, float start, float step,
-                      cudaStream_t s) {
-    DedispArgs a{out, out_stride, in, row_stride, row_len, d_dmshift, nchan, nout, tdms,
-                 start, step, 0};
+                      long long row_len, long long ring_len, long long t_base, int nchan, int nout,
+                      int tdms, const float* d_dmshift, const std::vector<float>& h_dmshift,
+                      float start, float step, cudaStream_t s) {
+    if (ring_len > 0 && (ring_len > row_stride || t_base < 0)) {
+        set_error("dedispersion: ring of %lld samples does not fit rows of %lld", ring_len, row_stride);
+        return PV_ERR_ARG;
+    }
+    DedispArgs a{out, out_stride, in, row_stride, row_len, ring_len, t_base % std::max(ring_len, 1LL),
+                 d_dmshift, nchan, nout, tdms, start, step, 0};
     const int spread16 = delay_spread(h_dmshift, tdms, 16, start, step);
     if ((size_t)2 * 4 * (1024 + spread16) * 4 <= 200 * 1024)
         return launch_dedisperse<16, 32, 4>(a, spread16, s);
@@ -257,8 +278,8 @@ extern "C" int pv_dedisperse_ex(float* d_out, long long out_stride, const float*
             return PV_ERR_ARG;
         }
     }
-    return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, nchans, nout, tdms,
-                                 d_dmshift, h, start_over_tsamp, step_over_tsamp, s);
+    return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, 0, 0, nchans, nout,
+                                 tdms, d_dmshift, h, start_over_tsamp, step_over_tsamp, s);
 }
 
 extern "C" int pv_dedisperse(float* d_out, long long out_bytes, const float* d_in,
@@ -273,4 +294,75 @@ extern "C" int pv_dedisperse(float* d_out, long long out_bytes, const float* d_i
     }
     return pv_dedisperse_ex(d_out, nout, d_in, num_samples, num_samples, nchans, nout, tdms,
                             d_dmshift, start_over_tsamp, step_over_tsamp, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+struct pv_dedisp_plan {
+    std::vector<float> h_dmshift;
+    float* d_dmshift = nullptr;
+    int nchan = 0, tdms = 0, max_shift = 0;
+    float start = 0.0f, step = 0.0f;
+};
+
+extern "C" int pv_dedisp_plan_create(pv_dedisp_plan** plan, const float* h_dmshift, int nchans,
+                                     int tdms, float start_over_tsamp, float step_over_tsamp) {
+    if (!plan || !h_dmshift || nchans <= 0 || tdms <= 0 || !(start_over_tsamp >= 0.0f) ||
+        !(step_over_tsamp >= 0.0f) || !std::isfinite(start_over_tsamp) ||
+        !std::isfinite(step_over_tsamp)) {
+        pv::set_error("pv_dedisp_plan_create: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const float vmax = std::fmaf((float)(tdms - 1), step_over_tsamp, start_over_tsamp);
+    int max_shift = 0;
+    for (int c = 0; c < nchans; ++c) {
+        if (!(h_dmshift[c] >= 0.0f) || !std::isfinite(h_dmshift[c]) ||
+            (double)h_dmshift[c] * vmax > 2.0e9) {
+            pv::set_error("pv_dedisp_plan_create: dmshift[%d] = %g is not a usable delay", c,
+                          h_dmshift[c]);
+            return PV_ERR_ARG;
+        }
+        max_shift = std::max(max_shift, (int)(h_dmshift[c] * vmax));
+    }
+    auto* p = new pv_dedisp_plan;
+    p->h_dmshift.assign(h_dmshift, h_dmshift + nchans);
+    p->nchan = nchans;
+    p->tdms = tdms;
+    p->start = start_over_tsamp;
+    p->step = step_over_tsamp;
+    p->max_shift = max_shift;
+    cudaError_t e = cudaMalloc(&p->d_dmshift, sizeof(float) * nchans);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(p->d_dmshift, h_dmshift, sizeof(float) * nchans, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        pv::set_error("pv_dedisp_plan_create: %s", cudaGetErrorString(e));
+        if (p->d_dmshift) cudaFree(p->d_dmshift);
+        delete p;
+        return PV_ERR_CUDA;
+    }
+    *plan = p;
+    return PV_OK;
+}
+
+extern "C" void pv_dedisp_plan_destroy(pv_dedisp_plan* p) {
+    if (!p) return;
+    if (p->d_dmshift) cudaFree(p->d_dmshift);
+    delete p;
+}
+
+extern "C" int pv_dedisp_plan_max_shift(const pv_dedisp_plan* p) { return p ? p->max_shift : -1; }
+
+extern "C" int pv_dedisp_plan_run(const pv_dedisp_plan* p, float* d_out, long long out_stride,
+                                  const float* d_in, long long row_stride, long long row_len,
+                                  long long ring_len, long long t_base, int nout, void* stream) {
+    if (!p || !d_out || !d_in || nout < 0 || out_stride < nout || row_stride <= 0 ||
+        (ring_len == 0 && (row_len < 0 || row_len > row_stride))) {
+        pv::set_error("pv_dedisp_plan_run: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    if (nout == 0) return PV_OK;
+    return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, ring_len, t_base,
+                                 p->nchan, nout, p->tdms, p->d_dmshift, p->h_dmshift, p->start,
+                                 p->step, pv::as_stream(stream));
 }

@@ -127,3 +127,68 @@ def test_analyser_capacity_truncates(pv, oracle, cuda):
     got, n = pv.analyse(torch.from_numpy(data).to(cuda), 1.0, 1.0, 6, cap=50)
     assert n == len(want) and len(got) == 50
     assert np.array_equal(got, want[:50].astype(got.dtype))
+
+
+def test_ring_write_transposes_and_wraps(pv, cuda):
+    import ctypes as C
+    import torch
+    L = pv.load()
+    L.pv_ring_write.argtypes = [C.c_void_p, C.c_longlong, C.c_longlong, C.c_longlong, C.c_void_p,
+                                C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(3)
+    nt, nsub, npol, nchan = 70, 5, 2, 8
+    nbins = nsub * nchan
+    stokes = rng.standard_normal((nt, nsub, npol, nchan)).astype(np.float32)
+    ring_len, stride, pos = 100, 104, 61
+    for inverted in (0, 1):
+        ring = torch.full((nbins, stride), -7.0, device=cuda)
+        pv.check(L.pv_ring_write(C.c_void_p(ring.data_ptr()), stride, ring_len, pos,
+                                 C.c_void_p(torch.from_numpy(stokes).to(cuda).data_ptr()), nt, nsub,
+                                 npol, nchan, inverted, C.c_void_p(0)))
+        torch.cuda.synchronize()
+        got = ring.cpu().numpy()
+        want = np.full((nbins, stride), -7.0, np.float32)
+        bins = stokes[:, :, 0, :].reshape(nt, nbins)
+        if inverted:
+            bins = bins[:, ::-1]
+        for t in range(nt):
+            want[:, (pos + t) % ring_len] = bins[t]
+        assert np.array_equal(got, want)
+
+
+def test_ring_mode_equals_linear(pv, oracle, cuda):
+    import ctypes as C
+    import torch
+    L = pv.load()
+    L.pv_dedisp_plan_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_float), C.c_int,
+                                        C.c_int, C.c_float, C.c_float]
+    L.pv_dedisp_plan_run.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
+                                     C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong,
+                                     C.c_int, C.c_void_p]
+    L.pv_dedisp_plan_max_shift.argtypes = [C.c_void_p]
+    rng = np.random.default_rng(4)
+    nchan, nout, tdms = 300, 1000, 70
+    k, _ = pv.dm_shifts(150.0, -0.03, nchan)
+    start, step = np.float32(0.0), np.float32(3.7)
+    plan = C.c_void_p()
+    pv.check(L.pv_dedisp_plan_create(C.byref(plan), k.ctypes.data_as(C.POINTER(C.c_float)), nchan,
+                                     tdms, float(start), float(step)))
+    ms = L.pv_dedisp_plan_max_shift(plan)
+    assert ms == oracle.shift_table(k, tdms, start, step).max()
+    ring_len = nout + ms
+    lin = rng.standard_normal((nchan, ring_len)).astype(np.float32)
+    want = oracle.dedisperse(np.concatenate([lin, np.zeros((nchan, 4), np.float32)], 1), nout, tdms,
+                             k, start, step)
+    for t_base in (0, 1, ring_len // 2, ring_len - 1):
+        stride = ring_len + 5
+        ring = np.zeros((nchan, stride), np.float32)
+        for t in range(ring_len):
+            ring[:, (t_base + t) % ring_len] = lin[:, t]
+        d_ring = torch.from_numpy(ring).to(cuda)
+        out = torch.empty((tdms, nout), device=cuda)
+        pv.check(L.pv_dedisp_plan_run(plan, C.c_void_p(out.data_ptr()), nout,
+                                      C.c_void_p(d_ring.data_ptr()), stride, 0, ring_len, t_base,
+                                      nout, C.c_void_p(0)))
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), want)
+    L.pv_dedisp_plan_destroy(plan)
