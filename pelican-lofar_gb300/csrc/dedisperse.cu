@@ -83,7 +83,9 @@ dedisperse_kernel(const DedispArgs a) {
         for (int c = c_begin; c < c_end; ++c) {
             const float k = a.dmshift[c];
             const int s0 = pv_shift(k, dv0);
-            const int span = min(TT + pv_shift(k, dv_last) - s0, a.slot);
+            // Samples the tile's stored outputs need: the last tile may be short.
+            const int valid = (int)min((long long)TT, (long long)a.nout - t0);
+            const int span = min(valid + pv_shift(k, dv_last) - s0, a.slot);
             const float* src = a.in + (long long)c * a.row_stride;
             float* dst = buf + (c - c_begin) * a.slot;
             if (a.ring_len > 0) {
@@ -179,9 +181,9 @@ int launch_dedisperse(DedispArgs a, int spread, cudaStream_t s) {
                       spread, smem);
         return PV_ERR_ARG;
     }
-    if (a.ring_len > 0 && a.ring_len < a.slot) {
+    if (a.ring_len > 0 && a.ring_len < std::min(TT, a.nout) + spread) {
         pv::set_error("dedispersion: ring of %lld samples is shorter than one tile span (%d)",
-                      a.ring_len, a.slot);
+                      a.ring_len, std::min(TT, a.nout) + spread);
         return PV_ERR_ARG;
     }
     auto kern = dedisperse_kernel<DMS, R, CS>;
