@@ -59,6 +59,11 @@ def _declare(L):
         "pv_delay_table": (i, [vp, vp, i, i, f, f, vp]),
         "pv_dedisperse": (i, [vp, ll, vp, f, f, i, i, vp, i, i, vp]),
         "pv_dedisperse_ex": (i, [vp, ll, vp, ll, ll, i, i, i, vp, f, f, vp]),
+        "pv_dedisp_plan_create": (i, [P(vp), P(C.c_float), i, i, f, f]),
+        "pv_dedisp_plan_destroy": (None, [vp]),
+        "pv_dedisp_plan_max_shift": (i, [vp]),
+        "pv_dedisp_plan_run": (i, [vp, vp, ll, vp, ll, ll, ll, ll, i, vp]),
+        "pv_ring_write": (i, [vp, ll, ll, ll, vp, i, i, i, i, i, vp]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
