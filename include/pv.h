@@ -137,6 +137,80 @@ int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp, float thr
                float rms, int bin_pow2, pv_event* d_events, long long cap,
                long long* h_count, void* stream);
 
+/* ------------------------------------------------------------------------
+ * A2/A3 PPFChanneliser (lib/src/PPFChanneliser.cpp:29-290,
+ * lib/src/PolyphaseCoefficients.cpp:77-364), A4 StokesGenerator
+ * (lib/src/StokesGenerator.cpp:40-108), A5 StokesIntegrator
+ * (lib/src/StokesIntegrator.cpp:32-119)
+ * ---------------------------------------------------------------------- */
+
+#define PV_WINDOW_HAMMING 0
+#define PV_WINDOW_BLACKMAN 1
+#define PV_WINDOW_GAUSSIAN 2
+#define PV_WINDOW_KAISER 3
+
+/* filter@filterWindow name -> PV_WINDOW_* (-1 and an error for others). */
+int pv_window_from_name(const char* name);
+/* PolyphaseCoefficients::genereateFilter: h_coeffs[t*nchan + c] (double). */
+int pv_fir_coefficients(int ntaps, int nchan, int window, double* h_coeffs);
+
+/* A channeliser with its per-(subband, polarisation) tap history on the
+ * device.  nchan (outputChannelsPerSubband) must be a power of two in
+ * 2..1024.  h_coeffs [ntaps][nchan] float, or NULL to design them for
+ * `window` as the reference does (then converted to float). */
+typedef struct pv_ppf pv_ppf;
+int pv_ppf_create(pv_ppf** ppf, int nchan, int ntaps, int window, const float* h_coeffs);
+void pv_ppf_destroy(pv_ppf* ppf);
+int pv_ppf_coefficients(const pv_ppf* ppf, float* h_out);
+/* Forgets the tap history (next call starts from zeros, as a new module). */
+int pv_ppf_reset(pv_ppf* ppf);
+/* PPFChanneliser::run: d_in complex float [nsub][npol][nblocks*nchan]
+ * (TimeSeriesDataSetC32, nTimesPerBlock = nchan); d_out complex float
+ * [nblocks][nsub][npol][nchan] (SpectrumDataSetC32). */
+int pv_ppf_run(pv_ppf* ppf, const float* d_in, int nsub, int npol, int nblocks, float* d_out,
+               void* stream);
+/* Fused PPF + Stokes + integration (dual polarisation): d_in as pv_ppf_run,
+ * or raw int16 complex samples when in_int16; d_stokes receives
+ * [nblocks/window][nsub][nstokes][nchan/bin] (SpectrumDataSetStokes after
+ * StokesIntegrator); *nu_out the number of integrated samples. */
+int pv_channelise(pv_ppf* ppf, const void* d_in, int in_int16, int nsub, int nblocks,
+                  int nstokes, int window, int bin, float* d_stokes, int* nu_out, void* stream);
+/* StokesGenerator::run: complex [nt][nsub][2][nchan] -> float
+ * [nt][nsub][nstokes][nchan], nstokes 1 (I) or 4 (I,Q,U,V). */
+int pv_stokes(const float* d_spectra, int nt, int nsub, int nchan, int nstokes, float* d_out,
+              void* stream);
+/* StokesIntegrator::run: [nt][nsub][npol][nchan] -> [nt/window][nsub][npol][nchan/bin]
+ * (window reduced to nt when larger, remainders dropped). */
+int pv_integrate(const float* d_in, int nt, int nsub, int npol, int nchan, int window, int bin,
+                 float* d_out, int* nu_out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * A6 RFI_Clipper (lib/src/RFI_Clipper.cpp:22-573) with BandPass,
+ * BandPassAdapter and BinMap
+ * ---------------------------------------------------------------------- */
+
+/* bp_text is the BandPassData file's contents (BandPassAdapter format).
+ * Arguments follow the XML: channelRejectionRMS, spectrumRejectionRMS,
+ * History@maximum, zeroDMing@active, computeRMSfromMean@active,
+ * Band@matching, and the element's active attribute. */
+typedef struct pv_rfi pv_rfi;
+int pv_rfi_create(pv_rfi** rfi, const char* bp_text, float channel_rejection_rms,
+                  float spectrum_rejection_rms, int history, int zero_dming,
+                  int compute_rms_from_mean, int band_matching, int active);
+void pv_rfi_destroy(pv_rfi* rfi);
+/* RFI_Clipper::run in place on device Stokes [nt][nsub][npol][nchan]
+ * (statistics from pol 0).  d_flags (optional, [nt][nsub*nchan] bytes):
+ * bit 0 channel clipped, bit 1 spectrum clipped.  The reference's weights
+ * stay 1 (RFI_Clipper.cpp:143,332). */
+int pv_rfi_run(pv_rfi* rfi, float* d_data, int nt, int nsub, int npol, int nchan,
+               unsigned char* d_flags, void* stream);
+/* [meanRunAve, rmsRunAve, bandpass mean, bandpass rms, bandpass offset,
+ *  stats counter, bad spectra, mean history size, rms history size,
+ *  unfilled last-good channels]; synchronous. */
+int pv_rfi_state(pv_rfi* rfi, double* h_out10);
+/* The rebinned bandpass model the first run used (host copy). */
+int pv_rfi_bandpass(pv_rfi* rfi, float* h_out, int nbins);
+
 #ifdef __cplusplus
 }
 #endif

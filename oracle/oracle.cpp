@@ -677,6 +677,22 @@ struct CircBuf {
 
 }  // namespace
 
+// Canonical FP64 reduction of the FP64 RFI variant: partial p (0..255) sums
+// x[p], x[p+256], ... in order; each group of 32 partials is reduced by the
+// halving tree (offsets 16, 8, 4, 2, 1) and the 8 group sums by offsets 4, 2, 1.
+static double tree_256(double* part) {
+    double w[8];
+    for (int g = 0; g < 8; ++g) {
+        double* q = part + 32 * g;
+        for (int off = 16; off >= 1; off >>= 1)
+            for (int l = 0; l < off; ++l) q[l] = q[l] + q[l + off];
+        w[g] = q[0];
+    }
+    for (int off = 4; off >= 1; off >>= 1)
+        for (int l = 0; l < off; ++l) w[l] = w[l] + w[l + off];
+    return w[0];
+}
+
 extern "C" double or_sum_canonical(const double* x, int n) {
     double part[256];
     for (int p = 0; p < 256; ++p) {
@@ -684,9 +700,7 @@ extern "C" double or_sum_canonical(const double* x, int n) {
         for (int i = p; i < n; i += 256) s += x[i];
         part[p] = s;
     }
-    for (int off = 128; off >= 1; off >>= 1)
-        for (int p = 0; p < off; ++p) part[p] = part[p] + part[p + off];
-    return part[0];
+    return tree_256(part);
 }
 
 // ===========================================================================
@@ -730,9 +744,7 @@ struct Rfi : RfiBase {
             for (int i = p; i < n; i += 256) s += (double)f(i);
             part[p] = s;
         }
-        for (int off = 128; off >= 1; off >>= 1)
-            for (int p = 0; p < off; ++p) part[p] = part[p] + part[p + off];
-        return (R)part[0];
+        return (R)tree_256(part);
     }
 
     int run(float* I, float* W, int nt, int nsub, int npol, int nchan, uint8_t* flags) override {
@@ -793,9 +805,7 @@ struct Rfi : RfiBase {
                             p1[bin % 256] += v;
                             p2[bin % 256] += v * v;
                         }
-                        for (int off = 128; off >= 1; off >>= 1)
-                            for (int p = 0; p < off; ++p) { p1[p] += p1[p + off]; p2[p] += p2[p + off]; }
-                        bm = (R)p1[0]; bms = (R)p2[0];
+                        bm = (R)tree_256(p1); bms = (R)tree_256(p2);
                     }
                     dmm[b] = (R)mini_data[b] - (R)mini_model[b];
                     if (!kF64) {

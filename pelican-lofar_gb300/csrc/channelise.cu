@@ -1,0 +1,438 @@
+// K1: the channeliser chain.
+//
+//   PPFChanneliser::run   (lib/src/PPFChanneliser.cpp:81-290)
+//   StokesGenerator::run  (lib/src/StokesGenerator.cpp:40-108)
+//   StokesIntegrator::run (lib/src/StokesIntegrator.cpp:32-119)
+//
+// One CTA takes one subband and a tile of BT consecutive PPF blocks (N
+// samples each) of both polarisations.  It stages the tile plus the T-1
+// preceding blocks (from the previous call's history where the tile starts
+// the chunk) in shared memory, applies the T-tap polyphase FIR per channel
+// (oldest tap first, FP32 products and sums in the reference's order),
+// transforms every block with a shared-memory radix-2 Stockham FFT (forward,
+// unnormalised, natural order, as FFTW_FORWARD) and then either writes the
+// complex spectra (SpectrumDataSetC32 layout) or forms Stokes parameters and
+// integrates them over `window` blocks and `bin` channels (the
+// SpectrumDataSetStokes layout), so the channelised voltages never reach
+// HBM.  Raw int16 station samples are accepted directly (the conversion to
+// float is exact).
+#include <algorithm>
+#include <vector>
+
+#include "pv_common.cuh"
+
+namespace pv {
+int fir_coefficients(int ntaps, int nchan, int window, std::vector<double>& out);
+}
+
+namespace {
+
+struct ChanArgs {
+    const void* in;          // [sub][pol][block*N] complex (float2 or short2)
+    int in_int16;            // 1: short2 samples
+    const float2* hist_in;   // [sub][pol][T-1][N] previous blocks (may be null: zeros)
+    float2* hist_out;        // [sub][pol][T-1][N] blocks carried to the next call
+    const float* coeffs;     // [T][N]
+    const float2* twiddle;   // [N/2] exp(-2 pi i k / N)
+    int nsub, npol, nblocks, N, T, log2n, BT;
+    // output
+    int mode;                // 0: complex spectra, 1: Stokes + integration
+    float2* spectra;         // mode 0: [block][sub][pol][N]
+    float* stokes;           // mode 1: [u][sub][nstokes][N/bin]
+    int nstokes, window, bin, nu;  // nu: complete windows written
+};
+
+__device__ __forceinline__ float2 load_sample(const ChanArgs& a, long long idx) {
+    if (a.in_int16) {
+        const short2 v = reinterpret_cast<const short2*>(a.in)[idx];
+        return make_float2((float)v.x, (float)v.y);
+    }
+    return reinterpret_cast<const float2*>(a.in)[idx];
+}
+
+__global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
+    extern __shared__ float2 sm[];
+    const int N = a.N, T = a.T, BT = a.BT, P = a.npol;
+    const int s = blockIdx.y;
+    const int b0 = blockIdx.x * BT;
+    const int nb = min(BT, a.nblocks - b0);  // blocks of this tile
+    const int H = T - 1;
+    const int rows = nb + H;                 // staged blocks per polarisation
+    float2* x = sm;                          // [P][BT+H][N]
+    float2* y = sm + (size_t)P * (BT + H) * N;    // [P][BT][N]
+    float2* tw = y + (size_t)P * BT * N;          // [N/2]
+    float* cf = reinterpret_cast<float*>(tw + N / 2);  // [T][N]
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    for (int i = tid; i < N / 2; i += nt) tw[i] = a.twiddle[i];
+    for (int i = tid; i < T * N; i += nt) cf[i] = a.coeffs[i];
+    // stage blocks b0-H .. b0+nb-1; negative blocks come from the history
+    for (int p = 0; p < P; ++p) {
+        const long long base = ((long long)s * P + p) * (long long)a.nblocks * N;
+        for (int i = tid; i < rows * N; i += nt) {
+            const int r = i / N, c = i - r * N;
+            const int b = b0 - H + r;
+            float2 v;
+            if (b >= 0) {
+                v = load_sample(a, base + (long long)b * N + c);
+            } else {
+                v = a.hist_in ? a.hist_in[(((long long)s * P + p) * H + (H + b)) * N + c]
+                              : make_float2(0.0f, 0.0f);
+            }
+            x[((size_t)p * (BT + H) + r) * N + c] = v;
+        }
+    }
+    __syncthreads();
+    // the last tile carries its final T-1 blocks (old history included when
+    // the chunk is shorter than that) to the next call
+    if (b0 + nb == a.nblocks && a.hist_out) {
+        for (int p = 0; p < P; ++p)
+            for (int i = tid; i < H * N; i += nt) {
+                const int r = i / N, c = i - r * N;
+                a.hist_out[(((long long)s * P + p) * H + r) * N + c] =
+                    x[((size_t)p * (BT + H) + nb + r) * N + c];
+            }
+    }
+    // FIR: y[p][b][c] = sum_t coeff[t][c] * x[p][b+t][c], oldest tap first
+    for (int i = tid; i < P * nb * N; i += nt) {
+        const int c = i % N, pb = i / N;
+        const int p = pb / nb, b = pb - p * nb;
+        const float2* xs = x + ((size_t)p * (BT + H) + b) * N + c;
+        float re = 0.0f, im = 0.0f;
+        for (int t = 0; t < T; ++t) {
+            const float k = cf[t * N + c];
+            const float2 v = xs[(size_t)t * N];
+            re = __fadd_rn(re, __fmul_rn(v.x, k));
+            im = __fadd_rn(im, __fmul_rn(v.y, k));
+        }
+        y[((size_t)p * BT + b) * N + c] = make_float2(re, im);
+    }
+    __syncthreads();
+    // Stockham radix-2 FFT of every (pol, block) row, ping-ponging y <-> x
+    float2* src = y;
+    float2* dst = x;
+    const int half = N / 2;
+    for (int ns = 1; ns < N; ns *= 2) {
+        const int tw_stride = N / (2 * ns);
+        for (int i = tid; i < P * nb * half; i += nt) {
+            const int j = i % half, row = i / half;
+            const int p = row / nb, b = row - p * nb;
+            const float2* r0 = src + ((size_t)p * BT + b) * N;
+            float2* d0 = dst + ((size_t)p * BT + b) * N;
+            const float2 u = r0[j];
+            const float2 v0 = r0[j + half];
+            const int k = j % ns;
+            const float2 w = tw[k * tw_stride];
+            const float2 v = make_float2(__fsub_rn(__fmul_rn(v0.x, w.x), __fmul_rn(v0.y, w.y)),
+                                         __fadd_rn(__fmul_rn(v0.x, w.y), __fmul_rn(v0.y, w.x)));
+            const int o = (j / ns) * ns * 2 + k;
+            d0[o] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+            d0[o + ns] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+        }
+        __syncthreads();
+        float2* t = src; src = dst; dst = t;
+    }
+    // src holds the spectra, rows of stride N with pol stride BT*N
+    if (a.mode == 0) {
+        for (int i = tid; i < P * nb * N; i += nt) {
+            const int c = i % N, pb = i / N;
+            const int b = pb % nb, p = pb / nb;
+            a.spectra[(((long long)(b0 + b) * a.nsub + s) * P + p) * N + c] =
+                src[((size_t)p * BT + b) * N + c];
+        }
+        return;
+    }
+    // Stokes (StokesGenerator.cpp:93-104) integrated over window blocks and bin
+    // channels in the integrator's order (StokesIntegrator.cpp:97-115).
+    const int nco = N / a.bin;
+    const int u0 = b0 / a.window;
+    const int nu_tile = nb / a.window;
+    for (int i = tid; i < nu_tile * a.nstokes * nco; i += nt) {
+        const int nc = i % nco, rest = i / nco;
+        const int k = rest % a.nstokes, ul = rest / a.nstokes;
+        const int u = u0 + ul;
+        if (u >= a.nu) continue;
+        float acc = 0.0f;
+        for (int tb = 0; tb < a.window; ++tb) {
+            const int b = ul * a.window + tb;
+            const float2* X = src + (size_t)b * N;
+            const float2* Y = src + ((size_t)BT + b) * N;
+            for (int c = nc * a.bin; c < (nc + 1) * a.bin; ++c) {
+                const float xr = X[c].x, xi = X[c].y, yr = Y[c].x, yi = Y[c].y;
+                const float px = __fadd_rn(__fmul_rn(xr, xr), __fmul_rn(xi, xi));
+                const float py = __fadd_rn(__fmul_rn(yr, yr), __fmul_rn(yi, yi));
+                float v;
+                if (k == 0) v = __fadd_rn(px, py);
+                else if (k == 1) v = __fsub_rn(px, py);
+                else if (k == 2) v = __fmul_rn(2.0f, __fadd_rn(__fmul_rn(xr, yr), __fmul_rn(xi, yi)));
+                else v = __fmul_rn(2.0f, __fsub_rn(__fmul_rn(xi, yr), __fmul_rn(xr, yi)));
+                acc = __fadd_rn(acc, v);
+            }
+        }
+        a.stokes[(((long long)u * a.nsub + s) * a.nstokes + k) * nco + nc] = acc;
+    }
+}
+
+// StokesGenerator::run on complex spectra [t][sub][2][N] (module-level call).
+__global__ void stokes_kernel(const float2* __restrict__ spectra, int nt, int nsub, int N, int nstokes,
+                              float* __restrict__ out) {
+    const long long n = (long long)nt * nsub * N;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % N);
+        const long long ts = i / N;
+        const float2 X = spectra[(ts * 2 + 0) * N + c];
+        const float2 Y = spectra[(ts * 2 + 1) * N + c];
+        const float xyr = __fadd_rn(__fmul_rn(X.x, Y.x), __fmul_rn(X.y, Y.y));
+        const float xyi = __fsub_rn(__fmul_rn(X.y, Y.x), __fmul_rn(X.x, Y.y));
+        const float px = __fadd_rn(__fmul_rn(X.x, X.x), __fmul_rn(X.y, X.y));
+        const float py = __fadd_rn(__fmul_rn(Y.x, Y.x), __fmul_rn(Y.y, Y.y));
+        float* o = out + ts * nstokes * N;
+        o[c] = __fadd_rn(px, py);
+        if (nstokes == 4) {
+            o[N + c] = __fsub_rn(px, py);
+            o[2 * N + c] = __fmul_rn(2.0f, xyr);
+            o[3 * N + c] = __fmul_rn(2.0f, xyi);
+        }
+    }
+}
+
+// StokesIntegrator::run on [t][sub][pol][nchan] (module-level call).
+__global__ void integrate_kernel(const float* __restrict__ in, int nsub, int npol, int nchan,
+                                 int window, int bin, int nu, float* __restrict__ out) {
+    const int nco = nchan / bin;
+    const long long n = (long long)nu * nsub * npol * nco;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int nc = (int)(i % nco);
+        const long long usp = i / nco;  // (u*nsub + s)*npol + p
+        const int p = (int)(usp % npol);
+        const long long us = usp / npol;
+        const int s = (int)(us % nsub);
+        const long long u = us / nsub;
+        float acc = 0.0f;
+        for (int tb = 0; tb < window; ++tb) {
+            const long long t = u * window + tb;
+            const float* v = in + (((t * nsub + s) * npol) + p) * nchan;
+            for (int c = nc * bin; c < (nc + 1) * bin; ++c) acc = __fadd_rn(acc, v[c]);
+        }
+        out[i] = acc;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// PPF state object
+// ---------------------------------------------------------------------------
+struct pv_ppf {
+    int nchan = 0, ntaps = 0, log2n = 0;
+    float* d_coeffs = nullptr;
+    float2* d_twiddle = nullptr;
+    float2* d_hist[2] = {nullptr, nullptr};
+    int cur = 0;
+    int nsub = 0, npol = 0;
+    bool have_hist = false;
+    std::vector<float> h_coeffs;
+};
+
+namespace {
+
+int tile_blocks(int N, int T, int P, int window, size_t* smem_out) {
+    // largest power-of-two tile (a multiple of the integration window) that
+    // fits in shared memory
+    for (int bt = 128; bt >= 1; bt /= 2) {
+        if (window > 0 && bt % window != 0) continue;
+        const size_t smem = ((size_t)P * (bt + T - 1) * N + (size_t)P * bt * N + N / 2) * sizeof(float2) +
+                            (size_t)T * N * sizeof(float);
+        if (smem <= 200 * 1024 && (size_t)P * bt * N <= 256 * 256) {
+            *smem_out = smem;
+            return bt;
+        }
+    }
+    return 0;
+}
+
+int prepare_history(pv_ppf* h, int nsub, int npol, cudaStream_t s) {
+    if (h->nsub == nsub && h->npol == npol && h->d_hist[0]) return PV_OK;
+    for (auto& p : h->d_hist)
+        if (p) { cudaFree(p); p = nullptr; }
+    const size_t bytes = (size_t)nsub * npol * (h->ntaps - 1) * h->nchan * sizeof(float2);
+    for (auto& p : h->d_hist) {
+        if (bytes == 0) continue;
+        PV_CUDA(cudaMalloc(&p, bytes), "allocate PPF history");
+        PV_CUDA(cudaMemsetAsync(p, 0, bytes, s), "clear PPF history");
+    }
+    h->nsub = nsub;
+    h->npol = npol;
+    h->cur = 0;
+    h->have_hist = false;
+    return PV_OK;
+}
+
+int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol, int nblocks,
+                   int mode, float2* d_spectra, float* d_stokes, int nstokes, int window, int bin,
+                   int* nu_out, cudaStream_t s) {
+    if (!h || !d_in || nsub <= 0 || npol <= 0 || nblocks <= 0) {
+        pv::set_error("PPFChanneliser: Empty time data blob");
+        return PV_ERR_ARG;
+    }
+    if (mode == 1 && (npol != 2 || (nstokes != 1 && nstokes != 4) || window <= 0 || bin <= 0 ||
+                      h->nchan % bin != 0)) {
+        pv::set_error("channelise: Stokes output needs 2 polarisations, 1 or 4 Stokes, "
+                      "window > 0 and a channel bin dividing nChannels");
+        return PV_ERR_ARG;
+    }
+    size_t smem = 0;
+    const int win_tile = mode == 1 ? std::min(window, nblocks) : 0;
+    const int bt = tile_blocks(h->nchan, h->ntaps, npol, win_tile, &smem);
+    if (bt == 0) {
+        pv::set_error("channelise: %d channels x window %d do not fit one tile", h->nchan, window);
+        return PV_ERR_ARG;
+    }
+    PV_TRY(prepare_history(h, nsub, npol, s));
+    const int w = mode == 1 ? std::min(window, nblocks) : 1;  // StokesIntegrator.cpp:53-59
+    const int nu = mode == 1 ? nblocks / w : 0;
+    ChanArgs a{};
+    a.in = d_in;
+    a.in_int16 = in_int16;
+    a.hist_in = h->have_hist ? h->d_hist[h->cur] : nullptr;
+    a.hist_out = h->d_hist[h->cur ^ 1];
+    a.coeffs = h->d_coeffs;
+    a.twiddle = h->d_twiddle;
+    a.nsub = nsub; a.npol = npol; a.nblocks = nblocks;
+    a.N = h->nchan; a.T = h->ntaps; a.log2n = h->log2n; a.BT = bt;
+    a.mode = mode; a.spectra = d_spectra; a.stokes = d_stokes;
+    a.nstokes = nstokes; a.window = w; a.bin = bin; a.nu = nu;
+    PV_CUDA(cudaFuncSetAttribute(channelise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem), "cudaFuncSetAttribute(channelise)");
+    dim3 grid((unsigned)pv::ceil_div(nblocks, bt), (unsigned)nsub);
+    if (nsub > 65535) {
+        pv::set_error("channelise: too many subbands");
+        return PV_ERR_ARG;
+    }
+    channelise_kernel<<<grid, 256, smem, s>>>(a);
+    PV_TRY(pv::check_launch("channelise_kernel"));
+    if (h->ntaps > 1) {
+        h->cur ^= 1;
+        h->have_hist = true;
+    }
+    if (nu_out) *nu_out = nu;
+    return PV_OK;
+}
+
+}  // namespace
+
+extern "C" int pv_ppf_create(pv_ppf** out, int nchan, int ntaps, int window,
+                             const float* h_coeffs) {
+    if (!out || nchan < 2 || ntaps < 1 || (nchan & (nchan - 1)) != 0 || nchan > 1024) {
+        pv::set_error("PPFChanneliser: channels must be a power of two in 2..1024 (got %d)", nchan);
+        return PV_ERR_CONFIG;
+    }
+    auto* h = new pv_ppf;
+    h->nchan = nchan;
+    h->ntaps = ntaps;
+    while ((1 << h->log2n) < nchan) ++h->log2n;
+    if (h_coeffs) {
+        h->h_coeffs.assign(h_coeffs, h_coeffs + (size_t)nchan * ntaps);
+    } else {
+        std::vector<double> c;
+        int rc = pv::fir_coefficients(ntaps, nchan, window, c);
+        if (rc != PV_OK) { delete h; return rc; }
+        h->h_coeffs.resize(c.size());
+        for (size_t i = 0; i < c.size(); ++i) h->h_coeffs[i] = (float)c[i];  // PPFChanneliser.cpp:212-217
+    }
+    std::vector<float2> tw(nchan / 2);
+    for (int k = 0; k < nchan / 2; ++k) {
+        const double ang = -2.0 * M_PI * k / nchan;
+        tw[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+    }
+    cudaError_t e = cudaMalloc(&h->d_coeffs, sizeof(float) * h->h_coeffs.size());
+    if (e == cudaSuccess) e = cudaMalloc(&h->d_twiddle, sizeof(float2) * tw.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->d_coeffs, h->h_coeffs.data(), sizeof(float) * h->h_coeffs.size(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->d_twiddle, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        pv::set_error("pv_ppf_create: %s", cudaGetErrorString(e));
+        if (h->d_coeffs) cudaFree(h->d_coeffs);
+        if (h->d_twiddle) cudaFree(h->d_twiddle);
+        delete h;
+        return PV_ERR_CUDA;
+    }
+    *out = h;
+    return PV_OK;
+}
+
+extern "C" void pv_ppf_destroy(pv_ppf* h) {
+    if (!h) return;
+    cudaFree(h->d_coeffs);
+    cudaFree(h->d_twiddle);
+    for (auto p : h->d_hist)
+        if (p) cudaFree(p);
+    delete h;
+}
+
+extern "C" int pv_ppf_coefficients(const pv_ppf* h, float* out) {
+    if (!h || !out) return PV_ERR_ARG;
+    std::copy(h->h_coeffs.begin(), h->h_coeffs.end(), out);
+    return PV_OK;
+}
+
+extern "C" int pv_ppf_reset(pv_ppf* h) {
+    if (!h) return PV_ERR_ARG;
+    h->have_hist = false;
+    for (auto p : h->d_hist)
+        if (p) cudaMemset(p, 0, (size_t)h->nsub * h->npol * (h->ntaps - 1) * h->nchan * sizeof(float2));
+    return PV_OK;
+}
+
+extern "C" int pv_ppf_run(pv_ppf* h, const float* d_in, int nsub, int npol, int nblocks,
+                          float* d_out, void* stream) {
+    return run_channelise(h, d_in, 0, nsub, npol, nblocks, 0, reinterpret_cast<float2*>(d_out),
+                          nullptr, 1, 1, 1, nullptr, pv::as_stream(stream));
+}
+
+extern "C" int pv_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int nblocks,
+                             int nstokes, int window, int bin, float* d_stokes, int* nu_out,
+                             void* stream) {
+    return run_channelise(h, d_in, in_int16, nsub, 2, nblocks, 1, nullptr, d_stokes, nstokes,
+                          window, bin, nu_out, pv::as_stream(stream));
+}
+
+extern "C" int pv_stokes(const float* d_spectra, int nt, int nsub, int nchan, int nstokes,
+                         float* d_out, void* stream) {
+    if (nstokes != 1 && nstokes != 4) {
+        pv::set_error("StokesGenerator: You can either generate 1 or 4 Stokes parameters.");
+        return PV_ERR_CONFIG;
+    }
+    if (!d_spectra || !d_out || nt < 0 || nsub <= 0 || nchan <= 0) {
+        pv::set_error("pv_stokes: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const long long n = (long long)nt * nsub * nchan;
+    if (n == 0) return PV_OK;
+    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(n, 256), pv::sm_count() * 16LL);
+    stokes_kernel<<<blocks, 256, 0, pv::as_stream(stream)>>>(
+        reinterpret_cast<const float2*>(d_spectra), nt, nsub, nchan, nstokes, d_out);
+    return pv::check_launch("stokes_kernel");
+}
+
+extern "C" int pv_integrate(const float* d_in, int nt, int nsub, int npol, int nchan, int window,
+                            int bin, float* d_out, int* nu_out, void* stream) {
+    if (!d_in || !d_out || nt < 0 || nsub <= 0 || npol <= 0 || nchan <= 0 || window <= 0 ||
+        bin <= 0 || nchan % bin != 0) {
+        pv::set_error("pv_integrate: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const int w = std::min(window, std::max(nt, 1));  // StokesIntegrator.cpp:53-59
+    const int nu = nt / w;
+    if (nu_out) *nu_out = nu;
+    const long long n = (long long)nu * nsub * npol * (nchan / bin);
+    if (n == 0) return PV_OK;
+    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(n, 256), pv::sm_count() * 16LL);
+    integrate_kernel<<<blocks, 256, 0, pv::as_stream(stream)>>>(d_in, nsub, npol, nchan, w, bin, nu,
+                                                               d_out);
+    return pv::check_launch("integrate_kernel");
+}

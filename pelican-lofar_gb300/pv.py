@@ -64,6 +64,21 @@ def _declare(L):
         "pv_dedisp_plan_max_shift": (i, [vp]),
         "pv_dedisp_plan_run": (i, [vp, vp, ll, vp, ll, ll, ll, ll, i, vp]),
         "pv_ring_write": (i, [vp, ll, ll, ll, vp, i, i, i, i, i, vp]),
+        "pv_window_from_name": (i, [C.c_char_p]),
+        "pv_fir_coefficients": (i, [i, i, i, P(C.c_double)]),
+        "pv_ppf_create": (i, [P(vp), i, i, i, vp]),
+        "pv_ppf_destroy": (None, [vp]),
+        "pv_ppf_coefficients": (i, [vp, P(C.c_float)]),
+        "pv_ppf_reset": (i, [vp]),
+        "pv_ppf_run": (i, [vp, vp, i, i, i, vp, vp]),
+        "pv_channelise": (i, [vp, vp, i, i, i, i, i, i, vp, P(i), vp]),
+        "pv_stokes": (i, [vp, i, i, i, i, vp, vp]),
+        "pv_integrate": (i, [vp, i, i, i, i, i, i, vp, P(i), vp]),
+        "pv_rfi_create": (i, [P(vp), C.c_char_p, f, f, i, i, i, i, i]),
+        "pv_rfi_destroy": (None, [vp]),
+        "pv_rfi_run": (i, [vp, vp, i, i, i, i, vp, vp]),
+        "pv_rfi_state": (i, [vp, P(C.c_double)]),
+        "pv_rfi_bandpass": (i, [vp, P(C.c_float), i]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
@@ -172,3 +187,113 @@ def analyse(d_data, threshold, rms, bin_pow2=6, cap=None, stream=None):
     k = min(n.value, cap)
     host = ev[: 4 * k].cpu().numpy().view(EVENT_DTYPE)
     return host.copy(), n.value
+
+
+# ---------------------------------------------------------------------------
+# channeliser chain and RFI clipper
+# ---------------------------------------------------------------------------
+
+WINDOWS = {"hamming": 0, "blackman": 1, "gaussian": 2, "kaiser": 3}
+
+
+def fir_coefficients(ntaps, nchan, window="kaiser"):
+    out = np.zeros((ntaps, nchan), np.float64)
+    check(load().pv_fir_coefficients(ntaps, nchan, WINDOWS[window],
+                                     out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+class PPF:
+    """Device channeliser with its tap history (PPFChanneliser)."""
+
+    def __init__(self, nchan, ntaps=8, window="kaiser", coeffs=None):
+        self.nchan, self.ntaps = nchan, ntaps
+        self.h = C.c_void_p()
+        c = None
+        if coeffs is not None:
+            self._c = np.ascontiguousarray(coeffs, np.float32)
+            c = self._c.ctypes.data_as(C.c_void_p)
+        check(load().pv_ppf_create(C.byref(self.h), nchan, ntaps, WINDOWS[window], c))
+
+    def coefficients(self):
+        out = np.zeros((self.ntaps, self.nchan), np.float32)
+        check(load().pv_ppf_coefficients(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def run(self, d_in, stream=None):
+        """d_in complex64 CUDA tensor [sub][pol][block*nchan] -> [block][sub][pol][nchan]."""
+        import torch
+        nsub, npol, n = d_in.shape
+        nblocks = n // self.nchan
+        out = torch.empty((nblocks, nsub, npol, self.nchan), dtype=torch.complex64, device=d_in.device)
+        check(load().pv_ppf_run(self.h, _ptr(d_in), nsub, npol, nblocks, _ptr(out), _stream(stream)))
+        return out
+
+    def channelise(self, d_in, nstokes=1, window=4, bin=1, stream=None):
+        """Fused PPF+Stokes+integration; d_in complex64 or int16 [sub][2][n(*2)]."""
+        import torch
+        int16 = d_in.dtype == torch.int16
+        nsub = d_in.shape[0]
+        n = d_in.shape[2] // (2 if int16 else 1)
+        nblocks = n // self.nchan
+        w = min(window, nblocks)
+        nu = nblocks // w
+        out = torch.empty((nu, nsub, nstokes, self.nchan // bin), dtype=torch.float32, device=d_in.device)
+        got = C.c_int()
+        check(load().pv_channelise(self.h, _ptr(d_in), int(int16), nsub, nblocks, nstokes, window, bin,
+                                   _ptr(out), C.byref(got), _stream(stream)))
+        assert got.value == nu
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_ppf_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def stokes(d_spectra, nstokes=1, stream=None):
+    import torch
+    nt, nsub, npol, nchan = d_spectra.shape
+    out = torch.empty((nt, nsub, nstokes, nchan), dtype=torch.float32, device=d_spectra.device)
+    check(load().pv_stokes(_ptr(d_spectra), nt, nsub, nchan, nstokes, _ptr(out), _stream(stream)))
+    return out
+
+
+def integrate(d_in, window, bin=1, stream=None):
+    import torch
+    nt, nsub, npol, nchan = d_in.shape
+    w = min(window, max(nt, 1))
+    out = torch.empty((nt // w, nsub, npol, nchan // bin), dtype=torch.float32, device=d_in.device)
+    nu = C.c_int()
+    check(load().pv_integrate(_ptr(d_in), nt, nsub, npol, nchan, window, bin, _ptr(out), C.byref(nu),
+                              _stream(stream)))
+    return out
+
+
+class RFI:
+    """Device RFI_Clipper."""
+
+    def __init__(self, bp_text, cr=10.0, sr=4.0, history=10, zero_dming=False, mean_over_rms=True,
+                 band_matching=True, active=True):
+        self.h = C.c_void_p()
+        check(load().pv_rfi_create(C.byref(self.h), bp_text.encode() if bp_text else None, cr, sr,
+                                   history, int(zero_dming), int(mean_over_rms), int(band_matching),
+                                   int(active)))
+
+    def run(self, d_data, flags=False, stream=None):
+        import torch
+        nt, nsub, npol, nchan = d_data.shape
+        fl = torch.zeros((nt, nsub * nchan), dtype=torch.uint8, device=d_data.device) if flags else None
+        check(load().pv_rfi_run(self.h, _ptr(d_data), nt, nsub, npol, nchan,
+                                _ptr(fl) if fl is not None else None, _stream(stream)))
+        return fl
+
+    def state(self):
+        out = np.zeros(10, np.float64)
+        check(load().pv_rfi_state(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_rfi_destroy(self.h)
+            self.h = C.c_void_p()

@@ -58,3 +58,27 @@ def make_bp_text(nbins, start, width, median, rms, coeffs=()):
              repr(float(width)), repr(float(rms)), repr(float(median))]
     lines += [repr(float(c)) for c in coeffs]
     return "\n".join(lines) + "\n"
+
+
+def voltages(rng, nsub, npol, nsamp, sigma=16.0):
+    """Complex int16 dual-pol station voltages [sub][pol][nsamp][2] (Gaussian,
+    rounded and saturated) and the same values as complex64."""
+    v = rng.normal(0.0, sigma, size=(nsub, npol, nsamp, 2))
+    v = np.clip(np.rint(v), -32768, 32767).astype(np.int16)
+    c = (v[..., 0].astype(np.float32) + 1j * v[..., 1].astype(np.float32)).astype(np.complex64)
+    return v, c
+
+
+def stokes_filterbank(rng, nt, nsub, nchan, level=1000.0, dof=8, rfi_channels=0.03, burst_rate=2e-3,
+                      shape=None):
+    """Positive Stokes-I spectra [t][sub][1][chan]: level * chi^2_dof/dof noise,
+    a fraction of channels with persistent narrowband RFI and occasional
+    broadband bursts."""
+    nbins = nsub * nchan
+    base = np.full(nbins, level, np.float64) if shape is None else np.asarray(shape, np.float64)
+    x = rng.gamma(dof / 2.0, 2.0 / dof, size=(nt, nbins)) * base
+    bad = rng.random(nbins) < rfi_channels
+    x[:, bad] *= 4.0
+    bursts = rng.random(nt) < burst_rate
+    x[bursts] *= 1.5
+    return x.astype(np.float32).reshape(nt, nsub, 1, nchan)

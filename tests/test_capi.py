@@ -55,3 +55,14 @@ def test_errors_are_reported_not_thrown(pv):
     rc = L.pv_dm_shifts(0.0, -1.0, 4, out.ctypes.data_as(C.POINTER(C.c_float)), C.byref(inv))
     assert rc == -3
     assert b"frequencyChannel1" in L.pv_last_error()
+
+
+def test_rfi_config_errors(pv):
+    """Configuration errors surface as status codes with the reference's text."""
+    import pytest
+    with pytest.raises(pv.PvError, match="BandPassData"):
+        pv.RFI("", cr=5.0)
+    with pytest.raises(pv.PvError, match="at least 6"):
+        pv.RFI("1\n2\n3\n")
+    inactive = pv.RFI("", active=False)
+    assert inactive is not None
