@@ -38,6 +38,8 @@ const char* pv_last_error(void);
 int pv_version(void);
 /* Number of kernels this library launched since load (all entry points). */
 long long pv_kernel_launches(void);
+/* cudaMemcpyAsync with cudaMemcpyDefault (host or device pointers). */
+int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
 
 /* ------------------------------------------------------------------------
  * A7 delay table — DedispersionModule::resize (lib/src/DedispersionModule.cpp:109-190)
@@ -210,6 +212,61 @@ int pv_rfi_run(pv_rfi* rfi, float* d_data, int nt, int nsub, int npol, int nchan
 int pv_rfi_state(pv_rfi* rfi, double* h_out10);
 /* The rebinned bandpass model the first run used (host copy). */
 int pv_rfi_bandpass(pv_rfi* rfi, float* h_out, int nbins);
+
+/* ------------------------------------------------------------------------
+ * One beam's device-resident chain, in the order of DedispersionPipeline::run
+ * (src/pipelines/udpstream/src/DedispersionPipeline.cpp:96-174) with the
+ * StokesIntegrator of UdpBFPipeline (UdpBFPipeline.cpp:80-92):
+ * PPF -> Stokes I -> integrate -> RFI_Clipper -> DedispersionModule ->
+ * DedispersionAnalyser, with the PPF tap history, the RFI state and the
+ * per-channel delay ring kept on the device between chunks.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    int nsub;           /* subbands */
+    int nchan_sub;      /* PPFChanneliser outputChannelsPerSubband */
+    int ntaps;          /* filter@nTaps */
+    int window;         /* filter@filterWindow, PV_WINDOW_* */
+    int int_time;       /* StokesIntegrator integrateTimeBins */
+    int int_chan;       /* StokesIntegrator integrateFrequencyChannels */
+    double fch1;        /* frequency of filterbank channel 0 (MHz) */
+    double foff;        /* filterbank channel width (MHz; > 0 ascending) */
+    double tsamp;       /* filterbank sample time (s) */
+    int tdms;           /* dedispersionSamples */
+    float dm_low;       /* dedispersionMinimum */
+    float dm_step;      /* dedispersionStepSize */
+    int chunk;          /* filterbank samples per chunk (= dedispersed samples per chunk) */
+    float threshold;    /* detectionThreshold@in_sigma */
+    int bin_pow2;       /* power2ForBinning */
+    long long event_capacity; /* events kept per chunk (0: 2^20) */
+    const char* bp_text;      /* RFI_Clipper BandPassData contents */
+    float cr, sr;             /* channelRejectionRMS, spectrumRejectionRMS */
+    int history;              /* History@maximum */
+    int zero_dming, rms_from_mean, band_matching, rfi_active;
+    int debug_taps;           /* keep the pre-RFI filterbank of the last chunk */
+} pv_beam_config;
+
+typedef struct pv_beam pv_beam;
+int pv_beam_create(pv_beam** beam, const pv_beam_config* config);
+void pv_beam_destroy(pv_beam* beam);
+/* Bytes of one chunk of voltages: nsub x 2 pols x chunk*int_time*nchan_sub
+ * complex samples of int16 (4 bytes) or float (8 bytes), layout
+ * [sub][pol][sample] (TimeSeriesDataSetC32 order). */
+long long pv_beam_input_bytes(const pv_beam* beam, int in_int16);
+/* Processes one chunk from device (or host) memory, asynchronously. */
+int pv_beam_process(pv_beam* beam, const void* d_voltages, int in_int16, void* stream);
+int pv_beam_process_host(pv_beam* beam, const void* h_voltages, int in_int16, void* stream);
+/* Events of the last dedispersed window (synchronises the stream): total
+ * count including the dummy, the first sample of the window (-1 while the
+ * ring is still filling), and up to cap events copied to h_events. */
+int pv_beam_events(pv_beam* beam, pv_event* h_events, long long cap, long long* h_count,
+                   long long* h_first_sample, void* stream);
+/* [dedispersion channels, max delay, lag in chunks, ring samples, inverted,
+ *  chunks processed, last window, ring bytes] */
+int pv_beam_info(const pv_beam* beam, long long* h_info8);
+/* Device views of the last chunk's filterbank (after RFI), its pre-RFI copy
+ * (debug_taps), the dedispersed window [tdms][chunk] and the ring. */
+int pv_beam_buffers(const pv_beam* beam, float** d_filterbank, float** d_filterbank_raw,
+                    float** d_dedispersed, float** d_ring);
 
 #ifdef __cplusplus
 }

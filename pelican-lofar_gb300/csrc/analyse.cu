@@ -149,6 +149,12 @@ __global__ void scan_add(long long* __restrict__ out, const long long* __restric
     if (g < n && blockIdx.x > 0) out[g] += block_off[blockIdx.x];
 }
 
+// total = 1 (the dummy) + events of every (DM, block) pair
+__global__ void analyse_total(const int* __restrict__ counts, const long long* __restrict__ offsets,
+                              long long npairs, long long* __restrict__ total) {
+    *total = npairs > 0 ? 1 + offsets[npairs - 1] + counts[npairs - 1] : 1;
+}
+
 long long scan_workspace(long long n) {
     long long total = 0;
     while (n > 1) {
@@ -177,38 +183,26 @@ int exclusive_scan(const T* in, long long* out, long long n, long long* ws, cuda
 
 template <int P>
 int run_analyse(const float* data, long long ld, int tdms, int nsamp, const Thresholds& thr,
-                pv_event* ev, long long cap, long long* h_count, int* counts, long long* offsets,
+                pv_event* ev, long long cap, long long* d_total, int* counts, long long* offsets,
                 long long* ws, cudaStream_t s) {
     const int nblocks = nsamp >> P;
     const long long npairs = (long long)tdms * nblocks;
     const bool vec4 = (ld % 4 == 0) && ((reinterpret_cast<uintptr_t>(data) & 15) == 0);
     const int threads = 128;
-    if (npairs == 0) {
-        if (cap > 0) {
-            pv_event dummy{0, 0, 1.0f, 0.0f};
-            PV_CUDA(cudaMemcpyAsync(ev, &dummy, sizeof(dummy), cudaMemcpyHostToDevice, s),
-                    "write dummy event");
-        }
-        PV_CUDA(cudaStreamSynchronize(s), "synchronise");
-        *h_count = 1;
-        return PV_OK;
+    if (npairs > 0) {
+        const unsigned blocks = (unsigned)pv::ceil_div<long long>(npairs, threads);
+        analyse_count<P><<<blocks, threads, 0, s>>>(data, ld, tdms, nblocks, thr, vec4, counts);
+        PV_TRY(pv::check_launch("analyse_count"));
+        PV_TRY(exclusive_scan<int>(counts, offsets, npairs, ws, s));
+        analyse_emit<P><<<blocks, threads, 0, s>>>(data, ld, tdms, nblocks, thr, vec4, counts,
+                                                   offsets, ev, cap);
+        PV_TRY(pv::check_launch("analyse_emit"));
+    } else if (cap > 0) {
+        analyse_emit<P><<<1, 32, 0, s>>>(data, ld, tdms, 0, thr, false, counts, offsets, ev, cap);
+        PV_TRY(pv::check_launch("analyse_emit"));
     }
-    const unsigned blocks = (unsigned)pv::ceil_div<long long>(npairs, threads);
-    analyse_count<P><<<blocks, threads, 0, s>>>(data, ld, tdms, nblocks, thr, vec4, counts);
-    PV_TRY(pv::check_launch("analyse_count"));
-    PV_TRY(exclusive_scan<int>(counts, offsets, npairs, ws, s));
-    analyse_emit<P><<<blocks, threads, 0, s>>>(data, ld, tdms, nblocks, thr, vec4, counts, offsets,
-                                               ev, cap);
-    PV_TRY(pv::check_launch("analyse_emit"));
-    long long last_off = 0;
-    int last_cnt = 0;
-    PV_CUDA(cudaMemcpyAsync(&last_off, offsets + npairs - 1, sizeof(long long),
-                            cudaMemcpyDeviceToHost, s), "read event offset");
-    PV_CUDA(cudaMemcpyAsync(&last_cnt, counts + npairs - 1, sizeof(int), cudaMemcpyDeviceToHost, s),
-            "read event count");
-    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
-    *h_count = 1 + last_off + last_cnt;
-    return PV_OK;
+    analyse_total<<<1, 1, 0, s>>>(counts, offsets, npairs, d_total);
+    return pv::check_launch("analyse_total");
 }
 
 }  // namespace
@@ -219,13 +213,15 @@ namespace pv {
 size_t analyse_scratch_bytes(int tdms, int nsamp, int bin_pow2) {
     const long long npairs = (long long)tdms * (nsamp >> bin_pow2);
     const long long n = std::max<long long>(npairs, 1);
-    return (size_t)n * sizeof(int) + (size_t)n * sizeof(long long) +
-           (size_t)(scan_workspace(n) + 2) * sizeof(long long) + 256;
+    const size_t bytes = (size_t)n * sizeof(int) + (size_t)n * sizeof(long long) +
+                         (size_t)(scan_workspace(n) + 2) * sizeof(long long) + 256;
+    return (bytes + 255) / 256 * 256;  // keeps anything placed after it aligned
 }
 
-// Analyser with caller-provided scratch (analyse_scratch_bytes bytes).
-int analyse_device(const float* data, long long ld, int tdms, int nsamp, float threshold,
-                   float rms, int bin_pow2, pv_event* ev, long long cap, long long* h_count,
+// Analyser with caller-provided scratch (analyse_scratch_bytes bytes);
+// asynchronous: the event total (dummy included) lands in *d_total.
+int analyse_launch(const float* data, long long ld, int tdms, int nsamp, float threshold,
+                   float rms, int bin_pow2, pv_event* ev, long long cap, long long* d_total,
                    void* scratch, cudaStream_t s) {
     Thresholds thr{};
     PV_TRY(pv_analyser_thresholds(threshold, rms, bin_pow2, thr.v));
@@ -238,7 +234,7 @@ int analyse_device(const float* data, long long ld, int tdms, int nsamp, float t
     int* counts = reinterpret_cast<int*>(p);
     switch (bin_pow2) {
 #define PV_CASE(P) \
-    case P: return run_analyse<P>(data, ld, tdms, nsamp, thr, ev, cap, h_count, counts, offsets, ws, s);
+    case P: return run_analyse<P>(data, ld, tdms, nsamp, thr, ev, cap, d_total, counts, offsets, ws, s);
         PV_CASE(0) PV_CASE(1) PV_CASE(2) PV_CASE(3) PV_CASE(4) PV_CASE(5) PV_CASE(6) PV_CASE(7)
         PV_CASE(8)
 #undef PV_CASE
@@ -278,9 +274,16 @@ extern "C" int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp
     }
     cudaStream_t s = pv::as_stream(stream);
     void* scratch = nullptr;
-    PV_TRY(pv::scratch_alloc(&scratch, pv::analyse_scratch_bytes(tdms, nsamp, bin_pow2), s));
-    const int rc = pv::analyse_device(d_data, ld, tdms, nsamp, threshold, rms, bin_pow2, d_events,
-                                      cap, h_count, scratch, s);
+    PV_TRY(pv::scratch_alloc(&scratch, pv::analyse_scratch_bytes(tdms, nsamp, bin_pow2) + 64, s));
+    long long* d_total = reinterpret_cast<long long*>(static_cast<char*>(scratch) +
+                                                      pv::analyse_scratch_bytes(tdms, nsamp, bin_pow2));
+    int rc = pv::analyse_launch(d_data, ld, tdms, nsamp, threshold, rms, bin_pow2, d_events, cap,
+                                d_total, scratch, s);
+    if (rc == PV_OK) {
+        rc = pv::cuda_status(cudaMemcpyAsync(h_count, d_total, sizeof(long long),
+                                             cudaMemcpyDeviceToHost, s), "read event count");
+        if (rc == PV_OK) rc = pv::cuda_status(cudaStreamSynchronize(s), "synchronise");
+    }
     pv::scratch_free(scratch, s);
     return rc;
 }

@@ -1,0 +1,218 @@
+// One beam's device-resident hot path (the DedispersionPipeline call order,
+// src/pipelines/udpstream/src/DedispersionPipeline.cpp:96-174, with the
+// StokesIntegrator of UdpBFPipeline.cpp:80-92):
+//
+//   int16 voltages -> K1 fused PPF + Stokes I + integration -> K2/K3 RFI clip
+//   (in place) -> transposed write into the per-channel ring -> K4
+//   dedispersion of the window whose delays are complete -> K5 analyser.
+//
+// Everything runs on the caller's stream with buffers allocated once, so a
+// chunk costs no host synchronisation until its events are read.  The ring
+// holds (L+1) chunks, L = ceil(max delay / chunk): chunk k completes the
+// delays of output window k-L (overlap-save), which is dedispersed and
+// searched as soon as chunk k lands.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pv_internal.cuh"
+
+struct pv_beam {
+    pv_beam_config cfg{};
+    pv_ppf* ppf = nullptr;
+    pv_rfi* rfi = nullptr;
+    pv_dedisp_plan* plan = nullptr;
+    int nchan_fb = 0;        // filterbank channels per subband after integration
+    int nbins = 0;           // dedispersion channels
+    int inverted = 0;
+    int max_shift = 0, lag = 0;
+    long long ring_len = 0, row_stride = 0;
+    float* d_ring = nullptr;
+    float* d_fb = nullptr;       // [chunk][nsub][1][nchan_fb]
+    float* d_fb_raw = nullptr;   // optional pre-RFI copy
+    float* d_out = nullptr;      // [tdms][chunk]
+    pv_event* d_events = nullptr;
+    long long cap = 0;
+    void* d_scratch = nullptr;
+    long long* d_total = nullptr;
+    long long* h_total = nullptr;  // pinned
+    void* d_in = nullptr;          // staging for host input
+    size_t in_bytes = 0;
+    long long chunks = 0;
+    long long window = -1;
+    float rms = 0.0f;
+};
+
+namespace {
+
+void destroy(pv_beam* b) {
+    if (b->ppf) pv_ppf_destroy(b->ppf);
+    if (b->rfi) pv_rfi_destroy(b->rfi);
+    if (b->plan) pv_dedisp_plan_destroy(b->plan);
+    for (void* p : {(void*)b->d_ring, (void*)b->d_fb, (void*)b->d_fb_raw, (void*)b->d_out,
+                    (void*)b->d_events, b->d_scratch, b->d_in})
+        if (p) cudaFree(p);
+    if (b->h_total) cudaFreeHost(b->h_total);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
+    if (!out || !c) return PV_ERR_ARG;
+    *out = nullptr;
+    if (c->nsub <= 0 || c->nchan_sub <= 0 || c->int_time <= 0 || c->int_chan <= 0 ||
+        c->nchan_sub % c->int_chan != 0 || c->chunk <= 0 || c->tdms <= 0 || c->tsamp <= 0.0) {
+        pv::set_error("pv_beam_create: invalid beam configuration");
+        return PV_ERR_CONFIG;
+    }
+    auto* b = new pv_beam;
+    b->cfg = *c;
+    b->cfg.bp_text = nullptr;
+    b->nchan_fb = c->nchan_sub / c->int_chan;
+    b->nbins = c->nsub * b->nchan_fb;
+    int rc = pv_ppf_create(&b->ppf, c->nchan_sub, c->ntaps, c->window, nullptr);
+    if (rc == PV_OK)
+        rc = pv_rfi_create(&b->rfi, c->bp_text, c->cr, c->sr, c->history, c->zero_dming,
+                           c->rms_from_mean, c->band_matching, c->rfi_active);
+    std::vector<float> k(b->nbins);
+    if (rc == PV_OK) rc = pv_dm_shifts(c->fch1, c->foff, b->nbins, k.data(), &b->inverted);
+    const float start = (c->dm_low < 0.0f ? 0.0f : c->dm_low) / (float)c->tsamp;
+    const float step = c->dm_step / (float)c->tsamp;
+    if (rc == PV_OK) rc = pv_dedisp_plan_create(&b->plan, k.data(), b->nbins, c->tdms, start, step);
+    if (rc != PV_OK) {
+        destroy(b);
+        return rc;
+    }
+    b->max_shift = pv_dedisp_plan_max_shift(b->plan);
+    b->lag = (b->max_shift + c->chunk - 1) / c->chunk;
+    b->ring_len = (long long)(b->lag + 1) * c->chunk;
+    b->row_stride = (b->ring_len + 31) / 32 * 32;
+    b->cap = c->event_capacity > 0 ? c->event_capacity : (1LL << 20);
+    b->rms = std::sqrt((float)b->nchan_fb * (float)c->nsub);  // DedispersionAnalyser.cpp:38
+    const size_t scratch = pv::analyse_scratch_bytes(c->tdms, c->chunk, c->bin_pow2);
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void**)&b->d_ring, sizeof(float) * b->nbins * (size_t)b->row_stride);
+    alloc((void**)&b->d_fb, sizeof(float) * (size_t)c->chunk * b->nbins);
+    if (c->debug_taps) alloc((void**)&b->d_fb_raw, sizeof(float) * (size_t)c->chunk * b->nbins);
+    alloc((void**)&b->d_out, sizeof(float) * (size_t)c->tdms * c->chunk);
+    alloc((void**)&b->d_events, sizeof(pv_event) * (size_t)b->cap);
+    alloc(&b->d_scratch, scratch + 256);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_total, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMemset(b->d_ring, 0, sizeof(float) * b->nbins * (size_t)b->row_stride);
+    if (e != cudaSuccess) {
+        pv::set_error("pv_beam_create: %s (ring of %lld x %lld samples)", cudaGetErrorString(e),
+                      (long long)b->nbins, b->row_stride);
+        destroy(b);
+        return PV_ERR_NOMEM;
+    }
+    b->d_total = reinterpret_cast<long long*>(static_cast<char*>(b->d_scratch) + scratch);
+    *out = b;
+    return PV_OK;
+}
+
+extern "C" void pv_beam_destroy(pv_beam* b) {
+    if (b) destroy(b);
+}
+
+extern "C" int pv_beam_info(const pv_beam* b, long long* h_info8) {
+    if (!b || !h_info8) return PV_ERR_ARG;
+    h_info8[0] = b->nbins;
+    h_info8[1] = b->max_shift;
+    h_info8[2] = b->lag;
+    h_info8[3] = b->ring_len;
+    h_info8[4] = b->inverted;
+    h_info8[5] = b->chunks;
+    h_info8[6] = b->window;
+    h_info8[7] = (long long)b->nbins * b->row_stride * (long long)sizeof(float);
+    return PV_OK;
+}
+
+extern "C" long long pv_beam_input_bytes(const pv_beam* b, int in_int16) {
+    if (!b) return -1;
+    return (long long)b->cfg.nsub * 2 * b->cfg.chunk * b->cfg.int_time * b->cfg.nchan_sub *
+           (in_int16 ? 4 : 8);
+}
+
+extern "C" int pv_beam_process(pv_beam* b, const void* d_voltages, int in_int16, void* stream) {
+    if (!b || !d_voltages) {
+        pv::set_error("pv_beam_process: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const pv_beam_config& c = b->cfg;
+    cudaStream_t s = pv::as_stream(stream);
+    const int nblocks = c.chunk * c.int_time;
+    int nu = 0;
+    PV_TRY(pv_channelise(b->ppf, d_voltages, in_int16, c.nsub, nblocks, 1, c.int_time, c.int_chan,
+                         b->d_fb, &nu, stream));
+    if (nu != c.chunk) {
+        pv::set_error("pv_beam_process: integration produced %d of %d samples", nu, c.chunk);
+        return PV_ERR_STATE;
+    }
+    if (b->d_fb_raw)
+        PV_CUDA(cudaMemcpyAsync(b->d_fb_raw, b->d_fb, sizeof(float) * (size_t)c.chunk * b->nbins,
+                                cudaMemcpyDeviceToDevice, s), "copy filterbank tap");
+    PV_TRY(pv_rfi_run(b->rfi, b->d_fb, c.chunk, c.nsub, 1, b->nchan_fb, nullptr, stream));
+    PV_TRY(pv::ring_write_device(b->d_ring, b->row_stride, b->ring_len, b->chunks * c.chunk, b->d_fb,
+                                 c.chunk, c.nsub, 1, b->nchan_fb, b->inverted, s));
+    b->chunks += 1;
+    if (b->chunks > b->lag) {
+        const long long w = b->chunks - 1 - b->lag;
+        PV_TRY(pv_dedisp_plan_run(b->plan, b->d_out, c.chunk, b->d_ring, b->row_stride, 0,
+                                  b->ring_len, (w * c.chunk) % b->ring_len, c.chunk, stream));
+        PV_TRY(pv::analyse_launch(b->d_out, c.chunk, c.tdms, c.chunk, c.threshold, b->rms,
+                                  c.bin_pow2, b->d_events, b->cap, b->d_total, b->d_scratch, s));
+        PV_CUDA(cudaMemcpyAsync(b->h_total, b->d_total, sizeof(long long), cudaMemcpyDeviceToHost, s),
+                "read event count");
+        b->window = w;
+    }
+    return PV_OK;
+}
+
+extern "C" int pv_beam_process_host(pv_beam* b, const void* h_voltages, int in_int16, void* stream) {
+    if (!b || !h_voltages) return PV_ERR_ARG;
+    const size_t bytes = (size_t)pv_beam_input_bytes(b, in_int16);
+    if (b->in_bytes < bytes) {
+        if (b->d_in) cudaFree(b->d_in);
+        b->d_in = nullptr;
+        b->in_bytes = 0;
+        PV_CUDA(cudaMalloc(&b->d_in, bytes), "allocate input staging");
+        b->in_bytes = bytes;
+    }
+    PV_CUDA(cudaMemcpyAsync(b->d_in, h_voltages, bytes, cudaMemcpyHostToDevice, pv::as_stream(stream)),
+            "copy voltages to the device");
+    return pv_beam_process(b, b->d_in, in_int16, stream);
+}
+
+extern "C" int pv_beam_events(pv_beam* b, pv_event* h_events, long long cap, long long* h_count,
+                              long long* h_first_sample, void* stream) {
+    if (!b || !h_count) return PV_ERR_ARG;
+    cudaStream_t s = pv::as_stream(stream);
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+    if (b->window < 0) {
+        *h_count = 0;
+        if (h_first_sample) *h_first_sample = -1;
+        return PV_OK;
+    }
+    *h_count = *b->h_total;
+    if (h_first_sample) *h_first_sample = b->window * b->cfg.chunk;
+    const long long n = std::min(std::min(*b->h_total, b->cap), cap);
+    if (h_events && n > 0)
+        PV_CUDA(cudaMemcpy(h_events, b->d_events, sizeof(pv_event) * n, cudaMemcpyDeviceToHost),
+                "copy events");
+    return PV_OK;
+}
+
+extern "C" int pv_beam_buffers(const pv_beam* b, float** d_filterbank, float** d_filterbank_raw,
+                               float** d_dedispersed, float** d_ring) {
+    if (!b) return PV_ERR_ARG;
+    if (d_filterbank) *d_filterbank = b->d_fb;
+    if (d_filterbank_raw) *d_filterbank_raw = b->d_fb_raw;
+    if (d_dedispersed) *d_dedispersed = b->d_out;
+    if (d_ring) *d_ring = b->d_ring;
+    return PV_OK;
+}

@@ -109,3 +109,14 @@ extern "C" int pv_maxshift(float dm_low, float dm_step, int tdms, const float* h
     }
     return PV_OK;
 }
+
+extern "C" int pv_device_copy(void* dst, const void* src, long long bytes, void* stream) {
+    if ((!dst || !src) && bytes > 0) {
+        pv::set_error("pv_device_copy: null pointer");
+        return PV_ERR_ARG;
+    }
+    if (bytes <= 0) return PV_OK;
+    PV_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDefault, pv::as_stream(stream)),
+            "pv_device_copy");
+    return PV_OK;
+}

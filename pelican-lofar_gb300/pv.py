@@ -79,6 +79,15 @@ def _declare(L):
         "pv_rfi_run": (i, [vp, vp, i, i, i, i, vp, vp]),
         "pv_rfi_state": (i, [vp, P(C.c_double)]),
         "pv_rfi_bandpass": (i, [vp, P(C.c_float), i]),
+        "pv_beam_create": (i, [P(vp), vp]),
+        "pv_beam_destroy": (None, [vp]),
+        "pv_beam_input_bytes": (ll, [vp, i]),
+        "pv_beam_process": (i, [vp, vp, i, vp]),
+        "pv_beam_process_host": (i, [vp, vp, i, vp]),
+        "pv_beam_events": (i, [vp, vp, ll, P(ll), P(ll), vp]),
+        "pv_beam_info": (i, [vp, P(ll)]),
+        "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
+        "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
@@ -297,3 +306,92 @@ class RFI:
         if getattr(self, "h", None) and self.h.value and _lib is not None:
             _lib.pv_rfi_destroy(self.h)
             self.h = C.c_void_p()
+
+
+# ---------------------------------------------------------------------------
+# beam pipeline
+# ---------------------------------------------------------------------------
+
+class BeamConfig(C.Structure):
+    _fields_ = [("nsub", C.c_int), ("nchan_sub", C.c_int), ("ntaps", C.c_int), ("window", C.c_int),
+                ("int_time", C.c_int), ("int_chan", C.c_int), ("fch1", C.c_double),
+                ("foff", C.c_double), ("tsamp", C.c_double), ("tdms", C.c_int),
+                ("dm_low", C.c_float), ("dm_step", C.c_float), ("chunk", C.c_int),
+                ("threshold", C.c_float), ("bin_pow2", C.c_int), ("event_capacity", C.c_longlong),
+                ("bp_text", C.c_char_p), ("cr", C.c_float), ("sr", C.c_float),
+                ("history", C.c_int), ("zero_dming", C.c_int), ("rms_from_mean", C.c_int),
+                ("band_matching", C.c_int), ("rfi_active", C.c_int), ("debug_taps", C.c_int)]
+
+
+def beam_config(**kw):
+    d = dict(ntaps=8, window=WINDOWS["kaiser"], int_time=4, int_chan=1, dm_low=0.0, threshold=6.0,
+             bin_pow2=6, event_capacity=0, cr=10.0, sr=4.0, history=10, zero_dming=0,
+             rms_from_mean=1, band_matching=1, rfi_active=1, debug_taps=0)
+    d.update(kw)
+    if isinstance(d.get("window"), str):
+        d["window"] = WINDOWS[d["window"]]
+    bp = d.pop("bp_text", None)
+    cfg = BeamConfig(**d)
+    cfg._bp = bp.encode() if isinstance(bp, str) else bp
+    cfg.bp_text = cfg._bp
+    return cfg
+
+
+class Beam:
+    """One beam's device-resident chain (PPF..analyser) through the C ABI."""
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        check(load().pv_beam_create(C.byref(self.h), C.byref(cfg)))
+
+    def info(self):
+        out = (C.c_longlong * 8)()
+        check(load().pv_beam_info(self.h, out))
+        keys = ["nbins", "max_shift", "lag", "ring_len", "inverted", "chunks", "window", "ring_bytes"]
+        return dict(zip(keys, list(out)))
+
+    def input_bytes(self, int16=True):
+        return load().pv_beam_input_bytes(self.h, int(int16))
+
+    def process(self, d_voltages, stream=None):
+        import torch
+        int16 = d_voltages.dtype == torch.int16
+        check(load().pv_beam_process(self.h, _ptr(d_voltages), int(int16), _stream(stream)))
+
+    def process_host(self, h_voltages, stream=None):
+        """h_voltages: numpy int16 [sub][2][n][2] or complex64 (pinned torch tensor also works)."""
+        if hasattr(h_voltages, "data_ptr"):
+            import torch
+            ptr, int16 = h_voltages.data_ptr(), h_voltages.dtype == torch.int16
+        else:
+            ptr, int16 = h_voltages.ctypes.data, h_voltages.dtype == np.int16
+        check(load().pv_beam_process_host(self.h, C.c_void_p(ptr), int(int16), _stream(stream)))
+
+    def events(self, cap=1 << 20, stream=None):
+        n, first = C.c_longlong(), C.c_longlong()
+        check(load().pv_beam_events(self.h, None, 0, C.byref(n), C.byref(first), _stream(stream)))
+        k = min(n.value, cap)
+        ev = np.zeros(k, EVENT_DTYPE)
+        if k:
+            check(load().pv_beam_events(self.h, C.c_void_p(ev.ctypes.data), k, C.byref(n),
+                                        C.byref(first), _stream(stream)))
+        return ev, n.value, first.value
+
+    def buffers(self):
+        p = [C.c_void_p() for _ in range(4)]
+        check(load().pv_beam_buffers(self.h, *[C.byref(x) for x in p]))
+        return [x.value for x in p]
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_beam_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def device_array(ptr, shape, device=None):
+    """A float32 torch copy of library-owned device memory."""
+    import torch
+    t = torch.empty(shape, dtype=torch.float32, device=device or "cuda")
+    check(load().pv_device_copy(_ptr(t), C.c_void_p(ptr), t.numel() * 4, _stream(None)))
+    return t

@@ -82,3 +82,48 @@ def stokes_filterbank(rng, nt, nsub, nchan, level=1000.0, dof=8, rfi_channels=0.
     bursts = rng.random(nt) < burst_rate
     x[bursts] *= 1.5
     return x.astype(np.float32).reshape(nt, nsub, 1, nchan)
+
+
+def inject_dispersed_pulse(vc, sub_freq0, sub_bw, tsamp_raw, dm, t0, width, snr_scale, rng,
+                           f_ref=None):
+    """Adds a dispersed broadband burst to complex voltages vc [sub][pol][n]
+    (in place, complex64).  The burst is complex Gaussian noise under a
+    Gaussian envelope of FWHM `width` seconds centred at t0 (seconds, at
+    f_ref); each subband is dispersed coherently by applying the group delay
+    k*DM*(f^-2 - f_ref^-2) per frequency (k = 4148.741601) in the Fourier
+    domain.  snr_scale is the burst's voltage variance relative to the noise
+    at the envelope peak."""
+    nsub, npol, n = vc.shape
+    sigma_env = width / 2.3548
+    if f_ref is None:
+        f_ref = sub_freq0 + (nsub - 0.5) * sub_bw  # top of the band
+    k_dm = 4148.741601
+    noise_var = float(np.mean(np.abs(vc[:, :, : min(n, 4096)]) ** 2)) / 2.0
+    for s in range(nsub):
+        fc = sub_freq0 + s * sub_bw
+        f_lo, f_hi = fc - sub_bw / 2, fc + sub_bw / 2
+        d_lo = k_dm * dm * (1 / f_lo ** 2 - 1 / f_ref ** 2)
+        d_hi = k_dm * dm * (1 / f_hi ** 2 - 1 / f_ref ** 2)
+        a = t0 + min(d_lo, d_hi) - 6 * sigma_env
+        b = t0 + max(d_lo, d_hi) + 6 * sigma_env
+        i0, i1 = int(a / tsamp_raw), int(np.ceil(b / tsamp_raw))
+        if i1 <= 0 or i0 >= n:
+            continue
+        L = 1 << int(np.ceil(np.log2(max(i1 - i0, 16) * 2)))
+        start = i0 - L // 4
+        t = (start + np.arange(L)) * tsamp_raw
+        env = np.exp(-0.5 * ((t - t0) / sigma_env) ** 2)
+        nu = np.fft.fftfreq(L, d=tsamp_raw) / 1e6  # MHz, baseband
+        order = np.argsort(nu)
+        f = fc + nu[order]
+        delay = k_dm * dm * (1 / f ** 2 - 1 / f_ref ** 2)  # seconds
+        # phase whose frequency derivative gives the group delay
+        dnu = (nu[1] - nu[0]) * 1e6
+        phase = np.empty(L)
+        phase[order] = -2 * np.pi * np.cumsum(delay) * dnu
+        for p in range(npol):
+            burst = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * np.sqrt(snr_scale * noise_var) * env
+            disp = np.fft.ifft(np.fft.fft(burst) * np.exp(1j * phase))
+            lo, hi = max(start, 0), min(start + L, n)
+            vc[s, p, lo:hi] += disp[lo - start:hi - start].astype(np.complex64)
+    return vc
