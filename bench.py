@@ -1,25 +1,29 @@
 #!/usr/bin/env python3
 """Throughput benchmark of the beam-processing hot path on GB300.
 
-Metric: DM-trial*channel*samples per second (the brute-force dedispersion
-work tdms*nchan*nout of every chunk processed), whole job.
+Metric: DM-trial*channel*samples per second: the brute-force dedispersion
+work (trials x channels x output samples) of every chunk that passes through
+the whole chain, divided by wall time on the device.
 
-Workload "fullband" (default): one beam of 244 LOFAR subbands from 110 MHz
-at 16 channels per subband (3904 channels), 327.68 us samples after x4
-integration, 16384 output samples per chunk, 2048 DM trials over 0-500
-pc/cm^3.  Per step (one chunk): the chunk's RFI-normalised filterbank is
-written into the device-resident per-channel ring, dedispersed over every
-trial and searched by the analyser.  The ring (3904 x 284,873 samples,
-4.45 GB) stays resident, so inputs are larger than L2 and no flush is
-needed.
+Workload "fullband-244sub" (default): one beam of 244 LOFAR subbands of
+195.3125 kHz from 110 MHz, dual-polarisation complex int16 voltages at 5.12 us
+(seeded Gaussian noise, sigma 16 per component, plus persistent narrowband
+sinusoids in 3% of the channels and broadband bursts about once per 10^4
+samples).  Per step (one chunk): 16-channel 8-tap Kaiser PPF per subband
+(3904 channels), Stokes I, x4 integration to 327.68 us, RFI_Clipper (5 sigma
+channel clip), the per-channel delay ring, brute-force dedispersion of 16384
+samples over 2048 trials of DM 0-500 pc/cm^3, and the 6-sigma analyser.  The
+voltages of one chunk (2.05 GB) and the ring (4.6 GB) exceed L2, so no flush
+is needed between steps.
 
-Modes: default ``--impl pv`` runs the library; ``--impl reference`` times the
-reference algorithm's CPU restatement (the reference itself cannot be built:
-it needs Qt4, Boost, FFTW3 and the pelican core) on the host cores.
+``--impl reference`` times the reference algorithm's CPU restatement (the
+reference cannot be built: it needs Qt4, Boost, FFTW3 and the pelican core) on
+the host cores: the oracle's OpenMP channeliser, Stokes, integrator and RFI
+clipper on the same chunk shape and its OpenMP brute-force dedispersion of the
+same formula, on a bounded sample extrapolated to one chunk.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -34,20 +38,27 @@ for p in (ROOT, PKG):
 
 import numpy as np
 
-K_DISP = 4148.741601
+SUB_BW = 0.1953125  # MHz
+RAW_TSAMP = 5.12e-6  # s
 
 
 def fullband_config():
-    nsub, nchan_sub = 244, 16
-    fch1_low = 110.0
-    sub_bw = 0.1953125
-    foff = sub_bw / nchan_sub
-    nchan = nsub * nchan_sub
-    tsamp = 5.12e-6 * nchan_sub * 4
-    tdms, dm_lo, dm_hi = 2048, 0.0, 500.0
-    return dict(workload="fullband-244sub-3904ch-2048dm", nsub=nsub, nchan_sub=nchan_sub,
-                nchan=nchan, fch1=fch1_low, foff=foff, tsamp=tsamp, tdms=tdms, dm_low=dm_lo,
-                dm_step=(dm_hi - dm_lo) / (tdms - 1), nout=16384, threshold=6.0, bin_pow2=6)
+    nsub, nchan_sub, int_time = 244, 16, 4
+    foff = SUB_BW / nchan_sub
+    f_sub0 = 110.0
+    tdms = 2048
+    return dict(workload="fullband-244sub-3904ch-2048dm-16384samp", nsub=nsub, nchan_sub=nchan_sub,
+                int_time=int_time, f_sub0=f_sub0, fch1=f_sub0 - (nchan_sub // 2) * foff, foff=foff,
+                tsamp=RAW_TSAMP * nchan_sub * int_time, tdms=tdms, dm_low=0.0,
+                dm_step=500.0 / (tdms - 1), chunk=16384, threshold=6.0, bin_pow2=6, cr=5.0, sr=4.0,
+                history=10000, window="kaiser")
+
+
+def bp_text(cfg, median=1000.0):
+    nbins = cfg["nsub"] * cfg["nchan_sub"]
+    start, width = cfg["fch1"], cfg["foff"]
+    return "\n".join(["# flat bandpass", str(nbins), repr(start), repr(start + width * nbins),
+                      repr(width), "50.0", repr(median)]) + "\n"
 
 
 def measured_peaks():
@@ -59,7 +70,7 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi samples taken during the timed region."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -88,8 +99,14 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-        sms = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sms = [num(s[1]) for s in self.samples if len(s) > 2 and num(s[1]) is not None]
+        mx = [num(s[2]) for s in self.samples if len(s) > 2 and num(s[2]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
         for s in self.samples:
@@ -102,89 +119,37 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# library arm
+# synthetic voltages
 # ---------------------------------------------------------------------------
 
-class FullbandBeam:
-    """One beam: resident ring, dedispersion plan, analyser buffers."""
+def device_voltages(cfg, dev, seed):
+    """int16 [sub][pol][n][2] on the device: noise, narrowband RFI, bursts."""
+    import torch
+    nsub, n = cfg["nsub"], cfg["chunk"] * cfg["int_time"] * cfg["nchan_sub"]
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    v = torch.randn((nsub, 2, n, 2), generator=g, device=dev, dtype=torch.float32) * 16.0
+    # persistent narrowband sinusoids in 3% of the channels at 20 sigma
+    nbins = nsub * cfg["nchan_sub"]
+    rng = np.random.default_rng(seed)
+    chans = rng.choice(nbins, size=max(1, int(0.03 * nbins)), replace=False)
+    t = torch.arange(n, device=dev, dtype=torch.float64)
+    for ch in chans:
+        s, c = divmod(int(ch), cfg["nchan_sub"])
+        f = (c - cfg["nchan_sub"] // 2) / cfg["nchan_sub"]  # cycles per sample within the subband
+        ph = 2 * np.pi * f * t + rng.uniform(0, 2 * np.pi)
+        v[s, :, :, 0] += (20 * 16.0 * torch.cos(ph)).float()
+        v[s, :, :, 1] += (20 * 16.0 * torch.sin(ph)).float()
+    # broadband bursts: 1 per 10^4 samples, 16 samples long, 3x the noise
+    nb = max(1, n // 10000)
+    for b0 in rng.integers(0, n - 16, size=nb):
+        v[:, :, int(b0):int(b0) + 16, :] *= 3.0
+    return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
 
-    def __init__(self, cfg, dev, seed):
-        import ctypes as C
-        import torch
-        import pv
-        self.cfg, self.dev, self.pv = cfg, dev, pv
-        L = pv.load()
-        self.L = L
-        k, inv = pv.dm_shifts(cfg["fch1"], cfg["foff"], cfg["nchan"])
-        self.inverted = inv
-        self.start = float(np.float32(cfg["dm_low"]) / np.float32(cfg["tsamp"]))
-        self.step_v = float(np.float32(cfg["dm_step"]) / np.float32(cfg["tsamp"]))
-        self.plan = C.c_void_p()
-        pv.check(L.pv_dedisp_plan_create(C.byref(self.plan), k.ctypes.data_as(C.POINTER(C.c_float)),
-                                         cfg["nchan"], cfg["tdms"], self.start, self.step_v))
-        L.pv_dedisp_plan_max_shift.restype = C.c_int
-        L.pv_dedisp_plan_max_shift.argtypes = [C.c_void_p]
-        L.pv_dedisp_plan_run.restype = C.c_int
-        L.pv_dedisp_plan_run.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
-                                         C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong,
-                                         C.c_int, C.c_void_p]
-        L.pv_ring_write.restype = C.c_int
-        L.pv_ring_write.argtypes = [C.c_void_p, C.c_longlong, C.c_longlong, C.c_longlong, C.c_void_p,
-                                    C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
-        self.max_shift = L.pv_dedisp_plan_max_shift(self.plan)
-        nout, nchan = cfg["nout"], cfg["nchan"]
-        self.ring_len = self.max_shift + nout
-        self.row_stride = (self.ring_len + 31) // 32 * 32
-        g = torch.Generator(device=dev)
-        g.manual_seed(seed)
-        self.ring = torch.randn((nchan, self.row_stride), generator=g, device=dev, dtype=torch.float32)
-        self.out = torch.empty((cfg["tdms"], nout), device=dev, dtype=torch.float32)
-        self.chunk_dev = torch.empty((nout, cfg["nsub"], 1, cfg["nchan_sub"]), device=dev,
-                                     dtype=torch.float32)
-        host = torch.randn((nout, cfg["nsub"], 1, cfg["nchan_sub"]), generator=torch.Generator().manual_seed(seed),
-                           dtype=torch.float32)
-        self.chunk_host = host.pin_memory()
-        self.chunk_dev.copy_(self.chunk_host)
-        self.cap = 1 << 20
-        self.events = torch.empty(self.cap * 4, dtype=torch.int32, device=dev)
-        self.pos = self.max_shift  # logical position of the next new sample
-        self.rms = float(np.sqrt(np.float32(cfg["nchan_sub"]) * np.float32(cfg["nsub"])))
-        self.n_events = 0
 
-    def units_per_step(self):
-        c = self.cfg
-        return c["tdms"] * c["nchan"] * c["nout"]
-
-    def step(self, stream, ev_pair=None, e2e=False):
-        import ctypes as C
-        import torch
-        pv, L, c = self.pv, self.L, self.cfg
-        s = C.c_void_p(stream.cuda_stream)
-        if e2e:
-            with torch.cuda.stream(stream):
-                self.chunk_dev.copy_(self.chunk_host, non_blocking=True)
-        pv.check(L.pv_ring_write(C.c_void_p(self.ring.data_ptr()), self.row_stride, self.ring_len,
-                                 self.pos, C.c_void_p(self.chunk_dev.data_ptr()), c["nout"], c["nsub"],
-                                 1, c["nchan_sub"], int(self.inverted), s))
-        t_base = (self.pos + c["nout"] - self.ring_len) % self.ring_len
-        if ev_pair is not None:
-            ev_pair[0].record(stream)
-        pv.check(L.pv_dedisp_plan_run(self.plan, C.c_void_p(self.out.data_ptr()), c["nout"],
-                                      C.c_void_p(self.ring.data_ptr()), self.row_stride, 0,
-                                      self.ring_len, t_base, c["nout"], s))
-        if ev_pair is not None:
-            ev_pair[1].record(stream)
-        n = C.c_longlong()
-        pv.check(L.pv_analyse(C.c_void_p(self.out.data_ptr()), c["nout"], c["tdms"], c["nout"],
-                              c["threshold"], self.rms, c["bin_pow2"], C.c_void_p(self.events.data_ptr()),
-                              self.cap, C.byref(n), s))
-        self.n_events = n.value
-        if e2e:
-            k = min(n.value, self.cap)
-            host_ev = self.events[: 4 * k].cpu()
-            self.last_d2h = host_ev.numel() * 4
-        self.pos += c["nout"]
-
+# ---------------------------------------------------------------------------
+# library arm
+# ---------------------------------------------------------------------------
 
 def run_pv(args, cfg):
     import torch
@@ -198,42 +163,68 @@ def run_pv(args, cfg):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    beam = FullbandBeam(cfg, dev, seed=1234 + rank)
+    bcfg = pv.beam_config(nsub=cfg["nsub"], nchan_sub=cfg["nchan_sub"], window=cfg["window"],
+                          int_time=cfg["int_time"], fch1=cfg["fch1"], foff=cfg["foff"],
+                          tsamp=cfg["tsamp"], tdms=cfg["tdms"], dm_low=cfg["dm_low"],
+                          dm_step=cfg["dm_step"], chunk=cfg["chunk"], threshold=cfg["threshold"],
+                          bin_pow2=cfg["bin_pow2"], bp_text=bp_text(cfg), cr=cfg["cr"],
+                          sr=cfg["sr"], history=cfg["history"], timing=1)
+    beam = pv.Beam(bcfg)
+    info = beam.info()
     stream = torch.cuda.Stream(device=dev)
+    volts = [device_voltages(cfg, dev, 1000 + 7 * rank + i) for i in range(2)]
+    host = volts[0].cpu().pin_memory()
+
+    def step(i, e2e=False):
+        if e2e:
+            beam.process_host(host, stream=stream)
+        else:
+            beam.process(volts[i % 2], stream=stream)
+        ev, n, first = beam.events(cap=1 << 16, stream=stream)
+        return ev, n
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
 
-    # device-resident inputs
-    for _ in range(args.warmup):
-        beam.step(stream)
+    # prime the delay ring (lag chunks) so that every timed chunk dedisperses
+    for i in range(info["lag"]):
+        step(i)
+    for i in range(args.warmup):
+        step(i)
     barrier()
     launches0 = pv.launches()
-    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    t_start, t_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lat_ms, stage = [], []
     clocks = ClockSampler(local)
     clocks.start()
+    t_start, t_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
     for i in range(args.steps):
-        beam.step(stream, kev[i])
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        ev, n = step(i)
+        c1.record(stream)
+        c1.synchronize()
+        lat_ms.append(c0.elapsed_time(c1))
+        stage.append(beam.stage_ms())
     t_stop.record(stream)
     barrier()
     clk = clocks.stop()
     launches = pv.launches() - launches0
     ms = t_start.elapsed_time(t_stop)
-    kernel_ms = [a.elapsed_time(b) for a, b in kev]
+    n_events = n
 
-    # end to end through host buffers
-    for _ in range(max(1, args.warmup // 2)):
-        beam.step(stream, e2e=True)
+    # end to end: host voltages in pinned memory, events back to the host
+    for i in range(max(1, args.warmup)):
+        step(i, e2e=True)
     barrier()
     e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_start.record(stream)
-    for _ in range(args.steps):
-        beam.step(stream, e2e=True)
+    d2h = 0
+    for i in range(args.steps):
+        ev, n = step(i, e2e=True)
+        d2h = 8 + ev.nbytes
     e_stop.record(stream)
     barrier()
     e2e_ms = e_start.elapsed_time(e_stop)
@@ -242,72 +233,125 @@ def run_pv(args, cfg):
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms, e2e_ms = float(t[0]), float(t[1])
-    units = beam.units_per_step() * args.steps * world
-    value = units / (ms / 1e3)
-    e2e_value = units / (e2e_ms / 1e3)
+    nbins = info["nbins"]
+    units_step = cfg["tdms"] * nbins * cfg["chunk"]
+    value = units_step * args.steps * world / (ms / 1e3)
+    e2e_value = units_step * args.steps * world / (e2e_ms / 1e3)
 
     peaks, peak_src = measured_peaks()
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
     fadd_peak = nsm * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
-    k_avg = float(np.mean(kernel_ms)) / 1e3
-    achieved = beam.units_per_step() / k_avg
+    st = {k: float(np.mean([s[k] for s in stage])) for k in stage[0]}
+    dd_s = st["dedisperse"] / 1e3
+    achieved = units_step / dd_s
+    in_bytes = beam.input_bytes(True)
+    fb_bytes = cfg["chunk"] * nbins * 4
+    chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
     roofline = {"kernel": "dedisperse_kernel", "bound": "fp32",
                 "achieved": achieved / 1e12, "peak": fadd_peak / 1e12, "unit": "Tadd/s",
                 "frac": achieved / fadd_peak, "traffic": None,
                 "peak_source": "%d SMs x 128 FP32 lanes x sm_max_mhz of MEASURED_PEAKS.json (%s)"
                                % (nsm, peak_src),
-                "kernel_ms": k_avg * 1e3,
-                "note": "one FP32 add per DM-trial*channel*sample; shared-memory reads cap the "
-                        "FP32-storage kernel at 1/4 of this peak"}
-    cpu = cpu_baseline(cfg, args, repeats=3) if (rank == 0 and not args.no_cpu) else None
-    h2d = beam.chunk_host.numel() * 4
+                "per_unit": "one FP32 add per DM-trial*channel*sample (%d per launch)" % units_step,
+                "kernel_ms": st["dedisperse"]}
+    roofline_chan = {"kernel": "channelise_kernel", "bound": "hbm", "achieved": chan_gbs,
+                     "peak": float(peaks.get("hbm_gbs", 6800.0)), "unit": "GB/s",
+                     "frac": chan_gbs / float(peaks.get("hbm_gbs", 6800.0)),
+                     "per_unit": "int16 voltages in (%d B) + float filterbank out (%d B) per chunk"
+                                 % (in_bytes, fb_bytes),
+                     "kernel_ms": st["channelise"], "peak_source": peak_src}
+    chunk_seconds = cfg["chunk"] * cfg["tsamp"]
+    cpu = cpu_baseline(cfg, args) if (rank == 0 and not args.no_cpu) else None
     line = {"metric": "DM-trial*chan*samples/s", "value": value, "unit": "DM-trial*chan*samples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian filterbank)",
-            "config": {"workload": cfg["workload"], "stage": "ring write + dedisperse + analyse",
-                       "nchan": cfg["nchan"], "tdms": cfg["tdms"], "nout": cfg["nout"],
-                       "ring_samples": beam.ring_len, "l2": "inputs larger than L2 (4.45 GB ring)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded Gaussian int16 voltages with narrowband and burst RFI",
+            "config": {"workload": cfg["workload"], "nsub": cfg["nsub"], "nchan": nbins,
+                       "tdms": cfg["tdms"], "dm_range": [0.0, 500.0], "chunk": cfg["chunk"],
+                       "tsamp_s": cfg["tsamp"], "ring_samples": info["ring_len"],
+                       "l2": "inputs larger than L2 (2.05 GB voltages per chunk, 4.6 GB ring)",
+                       "parallelism": "replicas" if world > 1 else "single beam"},
             "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": getattr(beam, "last_d2h", 0)},
-            "gpu_launches": launches, "clocks": clk, "roofline": roofline, "cpu_baseline": cpu}
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline,
+            "roofline_channeliser": roofline_chan,
+            "stage_ms": st,
+            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                           "p99": float(np.percentile(lat_ms, 99)),
+                           "chunk_duration": chunk_seconds * 1e3},
+            "events_last_chunk": n_events,
+            "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
 
 
-_CPU_BUF = {}
+# ---------------------------------------------------------------------------
+# CPU restatement (baseline / reference arm)
+# ---------------------------------------------------------------------------
+
+class CpuChain:
+    """The oracle's chain on a bounded sample of one chunk: an eighth of the
+    subbands through PPF/Stokes/integration (x8), the full-band RFI clipper on
+    one chunk of filterbank, and an eighth of the trials dedispersed over every
+    channel and the whole chunk (x8)."""
+
+    def __init__(self, cfg, sub_frac=8, trial_frac=8):
+        from oracle import pyoracle as po
+        po.build()
+        self.po, self.cfg = po, cfg
+        nsub, nch, it = cfg["nsub"], cfg["nchan_sub"], cfg["int_time"]
+        self.ns = max(1, nsub // sub_frac)
+        self.sub_scale = nsub / self.ns
+        self.nt = max(1, cfg["tdms"] // trial_frac)
+        self.trial_scale = cfg["tdms"] / self.nt
+        rng = np.random.default_rng(3)
+        n = cfg["chunk"] * it * nch
+        self.volt = (rng.standard_normal((self.ns, 2, n), dtype=np.float32) * 16 +
+                     1j * rng.standard_normal((self.ns, 2, n), dtype=np.float32) * 16).astype(np.complex64)
+        coeffs = po.fir_coefficients(8, nch, cfg["window"]).astype(np.float32)
+        self.ppf = po.PPF(nch, 8, coeffs)
+        self.fb = rng.gamma(8.0, 125.0, size=(cfg["chunk"], nsub, 1, nch)).astype(np.float32)
+        nbins = nsub * nch
+        self.k, _ = po.dm_shifts(cfg["fch1"], cfg["foff"], nbins)
+        self.start = np.float32(cfg["dm_low"]) / np.float32(cfg["tsamp"])
+        self.step = np.float32(cfg["dm_step"]) / np.float32(cfg["tsamp"])
+        ms = int(po.shift_table(self.k, self.nt, self.start, self.step).max())
+        self.buf = rng.standard_normal((nbins, cfg["chunk"] + ms + 1), dtype=np.float32)
+        self.rms = float(np.sqrt(np.float32(nch) * np.float32(nsub)))
+        self.sample = ("%d of %d subbands through PPF/Stokes/x%d integration (x%.0f), RFI on the "
+                       "full %d-channel chunk, %d of %d trials dedispersed and analysed over all "
+                       "channels and %d samples (x%.0f)"
+                       % (self.ns, nsub, it, self.sub_scale, nbins, self.nt, cfg["tdms"], cfg["chunk"],
+                          self.trial_scale))
+
+    def chunk_seconds(self):
+        po, cfg = self.po, self.cfg
+        t0 = time.perf_counter()
+        spec = self.ppf.run(self.volt.reshape(self.ns, 2, -1, cfg["nchan_sub"]))
+        st = po.integrate(po.stokes(spec, 1), cfg["int_time"], 1)
+        t1 = time.perf_counter()
+        r = po.RFI(bp_text(cfg), cr=cfg["cr"], sr=cfg["sr"], history=cfg["history"], mode=0)
+        fb = self.fb.copy()
+        t2 = time.perf_counter()
+        r.run(fb)
+        t3 = time.perf_counter()
+        out = po.dedisperse(self.buf, cfg["chunk"], self.nt, self.k, self.start, self.step)
+        po.analyse(out, cfg["threshold"], self.rms, cfg["bin_pow2"])
+        t4 = time.perf_counter()
+        del st
+        return (t1 - t0) * self.sub_scale + (t3 - t2) + (t4 - t3) * self.trial_scale
 
 
-def cpu_baseline(cfg, args, sample_trials=None, repeats=1):
-    """The oracle's OpenMP dedispersion of the same formula (every core) on a
-    bounded sample: the lowest trials over the full channel set and chunk."""
-    from oracle import pyoracle as po
-    po.build()
-    k, _ = po.dm_shifts(cfg["fch1"], cfg["foff"], cfg["nchan"])
-    start = np.float32(cfg["dm_low"]) / np.float32(cfg["tsamp"])
-    step = np.float32(cfg["dm_step"]) / np.float32(cfg["tsamp"])
-    tdms = cfg["tdms"]
-    nt = min(sample_trials or args.cpu_trials, tdms)
-    nout = cfg["nout"]
-    key = (cfg["nchan"], nout, nt)
-    if key not in _CPU_BUF:
-        ms = int(po.shift_table(k, nt, start, step).max())
-        rng = np.random.default_rng(5)
-        _CPU_BUF.clear()
-        _CPU_BUF[key] = rng.random((cfg["nchan"], nout + ms + 1), dtype=np.float32)
-    buf = _CPU_BUF[key]
-    t0 = time.perf_counter()
-    for _ in range(repeats):
-        po.dedisperse(buf, nout, nt, k, start, step)
-    dt = time.perf_counter() - t0
-    units = nt * cfg["nchan"] * nout * repeats
-    return {"value": units / dt, "unit": "DM-trial*chan*samples/s", "cores": po.num_threads(),
-            "kind": "port",
-            "sample": "%d x (%d of %d trials x %d channels x %d samples), %.1f s"
-                      % (repeats, nt, tdms, cfg["nchan"], nout, dt)}
+def cpu_baseline(cfg, args, repeats=1):
+    chain = CpuChain(cfg)
+    secs = [chain.chunk_seconds() for _ in range(repeats)]
+    units = cfg["tdms"] * cfg["nsub"] * cfg["nchan_sub"] * cfg["chunk"]
+    return {"value": units / float(np.median(secs)), "unit": "DM-trial*chan*samples/s",
+            "cores": chain.po.num_threads(), "kind": "port",
+            "sample": chain.sample + "; %.1f s per chunk extrapolated" % float(np.median(secs))}
 
 
 def run_reference(args, cfg):
@@ -315,30 +359,26 @@ def run_reference(args, cfg):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    vals = []
+    chain = CpuChain(cfg)
     for _ in range(args.warmup):
-        cpu_baseline(cfg, args, sample_trials=args.ref_trials)
-    t_all = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(cfg, args, sample_trials=args.ref_trials))
-    total = time.perf_counter() - t_all
-    value = float(np.mean([v["value"] for v in vals]))
-    units_per_step = cfg["tdms"] * cfg["nchan"] * cfg["nout"]
+        chain.chunk_seconds()
+    secs = [chain.chunk_seconds() for _ in range(args.steps)]
+    units = cfg["tdms"] * cfg["nsub"] * cfg["nchan_sub"] * cfg["chunk"]
+    value = units * len(secs) / float(np.sum(secs))
     line = {"impl": "reference", "metric": "DM-trial*chan*samples/s", "value": value,
             "unit": "DM-trial*chan*samples/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": units_per_step / value * 1e3,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Gaussian filterbank)",
-            "config": {"workload": cfg["workload"], "nchan": cfg["nchan"], "tdms": cfg["tdms"],
-                       "nout": cfg["nout"]},
+            "data": "synthetic: seeded Gaussian voltages and filterbank",
+            "config": {"workload": cfg["workload"], "nchan": cfg["nsub"] * cfg["nchan_sub"],
+                       "tdms": cfg["tdms"], "chunk": cfg["chunk"]},
             "cpu_baseline": {"value": value, "unit": "DM-trial*chan*samples/s",
-                             "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"] + " per step; the reference needs Qt4, "
-                                       "Boost, FFTW3 and pelican, so its algorithm's CPU "
-                                       "restatement is timed"},
+                             "cores": chain.po.num_threads(), "kind": "port",
+                             "sample": chain.sample + " per step; the reference needs Qt4, Boost, "
+                                       "FFTW3 and pelican, so its algorithm's CPU restatement is "
+                                       "timed"},
             "e2e": {"value": value, "unit": "DM-trial*chan*samples/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-            "wall_s": total}
+                    "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
@@ -348,17 +388,18 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pv", choices=["pv", "reference"])
-    ap.add_argument("--cpu-trials", type=int, default=512)
-    ap.add_argument("--ref-trials", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--tdms", type=int, default=None, help="override (profiling a smaller case)")
-    ap.add_argument("--nout", type=int, default=None, help="override (profiling a smaller case)")
+    ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
+    ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
+    ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
     args = ap.parse_args()
     cfg = fullband_config()
-    if args.tdms or args.nout:
-        tdms = args.tdms or cfg["tdms"]
-        cfg.update(tdms=tdms, nout=args.nout or cfg["nout"],
-                   dm_step=cfg["dm_step"], workload=cfg["workload"] + "-reduced")
+    if args.tdms or args.chunk or args.nsub:
+        if args.tdms:
+            cfg["tdms"] = args.tdms
+        cfg["chunk"] = args.chunk or cfg["chunk"]
+        cfg["nsub"] = args.nsub or cfg["nsub"]
+        cfg["workload"] += "-reduced(tdms=%d,chunk=%d,nsub=%d)" % (cfg["tdms"], cfg["chunk"], cfg["nsub"])
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

@@ -243,6 +243,7 @@ typedef struct {
     int history;              /* History@maximum */
     int zero_dming, rms_from_mean, band_matching, rfi_active;
     int debug_taps;           /* keep the pre-RFI filterbank of the last chunk */
+    int timing;               /* record CUDA events at the stage boundaries */
 } pv_beam_config;
 
 typedef struct pv_beam pv_beam;
@@ -263,6 +264,9 @@ int pv_beam_events(pv_beam* beam, pv_event* h_events, long long cap, long long* 
 /* [dedispersion channels, max delay, lag in chunks, ring samples, inverted,
  *  chunks processed, last window, ring bytes] */
 int pv_beam_info(const pv_beam* beam, long long* h_info8);
+/* Device time (ms) of the last dedispersed chunk's stages: channelise, RFI,
+ * ring write, dedisperse, analyse (needs timing = 1; synchronises). */
+int pv_beam_stage_ms(pv_beam* beam, float* h_ms5);
 /* Device views of the last chunk's filterbank (after RFI), its pre-RFI copy
  * (debug_taps), the dedispersed window [tdms][chunk] and the ring. */
 int pv_beam_buffers(const pv_beam* beam, float** d_filterbank, float** d_filterbank_raw,

@@ -399,10 +399,13 @@ extern "C" int or_ppf_run(or_ppf* p, const float* in, int nsub, int npol, int nb
         p->work.assign((size_t)nsub * npol, std::vector<float>((size_t)2 * N * T, 0.0f));
         p->oldest.assign((size_t)nsub * npol, 0);
     }
-    std::vector<float> y(2 * N);
-    std::vector<double> re(N), im(N);
-    for (int s = 0; s < nsub; ++s)
-        for (int q = 0; q < npol; ++q) {
+    // Subband/polarisation streams are independent (PPFChanneliser.cpp:139-183
+    // splits subbands over OpenMP threads).
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int sq = 0; sq < nsub * npol; ++sq) {
+        const int s = sq / npol, q = sq % npol;
+        std::vector<float> y(2 * N);
+        std::vector<double> re(N), im(N);
             std::vector<float>& wb = p->work[s * npol + q];
             int& old = p->oldest[s * npol + q];
             for (int b = 0; b < nblocks; ++b) {

@@ -42,6 +42,8 @@ struct pv_beam {
     long long chunks = 0;
     long long window = -1;
     float rms = 0.0f;
+    cudaEvent_t ev[6] = {};     // stage boundaries of the last chunk (timing mode)
+    bool timed = false;
 };
 
 namespace {
@@ -54,6 +56,8 @@ void destroy(pv_beam* b) {
                     (void*)b->d_events, b->d_scratch, b->d_in})
         if (p) cudaFree(p);
     if (b->h_total) cudaFreeHost(b->h_total);
+    for (auto e : b->ev)
+        if (e) cudaEventDestroy(e);
     delete b;
 }
 
@@ -111,6 +115,15 @@ extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
         return PV_ERR_NOMEM;
     }
     b->d_total = reinterpret_cast<long long*>(static_cast<char*>(b->d_scratch) + scratch);
+    if (c->timing) {
+        for (auto& ev : b->ev) {
+            if (cudaEventCreate(&ev) != cudaSuccess) {
+                pv::set_error("pv_beam_create: cudaEventCreate failed");
+                destroy(b);
+                return PV_ERR_CUDA;
+            }
+        }
+    }
     *out = b;
     return PV_OK;
 }
@@ -146,7 +159,11 @@ extern "C" int pv_beam_process(pv_beam* b, const void* d_voltages, int in_int16,
     const pv_beam_config& c = b->cfg;
     cudaStream_t s = pv::as_stream(stream);
     const int nblocks = c.chunk * c.int_time;
+    auto mark = [&](int i) {
+        if (c.timing) cudaEventRecord(b->ev[i], s);
+    };
     int nu = 0;
+    mark(0);
     PV_TRY(pv_channelise(b->ppf, d_voltages, in_int16, c.nsub, nblocks, 1, c.int_time, c.int_chan,
                          b->d_fb, &nu, stream));
     if (nu != c.chunk) {
@@ -156,19 +173,39 @@ extern "C" int pv_beam_process(pv_beam* b, const void* d_voltages, int in_int16,
     if (b->d_fb_raw)
         PV_CUDA(cudaMemcpyAsync(b->d_fb_raw, b->d_fb, sizeof(float) * (size_t)c.chunk * b->nbins,
                                 cudaMemcpyDeviceToDevice, s), "copy filterbank tap");
+    mark(1);
     PV_TRY(pv_rfi_run(b->rfi, b->d_fb, c.chunk, c.nsub, 1, b->nchan_fb, nullptr, stream));
+    mark(2);
     PV_TRY(pv::ring_write_device(b->d_ring, b->row_stride, b->ring_len, b->chunks * c.chunk, b->d_fb,
                                  c.chunk, c.nsub, 1, b->nchan_fb, b->inverted, s));
+    mark(3);
     b->chunks += 1;
+    b->timed = false;
     if (b->chunks > b->lag) {
         const long long w = b->chunks - 1 - b->lag;
         PV_TRY(pv_dedisp_plan_run(b->plan, b->d_out, c.chunk, b->d_ring, b->row_stride, 0,
                                   b->ring_len, (w * c.chunk) % b->ring_len, c.chunk, stream));
+        mark(4);
         PV_TRY(pv::analyse_launch(b->d_out, c.chunk, c.tdms, c.chunk, c.threshold, b->rms,
                                   c.bin_pow2, b->d_events, b->cap, b->d_total, b->d_scratch, s));
+        mark(5);
         PV_CUDA(cudaMemcpyAsync(b->h_total, b->d_total, sizeof(long long), cudaMemcpyDeviceToHost, s),
                 "read event count");
         b->window = w;
+        b->timed = c.timing != 0;
+    }
+    return PV_OK;
+}
+
+extern "C" int pv_beam_stage_ms(pv_beam* b, float* h_ms5) {
+    if (!b || !h_ms5) return PV_ERR_ARG;
+    if (!b->timed) {
+        pv::set_error("pv_beam_stage_ms: timing is off or no window was dedispersed yet");
+        return PV_ERR_STATE;
+    }
+    for (int i = 0; i < 5; ++i) {
+        PV_CUDA(cudaEventSynchronize(b->ev[i + 1]), "synchronise stage event");
+        PV_CUDA(cudaEventElapsedTime(&h_ms5[i], b->ev[i], b->ev[i + 1]), "stage time");
     }
     return PV_OK;
 }

@@ -87,6 +87,7 @@ def _declare(L):
         "pv_beam_events": (i, [vp, vp, ll, P(ll), P(ll), vp]),
         "pv_beam_info": (i, [vp, P(ll)]),
         "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
+        "pv_beam_stage_ms": (i, [vp, P(C.c_float)]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
@@ -320,13 +321,14 @@ class BeamConfig(C.Structure):
                 ("threshold", C.c_float), ("bin_pow2", C.c_int), ("event_capacity", C.c_longlong),
                 ("bp_text", C.c_char_p), ("cr", C.c_float), ("sr", C.c_float),
                 ("history", C.c_int), ("zero_dming", C.c_int), ("rms_from_mean", C.c_int),
-                ("band_matching", C.c_int), ("rfi_active", C.c_int), ("debug_taps", C.c_int)]
+                ("band_matching", C.c_int), ("rfi_active", C.c_int), ("debug_taps", C.c_int),
+                ("timing", C.c_int)]
 
 
 def beam_config(**kw):
     d = dict(ntaps=8, window=WINDOWS["kaiser"], int_time=4, int_chan=1, dm_low=0.0, threshold=6.0,
              bin_pow2=6, event_capacity=0, cr=10.0, sr=4.0, history=10, zero_dming=0,
-             rms_from_mean=1, band_matching=1, rfi_active=1, debug_taps=0)
+             rms_from_mean=1, band_matching=1, rfi_active=1, debug_taps=0, timing=0)
     d.update(kw)
     if isinstance(d.get("window"), str):
         d["window"] = WINDOWS[d["window"]]
@@ -377,6 +379,11 @@ class Beam:
             check(load().pv_beam_events(self.h, C.c_void_p(ev.ctypes.data), k, C.byref(n),
                                         C.byref(first), _stream(stream)))
         return ev, n.value, first.value
+
+    def stage_ms(self):
+        out = (C.c_float * 5)()
+        check(load().pv_beam_stage_ms(self.h, out))
+        return dict(zip(["channelise", "rfi", "ring_write", "dedisperse", "analyse"], list(out)))
 
     def buffers(self):
         p = [C.c_void_p() for _ in range(4)]
