@@ -96,6 +96,9 @@ int pv_dedisp_plan_create(pv_dedisp_plan** plan, const float* h_dmshift, int nch
 void pv_dedisp_plan_destroy(pv_dedisp_plan* plan);
 /* Largest integer delay of the plan (samples). */
 int pv_dedisp_plan_max_shift(const pv_dedisp_plan* plan);
+/* PV_OK, or PV_ERR_TIMEOUT if a pipelined launch's bounded wait gave up
+ * (synchronous read of the plan's device status word). */
+int pv_dedisp_plan_status(const pv_dedisp_plan* plan, int* h_status);
 /* Dedisperses nout samples.  Linear mode (ring_len == 0): rows of row_stride
  * floats, samples at or beyond row_len read as 0 (row_len == row_stride reads
  * on into the next row, as the reference's contiguous buffer does).  Ring
@@ -212,6 +215,9 @@ int pv_rfi_run(pv_rfi* rfi, float* d_data, int nt, int nsub, int npol, int nchan
 int pv_rfi_state(pv_rfi* rfi, double* h_out10);
 /* The rebinned bandpass model the first run used (host copy). */
 int pv_rfi_bandpass(pv_rfi* rfi, float* h_out, int nbins);
+/* Threads of the clipper's CTA for a band of nbins channels; also the number
+ * of FP32 partial sums of its channel reductions (256, 512 or 1024). */
+int pv_rfi_parts(int nbins);
 
 /* ------------------------------------------------------------------------
  * One beam's device-resident chain, in the order of DedispersionPipeline::run

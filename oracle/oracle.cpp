@@ -680,30 +680,34 @@ struct CircBuf {
 
 }  // namespace
 
-// Canonical FP64 reduction of the FP64 RFI variant: partial p (0..255) sums
-// x[p], x[p+256], ... in order; each group of 32 partials is reduced by the
-// halving tree (offsets 16, 8, 4, 2, 1) and the 8 group sums by offsets 4, 2, 1.
-static double tree_256(double* part) {
-    double w[8];
-    for (int g = 0; g < 8; ++g) {
+// Canonical reduction of the FP64 RFI variant over P partials (P a multiple
+// of 32): each group of 32 consecutive partials is reduced in double by the
+// halving tree of offsets 16, 8, 4, 2, 1, then the P/32 group sums by offsets
+// P/64, ..., 1.
+static double tree_p(double* part, int P) {
+    const int nw = P / 32;
+    double w[32];
+    for (int g = 0; g < nw; ++g) {
         double* q = part + 32 * g;
         for (int off = 16; off >= 1; off >>= 1)
             for (int l = 0; l < off; ++l) q[l] = q[l] + q[l + off];
         w[g] = q[0];
     }
-    for (int off = 4; off >= 1; off >>= 1)
+    for (int off = nw / 2; off >= 1; off >>= 1)
         for (int l = 0; l < off; ++l) w[l] = w[l] + w[l + off];
     return w[0];
 }
 
-extern "C" double or_sum_canonical(const double* x, int n) {
-    double part[256];
-    for (int p = 0; p < 256; ++p) {
-        double s = 0.0;
-        for (int i = p; i < n; i += 256) s += x[i];
+// Sum of n floats: partial p is the FP32 sum of x[p], x[p+P], ... in order
+// (from +0), widened to double and reduced by tree_p.
+extern "C" double or_sum_canonical(const float* x, int n, int P) {
+    double part[1024];
+    for (int p = 0; p < P; ++p) {
+        float s = 0.0f;
+        for (int i = p; i < n; i += P) s += x[i];
         part[p] = s;
     }
-    return tree_256(part);
+    return tree_p(part, P);
 }
 
 // ===========================================================================
@@ -733,21 +737,24 @@ struct Rfi : RfiBase {
     int bad_spectra = 0, num = 0, remaining_zeros = 0;
     std::vector<float> last_good;
 
-    // Sum of n values of f(i) in the mode's order.
+    int parts = 256;  // FP64 variant: number of FP32 partial sums (the GPU's threads)
+
+    // Sum of the float values f(i), i < n, in the mode's order: one sequential
+    // FP32 sum (reference), or the canonical partials + FP64 tree (variant).
     template <typename F>
     R channel_sum(int n, F f) const {
         if (!kF64) {
             float s = 0.0f;
-            for (int i = 0; i < n; ++i) s += (float)f(i);
+            for (int i = 0; i < n; ++i) s += f(i);
             return (R)s;
         }
-        double part[256];
-        for (int p = 0; p < 256; ++p) {
-            double s = 0.0;
-            for (int i = p; i < n; i += 256) s += (double)f(i);
+        double part[1024];
+        for (int p = 0; p < parts; ++p) {
+            float s = 0.0f;
+            for (int i = p; i < n; i += parts) s += f(i);
             part[p] = s;
         }
-        return (R)tree_256(part);
+        return (R)tree_p(part, parts);
     }
 
     int run(float* I, float* W, int nt, int nsub, int npol, int nchan, uint8_t* flags) override {
@@ -801,14 +808,16 @@ struct Rfi : RfiBase {
                         }
                         bm = s1; bms = s2;
                     } else {
-                        // partial p accumulates bins with bin % 256 == p
-                        double p1[256] = {0}, p2[256] = {0};
+                        // partial p: FP32 sums of the band's bins with bin % parts == p
+                        float f1[1024] = {0}, f2[1024] = {0};
                         for (unsigned bin = b * cpb; bin < (b + 1) * cpb; ++bin) {
-                            double v = at(bin);
-                            p1[bin % 256] += v;
-                            p2[bin % 256] += v * v;
+                            const float v = at(bin);
+                            f1[bin % parts] += v;
+                            f2[bin % parts] += v * v;
                         }
-                        bm = (R)tree_256(p1); bms = (R)tree_256(p2);
+                        double p1[1024], p2[1024];
+                        for (int q = 0; q < parts; ++q) { p1[q] = f1[q]; p2[q] = f2[q]; }
+                        bm = (R)tree_p(p1, parts); bms = (R)tree_p(p2, parts);
                     }
                     dmm[b] = (R)mini_data[b] - (R)mini_model[b];
                     if (!kF64) {
@@ -842,8 +851,8 @@ struct Rfi : RfiBase {
             for (unsigned bin = 0; bin < nbins; ++bin) {
                 float v = at(bin);
                 bool clip;
-                if (!kF64) clip = (float)((float)(v - (float)data_model) - bandpass[bin]) > (float)margin;
-                else clip = ((double)v - (double)data_model) - (double)bandpass[bin] > (double)margin;
+                // per-channel arithmetic is FP32 in both modes (RFI_Clipper.cpp:321)
+                clip = (float)((float)(v - (float)data_model) - bandpass[bin]) > (float)margin;
                 if (clip) {
                     clipped[bin] = 1;
                     unsigned s = bin / nchan, c = bin % nchan;
@@ -855,8 +864,8 @@ struct Rfi : RfiBase {
                     ++good_per_band[bin / cpb];
                 }
             }
-            R spectrum_sum = channel_sum((int)nbins, [&](int bin) -> R {
-                return clipped[bin] ? (R)0 : (R)at(bin);
+            R spectrum_sum = channel_sum((int)nbins, [&](int bin) -> float {
+                return clipped[bin] ? 0.0f : at(bin);
             });
             // Sequential float sum skips clipped channels entirely (adding 0.0f
             // to a float sum is exact, so the result is the same).
@@ -914,8 +923,7 @@ struct Rfi : RfiBase {
             // flatten, :478-494
             for (unsigned bin = 0; bin < nbins; ++bin) {
                 float& v = at(bin);
-                if (!kF64) v -= (float)(bandpass[bin] + (float)data_model);
-                else v = (float)((double)v - ((double)bandpass[bin] + (double)data_model));
+                v -= (float)(bandpass[bin] + (float)data_model);
                 vals[bin] = v;
             }
             R s1, s2;
@@ -924,8 +932,8 @@ struct Rfi : RfiBase {
                 for (unsigned bin = 0; bin < nbins; ++bin) { a += vals[bin]; b += vals[bin] * vals[bin]; }
                 s1 = a; s2 = b;
             } else {
-                s1 = channel_sum((int)nbins, [&](int bin) -> R { return (R)vals[bin]; });
-                s2 = channel_sum((int)nbins, [&](int bin) -> R { return (R)vals[bin] * (R)vals[bin]; });
+                s1 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin]; });
+                s2 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin] * vals[bin]; });
             }
             if (!kF64) {
                 float m = (float)s1 / nbins;
@@ -948,8 +956,9 @@ struct Rfi : RfiBase {
                         else v -= (float)mean_run;
                         v /= (float)spectrum_rms;
                     } else {
-                        double sub = zero_dming == 1 ? (double)spectrum_sum : (double)mean_run;
-                        v = (float)(((double)v - sub) / (double)spectrum_rms);
+                        const float sub = (float)(zero_dming == 1 ? (double)spectrum_sum : (double)mean_run);
+                        v -= sub;
+                        v /= (float)spectrum_rms;
                     }
                     if (v > cr) v = 0.0f;
                 }
@@ -1000,10 +1009,12 @@ struct or_rfi {
 
 extern "C" or_rfi* or_rfi_create(const char* bp_text, float cr_factor, float sr_factor,
                                  int max_history, int zero_dming, int use_mean_over_rms,
-                                 int band_matching, int mode, char* err, int errlen) {
+                                 int band_matching, int mode, int parts, char* err, int errlen) {
+    if (parts != 256 && parts != 512 && parts != 1024) parts = 256;
     RfiBase* impl;
     if (mode == 1) {
         auto* r = new Rfi<double>;
+        r->parts = parts;
         r->cr = cr_factor; r->sr = sr_factor; r->max_history = max_history;
         r->zero_dming = zero_dming; r->use_mor = use_mean_over_rms;
         r->mean_buf.cap = r->rms_buf.cap = (size_t)max_history;

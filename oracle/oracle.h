@@ -105,13 +105,15 @@ int or_integrate(const float* in, int nt, int nsub, int npol, int nchan,
 
 typedef struct or_rfi or_rfi;
 /* bp_text: the .bp file contents.  mode 0 restates the reference's FP32
- * arithmetic with sequential channel sums; mode 1 is the FP64 variant
- * (per-spectrum statistics and running averages in double, channel sums in
- * the canonical 256-way strided order described in or_sum_canonical).
- * Returns NULL and fills err (if given) on a parse error. */
+ * arithmetic with sequential channel sums.  mode 1 is the FP64 variant the
+ * library implements: per-channel arithmetic in the reference's FP32 form,
+ * channel sums as `parts` FP32 partials (partial p takes channels p, p+parts,
+ * ...) reduced by an FP64 tree (or_sum_canonical), and the per-spectrum
+ * statistics and running averages in double.  Returns NULL and fills err
+ * (if given) on a parse error. */
 or_rfi* or_rfi_create(const char* bp_text, float cr_factor, float sr_factor,
                       int max_history, int zero_dming, int use_mean_over_rms,
-                      int band_matching, int mode, char* err, int errlen);
+                      int band_matching, int mode, int parts, char* err, int errlen);
 void or_rfi_destroy(or_rfi*);
 /* In-place on I [t][sub][npol][nchan]; weights (same shape) are set to 1
  * where the reference writes them.  flags (optional, [t][nbins] uint8):
@@ -126,7 +128,7 @@ int or_rfi_bandpass(const or_rfi*, float* out, int nbins);
 
 /* Canonical FP64 reduction used by the FP64 RFI variant: 256 strided
  * sequential partials followed by a halving pairwise tree. */
-double or_sum_canonical(const double* x, int n);
+double or_sum_canonical(const float* x, int n, int parts);
 
 /* BandPass/BinMap checks against the reference's own unit tests. */
 typedef struct or_bandpass or_bandpass;

@@ -60,12 +60,12 @@ def lib():
             "or_ppf_run": (i, [vp, P(C.c_float), i, i, i, P(C.c_float)]),
             "or_stokes": (None, [P(C.c_float), i, i, i, i, P(C.c_float)]),
             "or_integrate": (i, [P(C.c_float), i, i, i, i, i, i, P(C.c_float)]),
-            "or_rfi_create": (vp, [C.c_char_p, f, f, i, i, i, i, i, C.c_char_p, i]),
+            "or_rfi_create": (vp, [C.c_char_p, f, f, i, i, i, i, i, i, C.c_char_p, i]),
             "or_rfi_destroy": (None, [vp]),
             "or_rfi_run": (i, [vp, P(C.c_float), P(C.c_float), i, i, i, i, vp]),
             "or_rfi_state": (None, [vp, P(C.c_double)]),
             "or_rfi_bandpass": (i, [vp, P(C.c_float), i]),
-            "or_sum_canonical": (d, [P(C.c_double), i]),
+            "or_sum_canonical": (d, [P(C.c_float), i, i]),
             "or_bandpass_create": (vp, [i, d, d, P(C.c_float), i]),
             "or_bandpass_destroy": (None, [vp]),
             "or_bandpass_set_rms": (None, [vp, f]),
@@ -211,10 +211,10 @@ class RFI:
     """RFI_Clipper restatement; mode 0 = reference FP32, mode 1 = FP64 variant."""
 
     def __init__(self, bp_text, cr=10.0, sr=4.0, history=10, zero_dming=False,
-                 mean_over_rms=True, band_matching=True, mode=0):
+                 mean_over_rms=True, band_matching=True, mode=0, parts=256):
         err = C.create_string_buffer(512)
         self.h = lib().or_rfi_create(bp_text.encode(), cr, sr, history, int(zero_dming),
-                                     int(mean_over_rms), int(band_matching), mode, err, 512)
+                                     int(mean_over_rms), int(band_matching), mode, parts, err, 512)
         if not self.h:
             raise ValueError(err.value.decode())
 
@@ -280,9 +280,14 @@ class DedispersionModule:
             self.h = None
 
 
-def sum_canonical(x):
-    x = np.ascontiguousarray(x, np.float64)
-    return lib().or_sum_canonical(_f64p(x), len(x))
+def sum_canonical(x, parts=256):
+    x = np.ascontiguousarray(x, np.float32)
+    return lib().or_sum_canonical(_f32p(x), len(x), parts)
+
+
+def rfi_parts(nbins):
+    """Partial-sum count (the GPU clipper's thread count) for a band of nbins."""
+    return 256 if nbins <= 1024 else (512 if nbins <= 4096 else 1024)
 
 
 def num_threads():

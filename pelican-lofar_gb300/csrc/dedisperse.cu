@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 #include "pv_common.cuh"
@@ -155,6 +156,184 @@ dedisperse_kernel(const DedispArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// K4 v2 (ring rows): TMA bulk copies into an mbarrier pipeline.
+//
+// Warp DMS is a producer: for every stage of CS channels it waits until the
+// consumers have released the stage buffer, posts the byte count on the
+// stage's "full" barrier and issues one cp.async.bulk per channel span (two
+// where the span wraps the ring).  Warps 0..DMS-1 are consumers (one trial
+// each): they wait on "full", add 32*R samples per channel from shared
+// memory in channel order and release the buffer on "empty".  Span starts are
+// rounded down to 16 bytes; the rounding offset is folded into the per-channel
+// offset table the producer writes beside the data.  Every wait is bounded by
+// %globaltimer; a wait that gives up records PV_ERR_TIMEOUT in *status.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Waits for the phase of the given parity; gives up after limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t_end = global_ns() + limit_ns;
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() > t_end) return false;
+    }
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
+
+template <int DMS, int R, int CS, int ST>
+__global__ void __launch_bounds__((DMS + 1) * 32, 1)
+dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int TT = 32 * R;
+    float* slots = reinterpret_cast<float*>(smem_raw);
+    int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * a.slot);
+    float* meta_k = reinterpret_cast<float*>(meta_off + ST * CS);
+    // slot is a multiple of 4 floats and 2*ST*CS words follow: 8-byte aligned
+    uint64_t* full = reinterpret_cast<uint64_t*>(meta_k + ST * CS);
+    uint64_t* empty = full + ST;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long t0 = (long long)blockIdx.x * TT;
+    const int d0 = blockIdx.y * DMS;
+    const int d_last = min(d0 + DMS, a.tdms) - 1;
+    const float dv0 = pv_trial_value(d0, a.start, a.step);
+    const float dv_last = pv_trial_value(d_last, a.start, a.step);
+    const int nstages = (a.nchan + CS - 1) / CS;
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < ST; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], DMS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == DMS) {
+        // ---------------- producer ----------------
+        const int valid = (int)min((long long)TT, (long long)a.nout - t0);
+        int issued = 0;
+        bool ok = true;
+        for (int st = 0; st < nstages && ok; ++st) {
+            const int b = st % ST;
+            const unsigned round = (unsigned)(st / ST);
+            if (!mbar_wait(&empty[b], (round & 1u) ^ 1u, kWaitLimitNs)) {
+                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                ok = false;
+                break;
+            }
+            const int c = st * CS + lane;
+            unsigned bytes = 0, piece1 = 0, piece2 = 0;
+            long long g_al = 0;
+            if (lane < CS && c < a.nchan) {
+                const float k = a.dmshift[c];
+                const int s0 = pv_shift(k, dv0);
+                const int span = valid + pv_shift(k, dv_last) - s0;
+                const long long g0 = (a.t_base + t0 + s0) % a.ring_len;
+                g_al = g0 & ~3LL;
+                const int base = (int)(g0 - g_al);
+                const unsigned n = (unsigned)((base + span + 3) & ~3);
+                piece1 = (unsigned)min((long long)n, a.ring_len - g_al);
+                piece2 = n - piece1;
+                bytes = n * 4u;
+                meta_off[b * CS + lane] = s0 - base;
+                meta_k[b * CS + lane] = k;
+                __threadfence_block();
+            }
+            unsigned total = bytes;
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&full[b], total);
+            __syncwarp();
+            if (bytes) {
+                const float* src = a.in + (long long)c * a.row_stride;
+                float* dst = slots + (size_t)(b * CS + lane) * a.slot;
+                bulk_g2s(dst, src + g_al, piece1 * 4u, &full[b]);
+                if (piece2) bulk_g2s(dst + piece1, src, piece2 * 4u, &full[b]);
+            }
+            issued = st + 1;
+        }
+        // On a give-up, wait (bounded) for the copies still in flight before
+        // the CTA's shared memory is released.
+        if (!ok) {
+            for (int st = max(0, issued - ST); st < issued; ++st)
+                mbar_wait(&full[st % ST], (unsigned)(st / ST) & 1u, kWaitLimitNs);
+        }
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    const int d = d0 + warp;
+    const bool active = d <= d_last;
+    const float dv = pv_trial_value(d, a.start, a.step);
+    float acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = 0.0f;
+    bool ok = true;
+    for (int st = 0; st < nstages; ++st) {
+        const int b = st % ST;
+        if (!mbar_wait(&full[b], (unsigned)(st / ST) & 1u, kWaitLimitNs)) {
+            if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+            ok = false;
+            break;
+        }
+        if (active) {
+            const int c_end = min(CS, a.nchan - st * CS);
+            for (int j = 0; j < c_end; ++j) {
+                const float k = meta_k[b * CS + j];
+                const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], a.slot - TT);
+                const float* row = slots + (size_t)(b * CS + j) * a.slot + off + lane;
+#pragma unroll
+                for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);
+    }
+    if (ok && active) {
+        float* o = a.out + (long long)d * a.out_stride;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const long long t = t0 + lane + 32 * r;
+            if (t < a.nout) o[t] = acc[r];
+        }
+    }
+}
+
 // Largest delay spread s(c, d0+DMS-1) - s(c, d0) over channels and DM tiles,
 // evaluated with the kernel's own float arithmetic on the host.
 int delay_spread(const std::vector<float>& dmshift, int tdms, int dms, float start, float step) {
@@ -198,22 +377,53 @@ int launch_dedisperse(DedispArgs a, int spread, cudaStream_t s) {
     return pv::check_launch("dedisperse_kernel");
 }
 
+template <int DMS, int R, int CS, int ST>
+int launch_dedisperse_tma(DedispArgs a, int spread, int* status, cudaStream_t s) {
+    constexpr int TT = 32 * R;
+    a.slot = (TT + spread + 8 + 3) & ~3;
+    const size_t smem = (size_t)ST * CS * a.slot * sizeof(float) + (size_t)ST * CS * 8 + 8 +
+                        (size_t)2 * ST * sizeof(uint64_t);
+    auto kern = dedisperse_tma_kernel<DMS, R, CS, ST>;
+    PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            "cudaFuncSetAttribute(dedisperse_tma)");
+    dim3 grid((unsigned)pv::ceil_div<long long>(a.nout, TT), (unsigned)pv::ceil_div(a.tdms, DMS));
+    kern<<<grid, (DMS + 1) * 32, smem, s>>>(a, status);
+    return pv::check_launch("dedisperse_tma_kernel");
+}
+
 }  // namespace
 
 namespace pv {
+
+// Shared-memory bytes of the TMA kernel for a given slot size.
+static size_t tma_smem(int st, int cs, int slot_floats) {
+    return (size_t)st * cs * slot_floats * sizeof(float) + (size_t)st * cs * 8 + 8 + 2 * st * 8;
+}
 
 // Chooses the tile for the delay spread: the widest trial tile whose channel
 // slots fit in shared memory with two buffers of CS channels.
 int dedisperse_device(float* out, long long out_stride, const float* in, long long row_stride,
                       long long row_len, long long ring_len, long long t_base, int nchan, int nout,
                       int tdms, const float* d_dmshift, const std::vector<float>& h_dmshift,
-                      float start, float step, cudaStream_t s) {
+                      float start, float step, cudaStream_t s, int* status) {
     if (ring_len > 0 && (ring_len > row_stride || t_base < 0)) {
         set_error("dedispersion: ring of %lld samples does not fit rows of %lld", ring_len, row_stride);
         return PV_ERR_ARG;
     }
     DedispArgs a{out, out_stride, in, row_stride, row_len, ring_len, t_base % std::max(ring_len, 1LL),
                  d_dmshift, nchan, nout, tdms, start, step, 0};
+    // Ring rows with 16-byte aligned spans go through the TMA pipeline.
+    if (status && ring_len > 0 && ring_len % 4 == 0 && row_stride % 4 == 0 &&
+        (reinterpret_cast<uintptr_t>(in) & 15) == 0 && getenv("PV_DEDISP_V1") == nullptr) {
+        const int spread16 = delay_spread(h_dmshift, tdms, 16, start, step);
+        const int slot = (1024 + spread16 + 8 + 3) & ~3;
+        // every copy (span + 16-byte rounding) must fit in one ring turn
+        const bool fits = ring_len >= (long long)std::min(1024, nout) + spread16 + 8;
+        if (fits && tma_smem(4, 4, slot) <= 220 * 1024)
+            return launch_dedisperse_tma<16, 32, 4, 4>(a, spread16, status, s);
+        if (fits && tma_smem(4, 2, slot) <= 220 * 1024)
+            return launch_dedisperse_tma<16, 32, 2, 4>(a, spread16, status, s);
+    }
     const int spread16 = delay_spread(h_dmshift, tdms, 16, start, step);
     if ((size_t)2 * 4 * (1024 + spread16) * 4 <= 200 * 1024)
         return launch_dedisperse<16, 32, 4>(a, spread16, s);
@@ -281,7 +491,7 @@ extern "C" int pv_dedisperse_ex(float* d_out, long long out_stride, const float*
         }
     }
     return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, 0, 0, nchans, nout,
-                                 tdms, d_dmshift, h, start_over_tsamp, step_over_tsamp, s);
+                                 tdms, d_dmshift, h, start_over_tsamp, step_over_tsamp, s, nullptr);
 }
 
 extern "C" int pv_dedisperse(float* d_out, long long out_bytes, const float* d_in,
@@ -304,6 +514,7 @@ extern "C" int pv_dedisperse(float* d_out, long long out_bytes, const float* d_i
 struct pv_dedisp_plan {
     std::vector<float> h_dmshift;
     float* d_dmshift = nullptr;
+    int* d_status = nullptr;  // PV_ERR_TIMEOUT if a pipeline wait gave up
     int nchan = 0, tdms = 0, max_shift = 0;
     float start = 0.0f, step = 0.0f;
 };
@@ -337,9 +548,12 @@ extern "C" int pv_dedisp_plan_create(pv_dedisp_plan** plan, const float* h_dmshi
     cudaError_t e = cudaMalloc(&p->d_dmshift, sizeof(float) * nchans);
     if (e == cudaSuccess)
         e = cudaMemcpy(p->d_dmshift, h_dmshift, sizeof(float) * nchans, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
         pv::set_error("pv_dedisp_plan_create: %s", cudaGetErrorString(e));
         if (p->d_dmshift) cudaFree(p->d_dmshift);
+        if (p->d_status) cudaFree(p->d_status);
         delete p;
         return PV_ERR_CUDA;
     }
@@ -350,7 +564,14 @@ extern "C" int pv_dedisp_plan_create(pv_dedisp_plan** plan, const float* h_dmshi
 extern "C" void pv_dedisp_plan_destroy(pv_dedisp_plan* p) {
     if (!p) return;
     if (p->d_dmshift) cudaFree(p->d_dmshift);
+    if (p->d_status) cudaFree(p->d_status);
     delete p;
+}
+
+extern "C" int pv_dedisp_plan_status(const pv_dedisp_plan* p, int* h_status) {
+    if (!p || !h_status) return PV_ERR_ARG;
+    PV_CUDA(cudaMemcpy(h_status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost), "read plan status");
+    return PV_OK;
 }
 
 extern "C" int pv_dedisp_plan_max_shift(const pv_dedisp_plan* p) { return p ? p->max_shift : -1; }
@@ -366,5 +587,5 @@ extern "C" int pv_dedisp_plan_run(const pv_dedisp_plan* p, float* d_out, long lo
     if (nout == 0) return PV_OK;
     return pv::dedisperse_device(d_out, out_stride, d_in, row_stride, row_len, ring_len, t_base,
                                  p->nchan, nout, p->tdms, p->d_dmshift, p->h_dmshift, p->start,
-                                 p->step, pv::as_stream(stream));
+                                 p->step, pv::as_stream(stream), p->d_status);
 }

@@ -29,7 +29,6 @@
 
 namespace {
 
-constexpr int kThreads = 256;
 
 // ---------------------------------------------------------------------------
 // Host: BinMap / BandPass (BinMap.cpp:37-68, BandPass.cpp:26-166)
@@ -221,12 +220,16 @@ struct RfiBuffers {
     const unsigned char* killed;  // [nbins] or null
 };
 
-// Halving-tree reduction of K doubles per thread in the canonical order.
+// Canonical reduction: every thread holds one FP32 partial per quantity; the
+// partials are widened to double and reduced by the halving tree of offsets
+// 16..1 inside each warp, then offsets NW/2..1 over the NW warp sums.
 template <int K>
-__device__ __forceinline__ void reduce_sum(double (&v)[K], double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ void reduce_sum(const float (&part)[K], double (&out)[K], double* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double v[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
+        v[k] = (double)part[k];
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
             const double o = __shfl_down_sync(0xffffffffu, v[k], off);
@@ -237,25 +240,26 @@ __device__ __forceinline__ void reduce_sum(double (&v)[K], double* red) {
 #pragma unroll
         for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
     __syncthreads();
-    if (threadIdx.x < K) {
-        double w[8];
+    if (warp == 0) {
 #pragma unroll
-        for (int g = 0; g < 8; ++g) w[g] = red[g * K + threadIdx.x];
-#pragma unroll
-        for (int off = 4; off >= 1; off >>= 1)
-#pragma unroll
-            for (int l = 0; l < off; ++l) w[l] = __dadd_rn(w[l], w[l + off]);
-        red[8 * K + threadIdx.x] = w[0];
+        for (int k = 0; k < K; ++k) {
+            double w = lane < nw ? red[lane * K + k] : 0.0;
+            for (int off = nw / 2; off >= 1; off >>= 1) {
+                const double o = __shfl_down_sync(0xffffffffu, w, off);
+                if (lane < off) w = __dadd_rn(w, o);
+            }
+            if (lane == 0) red[32 * K + k] = w;
+        }
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = red[8 * K + k];
+    for (int k = 0; k < K; ++k) out[k] = red[32 * K + k];
     __syncthreads();
 }
 
 template <int K>
 __device__ __forceinline__ void reduce_int(int (&v)[K], int* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = __reduce_add_sync(0xffffffffu, v[k]);
     if (lane == 0)
@@ -265,8 +269,7 @@ __device__ __forceinline__ void reduce_int(int (&v)[K], int* red) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         int s = 0;
-#pragma unroll
-        for (int g = 0; g < 8; ++g) s += red[g * K + k];
+        for (int g = 0; g < nw; ++g) s += red[g * K + k];
         v[k] = s;
     }
     __syncthreads();
@@ -274,7 +277,7 @@ __device__ __forceinline__ void reduce_int(int (&v)[K], int* red) {
 
 template <int K>
 __device__ __forceinline__ void reduce_min(float (&v)[K], float* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k)
 #pragma unroll
@@ -286,8 +289,7 @@ __device__ __forceinline__ void reduce_min(float (&v)[K], float* red) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         float m = red[k];
-#pragma unroll
-        for (int g = 1; g < 8; ++g) m = fminf(m, red[g * K + k]);
+        for (int g = 1; g < nw; ++g) m = fminf(m, red[g * K + k]);
         v[k] = m;
     }
     __syncthreads();
@@ -305,50 +307,69 @@ __device__ __forceinline__ float bp_value(const RfiConfig& cfg, const RfiBuffers
     return __fmul_rn(cfg.scale, tot);
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem_src) : "memory");
+}
+
+// Stages spectrum t (pol 0) into buf with cp.async.
+__device__ __forceinline__ void prefetch_spectrum(float* buf, const float* data, int t, int nbins,
+                                                  int nsub, int npol, int nchan) {
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) cp_async4(buf + i, data + elem(t, i, 0, nsub, npol, nchan));
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// One CTA per beam; blockDim.x == the partial count of the canonical sums.
+__global__ void __launch_bounds__(1024, 1)
 rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int nsub, int npol,
            int nchan, unsigned char* __restrict__ flags) {
     extern __shared__ float sh[];
     const int nbins = cfg.nbins, H = cfg.history;
-    float* bp = sh;              // [nbins]
-    float* spec = sh + nbins;    // [nbins]
-    double* red = reinterpret_cast<double*>(sh + 2 * nbins);  // reduction scratch (nbins is even)
-    int* redi = reinterpret_cast<int*>(red + 8 * 16 + 16);
-    float* redf = reinterpret_cast<float*>(redi + 8 * 8);
+    const int P = blockDim.x;
+    float* bp = sh;                   // [nbins]
+    float* specs = sh + nbins;        // [2][nbins] double-buffered spectra
+    double* red = reinterpret_cast<double*>(sh + 3 * nbins + (nbins & 1));  // [33*16]
+    int* redi = reinterpret_cast<int*>(red + 33 * 16);                       // [32*8]
+    float* redf = reinterpret_cast<float*>(redi + 32 * 8);                   // [32*16]
     const int tid = threadIdx.x;
     const int cpb = nbins / 8;
 
     RfiState st = *bufs.state;  // every thread keeps the same copy of the scalar state
-    for (int i = tid; i < nbins; i += kThreads) bp[i] = bp_value(cfg, bufs, st.params0, i);
-    __syncthreads();
+    for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, st.params0, i);
+    if (nt > 0) prefetch_spectrum(specs, data, 0, nbins, nsub, npol, nchan);
 
     for (int t = 0; t < nt; ++t) {
-        for (int i = tid; i < nbins; i += kThreads) spec[i] = data[elem(t, i, 0, nsub, npol, nchan)];
+        float* spec = specs + (t & 1) * nbins;
+        if (t + 1 < nt) {
+            prefetch_spectrum(specs + ((t + 1) & 1) * nbins, data, t + 1, nbins, nsub, npol, nchan);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
         __syncthreads();
         double data_model;
         double spectrum_rms = st.rms_carry;
         if (st.rms_size < H) {
             // adaptive phase, RFI_Clipper.cpp:214-278
-            float mins[16];
-            double sums[16];
+            float mins[16], part[16];
 #pragma unroll
-            for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; sums[b] = 0.0; sums[8 + b] = 0.0; }
-            for (int i = tid; i < nbins; i += kThreads) {
+            for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
+            for (int i = tid; i < nbins; i += P) {
                 const int band = i / cpb;
                 const float v = spec[i];
-                const double dv = v;
 #pragma unroll
                 for (int b = 0; b < 8; ++b) {
                     if (b == band) {
                         mins[b] = fminf(mins[b], v);
                         mins[8 + b] = fminf(mins[8 + b], bp[i]);
-                        sums[b] = __dadd_rn(sums[b], dv);
-                        sums[8 + b] = __dadd_rn(sums[8 + b], __dmul_rn(dv, dv));
+                        part[b] = __fadd_rn(part[b], v);
+                        part[8 + b] = __fadd_rn(part[8 + b], __fmul_rn(v, v));
                     }
                 }
             }
+            double sums[16];
             reduce_min<16>(mins, redf);
-            reduce_sum<16>(sums, red);
+            reduce_sum<16>(part, sums, red);
             double sig_min = 0.0, dmm[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
@@ -358,17 +379,17 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                 dmm[b] = (double)mins[b] - (double)mins[8 + b];
             }
             // the fifth smallest of the eight (std::nth_element at size/2)
-            for (int i = 1; i < 8; ++i) {
-                const double x = dmm[i];
-                int j = i - 1;
-                while (j >= 0 && dmm[j] > x) { dmm[j + 1] = dmm[j]; --j; }
-                dmm[j + 1] = x;
-            }
+#pragma unroll
+            for (int i = 1; i < 8; ++i)
+#pragma unroll
+                for (int j = i; j > 0; --j) {
+                    const double lo = fmin(dmm[j - 1], dmm[j]), hi = fmax(dmm[j - 1], dmm[j]);
+                    dmm[j - 1] = lo;
+                    dmm[j] = hi;
+                }
             spectrum_rms = sig_min;
             data_model = dmm[4];
-            // rms history push (not full)
             const int pos = (st.rms_head + st.rms_size) % H;
-            __syncthreads();
             if (tid == 0) bufs.rms_buf[pos] = spectrum_rms;
             st.rms_acc_prev = st.rms_acc;
             st.rms_acc = st.rms_acc + spectrum_rms;
@@ -388,29 +409,30 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             st.rms_head = (st.rms_head + 1) % H;
             data_model = 0.0;
         }
-        const double margin = (double)cfg.cr * st.rms_run;
-        // channel clipping, RFI_Clipper.cpp:313-342
-        double gsum[1] = {0.0};
+        const float dm_f = (float)data_model;
+        const float margin_f = (float)((double)cfg.cr * st.rms_run);
+        // channel clipping, RFI_Clipper.cpp:313-342 (FP32 as the reference)
+        float gpart[1] = {0.0f};
         int good[8];
 #pragma unroll
         for (int b = 0; b < 8; ++b) good[b] = 0;
-        for (int i = tid; i < nbins; i += kThreads) {
+        for (int i = tid; i < nbins; i += P) {
             const float v = spec[i];
-            const bool clip = ((double)v - data_model) - (double)bp[i] > margin;
+            const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[i]) > margin_f;
             if (clip) {
                 const float lg = bufs.last_good[i];
-                for (int p = 0; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = lg;
+                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = lg;
                 spec[i] = lg;
-                gsum[0] = __dadd_rn(gsum[0], 0.0);
             } else {
-                gsum[0] = __dadd_rn(gsum[0], (double)v);
+                gpart[0] = __fadd_rn(gpart[0], v);
                 const int band = i / cpb;
 #pragma unroll
                 for (int b = 0; b < 8; ++b) good[b] += (b == band);
             }
             if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
         }
-        reduce_sum<1>(gsum, red);
+        double gsum[1];
+        reduce_sum<1>(gpart, gsum, red);
         reduce_int<8>(good, redi);
         int total_good = 0;
 #pragma unroll
@@ -461,7 +483,7 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             __syncthreads();
         } else if (st.remaining_zeros != 0) {
             int filled[1] = {0};
-            for (int i = tid; i < nbins; i += kThreads) {
+            for (int i = tid; i < nbins; i += P) {
                 const float v = spec[i];
                 if (bufs.last_good[i] == 0.0f && v != 0.0f) {
                     bufs.last_good[i] = v;
@@ -472,30 +494,32 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             st.remaining_zeros -= filled[0];
         }
         if (spectrum_clip) {  // clipSample, RFI_Clipper.cpp:127-150
-            for (int i = tid; i < nbins; i += kThreads) {
-                for (int p = 0; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = -0.2f;
+            for (int i = tid; i < nbins; i += P) {
+                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = -0.2f;
                 spec[i] = -0.2f;
                 if (flags) flags[(long long)t * nbins + i] |= 2;
             }
         }
-        // flatten and normalise, RFI_Clipper.cpp:478-532
-        double s12[2] = {0.0, 0.0};
-        for (int i = tid; i < nbins; i += kThreads) {
-            const float v = (float)((double)spec[i] - ((double)bp[i] + data_model));
+        // flatten and normalise, RFI_Clipper.cpp:478-532 (FP32 per channel)
+        float s12[2] = {0.0f, 0.0f};
+        for (int i = tid; i < nbins; i += P) {
+            const float v = __fsub_rn(spec[i], __fadd_rn(bp[i], dm_f));
             spec[i] = v;
-            s12[0] = __dadd_rn(s12[0], (double)v);
-            s12[1] = __dadd_rn(s12[1], __dmul_rn((double)v, (double)v));
+            s12[0] = __fadd_rn(s12[0], v);
+            s12[1] = __fadd_rn(s12[1], __fmul_rn(v, v));
         }
-        reduce_sum<2>(s12, red);
-        const double m = s12[0] / nbins;
-        double rms = sqrt(s12[1] / nbins - m * m);
+        double sums2[2];
+        reduce_sum<2>(s12, sums2, red);
+        const double m = sums2[0] / nbins;
+        double rms = sqrt(sums2[1] / nbins - m * m);
         if (rms == 0.0) rms = 1.0;
         st.rms_carry = rms;
-        const double sub = cfg.zero_dming == 1 ? m : st.mean_run;
-        for (int i = tid; i < nbins; i += kThreads) {
+        const float sub_f = (float)(cfg.zero_dming == 1 ? m : st.mean_run);
+        const float rms_f = (float)rms;
+        for (int i = tid; i < nbins; i += P) {
             float v = spec[i];
             if (!spectrum_clip) {
-                v = (float)(((double)v - sub) / rms);
+                v = __fdiv_rn(__fsub_rn(v, sub_f), rms_f);
                 if (v > cfg.cr) v = 0.0f;
             }
             data[elem(t, i, 0, nsub, npol, nchan)] = v;
@@ -517,7 +541,7 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
         if (fabsf(delta) > 0.0f) {
             st.params0 = st.params0 + delta / cfg.scale;
             st.bp_mean = mean_f;
-            for (int i = tid; i < nbins; i += kThreads) bp[i] = bp_value(cfg, bufs, st.params0, i);
+            for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, st.params0, i);
         }
         st.bp_rms = (float)st.rms_run;
         st.num = (st.num + 1) % (10 * H);
@@ -687,17 +711,20 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     const int nbins = nsub * nchan;
     PV_TRY(setup(h, nbins, s));
     if (nt == 0) return PV_OK;
-    const size_t smem = sizeof(float) * (2 * (size_t)nbins + 2) + sizeof(double) * (8 * 16 + 16) +
-                        sizeof(int) * 64 + sizeof(float) * 8 * 16;
+    const int threads = pv_rfi_parts(nbins);
+    const size_t smem = sizeof(float) * (3 * (size_t)nbins + 2) + sizeof(double) * 33 * 16 +
+                        sizeof(int) * 32 * 8 + sizeof(float) * 32 * 16;
     if (smem > 227 * 1024) {
         pv::set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
         return PV_ERR_ARG;
     }
     PV_CUDA(cudaFuncSetAttribute(rfi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
             "cudaFuncSetAttribute(rfi)");
-    rfi_kernel<<<1, kThreads, smem, s>>>(h->cfg, h->dev, d_data, nt, nsub, npol, nchan, d_flags);
+    rfi_kernel<<<1, threads, smem, s>>>(h->cfg, h->dev, d_data, nt, nsub, npol, nchan, d_flags);
     return pv::check_launch("rfi_kernel");
 }
+
+extern "C" int pv_rfi_parts(int nbins) { return nbins <= 1024 ? 256 : (nbins <= 4096 ? 512 : 1024); }
 
 extern "C" int pv_rfi_state(pv_rfi* h, double* out10) {
     if (!h || !out10) return PV_ERR_ARG;

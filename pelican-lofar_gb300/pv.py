@@ -79,6 +79,7 @@ def _declare(L):
         "pv_rfi_run": (i, [vp, vp, i, i, i, i, vp, vp]),
         "pv_rfi_state": (i, [vp, P(C.c_double)]),
         "pv_rfi_bandpass": (i, [vp, P(C.c_float), i]),
+        "pv_rfi_parts": (i, [i]),
         "pv_beam_create": (i, [P(vp), vp]),
         "pv_beam_destroy": (None, [vp]),
         "pv_beam_input_bytes": (ll, [vp, i]),

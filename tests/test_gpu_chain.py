@@ -100,7 +100,7 @@ def test_rfi_bit_exact_fp64_variant(pv, oracle, cuda, case):
                       case["coeffs"])
     kw = dict(cr=5.0, sr=4.0, history=case["history"], zero_dming=case["zero_dm"])
     g = pv.RFI(bp, **kw)
-    o = oracle.RFI(bp, mode=1, **kw)
+    o = oracle.RFI(bp, mode=1, parts=pv.load().pv_rfi_parts(nsub * nchan), **kw)
     for sl in (slice(0, 1100), slice(1100, nt)):
         d = np.ascontiguousarray(data[sl])
         dd = torch.from_numpy(d).to(cuda)
@@ -120,6 +120,27 @@ def test_rfi_four_stokes_clips_all_polarisations(pv, oracle, cuda):
     bp = make_bp_text(256, BP_START, BP_WIDTH, 1000.0, 50.0)
     g = pv.RFI(bp, cr=5.0, history=1050)
     o = oracle.RFI(bp, cr=5.0, history=1050, mode=1)
+    dd = torch.from_numpy(np.ascontiguousarray(data)).to(cuda)
+    gf = g.run(dd, flags=True).cpu().numpy()
+    d = np.ascontiguousarray(data)
+    of = o.run(d, flags=True)
+    assert np.array_equal(gf, of) and np.array_equal(dd.cpu().numpy(), d)
+
+
+
+@pytest.mark.parametrize("nsub,nchan", [(128, 16), (96, 64)])
+def test_rfi_wide_bands_bit_exact(pv, oracle, cuda, nsub, nchan):
+    """2048 and 6144 channels: 512 and 1024 partial sums per reduction."""
+    import torch
+    rng = np.random.default_rng(nsub)
+    nt = 1250
+    nbins = nsub * nchan
+    data = stokes_filterbank(rng, nt, nsub, nchan)
+    bp = make_bp_text(nbins, BP_START, BP_WIDTH, 1000.0, 50.0)
+    parts = pv.load().pv_rfi_parts(nbins)
+    assert parts == (512 if nbins <= 4096 else 1024)
+    g = pv.RFI(bp, cr=5.0, history=1100)
+    o = oracle.RFI(bp, cr=5.0, history=1100, mode=1, parts=parts)
     dd = torch.from_numpy(np.ascontiguousarray(data)).to(cuda)
     gf = g.run(dd, flags=True).cpu().numpy()
     d = np.ascontiguousarray(data)
