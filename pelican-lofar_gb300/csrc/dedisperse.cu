@@ -195,13 +195,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
     return ok != 0;
 }
-// Waits for the phase of the given parity; gives up after limit_ns.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
-    if (mbar_try_wait(bar, parity)) return true;
+// Whole-warp wait for the phase of the given parity.  Every lane observes the
+// completion itself (acquire), and the give-up decision comes from lane 0's
+// clock, so the warp leaves the wait together.  Gives up after limit_ns.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
     const unsigned long long t_end = global_ns() + limit_ns;
+    bool done = false;
     for (;;) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() > t_end) return false;
+        if (!done) done = mbar_try_wait(bar, parity);
+        if (__all_sync(0xffffffffu, done)) return true;
+        const bool expired = __shfl_sync(0xffffffffu, global_ns() > t_end, 0);
+        if (expired) return false;
     }
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
@@ -210,7 +214,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
         ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kWaitLimitNs = 500000000ull;  // 0.5 s per wait
 
 template <int DMS, int R, int CS, int ST>
 __global__ void __launch_bounds__((DMS + 1) * 32, 1)
@@ -232,6 +236,8 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
     const float dv_last = pv_trial_value(d_last, a.start, a.step);
     const int nstages = (a.nchan + CS - 1) / CS;
 
+    // A launch in which some CTA already gave up stops here.
+    if (*(volatile int*)status != 0) return;
     if (threadIdx.x == 0) {
         for (int b = 0; b < ST; ++b) {
             mbar_init(&full[b], 1);
@@ -250,7 +256,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         for (int st = 0; st < nstages && ok; ++st) {
             const int b = st % ST;
             const unsigned round = (unsigned)(st / ST);
-            if (!mbar_wait(&empty[b], (round & 1u) ^ 1u, kWaitLimitNs)) {
+            if (!mbar_wait_warp(&empty[b], (round & 1u) ^ 1u, kWaitLimitNs)) {
                 if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                 ok = false;
                 break;
@@ -291,7 +297,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         // the CTA's shared memory is released.
         if (!ok) {
             for (int st = max(0, issued - ST); st < issued; ++st)
-                mbar_wait(&full[st % ST], (unsigned)(st / ST) & 1u, kWaitLimitNs);
+                mbar_wait_warp(&full[st % ST], (unsigned)(st / ST) & 1u, kWaitLimitNs);
         }
         return;
     }
@@ -306,7 +312,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
     bool ok = true;
     for (int st = 0; st < nstages; ++st) {
         const int b = st % ST;
-        if (!mbar_wait(&full[b], (unsigned)(st / ST) & 1u, kWaitLimitNs)) {
+        if (!mbar_wait_warp(&full[b], (unsigned)(st / ST) & 1u, kWaitLimitNs)) {
             if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
             ok = false;
             break;
