@@ -235,6 +235,12 @@ extern "C" int pv_beam_events(pv_beam* b, pv_event* h_events, long long cap, lon
         if (h_first_sample) *h_first_sample = -1;
         return PV_OK;
     }
+    int status = PV_OK;
+    PV_TRY(pv_dedisp_plan_status(b->plan, &status));
+    if (status != PV_OK) {
+        pv::set_error("pv_beam_events: a dedispersion pipeline wait gave up (status %d)", status);
+        return status;
+    }
     *h_count = *b->h_total;
     if (h_first_sample) *h_first_sample = b->window * b->cfg.chunk;
     const long long n = std::min(std::min(*b->h_total, b->cap), cap);

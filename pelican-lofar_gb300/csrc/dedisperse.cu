@@ -236,9 +236,10 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
     const float dv_last = pv_trial_value(d_last, a.start, a.step);
     const int nstages = (a.nchan + CS - 1) / CS;
 
-    // A launch in which some CTA already gave up stops here.
-    if (*(volatile int*)status != 0) return;
+    __shared__ int s_abort;
     if (threadIdx.x == 0) {
+        // a launch in which some CTA already gave up stops here
+        s_abort = *(volatile int*)status;
         for (int b = 0; b < ST; ++b) {
             mbar_init(&full[b], 1);
             mbar_init(&empty[b], DMS);
@@ -247,6 +248,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     }
     __syncthreads();
+    if (s_abort != 0) return;
 
     if (warp == DMS) {
         // ---------------- producer ----------------
