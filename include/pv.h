@@ -117,6 +117,32 @@ int pv_ring_write(float* d_ring, long long row_stride, long long ring_len, long 
                   const float* d_stokes, int nt, int nsub, int npol, int nchan, int inverted,
                   void* stream);
 
+/* A10 DedispersionModule::dedisperse with the reference's buffering
+ * (lib/src/DedispersionModule.cpp:109-325): buffers of buffer_samples =
+ * 2^timeBinsPerBufferPow2 samples, nout = buffer_samples - maxshift -
+ * remainingSamples outputs per full buffer, the next buffer starting with the
+ * previous one's last maxshift + remainingSamples samples.  Arguments follow
+ * the XML keys dedispersionSamples, dedispersionMinimum, dedispersionStepSize,
+ * frequencyChannel1@MHz, channelBandwidth@MHz. */
+typedef struct pv_ddmod pv_ddmod;
+int pv_ddmod_create(pv_ddmod** mod, int buffer_samples, int tdms, float dm_low, float dm_step,
+                    double fch1, double foff);
+void pv_ddmod_destroy(pv_ddmod* mod);
+/* Adds one Stokes blob [nt][nsub][npol][nchan] (host or device pointer; pol
+ * 0 is dedispersed) whose samples are tsamp seconds apart (the blob's
+ * getBlockRate()).  *completed receives the number of buffers that became
+ * full and were dedispersed (asynchronously on stream).  A maxshift larger
+ * than the buffer is a PV_ERR_CONFIG with the reference's message. */
+int pv_ddmod_add(pv_ddmod* mod, const float* stokes, int nt, int nsub, int npol, int nchan,
+                 double tsamp, int* completed, void* stream);
+/* Pops the oldest completed DedispersionSpectra: [tdms][nout] floats into out
+ * (host or device, cap_floats >= tdms*nout; NULL discards it), *nout (0 when
+ * none is ready) and the absolute index of its first input sample. */
+int pv_ddmod_pop(pv_ddmod* mod, float* out, long long cap_floats, int* nout,
+                 long long* first_sample, void* stream);
+/* [maxshift, remainingSamples, nout, channels, inverted, completed buffers queued] */
+int pv_ddmod_params(const pv_ddmod* mod, int* h_out6);
+
 /* ------------------------------------------------------------------------
  * A11 analyser — DedispersionAnalyser::analyse (lib/src/DedispersionAnalyser.cpp:30-203)
  * ---------------------------------------------------------------------- */

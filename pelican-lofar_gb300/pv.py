@@ -90,6 +90,12 @@ def _declare(L):
         "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
         "pv_beam_stage_ms": (i, [vp, P(C.c_float)]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
+        "pv_ddmod_create": (i, [P(vp), i, i, f, f, d, d]),
+        "pv_ddmod_destroy": (None, [vp]),
+        "pv_ddmod_add": (i, [vp, vp, i, i, i, i, d, P(i), vp]),
+        "pv_ddmod_pop": (i, [vp, vp, ll, P(i), P(ll), vp]),
+        "pv_ddmod_params": (i, [vp, P(i)]),
+        "pv_dedisp_plan_status": (i, [vp, P(i)]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
@@ -403,3 +409,40 @@ def device_array(ptr, shape, device=None):
     t = torch.empty(shape, dtype=torch.float32, device=device or "cuda")
     check(load().pv_device_copy(_ptr(t), C.c_void_p(ptr), t.numel() * 4, _stream(None)))
     return t
+
+
+class DedispersionModule:
+    """DedispersionModule with the reference's buffering (host numpy blobs in,
+    host DedispersionSpectra out)."""
+
+    def __init__(self, buffer_samples, tdms, dm_low, dm_step, fch1, foff):
+        self.tdms = tdms
+        self.h = C.c_void_p()
+        check(load().pv_ddmod_create(C.byref(self.h), buffer_samples, tdms, dm_low, dm_step, fch1,
+                                     foff))
+
+    def add(self, stokes, tsamp, stream=None):
+        s = np.ascontiguousarray(stokes, np.float32)
+        nt, nsub, npol, nchan = s.shape
+        done = C.c_int()
+        check(load().pv_ddmod_add(self.h, C.c_void_p(s.ctypes.data), nt, nsub, npol, nchan, tsamp,
+                                  C.byref(done), _stream(stream)))
+        outs = []
+        for _ in range(done.value):
+            p = self.params()
+            buf = np.empty((self.tdms, p["nout"]), np.float32)
+            n, first = C.c_int(), C.c_longlong()
+            check(load().pv_ddmod_pop(self.h, C.c_void_p(buf.ctypes.data), buf.size, C.byref(n),
+                                      C.byref(first), _stream(stream)))
+            outs.append((buf, first.value))
+        return outs
+
+    def params(self):
+        out = (C.c_int * 6)()
+        check(load().pv_ddmod_params(self.h, out))
+        return dict(zip(["maxshift", "remaining", "nout", "nchan", "inverted", "queued"], list(out)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_ddmod_destroy(self.h)
+            self.h = C.c_void_p()
