@@ -680,15 +680,15 @@ struct CircBuf {
 
 }  // namespace
 
-// Canonical reduction of the FP64 RFI variant over P partials (P a multiple
-// of 32): each group of 32 consecutive partials is reduced in double by the
-// halving tree of offsets 16, 8, 4, 2, 1, then the P/32 group sums by offsets
+// Canonical FP32 reduction of the RFI variant over P partials (P a multiple
+// of 32): each group of 32 consecutive partials is reduced by the halving
+// tree of offsets 16, 8, 4, 2, 1, then the P/32 group sums by offsets
 // P/64, ..., 1.
-static double tree_p(double* part, int P) {
+static float tree_p(float* part, int P) {
     const int nw = P / 32;
-    double w[32];
+    float w[32];
     for (int g = 0; g < nw; ++g) {
-        double* q = part + 32 * g;
+        float* q = part + 32 * g;
         for (int off = 16; off >= 1; off >>= 1)
             for (int l = 0; l < off; ++l) q[l] = q[l] + q[l + off];
         w[g] = q[0];
@@ -699,9 +699,9 @@ static double tree_p(double* part, int P) {
 }
 
 // Sum of n floats: partial p is the FP32 sum of x[p], x[p+P], ... in order
-// (from +0), widened to double and reduced by tree_p.
+// (from +0), reduced by tree_p.
 extern "C" double or_sum_canonical(const float* x, int n, int P) {
-    double part[1024];
+    float part[1024];
     for (int p = 0; p < P; ++p) {
         float s = 0.0f;
         for (int i = p; i < n; i += P) s += x[i];
@@ -724,44 +724,50 @@ struct RfiBase {
     float start_freq = 0.0f, end_freq = 0.0f;
 };
 
-// R = float: the reference's arithmetic.  R = double: the FP64 variant.
-template <typename R>
+// The reference's arithmetic (mode 0) and the library's variant (mode 1).
+// Mode 1 keeps every per-channel and per-spectrum expression in the
+// reference's FP32 form, replaces the sequential channel sums by `parts`
+// FP32 partials reduced by tree_p, and keeps the running averages and their
+// history buffers in FP64, updated with multiplications by 1/H and by the
+// reciprocal of meanOverRMS.
 struct Rfi : RfiBase {
-    static constexpr bool kF64 = sizeof(R) == 8;
+    bool f64;
+    int parts = 256;
     float cr, sr;
     int max_history, zero_dming, use_mor;
-    CircBuf<R> mean_buf, rms_buf;
-    R rms_run = 0, mean_run = 0, mean_over_rms = 0;
-    R spectrum_rms_carry = 0;  // function-scope spectrumRMS carried between spectra
+    CircBuf<double> mean_buf, rms_buf;   // mode 0 stores float values exactly
+    double rms_run = 0, mean_run = 0, mean_over_rms = 0, inv_mor = 0;
+    double rms_carry = 0;  // function-scope spectrumRMS carried between spectra
+    double acc_mean = 0, acc_mean_prev = 0, acc_rms = 0, acc_rms_prev = 0;
     float frac_bad_channels = 0.0f;
     int bad_spectra = 0, num = 0, remaining_zeros = 0;
     std::vector<float> last_good;
 
-    int parts = 256;  // FP64 variant: number of FP32 partial sums (the GPU's threads)
-
-    // Sum of the float values f(i), i < n, in the mode's order: one sequential
-    // FP32 sum (reference), or the canonical partials + FP64 tree (variant).
+    // mode 0: one sequential FP32 sum; mode 1: canonical partials + tree
     template <typename F>
-    R channel_sum(int n, F f) const {
-        if (!kF64) {
+    float channel_sum(int n, F f) const {
+        if (!f64) {
             float s = 0.0f;
             for (int i = 0; i < n; ++i) s += f(i);
-            return (R)s;
+            return s;
         }
-        double part[1024];
+        float part[1024];
         for (int p = 0; p < parts; ++p) {
             float s = 0.0f;
             for (int i = p; i < n; i += parts) s += f(i);
             part[p] = s;
         }
-        return (R)tree_p(part, parts);
+        return tree_p(part, parts);
     }
-
+    // mode 1 running sums: reference's accumulate() is the sequential sum of
+    // the buffer; the variant keeps it incrementally with the same order.
     int run(float* I, float* W, int nt, int nsub, int npol, int nchan, uint8_t* flags) override {
         const unsigned nbins = (unsigned)(nchan * nsub);
         if (nbins % 8 != 0) return -2;
         const float k = 4;
-        const R mmm = kF64 ? (R)(4.0 / std::sqrt(8.0)) : (R)(float)(k / ::sqrt(2.0 * k));
+        const float mmm = (float)(k / ::sqrt(2.0 * k));
+        const double inv_h = 1.0 / (double)max_history;
+        const double inv_sqrt_nbins = 1.0 / std::sqrt((double)nbins);
         if (last_good.size() != nbins) {
             last_good.resize(nbins, 0.0f);
             remaining_zeros = (int)nbins;
@@ -777,20 +783,17 @@ struct Rfi : RfiBase {
         std::vector<float> vals(nbins);
         for (unsigned t = 0; t < (unsigned)nt; ++t) {
             const std::vector<float> bandpass = bp.current_set();
-            float* I0 = I + idx(t, 0, 0);
-            // gather pol-0 values in bin order (bin = s*nchan + c)
             auto at = [&](unsigned bin) -> float& {
                 unsigned s = bin / nchan, c = bin % nchan;
                 return I[idx(t, s, 0) + c];
             };
-            (void)I0;
             bool good_spectrum = true;
-            R data_model;
-            R spectrum_rms = spectrum_rms_carry;
+            float data_model;
+            double spectrum_rms = rms_carry;
             if (!rms_buf.full()) {
-                float mini_data[8], mini_model[8];
+                // adaptive phase, RFI_Clipper.cpp:214-278
+                float mini_data[8], mini_model[8], band_sigma[8], dmm[8];
                 for (int b = 0; b < 8; ++b) { mini_data[b] = 1e6f; mini_model[b] = 1e6f; }
-                R band_sigma[8], dmm[8];
                 for (unsigned bin = 0; bin < nbins; ++bin) {
                     unsigned band = bin / cpb;
                     float v = at(bin);
@@ -798,8 +801,8 @@ struct Rfi : RfiBase {
                     if (bandpass[bin] < mini_model[band]) mini_model[band] = bandpass[bin];
                 }
                 for (int b = 0; b < 8; ++b) {
-                    R bm, bms;
-                    if (!kF64) {
+                    float bm, bms;
+                    if (!f64) {
                         float s1 = 0.0f, s2 = 0.0f;
                         for (unsigned bin = b * cpb; bin < (b + 1) * cpb; ++bin) {
                             float v = at(bin);
@@ -815,44 +818,58 @@ struct Rfi : RfiBase {
                             f1[bin % parts] += v;
                             f2[bin % parts] += v * v;
                         }
-                        double p1[1024], p2[1024];
-                        for (int q = 0; q < parts; ++q) { p1[q] = f1[q]; p2[q] = f2[q]; }
-                        bm = (R)tree_p(p1, parts); bms = (R)tree_p(p2, parts);
+                        bm = tree_p(f1, parts); bms = tree_p(f2, parts);
                     }
-                    dmm[b] = (R)mini_data[b] - (R)mini_model[b];
-                    if (!kF64) {
-                        float a = (float)bms / cpb;
-                        float m = (float)bm / cpb;
-                        float diff = a - m * m;  // std::pow(float,2) == m*m in float
-                        band_sigma[b] = (R)(float)::sqrt((double)diff);
-                    } else {
-                        double a = (double)bms / cpb, m = (double)bm / cpb;
-                        band_sigma[b] = (R)std::sqrt(a - m * m);
-                    }
+                    dmm[b] = mini_data[b] - mini_model[b];
+                    const float a = bms / cpb;
+                    const float m = bm / cpb;
+                    const float diff = a - m * m;  // std::pow(float,2) == m*m in float
+                    band_sigma[b] = (float)::sqrt((double)diff);
                 }
-                spectrum_rms = *std::min_element(band_sigma, band_sigma + 8);
+                const float srms = *std::min_element(band_sigma, band_sigma + 8);
                 std::nth_element(dmm, dmm + 4, dmm + 8);
                 data_model = dmm[4];
-                rms_buf.push_back(spectrum_rms);
-                rms_run = (R)(rms_buf.accumulate() / rms_buf.size());
-                if (rms_buf.full()) mean_over_rms = mean_run / rms_run;
-                data_model = data_model + mmm * rms_run;
+                if (!f64) {
+                    rms_buf.push_back(srms);
+                    rms_run = (float)(rms_buf.accumulate() / rms_buf.size());
+                    if (rms_buf.full()) mean_over_rms = (float)((float)mean_run / (float)rms_run);
+                    data_model = data_model + mmm * (float)rms_run;
+                } else {
+                    acc_rms_prev = acc_rms;
+                    acc_rms = acc_rms + (double)srms;
+                    rms_buf.push_back(srms);
+                    rms_run = acc_rms / (double)rms_buf.size();
+                    if (rms_buf.full()) {
+                        mean_over_rms = mean_run / rms_run;
+                        inv_mor = 1.0 / mean_over_rms;
+                    }
+                    data_model = data_model + mmm * (float)rms_run;
+                }
+                spectrum_rms = srms;
             } else {
-                rms_run -= (rms_buf.front() / (R)rms_buf.size());
-                rms_run += (rms_buf.back() / (R)rms_buf.cap);
-                if (use_mor) spectrum_rms = std::fabs(mean_run / mean_over_rms);
-                rms_buf.push_back(spectrum_rms);
-                data_model = 0.0;
+                // steady phase, RFI_Clipper.cpp:279-307
+                if (!f64) {
+                    float r = (float)rms_run;
+                    r -= ((float)rms_buf.front() / (float)rms_buf.size());
+                    r += ((float)rms_buf.back() / (float)rms_buf.cap);
+                    rms_run = r;
+                    if (use_mor) spectrum_rms = std::fabs((float)mean_run / (float)mean_over_rms);
+                    rms_buf.push_back((float)spectrum_rms);
+                } else {
+                    rms_run = rms_run - rms_buf.front() * inv_h;
+                    rms_run = rms_run + rms_buf.back() * inv_h;
+                    if (use_mor) spectrum_rms = std::fabs(mean_run * inv_mor);
+                    rms_buf.push_back(spectrum_rms);
+                }
+                data_model = 0.0f;
             }
-            const R margin = (R)cr * rms_run;
+            const float margin = cr * (float)rms_run;
             // channel clipping, :315-342
             std::vector<unsigned char> clipped(nbins, 0);
             int good_per_band[8] = {0};
             for (unsigned bin = 0; bin < nbins; ++bin) {
                 float v = at(bin);
-                bool clip;
-                // per-channel arithmetic is FP32 in both modes (RFI_Clipper.cpp:321)
-                clip = (float)((float)(v - (float)data_model) - bandpass[bin]) > (float)margin;
+                const bool clip = (float)((float)(v - data_model) - bandpass[bin]) > margin;
                 if (clip) {
                     clipped[bin] = 1;
                     unsigned s = bin / nchan, c = bin % nchan;
@@ -864,16 +881,13 @@ struct Rfi : RfiBase {
                     ++good_per_band[bin / cpb];
                 }
             }
-            R spectrum_sum = channel_sum((int)nbins, [&](int bin) -> float {
+            float spectrum_sum = channel_sum((int)nbins, [&](int bin) -> float {
                 return clipped[bin] ? 0.0f : at(bin);
             });
-            // Sequential float sum skips clipped channels entirely (adding 0.0f
-            // to a float sum is exact, so the result is the same).
             unsigned total_good = 0;
             for (int b = 0; b < 8; ++b) total_good += good_per_band[b];
             frac_bad_channels += (float)(nbins - total_good) / nbins;
-            if (!kF64) spectrum_sum = (R)((float)spectrum_sum / total_good);
-            else spectrum_sum = spectrum_sum / (R)total_good;
+            spectrum_sum /= total_good;
             unsigned bad_bands = 0;
             for (int b = 0; b < 8; ++b) {
                 if ((double)good_per_band[b] < 0.8 * cpb) ++bad_bands;
@@ -882,26 +896,49 @@ struct Rfi : RfiBase {
             if (total_good < 0.8 * nbins) bad_bands += 4;
             // mean history, :383-400
             if (!mean_buf.full()) {
-                mean_buf.push_back(spectrum_sum);
-                mean_run = (R)(mean_buf.accumulate() / mean_buf.size());
+                if (!f64) {
+                    mean_buf.push_back(spectrum_sum);
+                    mean_run = (float)(mean_buf.accumulate() / mean_buf.size());
+                } else {
+                    acc_mean_prev = acc_mean;
+                    acc_mean = acc_mean + (double)spectrum_sum;
+                    mean_buf.push_back(spectrum_sum);
+                    mean_run = acc_mean / (double)mean_buf.size();
+                }
             } else {
-                mean_run -= mean_buf.front() / (R)mean_buf.size();
-                mean_run += mean_buf.back() / (R)mean_buf.size();
+                if (!f64) {
+                    float mr = (float)mean_run;
+                    mr -= (float)mean_buf.front() / (float)mean_buf.size();
+                    mr += (float)mean_buf.back() / (float)mean_buf.size();
+                    mean_run = mr;
+                } else {
+                    mean_run = mean_run - mean_buf.front() * inv_h;
+                    mean_run = mean_run + mean_buf.back() * inv_h;
+                }
                 mean_buf.push_back(spectrum_sum);
             }
-            R tol;
-            if (!kF64) tol = (R)(float)((double)(sr * bp.rms()) / ::sqrt((double)nbins));
-            else tol = (double)sr * (double)bp.rms() / std::sqrt((double)nbins);
+            bool reject;
+            if (!f64) {
+                const float tol = (float)((double)(sr * bp.rms()) / ::sqrt((double)nbins));
+                reject = (float)(spectrum_sum - (float)mean_run) > tol;
+            } else {
+                const float tol = (float)((double)(sr * bp.rms()) * inv_sqrt_nbins);
+                reject = (double)spectrum_sum - mean_run > (double)tol;
+            }
             bool spectrum_clip = false;
             if (mean_buf.size() < 1000) {
                 spectrum_clip = true;
-            } else if (spectrum_sum - mean_run > tol || bad_bands >= 4) {
+            } else if (reject || bad_bands >= 4) {
                 spectrum_clip = true;
                 ++bad_spectra;
                 mean_buf.pop_back();
                 rms_buf.pop_back();
                 mean_buf.push_back(mean_buf.back());
                 rms_buf.push_back(rms_buf.back());
+                if (f64) {
+                    acc_mean = acc_mean_prev + mean_buf.back();
+                    acc_rms = acc_rms_prev + rms_buf.back();
+                }
             } else if (remaining_zeros != 0) {
                 for (unsigned bin = 0; bin < nbins; ++bin) {
                     float v = at(bin);
@@ -923,43 +960,22 @@ struct Rfi : RfiBase {
             // flatten, :478-494
             for (unsigned bin = 0; bin < nbins; ++bin) {
                 float& v = at(bin);
-                v -= (float)(bandpass[bin] + (float)data_model);
+                v -= (float)(bandpass[bin] + data_model);
                 vals[bin] = v;
             }
-            R s1, s2;
-            if (!kF64) {
-                float a = 0.0f, b = 0.0f;
-                for (unsigned bin = 0; bin < nbins; ++bin) { a += vals[bin]; b += vals[bin] * vals[bin]; }
-                s1 = a; s2 = b;
-            } else {
-                s1 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin]; });
-                s2 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin] * vals[bin]; });
-            }
-            if (!kF64) {
-                float m = (float)s1 / nbins;
-                float ms = (float)s2 / nbins;
-                float diff = ms - m * m;
-                spectrum_sum = m;
-                spectrum_rms = (R)(float)::sqrt((double)diff);
-            } else {
-                double m = (double)s1 / nbins;
-                spectrum_sum = m;
-                spectrum_rms = std::sqrt((double)s2 / nbins - m * m);
-            }
-            if (spectrum_rms == (R)0.0) spectrum_rms = 1.0;
-            spectrum_rms_carry = spectrum_rms;
+            const float s1 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin]; });
+            const float s2 = channel_sum((int)nbins, [&](int bin) -> float { return vals[bin] * vals[bin]; });
+            const float m = s1 / nbins;
+            const float ms = s2 / nbins;
+            float srms = (float)::sqrt((double)(ms - m * m));
+            if (srms == 0.0f) srms = 1.0f;
+            rms_carry = srms;
             if (good_spectrum) {
+                const float sub = (zero_dming == 1) ? (float)(zero_dming * m) : (float)mean_run;
                 for (unsigned bin = 0; bin < nbins; ++bin) {
                     float& v = at(bin);
-                    if (!kF64) {
-                        if (zero_dming == 1) v -= (float)(zero_dming * (float)spectrum_sum);
-                        else v -= (float)mean_run;
-                        v /= (float)spectrum_rms;
-                    } else {
-                        const float sub = (float)(zero_dming == 1 ? (double)spectrum_sum : (double)mean_run);
-                        v -= sub;
-                        v /= (float)spectrum_rms;
-                    }
+                    v -= sub;
+                    v /= srms;
                     if (v > cr) v = 0.0f;
                 }
             }
@@ -975,6 +991,7 @@ struct Rfi : RfiBase {
                 if (frac_bad_spectra > 99.0) {
                     rms_buf.q.clear();
                     mean_buf.q.clear();
+                    acc_mean = acc_mean_prev = acc_rms = acc_rms_prev = 0.0;
                 }
                 bad_spectra = 0;
                 frac_bad_channels = 0.0f;
@@ -988,8 +1005,8 @@ struct Rfi : RfiBase {
     }
 
     void state(double* out) const override {
-        out[0] = (double)mean_run;
-        out[1] = (double)rms_run;
+        out[0] = mean_run;
+        out[1] = rms_run;
         out[2] = bp.mean();
         out[3] = bp.rms();
         out[4] = bp.params.empty() ? 0.0 : bp.params[0];
@@ -1011,21 +1028,13 @@ extern "C" or_rfi* or_rfi_create(const char* bp_text, float cr_factor, float sr_
                                  int max_history, int zero_dming, int use_mean_over_rms,
                                  int band_matching, int mode, int parts, char* err, int errlen) {
     if (parts != 256 && parts != 512 && parts != 1024) parts = 256;
-    RfiBase* impl;
-    if (mode == 1) {
-        auto* r = new Rfi<double>;
-        r->parts = parts;
-        r->cr = cr_factor; r->sr = sr_factor; r->max_history = max_history;
-        r->zero_dming = zero_dming; r->use_mor = use_mean_over_rms;
-        r->mean_buf.cap = r->rms_buf.cap = (size_t)max_history;
-        impl = r;
-    } else {
-        auto* r = new Rfi<float>;
-        r->cr = cr_factor; r->sr = sr_factor; r->max_history = max_history;
-        r->zero_dming = zero_dming; r->use_mor = use_mean_over_rms;
-        r->mean_buf.cap = r->rms_buf.cap = (size_t)max_history;
-        impl = r;
-    }
+    Rfi* r = new Rfi;
+    r->f64 = mode == 1;
+    r->parts = parts;
+    r->cr = cr_factor; r->sr = sr_factor; r->max_history = max_history;
+    r->zero_dming = zero_dming; r->use_mor = use_mean_over_rms;
+    r->mean_buf.cap = r->rms_buf.cap = (size_t)max_history;
+    RfiBase* impl = r;
     std::string e;
     if (!parse_bp(bp_text, impl->bp, e)) {
         if (err && errlen > 0) std::snprintf(err, errlen, "%s", e.c_str());

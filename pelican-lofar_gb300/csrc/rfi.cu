@@ -197,7 +197,7 @@ int parse_bandpass(const char* text, Bandpass& bp) {
 // Device state
 // ---------------------------------------------------------------------------
 struct RfiState {
-    double mean_run, rms_run, mean_over_rms, rms_carry;
+    double mean_run, rms_run, mean_over_rms, inv_mor, rms_carry;
     double mean_acc, mean_acc_prev, rms_acc, rms_acc_prev;
     int mean_head, mean_size, rms_head, rms_size;
     int num, bad_spectra, remaining_zeros;
@@ -207,8 +207,8 @@ struct RfiState {
 
 struct RfiConfig {
     int nbins, history, zero_dming, use_mor, deg;
-    float cr, sr, scale;
-    double mmm, sqrt_nbins;
+    float cr, sr, scale, mmm_f;
+    double inv_sqrt_nbins;
 };
 
 struct RfiBuffers {
@@ -220,79 +220,40 @@ struct RfiBuffers {
     const unsigned char* killed;  // [nbins] or null
 };
 
-// Canonical reduction: every thread holds one FP32 partial per quantity; the
-// partials are widened to double and reduced by the halving tree of offsets
-// 16..1 inside each warp, then offsets NW/2..1 over the NW warp sums.
+// ---------------------------------------------------------------------------
+// Block reductions.  Every thread holds one FP32 partial per quantity (thread
+// p sums channels p, p+P, ... in order).  The canonical order reduces each
+// warp's 32 partials by the halving tree of offsets 16..1 and the NW warp
+// sums by offsets NW/2..1; thread 0 finishes the second stage and is the only
+// thread that sees the result.
+// ---------------------------------------------------------------------------
 template <int K>
-__device__ __forceinline__ void reduce_sum(const float (&part)[K], double (&out)[K], double* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double v[K];
+__device__ __forceinline__ void warp_tree(float (&v)[K], float* red /*[32][K]*/) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        v[k] = (double)part[k];
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
-            const double o = __shfl_down_sync(0xffffffffu, v[k], off);
-            if (lane < off) v[k] = __dadd_rn(v[k], o);
+            const float o = __shfl_down_sync(0xffffffffu, v[k], off);
+            if (lane < off) v[k] = __fadd_rn(v[k], o);
         }
     }
     if (lane == 0)
 #pragma unroll
         for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            double w = lane < nw ? red[lane * K + k] : 0.0;
-            for (int off = nw / 2; off >= 1; off >>= 1) {
-                const double o = __shfl_down_sync(0xffffffffu, w, off);
-                if (lane < off) w = __dadd_rn(w, o);
-            }
-            if (lane == 0) red[32 * K + k] = w;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < K; ++k) out[k] = red[32 * K + k];
-    __syncthreads();
 }
-
+// second stage, thread 0 only (after a barrier)
 template <int K>
-__device__ __forceinline__ void reduce_int(int (&v)[K], int* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = __reduce_add_sync(0xffffffffu, v[k]);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
-    __syncthreads();
+__device__ __forceinline__ void block_tree_finish(const float* red, float (&out)[K]) {
+    const int nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        int s = 0;
-        for (int g = 0; g < nw; ++g) s += red[g * K + k];
-        v[k] = s;
+        float w[32];
+        for (int g = 0; g < nw; ++g) w[g] = red[g * K + k];
+        for (int off = nw / 2; off >= 1; off >>= 1)
+            for (int l = 0; l < off; ++l) w[l] = __fadd_rn(w[l], w[l + off]);
+        out[k] = w[0];
     }
-    __syncthreads();
-}
-
-template <int K>
-__device__ __forceinline__ void reduce_min(float (&v)[K], float* red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], off));
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        float m = red[k];
-        for (int g = 1; g < nw; ++g) m = fminf(m, red[g * K + k]);
-        v[k] = m;
-    }
-    __syncthreads();
 }
 
 __device__ __forceinline__ long long elem(int t, int bin, int p, int nsub, int npol, int nchan) {
@@ -319,23 +280,37 @@ __device__ __forceinline__ void prefetch_spectrum(float* buf, const float* data,
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// Values thread 0 derives from the scalar state and broadcasts.
+struct Bcast {
+    float dm_f, margin_f, sub_f, rms_f, params0;
+    int adapt, spectrum_clip, do_fill, rebuild_bp;
+};
+
 // One CTA per beam; blockDim.x == the partial count of the canonical sums.
 __global__ void __launch_bounds__(1024, 1)
 rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int nsub, int npol,
            int nchan, unsigned char* __restrict__ flags) {
     extern __shared__ float sh[];
+    __shared__ Bcast bc;
     const int nbins = cfg.nbins, H = cfg.history;
     const int P = blockDim.x;
-    float* bp = sh;                   // [nbins]
-    float* specs = sh + nbins;        // [2][nbins] double-buffered spectra
-    double* red = reinterpret_cast<double*>(sh + 3 * nbins + (nbins & 1));  // [33*16]
-    int* redi = reinterpret_cast<int*>(red + 33 * 16);                       // [32*8]
-    float* redf = reinterpret_cast<float*>(redi + 32 * 8);                   // [32*16]
-    const int tid = threadIdx.x;
+    float* bp = sh;                                 // [nbins]
+    float* specs = sh + nbins;                      // [2][nbins] double-buffered spectra
+    float* red = sh + 3 * nbins;                    // [32][16]
+    int* redi = reinterpret_cast<int*>(red + 32 * 16);  // [32][9]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nw = P >> 5;
     const int cpb = nbins / 8;
+    const double inv_h = 1.0 / (double)H;
 
-    RfiState st = *bufs.state;  // every thread keeps the same copy of the scalar state
-    for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, st.params0, i);
+    // The scalar running state lives in thread 0 only.
+    RfiState st;
+    if (tid == 0) {
+        st = *bufs.state;
+        bc.params0 = st.params0;
+    }
+    __syncthreads();
+    for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, bc.params0, i);
     if (nt > 0) prefetch_spectrum(specs, data, 0, nbins, nsub, npol, nchan);
 
     for (int t = 0; t < nt; ++t) {
@@ -347,10 +322,10 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
         __syncthreads();
-        double data_model;
-        double spectrum_rms = st.rms_carry;
-        if (st.rms_size < H) {
-            // adaptive phase, RFI_Clipper.cpp:214-278
+        // ---- margin and data model (RFI_Clipper.cpp:214-311) ----
+        if (tid == 0) bc.adapt = st.rms_size < H;
+        __syncthreads();
+        if (bc.adapt) {
             float mins[16], part[16];
 #pragma unroll
             for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
@@ -367,55 +342,67 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                     }
                 }
             }
-            double sums[16];
-            reduce_min<16>(mins, redf);
-            reduce_sum<16>(part, sums, red);
-            double sig_min = 0.0, dmm[8];
 #pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const double a = sums[8 + b] / cpb, m = sums[b] / cpb;
-                const double sg = sqrt(a - m * m);
-                sig_min = (b == 0 || sg < sig_min) ? sg : sig_min;
-                dmm[b] = (double)mins[b] - (double)mins[8 + b];
-            }
-            // the fifth smallest of the eight (std::nth_element at size/2)
+            for (int k = 0; k < 16; ++k)
 #pragma unroll
-            for (int i = 1; i < 8; ++i)
+                for (int off = 16; off >= 1; off >>= 1) mins[k] = fminf(mins[k], __shfl_xor_sync(0xffffffffu, mins[k], off));
+            warp_tree<16>(part, red);
+            float* redm = reinterpret_cast<float*>(redi + 32 * 9);  // [32][16]
+            if (lane == 0)
 #pragma unroll
-                for (int j = i; j > 0; --j) {
-                    const double lo = fmin(dmm[j - 1], dmm[j]), hi = fmax(dmm[j - 1], dmm[j]);
-                    dmm[j - 1] = lo;
-                    dmm[j] = hi;
+                for (int k = 0; k < 16; ++k) redm[warp * 16 + k] = mins[k];
+            __syncthreads();
+            if (tid == 0) {
+                float sums[16];
+                block_tree_finish<16>(red, sums);
+                float dmm[8], srms = 0.0f;
+                for (int b = 0; b < 8; ++b) {
+                    float md = redm[b], mm = redm[8 + b];
+                    for (int g = 1; g < nw; ++g) {
+                        md = fminf(md, redm[g * 16 + b]);
+                        mm = fminf(mm, redm[g * 16 + 8 + b]);
+                    }
+                    dmm[b] = __fsub_rn(md, mm);
+                    const float a = __fdiv_rn(sums[8 + b], (float)cpb);
+                    const float m = __fdiv_rn(sums[b], (float)cpb);
+                    const float sg = __fsqrt_rn(__fsub_rn(a, __fmul_rn(m, m)));
+                    srms = (b == 0 || sg < srms) ? sg : srms;
                 }
-            spectrum_rms = sig_min;
-            data_model = dmm[4];
-            const int pos = (st.rms_head + st.rms_size) % H;
-            if (tid == 0) bufs.rms_buf[pos] = spectrum_rms;
-            st.rms_acc_prev = st.rms_acc;
-            st.rms_acc = st.rms_acc + spectrum_rms;
-            st.rms_size += 1;
-            st.rms_run = st.rms_acc / st.rms_size;
-            if (st.rms_size == H) st.mean_over_rms = st.mean_run / st.rms_run;
-            data_model = data_model + cfg.mmm * st.rms_run;
-        } else {
-            // steady phase, RFI_Clipper.cpp:279-307
+                for (int i = 1; i < 8; ++i)  // insertion sort: dmm[4] is the fifth smallest
+                    for (int j = i; j > 0 && dmm[j - 1] > dmm[j]; --j) {
+                        const float x = dmm[j]; dmm[j] = dmm[j - 1]; dmm[j - 1] = x;
+                    }
+                const int pos = (st.rms_head + st.rms_size) % H;
+                bufs.rms_buf[pos] = (double)srms;
+                st.rms_acc_prev = st.rms_acc;
+                st.rms_acc = st.rms_acc + (double)srms;
+                st.rms_size += 1;
+                st.rms_run = st.rms_acc / (double)st.rms_size;
+                if (st.rms_size == H) {
+                    st.mean_over_rms = st.mean_run / st.rms_run;
+                    st.inv_mor = 1.0 / st.mean_over_rms;
+                }
+                bc.dm_f = __fadd_rn(dmm[4], __fmul_rn(cfg.mmm_f, (float)st.rms_run));
+                bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
+            }
+        } else if (tid == 0) {
             const double front = bufs.rms_buf[st.rms_head];
             const double back = bufs.rms_buf[(st.rms_head + st.rms_size - 1) % H];
-            st.rms_run -= front / (double)st.rms_size;
-            st.rms_run += back / (double)H;
-            if (cfg.use_mor) spectrum_rms = fabs(st.mean_run / st.mean_over_rms);
-            __syncthreads();
-            if (tid == 0) bufs.rms_buf[st.rms_head] = spectrum_rms;  // full: overwrite the oldest
+            st.rms_run = st.rms_run - front * inv_h;
+            st.rms_run = st.rms_run + back * inv_h;
+            const double spectrum_rms = cfg.use_mor ? fabs(st.mean_run * st.inv_mor) : st.rms_carry;
+            bufs.rms_buf[st.rms_head] = spectrum_rms;  // full: overwrite the oldest
             st.rms_head = (st.rms_head + 1) % H;
-            data_model = 0.0;
+            bc.dm_f = 0.0f;
+            bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
         }
-        const float dm_f = (float)data_model;
-        const float margin_f = (float)((double)cfg.cr * st.rms_run);
-        // channel clipping, RFI_Clipper.cpp:313-342 (FP32 as the reference)
+        __syncthreads();
+        const float dm_f = bc.dm_f, margin_f = bc.margin_f;
+        // ---- channel clipping (RFI_Clipper.cpp:313-342), FP32 as the reference ----
         float gpart[1] = {0.0f};
-        int good[8];
+        int good[9];
 #pragma unroll
-        for (int b = 0; b < 8; ++b) good[b] = 0;
+        for (int b = 0; b < 9; ++b) good[b] = 0;
         for (int i = tid; i < nbins; i += P) {
             const float v = spec[i];
             const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[i]) > margin_f;
@@ -431,91 +418,135 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             }
             if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
         }
-        double gsum[1];
-        reduce_sum<1>(gpart, gsum, red);
-        reduce_int<8>(good, redi);
-        int total_good = 0;
+        warp_tree<1>(gpart, red);
 #pragma unroll
-        for (int b = 0; b < 8; ++b) total_good += good[b];
-        st.frac_bad_channels += (float)(nbins - total_good) / (float)nbins;
-        const double spectrum_sum = gsum[0] / (double)total_good;
-        int bad_bands = 0;
+        for (int k = 0; k < 8; ++k) good[k] = __reduce_add_sync(0xffffffffu, good[k]);
+        if (lane == 0)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) {
-            if ((double)good[b] < 0.8 * cpb) ++bad_bands;
-            if (good[b] == 0) bad_bands += 4;
-        }
-        if ((double)total_good < 0.8 * nbins) bad_bands += 4;
-        // mean history, RFI_Clipper.cpp:383-400
-        if (st.mean_size < H) {
-            const int pos = (st.mean_head + st.mean_size) % H;
-            if (tid == 0) bufs.mean_buf[pos] = spectrum_sum;
-            st.mean_acc_prev = st.mean_acc;
-            st.mean_acc = st.mean_acc + spectrum_sum;
-            st.mean_size += 1;
-            st.mean_run = st.mean_acc / st.mean_size;
-        } else {
-            const double front = bufs.mean_buf[st.mean_head];
-            const double back = bufs.mean_buf[(st.mean_head + st.mean_size - 1) % H];
-            st.mean_run -= front / (double)st.mean_size;
-            st.mean_run += back / (double)st.mean_size;
-            __syncthreads();  // every thread has read front/back before the overwrite
-            if (tid == 0) bufs.mean_buf[st.mean_head] = spectrum_sum;
-            st.mean_head = (st.mean_head + 1) % H;
-        }
-        __syncthreads();  // history writes visible
-        const double tol = (double)cfg.sr * (double)st.bp_rms / cfg.sqrt_nbins;
-        bool spectrum_clip = false;
-        if (st.mean_size < 1000) {
-            spectrum_clip = true;
-        } else if (spectrum_sum - st.mean_run > tol || bad_bands >= 4) {
-            spectrum_clip = true;
-            st.bad_spectra += 1;
-            // pop_back + push_back(back()): the newest entry takes the previous one's value
-            const int mlast = (st.mean_head + st.mean_size - 1) % H;
-            const int rlast = (st.rms_head + st.rms_size - 1) % H;
-            const double mprev = bufs.mean_buf[(mlast + H - 1) % H];
-            const double rprev = bufs.rms_buf[(rlast + H - 1) % H];
-            __syncthreads();
-            if (tid == 0) { bufs.mean_buf[mlast] = mprev; bufs.rms_buf[rlast] = rprev; }
-            st.mean_acc = st.mean_acc_prev + mprev;
-            st.rms_acc = st.rms_acc_prev + rprev;
-            __syncthreads();
-        } else if (st.remaining_zeros != 0) {
-            int filled[1] = {0};
-            for (int i = tid; i < nbins; i += P) {
-                const float v = spec[i];
-                if (bufs.last_good[i] == 0.0f && v != 0.0f) {
-                    bufs.last_good[i] = v;
-                    filled[0] += 1;
-                }
+            for (int k = 0; k < 8; ++k) redi[warp * 9 + k] = good[k];
+        __syncthreads();
+        if (tid == 0) {
+            float g[1];
+            block_tree_finish<1>(red, g);
+            int gb[8], total_good = 0;
+            for (int k = 0; k < 8; ++k) {
+                int sum = 0;
+                for (int w = 0; w < nw; ++w) sum += redi[w * 9 + k];
+                gb[k] = sum;
+                total_good += sum;
             }
-            reduce_int<1>(filled, redi);
-            st.remaining_zeros -= filled[0];
-        }
-        if (spectrum_clip) {  // clipSample, RFI_Clipper.cpp:127-150
-            for (int i = tid; i < nbins; i += P) {
-                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = -0.2f;
-                spec[i] = -0.2f;
-                if (flags) flags[(long long)t * nbins + i] |= 2;
+            st.frac_bad_channels = __fadd_rn(st.frac_bad_channels,
+                                             __fdiv_rn((float)(nbins - total_good), (float)nbins));
+            const float spectrum_sum = __fdiv_rn(g[0], (float)total_good);
+            int bad_bands = 0;
+            for (int b = 0; b < 8; ++b) {
+                if ((double)gb[b] < 0.8 * cpb) ++bad_bands;
+                if (gb[b] == 0) bad_bands += 4;
             }
+            if ((double)total_good < 0.8 * nbins) bad_bands += 4;
+            // mean history (RFI_Clipper.cpp:383-400)
+            if (st.mean_size < H) {
+                const int pos = (st.mean_head + st.mean_size) % H;
+                bufs.mean_buf[pos] = (double)spectrum_sum;
+                st.mean_acc_prev = st.mean_acc;
+                st.mean_acc = st.mean_acc + (double)spectrum_sum;
+                st.mean_size += 1;
+                st.mean_run = st.mean_acc / (double)st.mean_size;
+            } else {
+                const double front = bufs.mean_buf[st.mean_head];
+                const double back = bufs.mean_buf[(st.mean_head + st.mean_size - 1) % H];
+                st.mean_run = st.mean_run - front * inv_h;
+                st.mean_run = st.mean_run + back * inv_h;
+                bufs.mean_buf[st.mean_head] = (double)spectrum_sum;
+                st.mean_head = (st.mean_head + 1) % H;
+            }
+            const float tol = (float)((double)__fmul_rn(cfg.sr, st.bp_rms) * cfg.inv_sqrt_nbins);
+            int sclip = 0, fill = 0;
+            if (st.mean_size < 1000) {
+                sclip = 1;
+            } else if ((double)spectrum_sum - st.mean_run > (double)tol || bad_bands >= 4) {
+                sclip = 1;
+                st.bad_spectra += 1;
+                // pop_back + push_back(back()): the newest entry takes the previous one's value
+                const int mlast = (st.mean_head + st.mean_size - 1) % H;
+                const int rlast = (st.rms_head + st.rms_size - 1) % H;
+                const double mprev = bufs.mean_buf[(mlast + H - 1) % H];
+                const double rprev = bufs.rms_buf[(rlast + H - 1) % H];
+                bufs.mean_buf[mlast] = mprev;
+                bufs.rms_buf[rlast] = rprev;
+                st.mean_acc = st.mean_acc_prev + mprev;
+                st.rms_acc = st.rms_acc_prev + rprev;
+            } else if (st.remaining_zeros != 0) {
+                fill = 1;
+            }
+            bc.spectrum_clip = sclip;
+            bc.do_fill = fill;
         }
-        // flatten and normalise, RFI_Clipper.cpp:478-532 (FP32 per channel)
+        __syncthreads();
+        const bool spectrum_clip = bc.spectrum_clip != 0;
+        // ---- last good spectrum, clipSample, flatten (RFI_Clipper.cpp:441-494) ----
+        int filled = 0;
         float s12[2] = {0.0f, 0.0f};
         for (int i = tid; i < nbins; i += P) {
-            const float v = __fsub_rn(spec[i], __fadd_rn(bp[i], dm_f));
+            float v = spec[i];
+            if (bc.do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
+                bufs.last_good[i] = v;
+                ++filled;
+            }
+            if (spectrum_clip) {
+                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = -0.2f;
+                v = -0.2f;
+                if (flags) flags[(long long)t * nbins + i] |= 2;
+            }
+            v = __fsub_rn(v, __fadd_rn(bp[i], dm_f));
             spec[i] = v;
             s12[0] = __fadd_rn(s12[0], v);
             s12[1] = __fadd_rn(s12[1], __fmul_rn(v, v));
         }
-        double sums2[2];
-        reduce_sum<2>(s12, sums2, red);
-        const double m = sums2[0] / nbins;
-        double rms = sqrt(sums2[1] / nbins - m * m);
-        if (rms == 0.0) rms = 1.0;
-        st.rms_carry = rms;
-        const float sub_f = (float)(cfg.zero_dming == 1 ? m : st.mean_run);
-        const float rms_f = (float)rms;
+        warp_tree<2>(s12, red);
+        filled = __reduce_add_sync(0xffffffffu, filled);
+        if (lane == 0) redi[warp * 9 + 8] = filled;
+        __syncthreads();
+        if (tid == 0) {
+            float sums[2];
+            block_tree_finish<2>(red, sums);
+            for (int w = 0; w < nw; ++w) st.remaining_zeros -= redi[w * 9 + 8];
+            const float m = __fdiv_rn(sums[0], (float)nbins);
+            const float ms = __fdiv_rn(sums[1], (float)nbins);
+            float srms = __fsqrt_rn(__fsub_rn(ms, __fmul_rn(m, m)));
+            if (srms == 0.0f) srms = 1.0f;
+            st.rms_carry = (double)srms;
+            bc.sub_f = cfg.zero_dming == 1 ? m : (float)st.mean_run;
+            bc.rms_f = srms;
+            // statistics (RFI_Clipper.cpp:535-560)
+            if (st.num == 0) {
+                const float frac = (float)(100.0 * (float)st.bad_spectra / (float)(10 * H));
+                if (frac > 99.0f) {
+                    st.mean_size = st.rms_size = 0;
+                    st.mean_head = st.rms_head = 0;
+                    st.mean_acc = st.mean_acc_prev = st.rms_acc = st.rms_acc_prev = 0.0;
+                }
+                st.bad_spectra = 0;
+                st.frac_bad_channels = 0.0f;
+            }
+            // BandPass::setMean / setRMS (BandPass.cpp:44-74)
+            const float mean_f = (float)st.mean_run;
+            const float delta = __fsub_rn(mean_f, st.bp_mean);
+            bc.rebuild_bp = 0;
+            if (fabsf(delta) > 0.0f) {
+                st.params0 = __fadd_rn(st.params0, __fdiv_rn(delta, cfg.scale));
+                st.bp_mean = mean_f;
+                bc.rebuild_bp = 1;
+                bc.params0 = st.params0;
+            }
+            st.bp_rms = (float)st.rms_run;
+            st.num = (st.num + 1) % (10 * H);
+        }
+        __syncthreads();
+        // ---- normalise and store (RFI_Clipper.cpp:507-532) ----
+        const float sub_f = bc.sub_f, rms_f = bc.rms_f;
+        const bool rebuild = bc.rebuild_bp != 0;
+        const float p0 = bc.params0;
         for (int i = tid; i < nbins; i += P) {
             float v = spec[i];
             if (!spectrum_clip) {
@@ -523,28 +554,8 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                 if (v > cfg.cr) v = 0.0f;
             }
             data[elem(t, i, 0, nsub, npol, nchan)] = v;
+            if (rebuild) bp[i] = bp_value(cfg, bufs, p0, i);
         }
-        // statistics, RFI_Clipper.cpp:535-560
-        if (st.num == 0) {
-            const float frac = (float)(100.0 * (float)st.bad_spectra / (float)(10 * H));
-            if (frac > 99.0) {
-                st.mean_size = st.rms_size = 0;
-                st.mean_head = st.rms_head = 0;
-                st.mean_acc = st.mean_acc_prev = st.rms_acc = st.rms_acc_prev = 0.0;
-            }
-            st.bad_spectra = 0;
-            st.frac_bad_channels = 0.0f;
-        }
-        // BandPass::setMean / setRMS (BandPass.cpp:44-74)
-        const float mean_f = (float)st.mean_run;
-        const float delta = mean_f - st.bp_mean;
-        if (fabsf(delta) > 0.0f) {
-            st.params0 = st.params0 + delta / cfg.scale;
-            st.bp_mean = mean_f;
-            for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, st.params0, i);
-        }
-        st.bp_rms = (float)st.rms_run;
-        st.num = (st.num + 1) % (10 * H);
         __syncthreads();
     }
     if (tid == 0) *bufs.state = st;
@@ -626,8 +637,8 @@ int setup(pv_rfi* h, int nbins, cudaStream_t s) {
     h->cfg.cr = h->cr;
     h->cfg.sr = h->sr;
     h->cfg.scale = scale;
-    h->cfg.mmm = 4.0 / std::sqrt(8.0);  // k/sqrt(2k) with k = 4 degrees of freedom
-    h->cfg.sqrt_nbins = std::sqrt((double)nbins);
+    h->cfg.mmm_f = (float)(4.0f / std::sqrt(2.0 * 4.0f));  // k/sqrt(2k), k = 4 degrees of freedom
+    h->cfg.inv_sqrt_nbins = 1.0 / std::sqrt((double)nbins);
     RfiState st{};
     st.remaining_zeros = nbins;
     st.params0 = h->bp.params[0];
@@ -712,8 +723,8 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     PV_TRY(setup(h, nbins, s));
     if (nt == 0) return PV_OK;
     const int threads = pv_rfi_parts(nbins);
-    const size_t smem = sizeof(float) * (3 * (size_t)nbins + 2) + sizeof(double) * 33 * 16 +
-                        sizeof(int) * 32 * 8 + sizeof(float) * 32 * 16;
+    const size_t smem = sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 +
+                        sizeof(int) * 32 * 9 + sizeof(float) * 32 * 16;
     if (smem > 227 * 1024) {
         pv::set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
         return PV_ERR_ARG;
