@@ -168,6 +168,32 @@ int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp, float thr
                float rms, int bin_pow2, pv_event* d_events, long long cap,
                long long* h_count, void* stream);
 
+/* pv_analyse for callers that cannot allocate device memory.  This entry
+ * point has no counterpart in the reference.  It exists for code that must
+ * not call cudaMalloc once it runs: a real-time beam pipeline whose device
+ * memory was reserved up front under a fixed HBM budget (an allocation there
+ * would break the budget and stall the stream), or a host embedded in a
+ * framework that owns the device allocator.
+ *
+ * Same arguments and results as pv_analyse.  Its scratch (per-block event
+ * counts, offsets and scan workspace) is a fixed array in device memory
+ * that every GPU loading the library keeps until the process exits.  It
+ * holds at most PV_ANALYSE_NOALLOC_MAX_PAIRS (trial, block) pairs, i.e.
+ * tdms * floor(nsamp / 2^bin_pow2) <= 1,048,576, about 12.6 MB; larger calls
+ * return PV_ERR_ARG and a message naming the limit.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *
+ * The first call on each device looks up the array's device address with
+ * that device current; make that first call before any stream capture.
+ * Every call on a device shares the one array, so calls that overlap on the
+ * GPU (other streams, other host threads) race and corrupt each other's
+ * results; serialise them.  Nothing in the array needs clearing between
+ * calls: each launch writes everything it reads. */
+#define PV_ANALYSE_NOALLOC_MAX_PAIRS (1 << 20)
+int pv_analyse_noalloc(const float* d_data, long long ld, int tdms, int nsamp, float threshold,
+                       float rms, int bin_pow2, pv_event* d_events, long long cap,
+                       long long* h_count, void* stream);
+
 /* ------------------------------------------------------------------------
  * A2/A3 PPFChanneliser (lib/src/PPFChanneliser.cpp:29-290,
  * lib/src/PolyphaseCoefficients.cpp:77-364), A4 StokesGenerator

@@ -13,6 +13,7 @@
 // writes the events in the reference order.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "pv_common.cuh"
@@ -286,4 +287,87 @@ extern "C" int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp
     }
     pv::scratch_free(scratch, s);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// pv_analyse_noalloc: the analyser with its scratch in a fixed device array
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr long long noalloc_scan_workspace(long long n) {
+    return n > 1 ? 2 * ((n + kScanBlock - 1) / kScanBlock) +
+                       noalloc_scan_workspace((n + kScanBlock - 1) / kScanBlock)
+                 : 0;
+}
+constexpr size_t kNoAllocPairs = PV_ANALYSE_NOALLOC_MAX_PAIRS;
+constexpr size_t kNoAllocScratch =
+    ((kNoAllocPairs * (sizeof(int) + sizeof(long long)) +
+      (size_t)(noalloc_scan_workspace((long long)kNoAllocPairs) + 2) * sizeof(long long) + 256 +
+      255) / 256) * 256;
+// Scratch (counts, offsets, scan workspace) followed by the event total.
+// Every GPU that loads the library keeps this array until the process exits.
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch + 256];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device.  The host-side
+// name is only a stand-in, so the address is looked up once per device with
+// that device current.
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    PV_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) {
+        pv::set_error("pv_analyse_noalloc: device %d out of range", dev);
+        return PV_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            pv::set_error("pv_analyse_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return PV_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return PV_OK;
+}
+
+}  // namespace
+
+extern "C" int pv_analyse_noalloc(const float* d_data, long long ld, int tdms, int nsamp,
+                                  float threshold, float rms, int bin_pow2, pv_event* d_events,
+                                  long long cap, long long* h_count, void* stream) {
+    if (!h_count || tdms < 0 || nsamp < 0 || ld < nsamp || (cap > 0 && !d_events) ||
+        (tdms > 0 && nsamp > 0 && !d_data)) {
+        pv::set_error("pv_analyse_noalloc: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    if (bin_pow2 < 0 || bin_pow2 > kMaxPow2) {
+        pv::set_error("pv_analyse_noalloc: power2ForBinning must be in 0..%d", kMaxPow2);
+        return PV_ERR_ARG;
+    }
+    const long long pairs = (long long)tdms * (nsamp >> bin_pow2);
+    const size_t need = pv::analyse_scratch_bytes(tdms, nsamp, bin_pow2);
+    if (pairs > (long long)kNoAllocPairs || need > kNoAllocScratch) {
+        pv::set_error("pv_analyse_noalloc: %d trials x %d blocks of 2^%d samples = %lld pairs "
+                      "exceeds the fixed scratch limit of %lld pairs; use pv_analyse",
+                      tdms, nsamp >> bin_pow2, bin_pow2, pairs, (long long)kNoAllocPairs);
+        return PV_ERR_ARG;
+    }
+    void* scratch = nullptr;
+    PV_TRY(noalloc_scratch(&scratch));
+    // Nothing in the scratch needs clearing: the launch writes every count,
+    // offset, workspace entry and the total before it reads them.
+    long long* d_total = reinterpret_cast<long long*>(static_cast<char*>(scratch) + kNoAllocScratch);
+    cudaStream_t s = pv::as_stream(stream);
+    PV_TRY(pv::analyse_launch(d_data, ld, tdms, nsamp, threshold, rms, bin_pow2, d_events, cap,
+                              d_total, scratch, s));
+    PV_CUDA(cudaMemcpyAsync(h_count, d_total, sizeof(long long), cudaMemcpyDeviceToHost, s),
+            "read event count");
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+    return PV_OK;
 }
