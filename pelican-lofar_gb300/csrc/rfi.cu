@@ -280,57 +280,151 @@ __device__ __forceinline__ void prefetch_spectrum(float* buf, const float* data,
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-// Values thread 0 derives from the scalar state and broadcasts.
+// Values warp 0 derives from the scalar state and broadcasts.
 struct Bcast {
-    float dm_f, margin_f, sub_f, rms_f, params0;
-    int adapt, spectrum_clip, do_fill, rebuild_bp;
+    float dm_f, margin_f;        // for the next clip pass
+    float sub_f, rms_f, params0; // for the normalise pass
+    int adapt;                   // next spectrum starts in the adaptive phase
+    int spectrum_clip, do_fill, rebuild_bp;
 };
 
+// Channel geometry: bin -> pol-0 element offset within a spectrum, and band.
+struct Geo {
+    int nsub, npol, nchan, lg_nchan;  // lg_nchan < 0: nchan is not a power of two
+    int cpb;
+    __device__ __forceinline__ long long off(int bin) const {
+        int sb, c;
+        if (lg_nchan >= 0) { sb = bin >> lg_nchan; c = bin & (nchan - 1); }
+        else { sb = bin / nchan; c = bin - sb * nchan; }
+        return ((long long)sb * npol) * nchan + c;
+    }
+    __device__ __forceinline__ int band(int bin) const {
+        int b = 0;
+#pragma unroll
+        for (int k = 1; k < 8; ++k) b += bin >= k * cpb;
+        return b;
+    }
+};
+
+// Warp-0 tree over the NW warp partials red[g*K + k] (canonical second stage);
+// every lane of warp 0 returns the total.
+__device__ __forceinline__ float warp0_tree(const float* red, int K, int k, int nw) {
+    const int lane = threadIdx.x & 31;
+    float w = lane < nw ? red[lane * K + k] : 0.0f;
+    for (int off = nw / 2; off >= 1; off >>= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, w, off);
+        if (lane < off) w = __fadd_rn(w, o);
+    }
+    return __shfl_sync(0xffffffffu, w, 0);
+}
+__device__ __forceinline__ int warp0_isum(const int* redi, int K, int k, int nw) {
+    const int lane = threadIdx.x & 31;
+    return __reduce_add_sync(0xffffffffu, lane < nw ? redi[lane * K + k] : 0);
+}
+__device__ __forceinline__ float warp0_min(const float* redm, int K, int k, int nw) {
+    const int lane = threadIdx.x & 31;
+    float m = lane < nw ? redm[lane * K + k] : 1e30f;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    return m;
+}
+
+// History rings of the running averages as warp 0 sees them: the newest two
+// entries and the prefetched oldest entry stay in registers.
+struct Hist {
+    double last, prev, front;
+};
+
+// Steady-phase start of a spectrum (RFI_Clipper.cpp:279-307), run by warp 0
+// at the end of the previous spectrum: update rmsRunAve, push the spectrum's
+// RMS estimate and derive the channel margin.
+__device__ __forceinline__ void steady_start(RfiState& st, Hist& hr, const RfiConfig& cfg,
+                                             const RfiBuffers& bufs, double inv_h, Bcast& bc) {
+    const int H = cfg.history;
+    const int lane = threadIdx.x & 31;
+    st.rms_run = st.rms_run - hr.front * inv_h;
+    st.rms_run = st.rms_run + hr.last * inv_h;
+    const double spectrum_rms = cfg.use_mor ? fabs(st.mean_run * st.inv_mor) : st.rms_carry;
+    if (lane == 0) bufs.rms_buf[st.rms_head] = spectrum_rms;  // full: overwrite the oldest
+    st.rms_head = (st.rms_head + 1) % H;
+    hr.prev = hr.last;
+    hr.last = spectrum_rms;
+    hr.front = bufs.rms_buf[st.rms_head];  // oldest entry for the spectrum after next
+    if (lane == 0) {
+        bc.dm_f = 0.0f;
+        bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
+        bc.adapt = 0;
+    }
+}
+
 // One CTA per beam; blockDim.x == the partial count of the canonical sums.
+// Each thread owns channels tid, tid+P, ... in every pass, so per-channel data
+// (the spectrum, the bandpass, the last good value) never crosses threads and
+// the passes of consecutive spectra need barriers only around the block
+// reductions and warp 0's scalar work.
 __global__ void __launch_bounds__(1024, 1)
-rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int nsub, int npol,
-           int nchan, unsigned char* __restrict__ flags) {
+rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, Geo geo,
+           unsigned char* __restrict__ flags) {
     extern __shared__ float sh[];
     __shared__ Bcast bc;
     const int nbins = cfg.nbins, H = cfg.history;
     const int P = blockDim.x;
-    float* bp = sh;                                 // [nbins]
-    float* specs = sh + nbins;                      // [2][nbins] double-buffered spectra
-    float* red = sh + 3 * nbins;                    // [32][16]
-    int* redi = reinterpret_cast<int*>(red + 32 * 16);  // [32][9]
+    float* bp = sh;                                      // [nbins]
+    float* specs = sh + nbins;                           // [2][nbins]
+    float* red = sh + 3 * nbins;                         // [32][16]
+    float* redm = red + 32 * 16;                         // [32][16]
+    int* redi = reinterpret_cast<int*>(redm + 32 * 16);  // [32][9]
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nw = P >> 5;
-    const int cpb = nbins / 8;
     const double inv_h = 1.0 / (double)H;
+    const long long spec_elems = (long long)geo.nsub * geo.npol * geo.nchan;
 
-    // The scalar running state lives in thread 0 only.
-    RfiState st;
-    if (tid == 0) {
+    RfiState st;   // warp 0 only (every lane the same)
+    Hist hm, hr;   // mean and rms rings, warp 0 only
+    if (warp == 0) {
         st = *bufs.state;
-        bc.params0 = st.params0;
+        hm.last = st.mean_size > 0 ? bufs.mean_buf[(st.mean_head + st.mean_size - 1) % H] : 0.0;
+        hm.prev = st.mean_size > 1 ? bufs.mean_buf[(st.mean_head + st.mean_size - 2) % H] : 0.0;
+        hm.front = bufs.mean_buf[st.mean_head];
+        hr.last = st.rms_size > 0 ? bufs.rms_buf[(st.rms_head + st.rms_size - 1) % H] : 0.0;
+        hr.prev = st.rms_size > 1 ? bufs.rms_buf[(st.rms_head + st.rms_size - 2) % H] : 0.0;
+        hr.front = bufs.rms_buf[st.rms_head];
+        if (lane == 0) bc.params0 = st.params0;
+        if (nt > 0) {
+            if (st.rms_size < H) {
+                if (lane == 0) bc.adapt = 1;
+            } else {
+                steady_start(st, hr, cfg, bufs, inv_h, bc);
+            }
+        }
     }
     __syncthreads();
     for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, bc.params0, i);
-    if (nt > 0) prefetch_spectrum(specs, data, 0, nbins, nsub, npol, nchan);
+    auto prefetch = [&](int t) {
+        float* buf = specs + (t & 1) * nbins;
+        const float* src = data + (long long)t * spec_elems;
+        for (int i = tid; i < nbins; i += P) cp_async4(buf + i, src + geo.off(i));
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    if (nt > 0) prefetch(0);
 
     for (int t = 0; t < nt; ++t) {
         float* spec = specs + (t & 1) * nbins;
+        float* dst = data + (long long)t * spec_elems;
+        // the spectrum's channels are this thread's own copies: no barrier needed
         if (t + 1 < nt) {
-            prefetch_spectrum(specs + ((t + 1) & 1) * nbins, data, t + 1, nbins, nsub, npol, nchan);
+            prefetch(t + 1);
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");
         } else {
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
-        __syncthreads();
-        // ---- margin and data model (RFI_Clipper.cpp:214-311) ----
-        if (tid == 0) bc.adapt = st.rms_size < H;
-        __syncthreads();
+        // ---- adaptive phase start, RFI_Clipper.cpp:214-278 ----
         if (bc.adapt) {
             float mins[16], part[16];
 #pragma unroll
             for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
             for (int i = tid; i < nbins; i += P) {
-                const int band = i / cpb;
+                const int band = geo.band(i);
                 const float v = spec[i];
 #pragma unroll
                 for (int b = 0; b < 8; ++b) {
@@ -347,24 +441,20 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
 #pragma unroll
                 for (int off = 16; off >= 1; off >>= 1) mins[k] = fminf(mins[k], __shfl_xor_sync(0xffffffffu, mins[k], off));
             warp_tree<16>(part, red);
-            float* redm = reinterpret_cast<float*>(redi + 32 * 9);  // [32][16]
             if (lane == 0)
 #pragma unroll
                 for (int k = 0; k < 16; ++k) redm[warp * 16 + k] = mins[k];
             __syncthreads();
-            if (tid == 0) {
-                float sums[16];
-                block_tree_finish<16>(red, sums);
+            if (warp == 0) {
                 float dmm[8], srms = 0.0f;
                 for (int b = 0; b < 8; ++b) {
-                    float md = redm[b], mm = redm[8 + b];
-                    for (int g = 1; g < nw; ++g) {
-                        md = fminf(md, redm[g * 16 + b]);
-                        mm = fminf(mm, redm[g * 16 + 8 + b]);
-                    }
+                    const float s1 = warp0_tree(red, 16, b, nw);
+                    const float s2 = warp0_tree(red, 16, 8 + b, nw);
+                    const float md = warp0_min(redm, 16, b, nw);
+                    const float mm = warp0_min(redm, 16, 8 + b, nw);
                     dmm[b] = __fsub_rn(md, mm);
-                    const float a = __fdiv_rn(sums[8 + b], (float)cpb);
-                    const float m = __fdiv_rn(sums[b], (float)cpb);
+                    const float a = __fdiv_rn(s2, (float)geo.cpb);
+                    const float m = __fdiv_rn(s1, (float)geo.cpb);
                     const float sg = __fsqrt_rn(__fsub_rn(a, __fmul_rn(m, m)));
                     srms = (b == 0 || sg < srms) ? sg : srms;
                 }
@@ -373,7 +463,7 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                         const float x = dmm[j]; dmm[j] = dmm[j - 1]; dmm[j - 1] = x;
                     }
                 const int pos = (st.rms_head + st.rms_size) % H;
-                bufs.rms_buf[pos] = (double)srms;
+                if (lane == 0) bufs.rms_buf[pos] = (double)srms;
                 st.rms_acc_prev = st.rms_acc;
                 st.rms_acc = st.rms_acc + (double)srms;
                 st.rms_size += 1;
@@ -382,37 +472,33 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                     st.mean_over_rms = st.mean_run / st.rms_run;
                     st.inv_mor = 1.0 / st.mean_over_rms;
                 }
-                bc.dm_f = __fadd_rn(dmm[4], __fmul_rn(cfg.mmm_f, (float)st.rms_run));
-                bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
+                hr.prev = hr.last;
+                hr.last = (double)srms;
+                hr.front = bufs.rms_buf[st.rms_head];
+                if (lane == 0) {
+                    bc.dm_f = __fadd_rn(dmm[4], __fmul_rn(cfg.mmm_f, (float)st.rms_run));
+                    bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
+                }
             }
-        } else if (tid == 0) {
-            const double front = bufs.rms_buf[st.rms_head];
-            const double back = bufs.rms_buf[(st.rms_head + st.rms_size - 1) % H];
-            st.rms_run = st.rms_run - front * inv_h;
-            st.rms_run = st.rms_run + back * inv_h;
-            const double spectrum_rms = cfg.use_mor ? fabs(st.mean_run * st.inv_mor) : st.rms_carry;
-            bufs.rms_buf[st.rms_head] = spectrum_rms;  // full: overwrite the oldest
-            st.rms_head = (st.rms_head + 1) % H;
-            bc.dm_f = 0.0f;
-            bc.margin_f = __fmul_rn(cfg.cr, (float)st.rms_run);
+            __syncthreads();
         }
-        __syncthreads();
         const float dm_f = bc.dm_f, margin_f = bc.margin_f;
         // ---- channel clipping (RFI_Clipper.cpp:313-342), FP32 as the reference ----
         float gpart[1] = {0.0f};
-        int good[9];
+        int good[8];
 #pragma unroll
-        for (int b = 0; b < 9; ++b) good[b] = 0;
+        for (int b = 0; b < 8; ++b) good[b] = 0;
         for (int i = tid; i < nbins; i += P) {
             const float v = spec[i];
             const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[i]) > margin_f;
             if (clip) {
                 const float lg = bufs.last_good[i];
-                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = lg;
+                const long long o = geo.off(i);
+                for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = lg;
                 spec[i] = lg;
             } else {
                 gpart[0] = __fadd_rn(gpart[0], v);
-                const int band = i / cpb;
+                const int band = geo.band(i);
 #pragma unroll
                 for (int b = 0; b < 8; ++b) good[b] += (b == band);
             }
@@ -425,41 +511,40 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
 #pragma unroll
             for (int k = 0; k < 8; ++k) redi[warp * 9 + k] = good[k];
         __syncthreads();
-        if (tid == 0) {
-            float g[1];
-            block_tree_finish<1>(red, g);
+        // ---- warp 0: spectrum mean, history, rejection (RFI_Clipper.cpp:343-470) ----
+        if (warp == 0) {
+            const float gsum = warp0_tree(red, 1, 0, nw);
             int gb[8], total_good = 0;
+#pragma unroll
             for (int k = 0; k < 8; ++k) {
-                int sum = 0;
-                for (int w = 0; w < nw; ++w) sum += redi[w * 9 + k];
-                gb[k] = sum;
-                total_good += sum;
+                gb[k] = warp0_isum(redi, 9, k, nw);
+                total_good += gb[k];
             }
             st.frac_bad_channels = __fadd_rn(st.frac_bad_channels,
                                              __fdiv_rn((float)(nbins - total_good), (float)nbins));
-            const float spectrum_sum = __fdiv_rn(g[0], (float)total_good);
+            const float spectrum_sum = __fdiv_rn(gsum, (float)total_good);
             int bad_bands = 0;
+#pragma unroll
             for (int b = 0; b < 8; ++b) {
-                if ((double)gb[b] < 0.8 * cpb) ++bad_bands;
+                if ((double)gb[b] < 0.8 * geo.cpb) ++bad_bands;
                 if (gb[b] == 0) bad_bands += 4;
             }
             if ((double)total_good < 0.8 * nbins) bad_bands += 4;
-            // mean history (RFI_Clipper.cpp:383-400)
             if (st.mean_size < H) {
                 const int pos = (st.mean_head + st.mean_size) % H;
-                bufs.mean_buf[pos] = (double)spectrum_sum;
+                if (lane == 0) bufs.mean_buf[pos] = (double)spectrum_sum;
                 st.mean_acc_prev = st.mean_acc;
                 st.mean_acc = st.mean_acc + (double)spectrum_sum;
                 st.mean_size += 1;
                 st.mean_run = st.mean_acc / (double)st.mean_size;
             } else {
-                const double front = bufs.mean_buf[st.mean_head];
-                const double back = bufs.mean_buf[(st.mean_head + st.mean_size - 1) % H];
-                st.mean_run = st.mean_run - front * inv_h;
-                st.mean_run = st.mean_run + back * inv_h;
-                bufs.mean_buf[st.mean_head] = (double)spectrum_sum;
+                st.mean_run = st.mean_run - hm.front * inv_h;
+                st.mean_run = st.mean_run + hm.last * inv_h;
+                if (lane == 0) bufs.mean_buf[st.mean_head] = (double)spectrum_sum;
                 st.mean_head = (st.mean_head + 1) % H;
             }
+            hm.prev = hm.last;
+            hm.last = (double)spectrum_sum;
             const float tol = (float)((double)__fmul_rn(cfg.sr, st.bp_rms) * cfg.inv_sqrt_nbins);
             int sclip = 0, fill = 0;
             if (st.mean_size < 1000) {
@@ -470,31 +555,38 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                 // pop_back + push_back(back()): the newest entry takes the previous one's value
                 const int mlast = (st.mean_head + st.mean_size - 1) % H;
                 const int rlast = (st.rms_head + st.rms_size - 1) % H;
-                const double mprev = bufs.mean_buf[(mlast + H - 1) % H];
-                const double rprev = bufs.rms_buf[(rlast + H - 1) % H];
-                bufs.mean_buf[mlast] = mprev;
-                bufs.rms_buf[rlast] = rprev;
-                st.mean_acc = st.mean_acc_prev + mprev;
-                st.rms_acc = st.rms_acc_prev + rprev;
+                if (lane == 0) {
+                    bufs.mean_buf[mlast] = hm.prev;
+                    bufs.rms_buf[rlast] = hr.prev;
+                }
+                hm.last = hm.prev;
+                hr.last = hr.prev;
+                st.mean_acc = st.mean_acc_prev + hm.prev;
+                st.rms_acc = st.rms_acc_prev + hr.prev;
             } else if (st.remaining_zeros != 0) {
                 fill = 1;
             }
-            bc.spectrum_clip = sclip;
-            bc.do_fill = fill;
+            hm.front = bufs.mean_buf[st.mean_head];  // oldest entry for the next spectrum
+            if (lane == 0) {
+                bc.spectrum_clip = sclip;
+                bc.do_fill = fill;
+            }
         }
         __syncthreads();
         const bool spectrum_clip = bc.spectrum_clip != 0;
+        const bool do_fill = bc.do_fill != 0;
         // ---- last good spectrum, clipSample, flatten (RFI_Clipper.cpp:441-494) ----
         int filled = 0;
         float s12[2] = {0.0f, 0.0f};
         for (int i = tid; i < nbins; i += P) {
             float v = spec[i];
-            if (bc.do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
+            if (do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
                 bufs.last_good[i] = v;
                 ++filled;
             }
             if (spectrum_clip) {
-                for (int p = 1; p < npol; ++p) data[elem(t, i, p, nsub, npol, nchan)] = -0.2f;
+                const long long o = geo.off(i);
+                for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = -0.2f;
                 v = -0.2f;
                 if (flags) flags[(long long)t * nbins + i] |= 2;
             }
@@ -507,17 +599,17 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
         filled = __reduce_add_sync(0xffffffffu, filled);
         if (lane == 0) redi[warp * 9 + 8] = filled;
         __syncthreads();
-        if (tid == 0) {
-            float sums[2];
-            block_tree_finish<2>(red, sums);
-            for (int w = 0; w < nw; ++w) st.remaining_zeros -= redi[w * 9 + 8];
-            const float m = __fdiv_rn(sums[0], (float)nbins);
-            const float ms = __fdiv_rn(sums[1], (float)nbins);
+        // ---- warp 0: normalisation constants, statistics, bandpass, next start ----
+        if (warp == 0) {
+            const float s1 = warp0_tree(red, 2, 0, nw);
+            const float s2 = warp0_tree(red, 2, 1, nw);
+            st.remaining_zeros -= warp0_isum(redi, 9, 8, nw);
+            const float m = __fdiv_rn(s1, (float)nbins);
+            const float ms = __fdiv_rn(s2, (float)nbins);
             float srms = __fsqrt_rn(__fsub_rn(ms, __fmul_rn(m, m)));
             if (srms == 0.0f) srms = 1.0f;
             st.rms_carry = (double)srms;
-            bc.sub_f = cfg.zero_dming == 1 ? m : (float)st.mean_run;
-            bc.rms_f = srms;
+            const float sub_f = cfg.zero_dming == 1 ? m : (float)st.mean_run;
             // statistics (RFI_Clipper.cpp:535-560)
             if (st.num == 0) {
                 const float frac = (float)(100.0 * (float)st.bad_spectra / (float)(10 * H));
@@ -525,6 +617,8 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                     st.mean_size = st.rms_size = 0;
                     st.mean_head = st.rms_head = 0;
                     st.mean_acc = st.mean_acc_prev = st.rms_acc = st.rms_acc_prev = 0.0;
+                    hm.front = bufs.mean_buf[0];
+                    hr.front = bufs.rms_buf[0];
                 }
                 st.bad_spectra = 0;
                 st.frac_bad_channels = 0.0f;
@@ -532,18 +626,31 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
             // BandPass::setMean / setRMS (BandPass.cpp:44-74)
             const float mean_f = (float)st.mean_run;
             const float delta = __fsub_rn(mean_f, st.bp_mean);
-            bc.rebuild_bp = 0;
+            int rebuild = 0;
             if (fabsf(delta) > 0.0f) {
                 st.params0 = __fadd_rn(st.params0, __fdiv_rn(delta, cfg.scale));
                 st.bp_mean = mean_f;
-                bc.rebuild_bp = 1;
-                bc.params0 = st.params0;
+                rebuild = 1;
             }
             st.bp_rms = (float)st.rms_run;
             st.num = (st.num + 1) % (10 * H);
+            if (lane == 0) {
+                bc.sub_f = sub_f;
+                bc.rms_f = srms;
+                bc.rebuild_bp = rebuild;
+                bc.params0 = st.params0;
+            }
+            // the next spectrum's start (its margin needs only this state)
+            if (t + 1 < nt) {
+                if (st.rms_size < H) {
+                    if (lane == 0) bc.adapt = 1;
+                } else {
+                    steady_start(st, hr, cfg, bufs, inv_h, bc);
+                }
+            }
         }
         __syncthreads();
-        // ---- normalise and store (RFI_Clipper.cpp:507-532) ----
+        // ---- normalise and store (RFI_Clipper.cpp:507-532); rebuild the bandpass ----
         const float sub_f = bc.sub_f, rms_f = bc.rms_f;
         const bool rebuild = bc.rebuild_bp != 0;
         const float p0 = bc.params0;
@@ -553,10 +660,9 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, int
                 v = __fdiv_rn(__fsub_rn(v, sub_f), rms_f);
                 if (v > cfg.cr) v = 0.0f;
             }
-            data[elem(t, i, 0, nsub, npol, nchan)] = v;
+            dst[geo.off(i)] = v;
             if (rebuild) bp[i] = bp_value(cfg, bufs, p0, i);
         }
-        __syncthreads();
     }
     if (tid == 0) *bufs.state = st;
 }
@@ -723,15 +829,17 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     PV_TRY(setup(h, nbins, s));
     if (nt == 0) return PV_OK;
     const int threads = pv_rfi_parts(nbins);
-    const size_t smem = sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 +
-                        sizeof(int) * 32 * 9 + sizeof(float) * 32 * 16;
+    const size_t smem = sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 * 2 +
+                        sizeof(int) * 32 * 9;
     if (smem > 227 * 1024) {
         pv::set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
         return PV_ERR_ARG;
     }
     PV_CUDA(cudaFuncSetAttribute(rfi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
             "cudaFuncSetAttribute(rfi)");
-    rfi_kernel<<<1, threads, smem, s>>>(h->cfg, h->dev, d_data, nt, nsub, npol, nchan, d_flags);
+    Geo geo{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1,
+            nbins / 8};
+    rfi_kernel<<<1, threads, smem, s>>>(h->cfg, h->dev, d_data, nt, geo, d_flags);
     return pv::check_launch("rfi_kernel");
 }
 
