@@ -17,9 +17,10 @@
 // HBM.  Raw int16 station samples are accepted directly (the conversion to
 // float is exact).
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
-#include "pv_common.cuh"
+#include "pv_internal.cuh"
 
 namespace pv {
 int fir_coefficients(int ntaps, int nchan, int window, std::vector<double>& out);
@@ -48,6 +49,17 @@ __device__ __forceinline__ float2 load_sample(const ChanArgs& a, long long idx) 
         return make_float2((float)v.x, (float)v.y);
     }
     return reinterpret_cast<const float2*>(a.in)[idx];
+}
+
+// The upper output of a radix-2 decimation-in-frequency butterfly,
+// (u - v) * w, with the rounding every channeliser kernel uses: the lower
+// output is u + v.  Both kernels evaluate each butterfly identically, so their
+// spectra agree bit for bit.
+__device__ __forceinline__ float2 twiddle_mul(float2 d, float2 w) {
+    return make_float2(fmaf(d.x, w.x, __fmul_rn(-d.y, w.y)), fmaf(d.x, w.y, __fmul_rn(d.y, w.x)));
+}
+__device__ __forceinline__ float2 dif_upper(float2 u, float2 v, float2 w) {
+    return twiddle_mul(make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y)), w);
 }
 
 __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
@@ -108,37 +120,32 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
         y[((size_t)p * BT + b) * N + c] = make_float2(re, im);
     }
     __syncthreads();
-    // Stockham radix-2 FFT of every (pol, block) row, ping-ponging y <-> x
-    float2* src = y;
-    float2* dst = x;
-    const int half = N / 2;
-    for (int ns = 1; ns < N; ns *= 2) {
-        const int tw_stride = N / (2 * ns);
+    // In-place radix-2 decimation-in-frequency FFT of every (pol, block) row
+    // of y (dif_upper gives the butterfly arithmetic); row position i then
+    // holds channel bitrev(i).
+    const int half = N / 2, lg = a.log2n;
+    for (int lh = lg - 1; lh >= 0; --lh) {
+        const int h = 1 << lh;
         for (int i = tid; i < P * nb * half; i += nt) {
-            const int j = i % half, row = i / half;
+            const int j = i & (half - 1), row = i >> (lg - 1);
             const int p = row / nb, b = row - p * nb;
-            const float2* r0 = src + ((size_t)p * BT + b) * N;
-            float2* d0 = dst + ((size_t)p * BT + b) * N;
-            const float2 u = r0[j];
-            const float2 v0 = r0[j + half];
-            const int k = j % ns;
-            const float2 w = tw[k * tw_stride];
-            const float2 v = make_float2(__fsub_rn(__fmul_rn(v0.x, w.x), __fmul_rn(v0.y, w.y)),
-                                         __fadd_rn(__fmul_rn(v0.x, w.y), __fmul_rn(v0.y, w.x)));
-            const int o = (j / ns) * ns * 2 + k;
-            d0[o] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
-            d0[o + ns] = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+            float2* r = y + ((size_t)p * BT + b) * N;
+            const int lo = ((j >> lh) << (lh + 1)) + (j & (h - 1));
+            const float2 u = r[lo], v = r[lo + h];
+            r[lo] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
+            r[lo + h] = dif_upper(u, v, tw[(j & (h - 1)) << (lg - 1 - lh)]);
         }
         __syncthreads();
-        float2* t = src; src = dst; dst = t;
     }
+    const float2* src = y;
+    const int rev = 32 - lg;
     // src holds the spectra, rows of stride N with pol stride BT*N
     if (a.mode == 0) {
         for (int i = tid; i < P * nb * N; i += nt) {
             const int c = i % N, pb = i / N;
             const int b = pb % nb, p = pb / nb;
             a.spectra[(((long long)(b0 + b) * a.nsub + s) * P + p) * N + c] =
-                src[((size_t)p * BT + b) * N + c];
+                src[((size_t)p * BT + b) * N + (__brev(c) >> rev)];
         }
         return;
     }
@@ -158,7 +165,8 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
             const float2* X = src + (size_t)b * N;
             const float2* Y = src + ((size_t)BT + b) * N;
             for (int c = nc * a.bin; c < (nc + 1) * a.bin; ++c) {
-                const float xr = X[c].x, xi = X[c].y, yr = Y[c].x, yi = Y[c].y;
+                const int i = __brev(c) >> rev;
+                const float xr = X[i].x, xi = X[i].y, yr = Y[i].x, yi = Y[i].y;
                 const float px = __fadd_rn(__fmul_rn(xr, xr), __fmul_rn(xi, xi));
                 const float py = __fadd_rn(__fmul_rn(yr, yr), __fmul_rn(yi, yi));
                 float v;
@@ -170,6 +178,193 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
             }
         }
         a.stokes[(((long long)u * a.nsub + s) * a.nstokes + k) * nco + nc] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K1 fast path: Stokes I of a dual-polarisation, 8-tap PPF with N = 16, 32 or
+// 64 channels, integrated over `window` blocks without channel binning -- the
+// beam pipelines' configuration.  One warp runs one subband over a range of
+// kRangeBlocks consecutive blocks: lanes 0-15 hold polarisation X and lanes
+// 16-31 polarisation Y, lane j holding channels j, j+16, ... (M = N/16 of
+// them).  The 8-block FIR window stays in registers, the FFT's stages of
+// stride >= 16 run inside each lane and those of stride 8..1 across lanes
+// with shuffles, and lane j+16 hands |Y|^2 to lane j, which integrates
+// I = |X|^2 + |Y|^2.  Every FIR product and sum, FFT butterfly, Stokes and
+// integration step is evaluated exactly as channelise_kernel evaluates it, so
+// the two kernels' outputs are bit-identical.  Inputs are read once (plus 7
+// warm-up blocks per range); raw loads run 8 blocks ahead of the arithmetic.
+//
+// Jobs (one per beam) are laid out one after another in warp space, so one
+// launch channelises any number of beams with the same N.
+// ---------------------------------------------------------------------------
+constexpr int kRangeBlocks = 256;
+constexpr int kFastTaps = 8;
+
+template <bool I16>
+struct RawSample;
+template <>
+struct RawSample<true> {
+    using type = int;  // short2 bits
+    static __device__ __forceinline__ float2 f2(int v) {
+        const short2 s = *reinterpret_cast<const short2*>(&v);
+        return make_float2((float)s.x, (float)s.y);
+    }
+};
+template <>
+struct RawSample<false> {
+    using type = float2;
+    static __device__ __forceinline__ float2 f2(float2 v) { return v; }
+};
+
+template <int N, bool I16>
+__global__ void __launch_bounds__(128)
+chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant__ pv::ChanJob one, int njobs,
+                     long long nwarps, const long long* __restrict__ d_step) {
+    constexpr int M = N / 16, T = kFastTaps, H = T - 1;
+    constexpr int LOGN = M == 1 ? 4 : (M == 2 ? 5 : 6);
+    using Raw = typename RawSample<I16>::type;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gw >= nwarps) return;
+    int lo = 0, hi = njobs - 1;  // the job whose warps include gw
+    while (jobs && lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].warp_begin <= gw) lo = mid;
+        else hi = mid - 1;
+    }
+    const pv::ChanJob& J = jobs ? jobs[lo] : one;
+    const int nblocks = J.nblocks, window = J.window, nu = J.nu, nsub = J.nsub;
+    const long long local = gw - J.warp_begin;
+    const int s = (int)(local / J.nranges);
+    const int r = (int)(local - (long long)s * J.nranges);
+    const int B0 = r * kRangeBlocks;
+    const int B1 = min(B0 + kRangeBlocks, nblocks);
+    const int lane = threadIdx.x & 31, pol = lane >> 4, j = lane & 15;
+    const long long row = (long long)s * 2 + pol;
+    const int par = d_step ? (int)(*d_step & 1) : 0;
+    const float2* hin = J.hist[par];
+    float2* hout = J.hist[par ^ 1];
+    const Raw* in = reinterpret_cast<const Raw*>(J.in) + row * nblocks * N + j;
+
+    float cf[T][M];
+#pragma unroll
+    for (int t = 0; t < T; ++t)
+#pragma unroll
+        for (int m = 0; m < M; ++m) cf[t][m] = J.coeffs[t * N + j + 16 * m];
+    // twiddles: in-lane stages (stride 16*hm, hm = M/2..1) then lane stages
+    float2 twr[M > 1 ? M - 1 : 1];
+#pragma unroll
+    for (int hm = M / 2; hm >= 1; hm >>= 1)
+#pragma unroll
+        for (int q = 0; q < hm; ++q) twr[M - 2 * hm + q] = J.twiddle[(j + 16 * q) * (M / (2 * hm))];
+    float2 tws[4];
+    float sgn[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int h = 8 >> q;
+        const bool upper = (j & h) != 0;
+        tws[q] = upper ? J.twiddle[(j & (h - 1)) * (N / (2 * h))] : make_float2(1.0f, 0.0f);
+        sgn[q] = upper ? -1.0f : 1.0f;
+    }
+
+    // FIR window: slot b & 7 holds block b (B0 is a multiple of 8)
+    float2 ring[T][M];
+#pragma unroll
+    for (int q = 1; q < T; ++q) {
+        const int b = B0 - T + q;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            if (b >= 0) ring[q][m] = RawSample<I16>::f2(in[(long long)b * N + 16 * m]);
+            else ring[q][m] = hin ? hin[(row * H + (H + b)) * N + j + 16 * m] : make_float2(0.0f, 0.0f);
+        }
+    }
+    Raw cur[T][M];
+#pragma unroll
+    for (int q = 0; q < T; ++q)
+#pragma unroll
+        for (int m = 0; m < M; ++m)
+            if (B0 + q < B1) cur[q][m] = in[(long long)(B0 + q) * N + 16 * m];
+
+    float acc[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) acc[m] = 0.0f;
+    int wleft = window;
+    int u = B0 / window;
+    for (int g0 = B0; g0 < B1; g0 += T) {
+#pragma unroll
+        for (int q = 0; q < T; ++q) {
+            const int b = g0 + q;
+            if (b >= B1) break;
+#pragma unroll
+            for (int m = 0; m < M; ++m) ring[q][m] = RawSample<I16>::f2(cur[q][m]);
+            if (b + T < B1) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) cur[q][m] = in[(long long)(b + T) * N + 16 * m];
+            }
+            // FIR, oldest tap (block b-7, slot q+1) first
+            float2 y[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                float re = 0.0f, im = 0.0f;
+#pragma unroll
+                for (int t = 0; t < T; ++t) {
+                    const float2 v = ring[(q + 1 + t) & (T - 1)][m];
+                    re = __fadd_rn(re, __fmul_rn(v.x, cf[t][m]));
+                    im = __fadd_rn(im, __fmul_rn(v.y, cf[t][m]));
+                }
+                y[m] = make_float2(re, im);
+            }
+            // FFT stages of stride 16*hm inside the lane
+#pragma unroll
+            for (int hm = M / 2; hm >= 1; hm >>= 1)
+#pragma unroll
+                for (int m = 0; m < M; ++m)
+                    if ((m & hm) == 0) {
+                        const float2 a = y[m], c = y[m + hm];
+                        y[m] = make_float2(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y));
+                        y[m + hm] = dif_upper(a, c, twr[M - 2 * hm + (m & (hm - 1))]);
+                    }
+            // stages of stride 8..1 across lanes: d = a + b (lower lane) or
+            // a - b (upper lane) -- exact sign flips -- then (d * w), w = 1 below
+#pragma unroll
+            for (int q2 = 0; q2 < 4; ++q2) {
+                const int h = 8 >> q2;
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const float ox = __shfl_xor_sync(0xffffffffu, y[m].x, h);
+                    const float oy = __shfl_xor_sync(0xffffffffu, y[m].y, h);
+                    const float2 d = make_float2(fmaf(sgn[q2], y[m].x, ox), fmaf(sgn[q2], y[m].y, oy));
+                    y[m] = twiddle_mul(d, tws[q2]);
+                }
+            }
+            // Stokes I = |X|^2 + |Y|^2 and integration
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const float p = __fadd_rn(__fmul_rn(y[m].x, y[m].x), __fmul_rn(y[m].y, y[m].y));
+                const float py = __shfl_down_sync(0xffffffffu, p, 16);
+                acc[m] = __fadd_rn(acc[m], __fadd_rn(p, py));
+            }
+            if (--wleft == 0) {
+                if (pol == 0 && u < nu) {
+                    float* o = J.out + ((long long)u * nsub + s) * N;
+#pragma unroll
+                    for (int m = 0; m < M; ++m) o[__brev(j + 16 * m) >> (32 - LOGN)] = acc[m];
+                }
+#pragma unroll
+                for (int m = 0; m < M; ++m) acc[m] = 0.0f;
+                wleft = window;
+                ++u;
+            }
+        }
+    }
+    // the range that ends the chunk carries its last 7 blocks to the next call
+    if (hout && B1 == nblocks) {
+#pragma unroll
+        for (int q = 0; q < H; ++q)
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+                hout[(row * H + q) * N + j + 16 * m] =
+                    RawSample<I16>::f2(in[(long long)(nblocks - H + q) * N + 16 * m]);
     }
 }
 
@@ -270,6 +465,44 @@ int prepare_history(pv_ppf* h, int nsub, int npol, cudaStream_t s) {
     return PV_OK;
 }
 
+}  // namespace
+
+namespace pv {
+
+bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window, int bin,
+                         int nblocks) {
+    return (nchan == 16 || nchan == 32 || nchan == 64) && ntaps == kFastTaps && npol == 2 &&
+           nstokes == 1 && bin == 1 && window > 0 && kRangeBlocks % window == 0 &&
+           nblocks >= kFastTaps - 1;
+}
+
+int chan_job_warps(ChanJob& job) {
+    job.nranges = ceil_div(job.nblocks, kRangeBlocks);
+    return job.nsub * job.nranges;
+}
+
+int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
+                     long long nwarps, const long long* d_step, cudaStream_t s) {
+    if (nwarps <= 0) return PV_OK;
+    const unsigned grid = (unsigned)ceil_div<long long>(nwarps, 4);
+#define PV_CHAN_FAST(NN)                                                                         \
+    if (nchan == NN) {                                                                           \
+        if (in_int16) chan_stokes_i_kernel<NN, true><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, d_step);  \
+        else chan_stokes_i_kernel<NN, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, d_step);          \
+        return check_launch("chan_stokes_i_kernel");                                            \
+    }
+    PV_CHAN_FAST(16)
+    PV_CHAN_FAST(32)
+    PV_CHAN_FAST(64)
+#undef PV_CHAN_FAST
+    set_error("channelise: no fast kernel for %d channels", nchan);
+    return PV_ERR_ARG;
+}
+
+}  // namespace pv
+
+namespace {
+
 int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol, int nblocks,
                    int mode, float2* d_spectra, float* d_stokes, int nstokes, int window, int bin,
                    int* nu_out, cudaStream_t s) {
@@ -293,6 +526,26 @@ int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol
     PV_TRY(prepare_history(h, nsub, npol, s));
     const int w = mode == 1 ? std::min(window, nblocks) : 1;  // StokesIntegrator.cpp:53-59
     const int nu = mode == 1 ? nblocks / w : 0;
+    if (mode == 1 && pv::chan_fast_supported(h->nchan, h->ntaps, npol, nstokes, w, bin, nblocks) &&
+        getenv("PV_CHAN_GENERIC") == nullptr) {
+        pv::ChanJob job{};
+        job.in = d_in;
+        job.hist[0] = h->have_hist ? h->d_hist[h->cur] : nullptr;
+        job.hist[1] = h->d_hist[h->cur ^ 1];
+        job.coeffs = h->d_coeffs;
+        job.twiddle = h->d_twiddle;
+        job.out = d_stokes;
+        job.nsub = nsub;
+        job.nblocks = nblocks;
+        job.window = w;
+        job.nu = nu;
+        const long long nwarps = pv::chan_job_warps(job);
+        PV_TRY(pv::launch_chan_fast(h->nchan, in_int16, nullptr, job, 1, nwarps, nullptr, s));
+        h->cur ^= 1;
+        h->have_hist = true;
+        if (nu_out) *nu_out = nu;
+        return PV_OK;
+    }
     ChanArgs a{};
     a.in = d_in;
     a.in_int16 = in_int16;
