@@ -330,6 +330,49 @@ int pv_beam_stage_ms(pv_beam* beam, float* h_ms5);
 int pv_beam_buffers(const pv_beam* beam, float** d_filterbank, float** d_filterbank_raw,
                     float** d_dedispersed, float** d_ring);
 
+/* ------------------------------------------------------------------------
+ * Batched beams (the serving form).  No counterpart in the reference, whose
+ * pipelines run one beam per process: many beams, each configured as for
+ * pv_beam_create, advance one chunk per step, every stage of all beams in a
+ * few launches (one persistent dedispersion launch over every beam's DM x
+ * time tiles), optionally replayed from one captured CUDA graph.  A beam's
+ * events equal those of the same beam run alone through pv_beam.
+ * Restrictions: every beam has the same chunk (a multiple of 4 spectra), 8
+ * PPF taps, 16, 32 or 64 channels per subband, int_chan = 1 and an int_time
+ * dividing 256; input is complex int16.
+ * ------------------------------------------------------------------------ */
+typedef struct pv_batch pv_batch;
+#define PV_BATCH_TUNE 1   /* autotune the dedispersion DM x time tile shape */
+#define PV_BATCH_GRAPH 2  /* capture one step as a CUDA graph, replay it per step */
+#define PV_BATCH_TIMING 4 /* record stage times of every step */
+#define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
+#define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
+int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
+void pv_batch_destroy(pv_batch* batch);
+/* The device buffer beam's voltages are read from at the next step
+ * (pv_beam_input_bytes(.., 1) bytes, [sub][pol][sample] complex int16). */
+int pv_batch_input(pv_batch* batch, int beam, void** d_voltages, long long* bytes);
+/* One step of every beam from the input buffers, asynchronously. */
+int pv_batch_run(pv_batch* batch, void* stream);
+/* Copies h_voltages[beam] (host, pinned for speed) to the input buffers, then runs. */
+int pv_batch_run_host(pv_batch* batch, const void* const* h_voltages, void* stream);
+/* As pv_beam_events, for one beam of the batch (synchronises the stream). */
+int pv_batch_events(pv_batch* batch, int beam, pv_event* h_events, long long cap,
+                    long long* h_count, long long* h_first_sample, void* stream);
+/* As pv_beam_info, for one beam of the batch. */
+int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
+/* Dedispersion tiling: [variant, time tile, channels per stage, stages,
+ * slot floats, tiles, CTAs, shared bytes], the DM tile height of every beam,
+ * the autotuner's time (ms) of each variant (-1: not timed or not usable) and
+ * the kernels one graph replay launches (0 without a graph).  Any may be NULL. */
+int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tune_ms4,
+                   long long* h_graph_kernels);
+/* Device time (ms) of the last step's stages (PV_BATCH_TIMING): channelise,
+ * RFI, ring write, dedisperse, analyse. */
+int pv_batch_stage_ms(pv_batch* batch, float* h_ms5);
+int pv_batch_buffers(const pv_batch* batch, int beam, float** d_filterbank, float** d_dedispersed,
+                     float** d_ring);
+
 #ifdef __cplusplus
 }
 #endif

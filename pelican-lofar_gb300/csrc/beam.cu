@@ -18,34 +18,6 @@
 
 #include "pv_internal.cuh"
 
-struct pv_beam {
-    pv_beam_config cfg{};
-    pv_ppf* ppf = nullptr;
-    pv_rfi* rfi = nullptr;
-    pv_dedisp_plan* plan = nullptr;
-    int nchan_fb = 0;        // filterbank channels per subband after integration
-    int nbins = 0;           // dedispersion channels
-    int inverted = 0;
-    int max_shift = 0, lag = 0;
-    long long ring_len = 0, row_stride = 0;
-    float* d_ring = nullptr;
-    float* d_fb = nullptr;       // [chunk][nsub][1][nchan_fb]
-    float* d_fb_raw = nullptr;   // optional pre-RFI copy
-    float* d_out = nullptr;      // [tdms][chunk]
-    pv_event* d_events = nullptr;
-    long long cap = 0;
-    void* d_scratch = nullptr;
-    long long* d_total = nullptr;
-    long long* h_total = nullptr;  // pinned
-    void* d_in = nullptr;          // staging for host input
-    size_t in_bytes = 0;
-    long long chunks = 0;
-    long long window = -1;
-    float rms = 0.0f;
-    cudaEvent_t ev[6] = {};     // stage boundaries of the last chunk (timing mode)
-    bool timed = false;
-};
-
 namespace {
 
 void destroy(pv_beam* b) {

@@ -7,18 +7,18 @@
 // pos+t lands at physical column (pos+t) mod ring_len.  The noise-template
 // substitution of DedispersionBuffer.cpp:169 is omitted: the reference's
 // weights are always 1, which makes it the identity.
-#include "pv_common.cuh"
+#include "pv_internal.cuh"
 
 namespace {
 
 constexpr int kTile = 32;
 
-__global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride, long long ring_len,
-                                  long long pos, const float* __restrict__ stokes, int nt, int nsub,
-                                  int npol, int nchan, int inverted) {
+__device__ __forceinline__ void ring_write_tile(float* __restrict__ ring, long long row_stride,
+                                                long long ring_len, long long pos,
+                                                const float* __restrict__ stokes, int nt, int nsub,
+                                                int npol, int nchan, int inverted, int t0, int b0) {
     __shared__ float tile[kTile][kTile + 1];
     const int nbins = nsub * nchan;
-    const int t0 = blockIdx.x * kTile, b0 = blockIdx.y * kTile;
     // read: rows of the tile are samples, columns are bins (coalesced in bins)
     for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
         const int t = t0 + i, b = b0 + threadIdx.x;
@@ -40,6 +40,31 @@ __global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride
     }
 }
 
+__global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride, long long ring_len,
+                                  long long pos, const float* __restrict__ stokes, int nt, int nsub,
+                                  int npol, int nchan, int inverted) {
+    ring_write_tile(ring, row_stride, ring_len, pos, stokes, nt, nsub, npol, nchan, inverted,
+                    blockIdx.x * kTile, blockIdx.y * kTile);
+}
+
+// The rings of many beams: CTAs are laid out job after job; a job's chunk
+// lands at logical position (*d_step) * nt.
+__global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
+                                        const long long* __restrict__ d_step) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].block_begin <= (long long)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const pv::RingJob& J = jobs[lo];
+    const int local = (int)(blockIdx.x - J.block_begin);
+    const int tiles_t = (J.nt + kTile - 1) / kTile;
+    const int bt = local / tiles_t, tt = local - bt * tiles_t;
+    ring_write_tile(J.ring, J.row_stride, J.ring_len, *d_step * J.nt, J.stokes, J.nt, J.nsub, 1,
+                    J.nchan, J.inverted, tt * kTile, bt * kTile);
+}
+
 }  // namespace
 
 namespace pv {
@@ -52,6 +77,17 @@ int ring_write_device(float* ring, long long row_stride, long long ring_len, lon
     ring_write_kernel<<<grid, dim3(kTile, 8), 0, s>>>(ring, row_stride, ring_len, pos, stokes, nt,
                                                      nsub, npol, nchan, inverted);
     return check_launch("ring_write_kernel");
+}
+
+int ring_job_blocks(const RingJob& j) {
+    return ceil_div(j.nt, kTile) * ceil_div(j.nsub * j.nchan, kTile);
+}
+
+int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const long long* d_step,
+                     cudaStream_t s) {
+    if (nblocks <= 0) return PV_OK;
+    ring_write_batch_kernel<<<(unsigned)nblocks, dim3(kTile, 8), 0, s>>>(d_jobs, njobs, d_step);
+    return check_launch("ring_write_batch_kernel");
 }
 
 }  // namespace pv

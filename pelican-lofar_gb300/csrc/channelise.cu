@@ -576,6 +576,18 @@ int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol
 
 }  // namespace
 
+namespace pv {
+int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
+               int* ntaps) {
+    if (!h) return PV_ERR_ARG;
+    *d_coeffs = h->d_coeffs;
+    *d_twiddle = h->d_twiddle;
+    *nchan = h->nchan;
+    *ntaps = h->ntaps;
+    return PV_OK;
+}
+}  // namespace pv
+
 extern "C" int pv_ppf_create(pv_ppf** out, int nchan, int ntaps, int window,
                              const float* h_coeffs) {
     if (!out || nchan < 2 || ntaps < 1 || (nchan & (nchan - 1)) != 0 || nchan > 1024) {

@@ -18,9 +18,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
+#include <map>
 #include <vector>
 
-#include "pv_common.cuh"
+#include "pv_internal.cuh"
 
 namespace {
 
@@ -342,6 +343,190 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// K4 batched (ring rows of many beams): one persistent launch works through a
+// list of (beam, DM tile, time tile) tiles taken from a global counter, so
+// beams of any channel count, trial count and delay range share the GPU in
+// one launch.  The pipeline is the one of dedisperse_tma_kernel and runs on
+// across tile boundaries: the producer warp takes the next tile, records it
+// beside the tile's first stage and streams its channel spans; consumers
+// learn the tile from that record when the stage arrives.  A beam's DM tile
+// height (1..16 trials, one warp each) is chosen on the host so that its
+// delay spread fits the launch's channel slot; warps above it idle on that
+// beam's tiles.  The output window of a beam at device step k is k - lag
+// (its ring then holds every delay of that window); beams with k < lag are
+// skipped.  All waits are bounded as in dedisperse_tma_kernel.
+// ---------------------------------------------------------------------------
+template <int R, int CS, int ST>
+__global__ void __launch_bounds__(17 * 32, 1)
+dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles,
+                        int ntiles, int slot, int* __restrict__ counter,
+                        const long long* __restrict__ d_step, int* __restrict__ status) {
+    constexpr int DMS = 16;
+    constexpr int TT = 32 * R;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* slots = reinterpret_cast<float*>(smem_raw);
+    int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * slot);
+    float* meta_k = reinterpret_cast<float*>(meta_off + ST * CS);
+    int* s_first = reinterpret_cast<int*>(meta_k + ST * CS);  // [2*ST], ST used
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_first + 2 * ST);
+    uint64_t* empty = full + ST;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long step = *d_step;
+
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) {
+        s_abort = *(volatile int*)status;
+        for (int b = 0; b < ST; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], DMS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (s_abort != 0) return;
+
+    if (warp == DMS) {
+        // ---------------- producer ----------------
+        unsigned gs = 0;
+        bool ok = true;
+        for (;;) {
+            int tile = -1;  // next tile of a beam that has a window at this step
+            for (;;) {
+                int t = 0;
+                if (lane == 0) t = atomicAdd(counter, 1);
+                t = __shfl_sync(0xffffffffu, t, 0);
+                if (t >= ntiles) break;
+                if (step >= jobs[tiles[t].job].lag) {
+                    tile = t;
+                    break;
+                }
+            }
+            const int b_first = gs % ST;
+            if (!mbar_wait_warp(&empty[b_first], ((gs / ST) & 1u) ^ 1u, kWaitLimitNs)) {
+                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                ok = false;
+                break;
+            }
+            if (tile < 0) {  // no work left: release the consumers
+                if (lane == 0) {
+                    s_first[b_first] = -1;
+                    mbar_arrive(&full[b_first]);
+                }
+                break;
+            }
+            const pv::DdTile tt = tiles[tile];
+            const pv::DdJob& J = jobs[tt.job];
+            const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
+            const float dv0 = pv_trial_value(tt.d0, J.start, J.step);
+            const float dv_last = pv_trial_value(d_last, J.start, J.step);
+            const int valid = min(TT, J.nout - tt.t0);
+            const long long t_base = ((step - J.lag) * J.chunk) % J.ring_len;
+            const int nst = (J.nchan + CS - 1) / CS;
+            for (int st = 0; st < nst; ++st) {
+                const int b = gs % ST;
+                if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, kWaitLimitNs)) {
+                    if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                    ok = false;
+                    break;
+                }
+                if (st == 0 && lane == 0) s_first[b] = tile;
+                const int c = st * CS + lane;
+                unsigned bytes = 0, piece1 = 0, piece2 = 0;
+                long long g_al = 0;
+                if (lane < CS && c < J.nchan) {
+                    const float k = J.dmshift[c];
+                    const int s0 = pv_shift(k, dv0);
+                    const int span = valid + pv_shift(k, dv_last) - s0;
+                    const long long g0 = (t_base + tt.t0 + s0) % J.ring_len;
+                    g_al = g0 & ~3LL;
+                    const int base = (int)(g0 - g_al);
+                    const unsigned n = (unsigned)((base + span + 3) & ~3);
+                    piece1 = (unsigned)min((long long)n, J.ring_len - g_al);
+                    piece2 = n - piece1;
+                    bytes = n * 4u;
+                    meta_off[b * CS + lane] = s0 - base;
+                    meta_k[b * CS + lane] = k;
+                }
+                __threadfence_block();
+                unsigned total = bytes;
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+                __syncwarp();
+                if (lane == 0) mbar_arrive_expect_tx(&full[b], total);
+                __syncwarp();
+                if (bytes) {
+                    const float* src = J.ring + (long long)c * J.row_stride;
+                    float* dst = slots + (size_t)(b * CS + lane) * slot;
+                    bulk_g2s(dst, src + g_al, piece1 * 4u, &full[b]);
+                    if (piece2) bulk_g2s(dst + piece1, src, piece2 * 4u, &full[b]);
+                }
+                ++gs;
+            }
+            if (!ok) break;
+        }
+        if (!ok) {
+            // wait (bounded) for the copies still in flight
+            for (unsigned g = gs > (unsigned)ST ? gs - ST : 0; g < gs; ++g)
+                mbar_wait_warp(&full[g % ST], (g / ST) & 1u, kWaitLimitNs);
+        }
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    unsigned gs = 0;
+    for (;;) {
+        const int b0 = gs % ST;
+        if (!mbar_wait_warp(&full[b0], (gs / ST) & 1u, kWaitLimitNs)) {
+            if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+            return;
+        }
+        const int tile = *(volatile int*)&s_first[b0];
+        if (tile < 0) return;
+        const pv::DdTile tt = tiles[tile];
+        const pv::DdJob& J = jobs[tt.job];
+        const int d = tt.d0 + warp;
+        const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
+        const bool active = warp < J.dms && d <= d_last;
+        const float dv = pv_trial_value(d, J.start, J.step);
+        const int nchan = J.nchan;
+        const int nst = (nchan + CS - 1) / CS;
+        float acc[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = 0.0f;
+        for (int st = 0; st < nst; ++st) {
+            const int b = gs % ST;
+            if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, kWaitLimitNs)) {
+                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                return;
+            }
+            if (active) {
+                const int c_end = min(CS, nchan - st * CS);
+                for (int j = 0; j < c_end; ++j) {
+                    const float k = meta_k[b * CS + j];
+                    const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT);
+                    const float* row = slots + (size_t)(b * CS + j) * slot + off + lane;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[b]);
+            ++gs;
+        }
+        if (active) {
+            float* o = J.out + (long long)d * J.out_stride;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const long long t = tt.t0 + lane + 32 * r;
+                if (t < J.nout) o[t] = acc[r];
+            }
+        }
+    }
+}
+
 // Largest delay spread s(c, d0+DMS-1) - s(c, d0) over channels and DM tiles,
 // evaluated with the kernel's own float arithmetic on the host.
 int delay_spread(const std::vector<float>& dmshift, int tdms, int dms, float start, float step) {
@@ -444,6 +629,303 @@ int dedisperse_device(float* out, long long out_stride, const float* in, long lo
     const int spread1 = delay_spread(h_dmshift, tdms, 1, start, step);
     return launch_dedisperse<1, 16, 1>(a, spread1, s);
 }
+
+}  // namespace pv
+
+// ---------------------------------------------------------------------------
+// Batched dedispersion set-up and the DM x time tile autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Variant {
+    int R, CS, ST;
+};
+// Time tile 32R samples, CS channels per pipeline stage, ST stages in flight.
+constexpr Variant kVariants[] = {{32, 4, 4}, {32, 2, 4}, {16, 4, 4}, {32, 8, 2}};
+constexpr int kNumVariants = 4;
+constexpr size_t kBatchSmemBudget = 220 * 1024;
+
+size_t batch_smem(const Variant& v, int slot) {
+    return (size_t)4 * v.ST * v.CS * slot + (size_t)8 * v.ST * v.CS + (size_t)8 * v.ST + 16 * v.ST;
+}
+
+template <int R, int CS, int ST>
+int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem,
+                   int grid, int* counter, const long long* d_step, int* status, cudaStream_t s,
+                   bool set_attr) {
+    auto kern = dedisperse_batch_kernel<R, CS, ST>;
+    if (set_attr) {
+        PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                "cudaFuncSetAttribute(dedisperse_batch)");
+        return PV_OK;
+    }
+    PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
+    kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, d_step, status);
+    return pv::check_launch("dedisperse_batch_kernel");
+}
+
+int launch_batch(int variant, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot,
+                 size_t smem, int grid, int* counter, const long long* d_step, int* status,
+                 cudaStream_t s, bool set_attr) {
+    switch (variant) {
+#define PV_VAR(I, R, CS, ST) \
+    case I: return launch_batch_t<R, CS, ST>(jobs, tiles, ntiles, slot, smem, grid, counter, d_step, status, s, set_attr);
+        PV_VAR(0, 32, 4, 4)
+        PV_VAR(1, 32, 2, 4)
+        PV_VAR(2, 16, 4, 4)
+        PV_VAR(3, 32, 8, 2)
+#undef PV_VAR
+    }
+    pv::set_error("dedispersion: unknown tile variant %d", variant);
+    return PV_ERR_ARG;
+}
+
+// Upper bound of delay_spread from the largest delay constant alone (the
+// per-channel truncations differ from the exact products by under one sample
+// each, plus the float rounding of the products).
+int spread_bound(float kmax, int tdms, int dms, float start, float step) {
+    double worst = 0.0;
+    for (int d0 = 0; d0 < tdms; d0 += dms) {
+        const int dl = std::min(d0 + dms, tdms) - 1;
+        const float v0 = std::fmaf((float)d0, step, start);
+        const float vl = std::fmaf((float)dl, step, start);
+        worst = std::max(worst, (double)kmax * ((double)vl - (double)v0) +
+                                    (double)kmax * ((double)vl + (double)v0) * 2.4e-7);
+    }
+    return (int)worst + 2;
+}
+
+}  // namespace
+
+namespace pv {
+
+struct DdBatch {
+    int variant = 0, slot = 0, grid = 0, ntiles = 0;
+    size_t smem = 0;
+    DdJob* d_jobs = nullptr;
+    DdTile* d_tiles = nullptr;
+    int* d_counter = nullptr;
+    int* d_status = nullptr;
+    std::vector<int> dms;
+    std::vector<float> tune_ms;
+};
+
+void dd_batch_destroy(DdBatch* b) {
+    if (!b) return;
+    for (void* p : {(void*)b->d_jobs, (void*)b->d_tiles, (void*)b->d_counter, (void*)b->d_status})
+        if (p) cudaFree(p);
+    delete b;
+}
+
+namespace {
+
+struct Shape {
+    int slot = 0;
+    size_t smem = 0;
+    std::vector<int> dms;
+    std::vector<DdTile> tiles;
+};
+
+// DM tile heights, slot size and tile list of one variant; false if some beam
+// cannot be tiled (its ring is shorter than a tile span).
+bool build_shape(const Variant& v, const DdBeam* beams, int n, std::vector<std::map<int, int>>& exact,
+                 Shape& out) {
+    const int TT = 32 * v.R;
+    const size_t fixed = batch_smem(v, 0);
+    const int slot_cap = (int)(((kBatchSmemBudget - fixed) / (4 * (size_t)v.ST * v.CS)) & ~(size_t)3);
+    if (slot_cap < TT + 8) return false;
+    out.dms.assign(n, 1);
+    out.slot = 0;
+    for (int i = 0; i < n; ++i) {
+        const DdBeam& B = beams[i];
+        float kmax = 0.0f;
+        for (int c = 0; c < B.nchan; ++c) kmax = std::max(kmax, B.h_dmshift[c]);
+        int dms = 16, sp = 0;
+        for (; dms >= 1; --dms) {
+            if (TT + spread_bound(kmax, B.tdms, dms, B.start, B.step) + 8 > slot_cap) continue;
+            auto it = exact[i].find(dms);
+            if (it == exact[i].end()) {
+                std::vector<float> k(B.h_dmshift, B.h_dmshift + B.nchan);
+                it = exact[i].emplace(dms, delay_spread(k, B.tdms, dms, B.start, B.step)).first;
+            }
+            sp = it->second;
+            if (TT + sp + 8 <= slot_cap) break;
+        }
+        if (dms < 1) return false;
+        if (B.ring_len < (long long)std::min(TT, B.nout) + sp + 8) return false;
+        out.dms[i] = dms;
+        out.slot = std::max(out.slot, (TT + sp + 8 + 3) & ~3);
+    }
+    out.smem = batch_smem(v, out.slot);
+    // tiles, beams with the most work per tile first, time tiles outer
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long long)beams[a].nchan * out.dms[a] > (long long)beams[b].nchan * out.dms[b];
+    });
+    out.tiles.clear();
+    for (int i : order)
+        for (int t0 = 0; t0 < beams[i].nout; t0 += TT)
+            for (int d0 = 0; d0 < beams[i].tdms; d0 += out.dms[i]) out.tiles.push_back({i, d0, t0});
+    return true;
+}
+
+int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant) {
+    std::vector<DdJob> jobs(n);
+    int max_lag = 0;
+    for (int i = 0; i < n; ++i) {
+        const DdBeam& B = beams[i];
+        jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.nchan,
+                        B.nout, B.tdms, B.lag, B.chunk, sh.dms[i], B.start, B.step};
+        max_lag = std::max(max_lag, B.lag);
+    }
+    (void)max_lag;
+    if (b->d_jobs) cudaFree(b->d_jobs);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    b->d_jobs = nullptr;
+    b->d_tiles = nullptr;
+    PV_CUDA(cudaMalloc(&b->d_jobs, sizeof(DdJob) * n), "allocate dedispersion jobs");
+    PV_CUDA(cudaMalloc(&b->d_tiles, sizeof(DdTile) * std::max<size_t>(sh.tiles.size(), 1)),
+            "allocate dedispersion tiles");
+    PV_CUDA(cudaMemcpy(b->d_jobs, jobs.data(), sizeof(DdJob) * n, cudaMemcpyHostToDevice),
+            "copy dedispersion jobs");
+    PV_CUDA(cudaMemcpy(b->d_tiles, sh.tiles.data(), sizeof(DdTile) * sh.tiles.size(),
+                       cudaMemcpyHostToDevice), "copy dedispersion tiles");
+    b->variant = variant;
+    b->slot = sh.slot;
+    b->smem = sh.smem;
+    b->ntiles = (int)sh.tiles.size();
+    b->dms = sh.dms;
+    b->grid = std::max(1, std::min(b->ntiles, sm_count()));
+    return launch_batch(variant, nullptr, nullptr, 0, 0, b->smem, 0, nullptr, nullptr, nullptr,
+                        nullptr, true);
+}
+
+}  // namespace
+
+int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cudaStream_t s) {
+    if (!out || !beams || n <= 0) {
+        set_error("dedispersion batch: no beams");
+        return PV_ERR_ARG;
+    }
+    for (int i = 0; i < n; ++i) {
+        const DdBeam& B = beams[i];
+        if (B.ring_len <= 0 || B.ring_len % 4 != 0 || B.row_stride % 4 != 0 || B.ring_len > B.row_stride ||
+            (reinterpret_cast<uintptr_t>(B.ring) & 15) != 0 || B.nout <= 0 || B.tdms <= 0 ||
+            B.nchan <= 0 || B.lag < 0 || B.chunk <= 0) {
+            set_error("dedispersion batch: beam %d needs a 16-byte aligned ring of a multiple of 4 "
+                      "samples", i);
+            return PV_ERR_ARG;
+        }
+    }
+    auto* b = new DdBatch;
+    std::vector<std::map<int, int>> exact(n);
+    int rc = PV_OK;
+    if (cudaMalloc(&b->d_counter, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess ||
+        cudaMemset(b->d_status, 0, sizeof(int)) != cudaSuccess) {
+        set_error("dedispersion batch: cannot allocate counters");
+        dd_batch_destroy(b);
+        return PV_ERR_NOMEM;
+    }
+    Shape sh;
+    if (variant >= 0) {
+        if (variant >= kNumVariants || !build_shape(kVariants[variant], beams, n, exact, sh)) {
+            set_error("dedispersion batch: tile variant %d cannot hold these beams", variant);
+            dd_batch_destroy(b);
+            return PV_ERR_ARG;
+        }
+        rc = upload(b, beams, n, sh, variant);
+    } else {
+        // Autotuner: time every variant that can tile the beams on the rings as
+        // they are, with every beam treated as ready, and keep the fastest.
+        long long* d_tstep = nullptr;
+        long long max_lag = 0;
+        for (int i = 0; i < n; ++i) max_lag = std::max<long long>(max_lag, beams[i].lag);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        PV_CUDA(cudaMalloc(&d_tstep, sizeof(long long)), "allocate tuning step");
+        PV_CUDA(cudaMemcpy(d_tstep, &max_lag, sizeof(long long), cudaMemcpyHostToDevice), "copy tuning step");
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 1e30f;
+        int best_v = -1;
+        b->tune_ms.assign(kNumVariants, -1.0f);
+        for (int v = 0; v < kNumVariants && rc == PV_OK; ++v) {
+            Shape cand;
+            if (!build_shape(kVariants[v], beams, n, exact, cand)) continue;
+            rc = upload(b, beams, n, cand, v);
+            if (rc != PV_OK) break;
+            float ms = 0.0f;
+            for (int it = 0; it < 3 && rc == PV_OK; ++it) {
+                if (it == 1) cudaEventRecord(e0, s);
+                rc = launch_batch(v, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
+                                  b->d_counter, d_tstep, b->d_status, s, false);
+            }
+            if (rc != PV_OK) break;
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = cuda_status(cudaGetLastError(), "dedispersion tuning");
+                break;
+            }
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms *= 0.5f;
+            b->tune_ms[v] = ms;
+            if (ms < best) {
+                best = ms;
+                best_v = v;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d_tstep);
+        int st = 0;
+        if (rc == PV_OK) rc = cuda_status(cudaMemcpy(&st, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+        if (rc == PV_OK && st != PV_OK) {
+            set_error("dedispersion tuning: a pipeline wait gave up");
+            rc = st;
+        }
+        if (rc == PV_OK && best_v < 0) {
+            set_error("dedispersion batch: no tile variant can hold these beams");
+            rc = PV_ERR_ARG;
+        }
+        if (rc == PV_OK) {
+            build_shape(kVariants[best_v], beams, n, exact, sh);
+            rc = upload(b, beams, n, sh, best_v);
+        }
+    }
+    if (rc != PV_OK) {
+        dd_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return PV_OK;
+}
+
+int dd_batch_launch(DdBatch* b, const long long* d_step, cudaStream_t s) {
+    return launch_batch(b->variant, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
+                        b->d_counter, d_step, b->d_status, s, false);
+}
+
+int dd_batch_status(const DdBatch* b, int* h_status) {
+    PV_CUDA(cudaMemcpy(h_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "read status");
+    return PV_OK;
+}
+
+int dd_batch_shape(const DdBatch* b, int* h8) {
+    const Variant& v = kVariants[b->variant];
+    h8[0] = b->variant;
+    h8[1] = 32 * v.R;
+    h8[2] = v.CS;
+    h8[3] = v.ST;
+    h8[4] = b->slot;
+    h8[5] = b->ntiles;
+    h8[6] = b->grid;
+    h8[7] = (int)b->smem;
+    return PV_OK;
+}
+
+const std::vector<int>& dd_batch_dms(const DdBatch* b) { return b->dms; }
+const std::vector<float>& dd_batch_tune_ms(const DdBatch* b) { return b->tune_ms; }
 
 }  // namespace pv
 
@@ -581,6 +1063,20 @@ extern "C" int pv_dedisp_plan_status(const pv_dedisp_plan* p, int* h_status) {
     PV_CUDA(cudaMemcpy(h_status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost), "read plan status");
     return PV_OK;
 }
+
+namespace pv {
+int plan_tables(const pv_dedisp_plan* p, const float** d_dmshift, const float** h_dmshift,
+                int* nchan, int* tdms, float* start, float* step) {
+    if (!p) return PV_ERR_ARG;
+    *d_dmshift = p->d_dmshift;
+    *h_dmshift = p->h_dmshift.data();
+    *nchan = p->nchan;
+    *tdms = p->tdms;
+    *start = p->start;
+    *step = p->step;
+    return PV_OK;
+}
+}  // namespace pv
 
 extern "C" int pv_dedisp_plan_max_shift(const pv_dedisp_plan* p) { return p ? p->max_shift : -1; }
 

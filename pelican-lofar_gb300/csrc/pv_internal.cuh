@@ -7,6 +7,80 @@
 
 namespace pv {
 
+// One beam's share of a Stokes-I channeliser launch (chan_stokes_i_kernel).
+struct ChanJob {
+    const void* in;          // [sub][2][nblocks*N] short2 or float2 voltages
+    float2* hist[2];         // [sub][2][7][N]: hist[step & 1] is read (null: zeros), the other written
+    const float* coeffs;     // [8][N]
+    const float2* twiddle;   // [N/2] exp(-2 pi i k / N)
+    float* out;              // [nu][sub][N] Stokes I
+    long long warp_begin;    // first warp of this job in the launch
+    int nsub, nblocks, window, nu, nranges;
+};
+bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window, int bin, int nblocks);
+int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
+int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
+                     long long nwarps, const long long* d_step, cudaStream_t s);
+// coefficient [T][N] and twiddle [N/2] tables of a PPF handle
+int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
+               int* ntaps);
+// delay constants (device and host) and trial scaling of a dedispersion plan
+int plan_tables(const pv_dedisp_plan* p, const float** d_dmshift, const float** h_dmshift,
+                int* nchan, int* tdms, float* start, float* step);
+
+// Batched dedispersion (dedisperse.cu): one beam's ring and window.
+struct DdBeam {
+    float* out;
+    long long out_stride;
+    const float* ring;
+    long long row_stride, ring_len;
+    const float* d_dmshift;
+    const float* h_dmshift;
+    int nchan, nout, tdms, lag, chunk;
+    float start, step;  // trial value = start + d*step, in samples per unit delay constant
+};
+struct DdJob {
+    float* out;
+    long long out_stride;
+    const float* ring;
+    long long row_stride, ring_len;
+    const float* dmshift;
+    int nchan, nout, tdms, lag, chunk, dms;
+    float start, step;
+};
+struct DdTile {
+    int job, d0, t0;
+};
+struct DdBatch;
+// variant < 0 runs the autotuner over the DM x time tile variants
+int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cudaStream_t s);
+int dd_batch_launch(DdBatch* b, const long long* d_step, cudaStream_t s);
+int dd_batch_status(const DdBatch* b, int* h_status);
+int dd_batch_shape(const DdBatch* b, int* h8);
+const std::vector<int>& dd_batch_dms(const DdBatch* b);
+const std::vector<float>& dd_batch_tune_ms(const DdBatch* b);
+void dd_batch_destroy(DdBatch* b);
+
+// Batched RFI clippers (rfi.cu).
+struct RfiBatch;
+int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
+                     const int* nchan, int n, int nt, cudaStream_t s);
+int rfi_batch_launch(RfiBatch* b, cudaStream_t s);
+int rfi_batch_launches(const RfiBatch* b);
+void rfi_batch_destroy(RfiBatch* b);
+
+// Batched ring writes (buffer.cu): stokes [nt][nsub][1][nchan] of one beam.
+struct RingJob {
+    float* ring;
+    long long row_stride, ring_len;
+    const float* stokes;
+    int nt, nsub, nchan, inverted;
+    long long block_begin;  // first CTA of this job
+};
+int ring_job_blocks(const RingJob& j);
+int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const long long* d_step,
+                     cudaStream_t s);
+
 int ring_write_device(float* ring, long long row_stride, long long ring_len, long long pos,
                       const float* stokes, int nt, int nsub, int npol, int nchan, int inverted,
                       cudaStream_t s);
@@ -17,3 +91,32 @@ int analyse_launch(const float* data, long long ld, int tdms, int nsamp, float t
                    cudaStream_t s);
 
 }  // namespace pv
+
+// One beam's device-resident chain state (beam.cu); the batch engine reuses it.
+struct pv_beam {
+    pv_beam_config cfg{};
+    pv_ppf* ppf = nullptr;
+    pv_rfi* rfi = nullptr;
+    pv_dedisp_plan* plan = nullptr;
+    int nchan_fb = 0;        // filterbank channels per subband after integration
+    int nbins = 0;           // dedispersion channels
+    int inverted = 0;
+    int max_shift = 0, lag = 0;
+    long long ring_len = 0, row_stride = 0;
+    float* d_ring = nullptr;
+    float* d_fb = nullptr;       // [chunk][nsub][1][nchan_fb]
+    float* d_fb_raw = nullptr;   // optional pre-RFI copy
+    float* d_out = nullptr;      // [tdms][chunk]
+    pv_event* d_events = nullptr;
+    long long cap = 0;
+    void* d_scratch = nullptr;
+    long long* d_total = nullptr;
+    long long* h_total = nullptr;  // pinned
+    void* d_in = nullptr;          // staging for host input
+    size_t in_bytes = 0;
+    long long chunks = 0;
+    long long window = -1;
+    float rms = 0.0f;
+    cudaEvent_t ev[6] = {};     // stage boundaries of the last chunk (timing mode)
+    bool timed = false;
+};

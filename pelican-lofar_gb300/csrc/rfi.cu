@@ -25,7 +25,7 @@
 #include <tuple>
 #include <vector>
 
-#include "pv_common.cuh"
+#include "pv_internal.cuh"
 
 namespace {
 
@@ -362,9 +362,9 @@ __device__ __forceinline__ void steady_start(RfiState& st, Hist& hr, const RfiCo
 // (the spectrum, the bandpass, the last good value) never crosses threads and
 // the passes of consecutive spectra need barriers only around the block
 // reductions and warp 0's scalar work.
-__global__ void __launch_bounds__(1024, 1)
-rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, Geo geo,
-           unsigned char* __restrict__ flags) {
+__device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers& bufs,
+                                         float* __restrict__ data, int nt, const Geo& geo,
+                                         unsigned char* __restrict__ flags) {
     extern __shared__ float sh[];
     __shared__ Bcast bc;
     const int nbins = cfg.nbins, H = cfg.history;
@@ -667,6 +667,73 @@ rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, Geo
     if (tid == 0) *bufs.state = st;
 }
 
+// MAXT is the block size (the partial count), which sets the register budget.
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
+rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, Geo geo,
+           unsigned char* __restrict__ flags) {
+    rfi_body(cfg, bufs, data, nt, geo, flags);
+}
+
+// One beam's clipper in a batched launch.
+struct RfiJob {
+    RfiConfig cfg;
+    RfiBuffers bufs;
+    float* data;
+    unsigned char* flags;
+    Geo geo;
+    int nt;
+};
+
+// The clippers of many beams at once: CTA b runs job b (every job of a launch
+// has the same partial count, the block size).
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) rfi_batch_kernel(const RfiJob* __restrict__ jobs) {
+    const RfiConfig cfg = jobs[blockIdx.x].cfg;
+    const RfiBuffers bufs = jobs[blockIdx.x].bufs;
+    const Geo geo = jobs[blockIdx.x].geo;
+    rfi_body(cfg, bufs, jobs[blockIdx.x].data, jobs[blockIdx.x].nt, geo, jobs[blockIdx.x].flags);
+}
+
+size_t rfi_smem_bytes(int nbins) {
+    return sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 * 2 + sizeof(int) * 32 * 9;
+}
+
+// Sets the shared-memory attribute of both kernels of a block size and
+// launches one of them: jobs != null selects the batched kernel.
+template <int MAXT>
+int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& cfg,
+                 const RfiBuffers& bufs, float* data, int nt, const Geo& geo, unsigned char* flags,
+                 cudaStream_t s) {
+    if (jobs) {
+        if (nblocks == 0) {  // set-up call: the attribute only, before any stream capture
+            PV_CUDA(cudaFuncSetAttribute(rfi_batch_kernel<MAXT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "cudaFuncSetAttribute(rfi batch)");
+            return PV_OK;
+        }
+        rfi_batch_kernel<MAXT><<<nblocks, MAXT, smem, s>>>(jobs);
+        return pv::check_launch("rfi_batch_kernel");
+    }
+    PV_CUDA(cudaFuncSetAttribute(rfi_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem), "cudaFuncSetAttribute(rfi)");
+    rfi_kernel<MAXT><<<1, MAXT, smem, s>>>(cfg, bufs, data, nt, geo, flags);
+    return pv::check_launch("rfi_kernel");
+}
+
+int rfi_launch(int parts, size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& cfg,
+               const RfiBuffers& bufs, float* data, int nt, const Geo& geo, unsigned char* flags,
+               cudaStream_t s) {
+    switch (parts) {
+        case 256: return rfi_launch_t<256>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
+        case 512: return rfi_launch_t<512>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
+        case 1024: return rfi_launch_t<1024>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
+        default:
+            pv::set_error("RFI_Clipper: no kernel for %d partial sums", parts);
+            return PV_ERR_ARG;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -829,18 +896,14 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     PV_TRY(setup(h, nbins, s));
     if (nt == 0) return PV_OK;
     const int threads = pv_rfi_parts(nbins);
-    const size_t smem = sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 * 2 +
-                        sizeof(int) * 32 * 9;
+    const size_t smem = rfi_smem_bytes(nbins);
     if (smem > 227 * 1024) {
         pv::set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
         return PV_ERR_ARG;
     }
-    PV_CUDA(cudaFuncSetAttribute(rfi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-            "cudaFuncSetAttribute(rfi)");
     Geo geo{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1,
             nbins / 8};
-    rfi_kernel<<<1, threads, smem, s>>>(h->cfg, h->dev, d_data, nt, geo, d_flags);
-    return pv::check_launch("rfi_kernel");
+    return rfi_launch(threads, smem, 1, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
 extern "C" int pv_rfi_parts(int nbins) { return nbins <= 1024 ? 256 : (nbins <= 4096 ? 512 : 1024); }
@@ -874,3 +937,101 @@ extern "C" int pv_rfi_bandpass(pv_rfi* h, float* out, int nbins) {
     std::copy(h->h_bp.begin(), h->h_bp.end(), out);
     return PV_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched clippers: the RFI_Clipper of every beam of a batch, one CTA per
+// beam, one launch per partial-count class.
+// ---------------------------------------------------------------------------
+namespace pv {
+
+struct RfiBatch {
+    struct Class {
+        int parts = 0;
+        size_t smem = 0;
+        RfiJob* d_jobs = nullptr;
+        int njobs = 0;
+    };
+    std::vector<Class> classes;
+};
+
+void rfi_batch_destroy(RfiBatch* b) {
+    if (!b) return;
+    for (auto& c : b->classes)
+        if (c.d_jobs) cudaFree(c.d_jobs);
+    delete b;
+}
+
+int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
+                     const int* nchan, int n, int nt, cudaStream_t s) {
+    auto* b = new RfiBatch;
+    std::vector<std::vector<RfiJob>> jobs;
+    for (int i = 0; i < n; ++i) {
+        pv_rfi* h = handles[i];
+        if (!h || !h->active) continue;
+        const int nbins = nsub[i] * nchan[i];
+        int rc = setup(h, nbins, s);
+        const size_t smem = rfi_smem_bytes(nbins);
+        if (rc == PV_OK && smem > 227 * 1024) {
+            set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
+            rc = PV_ERR_ARG;
+        }
+        if (rc != PV_OK) {
+            rfi_batch_destroy(b);
+            return rc;
+        }
+        const int parts = pv_rfi_parts(nbins);
+        size_t k = 0;
+        while (k < b->classes.size() && b->classes[k].parts != parts) ++k;
+        if (k == b->classes.size()) {
+            b->classes.emplace_back();
+            b->classes[k].parts = parts;
+            jobs.emplace_back();
+        }
+        b->classes[k].smem = std::max(b->classes[k].smem, smem);
+        RfiJob j{};
+        j.cfg = h->cfg;
+        j.bufs = h->dev;
+        j.data = data[i];
+        j.flags = nullptr;
+        j.geo = Geo{nsub[i], 1, nchan[i],
+                    (nchan[i] & (nchan[i] - 1)) == 0 ? __builtin_ctz((unsigned)nchan[i]) : -1, nbins / 8};
+        j.nt = nt;
+        jobs[k].push_back(j);
+    }
+    for (size_t k = 0; k < b->classes.size(); ++k) {
+        auto& c = b->classes[k];
+        c.njobs = (int)jobs[k].size();
+        cudaError_t e = cudaMalloc(&c.d_jobs, sizeof(RfiJob) * jobs[k].size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(c.d_jobs, jobs[k].data(), sizeof(RfiJob) * jobs[k].size(),
+                           cudaMemcpyHostToDevice);
+        int rc = e == cudaSuccess ? PV_OK : cuda_status(e, "RFI batch jobs");
+        // set the kernel attribute now, outside any stream capture
+        if (rc == PV_OK)
+            rc = rfi_launch(c.parts, c.smem, 0, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0, Geo{},
+                            nullptr, s);
+        if (rc != PV_OK) {
+            rfi_batch_destroy(b);
+            return rc;
+        }
+    }
+    *out = b;
+    return PV_OK;
+}
+
+int rfi_batch_launch(RfiBatch* b, cudaStream_t s) {
+    for (auto& c : b->classes) {
+        if (c.njobs == 0) continue;
+        PV_TRY(rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0,
+                          Geo{}, nullptr, s));
+    }
+    return PV_OK;
+}
+
+int rfi_batch_launches(const RfiBatch* b) {
+    int n = 0;
+    for (auto& c : b->classes) n += c.njobs > 0;
+    return n;
+}
+
+}  // namespace pv

@@ -89,6 +89,16 @@ def _declare(L):
         "pv_beam_info": (i, [vp, P(ll)]),
         "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
         "pv_beam_stage_ms": (i, [vp, P(C.c_float)]),
+        "pv_batch_create": (i, [P(vp), vp, i, i]),
+        "pv_batch_destroy": (None, [vp]),
+        "pv_batch_input": (i, [vp, i, P(vp), P(ll)]),
+        "pv_batch_run": (i, [vp, vp]),
+        "pv_batch_run_host": (i, [vp, P(vp), vp]),
+        "pv_batch_events": (i, [vp, i, vp, ll, P(ll), P(ll), vp]),
+        "pv_batch_info": (i, [vp, i, P(ll)]),
+        "pv_batch_tiles": (i, [vp, P(i), P(i), P(C.c_float), P(ll)]),
+        "pv_batch_stage_ms": (i, [vp, P(C.c_float)]),
+        "pv_batch_buffers": (i, [vp, i, P(vp), P(vp), P(vp)]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_ddmod_create": (i, [P(vp), i, i, f, f, d, d]),
         "pv_ddmod_destroy": (None, [vp]),
@@ -400,6 +410,85 @@ class Beam:
     def __del__(self):
         if getattr(self, "h", None) and self.h.value and _lib is not None:
             _lib.pv_beam_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING = 1, 2, 4
+
+
+class Batch:
+    """Many beams advanced one chunk per step by batched launches (pv_batch)."""
+
+    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0):
+        self.cfgs = list(cfgs)
+        self._arr = (BeamConfig * len(self.cfgs))(*self.cfgs)
+        flags = (BATCH_TUNE if tune else (variant << 8)) | (BATCH_GRAPH if graph else 0) | \
+            (BATCH_TIMING if timing else 0)
+        self.h = C.c_void_p()
+        check(load().pv_batch_create(C.byref(self.h), self._arr, len(self.cfgs), flags))
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def input(self, beam):
+        p, n = C.c_void_p(), C.c_longlong()
+        check(load().pv_batch_input(self.h, beam, C.byref(p), C.byref(n)))
+        return p.value, n.value
+
+    def set_input(self, beam, d_voltages, stream=None):
+        """Device-to-device copy of one beam's int16 voltages into its input buffer."""
+        p, n = self.input(beam)
+        assert d_voltages.numel() * d_voltages.element_size() == n
+        check(load().pv_device_copy(C.c_void_p(p), _ptr(d_voltages), n, _stream(stream)))
+
+    def run(self, stream=None):
+        check(load().pv_batch_run(self.h, _stream(stream)))
+
+    def run_host(self, h_voltages, stream=None):
+        ptrs = (C.c_void_p * len(h_voltages))(
+            *[C.c_void_p(v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data) for v in h_voltages])
+        check(load().pv_batch_run_host(self.h, ptrs, _stream(stream)))
+
+    def events(self, beam, cap=1 << 20, stream=None):
+        n, first = C.c_longlong(), C.c_longlong()
+        check(load().pv_batch_events(self.h, beam, None, 0, C.byref(n), C.byref(first), _stream(stream)))
+        k = min(n.value, cap)
+        ev = np.zeros(k, EVENT_DTYPE)
+        if k:
+            check(load().pv_batch_events(self.h, beam, C.c_void_p(ev.ctypes.data), k, C.byref(n),
+                                         C.byref(first), _stream(stream)))
+        return ev, n.value, first.value
+
+    def info(self, beam):
+        out = (C.c_longlong * 8)()
+        check(load().pv_batch_info(self.h, beam, out))
+        keys = ["nbins", "max_shift", "lag", "ring_len", "inverted", "steps", "window", "ring_bytes"]
+        return dict(zip(keys, list(out)))
+
+    def tiles(self):
+        shape, dms = (C.c_int * 8)(), (C.c_int * len(self.cfgs))()
+        tune, nk = (C.c_float * 4)(), C.c_longlong()
+        check(load().pv_batch_tiles(self.h, shape, dms, tune, C.byref(nk)))
+        keys = ["variant", "time_tile", "chan_per_stage", "stages", "slot", "tiles", "ctas", "smem"]
+        d = dict(zip(keys, list(shape)))
+        d["dms"] = list(dms)
+        d["tune_ms"] = list(tune)
+        d["graph_kernels"] = nk.value
+        return d
+
+    def stage_ms(self):
+        out = (C.c_float * 5)()
+        check(load().pv_batch_stage_ms(self.h, out))
+        return dict(zip(["channelise", "rfi", "ring_write", "dedisperse", "analyse"], list(out)))
+
+    def buffers(self, beam):
+        p = [C.c_void_p() for _ in range(3)]
+        check(load().pv_batch_buffers(self.h, beam, *[C.byref(x) for x in p]))
+        return [x.value for x in p]
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_batch_destroy(self.h)
             self.h = C.c_void_p()
 
 

@@ -1,0 +1,117 @@
+"""The batched engine (pv_batch) against the same beams run alone through the
+single-beam chain (pv_beam, itself checked stage by stage against the
+oracle): every beam's filterbank, dedispersed window and event list are
+bit-identical in the batch, with and without graph capture, for every
+dedispersion tile variant."""
+import numpy as np
+import pytest
+
+from gen import make_bp_text, voltages
+
+pytestmark = pytest.mark.gpu
+
+SUB_BW = 0.1953125  # MHz
+
+
+def beam_kw(nsub, nch, tdms, dm_step, f0=140.0, descending=False, chunk=512, threshold=4.0, **extra):
+    foff = SUB_BW / nch
+    fch1 = f0 - (nch // 2) * foff
+    if descending:
+        fch1, foff = fch1 + foff * (nsub * nch - 1), -foff
+    tsamp = 5.12e-6 * nch * 4
+    kw = dict(nsub=nsub, nchan_sub=nch, window="kaiser", fch1=fch1, foff=foff, tsamp=tsamp,
+              tdms=tdms, dm_step=dm_step, chunk=chunk, threshold=threshold, cr=5.0, sr=4.0,
+              history=1000, bin_pow2=4, zero_dming=1)  # zero-DMing as every reference pipeline XML
+    kw.update(extra)
+    return kw
+
+
+def calibrated(pv, cuda, kw, rng):
+    """The beam config with a flat bandpass at the filterbank's own mean and rms."""
+    import torch
+    nbins = kw["nsub"] * kw["nchan_sub"]
+    probe = pv.Beam(pv.beam_config(**dict(kw, rfi_active=0, bp_text=None, tdms=8)))
+    v16, _ = voltages(rng, kw["nsub"], 2, kw["chunk"] * 4 * kw["nchan_sub"])
+    probe.process(torch.from_numpy(v16.reshape(kw["nsub"], 2, -1)).to(cuda))
+    torch.cuda.synchronize()
+    fb = pv.device_array(probe.buffers()[0], (kw["chunk"], nbins)).cpu().numpy()
+    lo = min(kw["fch1"], kw["fch1"] + kw["foff"] * (nbins - 1))
+    bp = make_bp_text(nbins, lo, abs(kw["foff"]), float(fb.mean()), float(fb.std()))
+    return pv.beam_config(**dict(kw, bp_text=bp))
+
+
+MIX = [
+    dict(nsub=6, nch=16, tdms=40, dm_step=0.5),
+    dict(nsub=4, nch=64, tdms=64, dm_step=1.0),
+    dict(nsub=12, nch=16, tdms=64, dm_step=10.0),           # wide delay spread: short DM tiles
+    dict(nsub=3, nch=32, tdms=100, dm_step=0.4, descending=True),
+    dict(nsub=8, nch=16, tdms=33, dm_step=0.9, threshold=5.0),
+]
+
+
+@pytest.fixture(scope="module")
+def mix_configs(pv, cuda):
+    rng = np.random.default_rng(2024)
+    return [calibrated(pv, cuda, beam_kw(**m), rng) for m in MIX]
+
+
+@pytest.mark.parametrize("tune,graph,variant", [(True, True, 0), (False, False, 1), (False, True, 3)])
+def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant):
+    import torch
+    cfgs = mix_configs
+    batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant)
+    alone = [pv.Beam(c) for c in cfgs]
+    lags = [batch.info(i)["lag"] for i in range(len(cfgs))]
+    assert lags == [b.info()["lag"] for b in alone]
+    shape = batch.tiles()
+    assert shape["tiles"] > 0 and all(1 <= d <= 16 for d in shape["dms"])
+    if not tune and variant in (0, 3):  # 16 channel slots of ~3.5k samples
+        assert min(shape["dms"]) < 16  # the wide-spread beam needs a short DM tile
+    if graph:
+        assert shape["graph_kernels"] >= len(cfgs)
+    rng = np.random.default_rng(7)
+    compared = events_seen = 0
+    for step in range(max(lags) + 3):
+        ins = []
+        for c in cfgs:
+            v16, _ = voltages(rng, c.nsub, 2, c.chunk * 4 * c.nchan_sub)
+            ins.append(torch.from_numpy(v16.reshape(c.nsub, 2, -1)).to(cuda))
+        for i, x in enumerate(ins):
+            batch.set_input(i, x)
+            alone[i].process(x)
+        batch.run()
+        torch.cuda.synchronize()
+        for i, (c, b) in enumerate(zip(cfgs, alone)):
+            nbins = c.nsub * c.nchan_sub
+            fb_b, out_b, _ = batch.buffers(i)
+            fb_a, _, out_a, _ = b.buffers()
+            assert np.array_equal(pv.device_array(fb_b, (c.chunk, nbins)).cpu().numpy(),
+                                  pv.device_array(fb_a, (c.chunk, nbins)).cpu().numpy())
+            eb, nb, firstb = batch.events(i)
+            ea, na, firsta = b.events()
+            assert (nb, firstb) == (na, firsta)
+            assert np.array_equal(eb, ea)
+            if firsta >= 0:
+                assert np.array_equal(pv.device_array(out_b, (c.tdms, c.chunk)).cpu().numpy(),
+                                      pv.device_array(out_a, (c.tdms, c.chunk)).cpu().numpy())
+                compared += 1
+                events_seen += na - 1
+    assert compared >= len(cfgs) * 3
+    assert events_seen > 0
+
+
+def test_batch_autotuner_times_the_variants(pv, cuda, mix_configs):
+    batch = pv.Batch(mix_configs[:2], tune=True, graph=False)
+    t = batch.tiles()
+    timed = [x for x in t["tune_ms"] if x > 0]
+    assert len(timed) >= 2
+    assert t["tune_ms"][t["variant"]] == min(timed)
+
+
+def test_batch_rejects_unsupported_beams(pv, cuda, mix_configs):
+    bad = pv.beam_config(**dict(beam_kw(4, 8, 16, 1.0), bp_text=None, rfi_active=0))
+    with pytest.raises(pv.PvError, match="batched channeliser"):
+        pv.Batch([mix_configs[0], bad])
+    other_chunk = pv.beam_config(**dict(beam_kw(4, 16, 16, 1.0, chunk=256), bp_text=None, rfi_active=0))
+    with pytest.raises(pv.PvError, match="same chunk"):
+        pv.Batch([mix_configs[0], other_chunk])
