@@ -3,24 +3,38 @@
 
 Metric: DM-trial*channel*samples per second: the brute-force dedispersion
 work (trials x channels x output samples) of every chunk that passes through
-the whole chain, divided by wall time on the device.
+the whole chain (PPF, Stokes I, x4 integration, RFI clipper, delay ring,
+dedispersion, analyser), divided by wall time on the device.
 
-Workload "fullband-244sub" (default): one beam of 244 LOFAR subbands of
-195.3125 kHz from 110 MHz, dual-polarisation complex int16 voltages at 5.12 us
-(seeded Gaussian noise, sigma 16 per component, plus persistent narrowband
-sinusoids in 3% of the channels and broadband bursts about once per 10^4
-samples).  Per step (one chunk): 16-channel 8-tap Kaiser PPF per subband
-(3904 channels), Stokes I, x4 integration to 327.68 us, RFI_Clipper (5 sigma
-channel clip), the per-channel delay ring, brute-force dedispersion of 16384
-samples over 2048 trials of DM 0-500 pc/cm^3, and the 6-sigma analyser.  The
-voltages of one chunk (2.05 GB) and the ring (4.6 GB) exceed L2, so no flush
-is needed between steps.
+Workload "batch64" (default): 64 uneven beams advanced one chunk of 4096
+integrated spectra per step by the batched engine (pv_batch: every stage of
+all beams in a few launches, one persistent dedispersion launch over every
+beam's DM x time tiles with autotuned tile shapes, the step replayed from a
+captured CUDA graph).  Beams are drawn with seed 64: subbands from {31, 61,
+122, 244} LOFAR subbands of 195.3125 kHz from 110 MHz, 16 or 64 channels per
+subband (8-tap Kaiser PPF), x4 integration (327.68 us or 1.31 ms), DM ranges
+0-250 or 0-1000 pc/cm^3 in 1024, 2048 or 4096 trials, 5 sigma channel
+clipping with zero-DMing and a 10000-spectrum history (the reference's
+pipeline XML settings), 6 sigma detection.  Voltages: seeded Gaussian noise
+(sigma 16 per component), persistent narrowband sinusoids in 3% of the
+channels at 20 sigma, broadband bursts about once per 10^4 samples and 0-5
+dispersed pulses per beam.  The same beams also run through the plain
+per-beam chain (pv_beam: the same kernels one beam after another, events
+read back after every beam), timed in the same run: "plain" and
+"batched_over_plain" in the JSON line.  Rings start prefilled (as if each
+beam's stream had been preceded by silence) so every beam dedisperses a
+window from the first step; the work per step is the steady-state work.
+The ring (154 GB) and voltages (45 GB per step) exceed L2, so no flush is
+needed between steps.
+
+Workload "fullband": one beam of 244 subbands (3904 channels), 2048 trials of
+DM 0-500, chunks of 16384 spectra, through the single-beam chain.
 
 ``--impl reference`` times the reference algorithm's CPU restatement (the
 reference cannot be built: it needs Qt4, Boost, FFTW3 and the pelican core) on
 the host cores: the oracle's OpenMP channeliser, Stokes, integrator and RFI
-clipper on the same chunk shape and its OpenMP brute-force dedispersion of the
-same formula, on a bounded sample extrapolated to one chunk.
+clipper and its OpenMP brute-force dedispersion of the same formula, on a
+bounded sample of the same workload extrapolated to whole chunks.
 """
 import argparse
 import json
@@ -42,16 +56,41 @@ SUB_BW = 0.1953125  # MHz
 RAW_TSAMP = 5.12e-6  # s
 
 
-def fullband_config():
-    nsub, nchan_sub, int_time = 244, 16, 4
+def beam_dict(nsub, nchan_sub, dm_max, tdms, chunk, **kw):
+    int_time = 4
     foff = SUB_BW / nchan_sub
     f_sub0 = 110.0
-    tdms = 2048
-    return dict(workload="fullband-244sub-3904ch-2048dm-16384samp", nsub=nsub, nchan_sub=nchan_sub,
-                int_time=int_time, f_sub0=f_sub0, fch1=f_sub0 - (nchan_sub // 2) * foff, foff=foff,
-                tsamp=RAW_TSAMP * nchan_sub * int_time, tdms=tdms, dm_low=0.0,
-                dm_step=500.0 / (tdms - 1), chunk=16384, threshold=6.0, bin_pow2=6, cr=5.0, sr=4.0,
-                history=10000, window="kaiser")
+    d = dict(nsub=nsub, nchan_sub=nchan_sub, int_time=int_time, f_sub0=f_sub0,
+             fch1=f_sub0 - (nchan_sub // 2) * foff, foff=foff, tsamp=RAW_TSAMP * nchan_sub * int_time,
+             tdms=tdms, dm_low=0.0, dm_max=dm_max, dm_step=dm_max / (tdms - 1), chunk=chunk,
+             threshold=6.0, bin_pow2=6, cr=5.0, sr=4.0, history=10000, zero_dming=1, window="kaiser",
+             pulses=[])
+    d.update(kw)
+    return d
+
+
+def fullband_config():
+    d = beam_dict(244, 16, 500.0, 2048, 16384)
+    d["workload"] = "fullband-244sub-3904ch-2048dm-16384samp"
+    return d
+
+
+def batch_configs(nbeams=64, chunk=4096, seed=64):
+    """The 64-beam mix: uneven subband counts, channel counts, DM ranges and
+    trial counts, 0-5 dispersed pulses each (DM uniform in 10..0.9*DM max,
+    width 0.5-5 ms, at a uniform time in the chunk)."""
+    rng = np.random.default_rng(seed)
+    beams = []
+    for _ in range(nbeams):
+        nsub = int(rng.choice([31, 61, 122, 244]))
+        nch = int(rng.choice([16, 64]))
+        dm_max = float(rng.choice([250.0, 1000.0]))
+        tdms = int(rng.choice([1024, 2048, 4096]))
+        npulse = int(rng.integers(0, 6))
+        pulses = [(float(rng.uniform(10.0, 0.9 * dm_max)), float(rng.uniform(0.5e-3, 5e-3)),
+                   float(rng.uniform(0.1, 0.9))) for _ in range(npulse)]
+        beams.append(beam_dict(nsub, nch, dm_max, tdms, chunk, pulses=pulses))
+    return beams
 
 
 def bp_text(cfg, median=1000.0):
@@ -144,12 +183,39 @@ def device_voltages(cfg, dev, seed):
     nb = max(1, n // 10000)
     for b0 in rng.integers(0, n - 16, size=nb):
         v[:, :, int(b0):int(b0) + 16, :] *= 3.0
+    # dispersed pulses (dm, width s, position as a fraction of the chunk):
+    # Gaussian amplitude envelopes delayed per subband by the cold-plasma
+    # delay at the subband centre frequency
+    f_top = cfg["f_sub0"] + (nsub - 1) * SUB_BW
+    for dm, width, pos in cfg.get("pulses", []):
+        sig = max(width / 2.355 / RAW_TSAMP, 1.0)
+        for s in range(nsub):
+            f = cfg["f_sub0"] + s * SUB_BW
+            delay = 4148.741601 * dm * (1.0 / f ** 2 - 1.0 / f_top ** 2) / RAW_TSAMP
+            c0 = pos * n + delay
+            lo, hi = int(c0 - 4 * sig), int(c0 + 4 * sig) + 1
+            if hi <= 0 or lo >= n:
+                continue
+            lo, hi = max(lo, 0), min(hi, n)
+            tt = torch.arange(lo, hi, device=dev, dtype=torch.float32)
+            env = 1.0 + 1.5 * torch.exp(-0.5 * ((tt - c0) / sig) ** 2)
+            v[s, :, lo:hi, :] *= env[None, :, None]
     return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
 
 
 # ---------------------------------------------------------------------------
 # library arm
 # ---------------------------------------------------------------------------
+
+def pv_config(pv, cfg, **over):
+    kw = dict(nsub=cfg["nsub"], nchan_sub=cfg["nchan_sub"], window=cfg["window"],
+              int_time=cfg["int_time"], fch1=cfg["fch1"], foff=cfg["foff"], tsamp=cfg["tsamp"],
+              tdms=cfg["tdms"], dm_low=cfg["dm_low"], dm_step=cfg["dm_step"], chunk=cfg["chunk"],
+              threshold=cfg["threshold"], bin_pow2=cfg["bin_pow2"], bp_text=bp_text(cfg),
+              cr=cfg["cr"], sr=cfg["sr"], history=cfg["history"], zero_dming=cfg["zero_dming"])
+    kw.update(over)
+    return pv.beam_config(**kw)
+
 
 def run_pv(args, cfg):
     import torch
@@ -163,13 +229,7 @@ def run_pv(args, cfg):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    bcfg = pv.beam_config(nsub=cfg["nsub"], nchan_sub=cfg["nchan_sub"], window=cfg["window"],
-                          int_time=cfg["int_time"], fch1=cfg["fch1"], foff=cfg["foff"],
-                          tsamp=cfg["tsamp"], tdms=cfg["tdms"], dm_low=cfg["dm_low"],
-                          dm_step=cfg["dm_step"], chunk=cfg["chunk"], threshold=cfg["threshold"],
-                          bin_pow2=cfg["bin_pow2"], bp_text=bp_text(cfg), cr=cfg["cr"],
-                          sr=cfg["sr"], history=cfg["history"], timing=1)
-    beam = pv.Beam(bcfg)
+    beam = pv.Beam(pv_config(pv, cfg, timing=1))
     info = beam.info()
     stream = torch.cuda.Stream(device=dev)
     volts = [device_voltages(cfg, dev, 1000 + 7 * rank + i) for i in range(2)]
@@ -268,7 +328,7 @@ def run_pv(args, cfg):
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded Gaussian int16 voltages with narrowband and burst RFI",
             "config": {"workload": cfg["workload"], "nsub": cfg["nsub"], "nchan": nbins,
-                       "tdms": cfg["tdms"], "dm_range": [0.0, 500.0], "chunk": cfg["chunk"],
+                       "tdms": cfg["tdms"], "dm_range": [0.0, cfg["dm_max"]], "chunk": cfg["chunk"],
                        "tsamp_s": cfg["tsamp"], "ring_samples": info["ring_len"],
                        "l2": "inputs larger than L2 (2.05 GB voltages per chunk, 4.6 GB ring)",
                        "parallelism": "replicas" if world > 1 else "single beam"},
@@ -288,6 +348,192 @@ def run_pv(args, cfg):
         dist.destroy_process_group()
 
 
+def run_batch(args, cfgs, workload):
+    """The batched engine over many beams against the plain per-beam chain."""
+    import torch
+    import torch.distributed as dist
+    import pv
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    nb = len(cfgs)
+    units = [c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs]
+    units_step = sum(units)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    def seed(i):
+        return 5000 + 131 * rank + i
+
+    # ---------------- plain per-beam chain ----------------
+    # every beam's chunk resident on the device; host copies for the end-to-end pass
+    volts = [device_voltages(c, dev, seed(i)) for i, c in enumerate(cfgs)]
+    hosts = [v.cpu().pin_memory() for v in volts]
+    beams = [pv.Beam(pv_config(pv, c, prefilled=1)) for c in cfgs]
+
+    def plain_step(e2e=False):
+        d2h = 0
+        for i, b in enumerate(beams):
+            if e2e:
+                b.process_host(hosts[i], stream=stream)
+            else:
+                b.process(volts[i], stream=stream)
+            ev, n, _ = b.events(cap=1 << 16, stream=stream)  # synchronises: job per buffer
+            d2h += 8 + ev.nbytes
+        return d2h
+
+    plain_steps = max(2, args.steps // 2)
+    for _ in range(args.warmup):
+        plain_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        plain_step()
+    barrier()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        plain_step(e2e=True)
+    barrier()
+    plain_e2e_ms = (time.perf_counter() - t0) * 1e3
+    del beams, volts
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+    # ---------------- batched engine ----------------
+    batch = pv.Batch([pv_config(pv, c, prefilled=1) for c in cfgs], tune=True, graph=True, timing=True)
+    for i, c in enumerate(cfgs):
+        v = device_voltages(c, dev, seed(i))
+        batch.set_input(i, v, stream=stream)
+        stream.synchronize()
+        del v
+    torch.cuda.empty_cache()
+    infos = [batch.info(i) for i in range(nb)]
+    tiles = batch.tiles()
+    for _ in range(args.warmup):
+        batch.run(stream=stream)
+    barrier()
+    launches0 = pv.launches()
+    lat_ms, stage = [], []
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_start, t_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for _ in range(args.steps):
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        batch.run(stream=stream)
+        c1.record(stream)
+        c1.synchronize()
+        lat_ms.append(c0.elapsed_time(c1))
+        stage.append(batch.stage_ms())
+    t_stop.record(stream)
+    barrier()
+    clk = clocks.stop()
+    launches = pv.launches() - launches0
+    ms = t_start.elapsed_time(t_stop)
+    n_events = sum(batch.events(i, cap=0, stream=stream)[1] - 1 for i in range(nb))
+
+    # end to end: every beam's voltages from pinned host memory, events back
+    def e2e_step():
+        batch.run_host(hosts, stream=stream)
+        d2h = 0
+        for i in range(nb):
+            ev, n, _ = batch.events(i, cap=1 << 16, stream=stream)
+            d2h += 8 + ev.nbytes
+        return d2h
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    e_start, e_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    d2h = 0
+    for _ in range(args.steps):
+        d2h = e2e_step()
+    e_stop.record(stream)
+    barrier()
+    e2e_ms = e_start.elapsed_time(e_stop)
+
+    t = torch.tensor([ms, e2e_ms, plain_ms, plain_e2e_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms, e2e_ms, plain_ms, plain_e2e_ms = [float(x) for x in t]
+    value = units_step * args.steps * world / (ms / 1e3)
+    e2e_value = units_step * args.steps * world / (e2e_ms / 1e3)
+    plain_value = units_step * plain_steps * world / (plain_ms / 1e3)
+    plain_e2e = units_step * plain_steps * world / (plain_e2e_ms / 1e3)
+
+    peaks, peak_src = measured_peaks()
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fadd_peak = nsm * 128 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    st = {k: float(np.mean([x[k] for x in stage])) for k in stage[0]}
+    achieved = units_step / (st["dedisperse"] / 1e3)
+    in_bytes = sum(batch.input(i)[1] for i in range(nb))
+    fb_bytes = sum(c["chunk"] * c["nsub"] * c["nchan_sub"] * 4 for c in cfgs)
+    chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
+    roofline = {"kernel": "dedisperse_batch_kernel", "bound": "fp32",
+                "achieved": achieved / 1e12, "peak": fadd_peak / 1e12, "unit": "Tadd/s",
+                "frac": achieved / fadd_peak, "traffic": None,
+                "peak_source": "%d SMs x 128 FP32 lanes x sm_max_mhz of MEASURED_PEAKS.json (%s)"
+                               % (nsm, peak_src),
+                "per_unit": "one FP32 add per DM-trial*channel*sample (%d per launch)" % units_step,
+                "kernel_ms": st["dedisperse"]}
+    roofline_chan = {"kernel": "chan_stokes_i_kernel", "bound": "hbm", "achieved": chan_gbs,
+                     "peak": hbm, "unit": "GB/s", "frac": chan_gbs / hbm,
+                     "per_unit": "int16 voltages in (%d B) + float filterbank out (%d B) per step"
+                                 % (in_bytes, fb_bytes),
+                     "kernel_ms": st["channelise"], "peak_source": peak_src}
+    chunk_s = [c["chunk"] * c["tsamp"] for c in cfgs]
+    ring_gb = sum(x["ring_bytes"] for x in infos) / 1e9
+    cpu = cpu_baseline_mix(cfgs) if (rank == 0 and not args.no_cpu) else None
+    line = {"metric": "DM-trial*chan*samples/s", "value": value, "unit": "DM-trial*chan*samples/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded Gaussian int16 voltages with narrowband and burst RFI and "
+                    "dispersed pulses",
+            "config": {"workload": workload, "beams": nb, "chunk": cfgs[0]["chunk"],
+                       "nchan_total": sum(c["nsub"] * c["nchan_sub"] for c in cfgs),
+                       "tdms_total": sum(c["tdms"] for c in cfgs), "ring_gb": ring_gb,
+                       "input_gb_per_step": in_bytes / 1e9, "seed": 64,
+                       "l2": "inputs larger than L2 (%.0f GB voltages per step, %.0f GB rings)"
+                             % (in_bytes / 1e9, ring_gb),
+                       "start": "prefilled rings (silence before each stream)",
+                       "parallelism": "replicas" if world > 1 else "one GPU, all beams batched"},
+            "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h},
+            "plain": {"value": plain_value, "e2e": plain_e2e, "steps": plain_steps,
+                      "ms_per_step": plain_ms / plain_steps,
+                      "what": "pv_beam per beam, one after another, events read back per beam"},
+            "batched_over_plain": value / plain_value,
+            "batched_over_plain_e2e": e2e_value / plain_e2e,
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline,
+            "roofline_channeliser": roofline_chan, "stage_ms": st,
+            "tiles": {k: tiles[k] for k in ("variant", "time_tile", "chan_per_stage", "stages",
+                                             "slot", "tiles", "ctas", "tune_ms", "graph_kernels")},
+            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                           "p99": float(np.percentile(lat_ms, 99)),
+                           "chunk_duration_min": min(chunk_s) * 1e3,
+                           "chunk_duration_max": max(chunk_s) * 1e3},
+            "events_last_step": n_events,
+            "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
 # ---------------------------------------------------------------------------
 # CPU restatement (baseline / reference arm)
 # ---------------------------------------------------------------------------
@@ -298,7 +544,7 @@ class CpuChain:
     one chunk of filterbank, and an eighth of the trials dedispersed over every
     channel and the whole chunk (x8)."""
 
-    def __init__(self, cfg, sub_frac=8, trial_frac=8):
+    def __init__(self, cfg, sub_frac=8, trial_frac=8, add_budget=None):
         from oracle import pyoracle as po
         po.build()
         self.po, self.cfg = po, cfg
@@ -306,6 +552,8 @@ class CpuChain:
         self.ns = max(1, nsub // sub_frac)
         self.sub_scale = nsub / self.ns
         self.nt = max(1, cfg["tdms"] // trial_frac)
+        if add_budget:  # trials so that one sample costs about add_budget adds
+            self.nt = int(max(1, min(cfg["tdms"], add_budget // (nsub * nch * cfg["chunk"]))))
         self.trial_scale = cfg["tdms"] / self.nt
         rng = np.random.default_rng(3)
         n = cfg["chunk"] * it * nch
@@ -333,7 +581,8 @@ class CpuChain:
         spec = self.ppf.run(self.volt.reshape(self.ns, 2, -1, cfg["nchan_sub"]))
         st = po.integrate(po.stokes(spec, 1), cfg["int_time"], 1)
         t1 = time.perf_counter()
-        r = po.RFI(bp_text(cfg), cr=cfg["cr"], sr=cfg["sr"], history=cfg["history"], mode=0)
+        r = po.RFI(bp_text(cfg), cr=cfg["cr"], sr=cfg["sr"], history=cfg["history"],
+                   zero_dming=cfg.get("zero_dming", 0), mode=0)
         fb = self.fb.copy()
         t2 = time.perf_counter()
         r.run(fb)
@@ -354,27 +603,66 @@ def cpu_baseline(cfg, args, repeats=1):
             "sample": chain.sample + "; %.1f s per chunk extrapolated" % float(np.median(secs))}
 
 
-def run_reference(args, cfg):
+MIX_SAMPLE = 4  # beams of the mix timed on the CPU
+MIX_ADDS = 1.2e10  # dedispersion adds per sampled beam
+
+
+def cpu_mix_sample(cfgs):
+    return [CpuChain(c, add_budget=MIX_ADDS) for c in cfgs[:MIX_SAMPLE]]
+
+
+def cpu_mix_seconds(chains, cfgs):
+    """CPU seconds per step of the whole mix: the sampled beams' chain time
+    scaled by the mix's work over the sampled beams' work."""
+    secs = [ch.chunk_seconds() for ch in chains]
+    units = [c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs]
+    return float(np.sum(secs)) * sum(units) / sum(units[:len(chains)])
+
+
+def cpu_baseline_mix(cfgs):
+    chains = cpu_mix_sample(cfgs)
+    secs = cpu_mix_seconds(chains, cfgs)
+    units = sum(c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs)
+    return {"value": units / secs, "unit": "DM-trial*chan*samples/s",
+            "cores": chains[0].po.num_threads(), "kind": "port",
+            "sample": "first %d beams of the mix, each: %s; scaled to the %d-beam step by work "
+                      "(%.1f s per step)" % (len(chains), "; ".join(ch.sample for ch in chains),
+                                             len(cfgs), secs)}
+
+
+def run_reference(args, cfgs, workload):
+    """The reference arm: the reference algorithm's CPU restatement on the host
+    cores, on the same workload (a bounded sample per step, scaled to whole
+    steps by work)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    chain = CpuChain(cfg)
+    if len(cfgs) == 1:
+        chains = [CpuChain(cfgs[0])]
+        step_secs = lambda: chains[0].chunk_seconds()  # noqa: E731
+        sample = chains[0].sample
+    else:
+        chains = cpu_mix_sample(cfgs)
+        step_secs = lambda: cpu_mix_seconds(chains, cfgs)  # noqa: E731
+        sample = ("first %d beams of the %d-beam mix, scaled to the step by work: "
+                  % (len(chains), len(cfgs)) + "; ".join(ch.sample for ch in chains))
     for _ in range(args.warmup):
-        chain.chunk_seconds()
-    secs = [chain.chunk_seconds() for _ in range(args.steps)]
-    units = cfg["tdms"] * cfg["nsub"] * cfg["nchan_sub"] * cfg["chunk"]
+        step_secs()
+    secs = [step_secs() for _ in range(args.steps)]
+    units = sum(c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs)
     value = units * len(secs) / float(np.sum(secs))
     line = {"impl": "reference", "metric": "DM-trial*chan*samples/s", "value": value,
             "unit": "DM-trial*chan*samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded Gaussian voltages and filterbank",
-            "config": {"workload": cfg["workload"], "nchan": cfg["nsub"] * cfg["nchan_sub"],
-                       "tdms": cfg["tdms"], "chunk": cfg["chunk"]},
+            "config": {"workload": workload, "beams": len(cfgs),
+                       "nchan_total": sum(c["nsub"] * c["nchan_sub"] for c in cfgs),
+                       "tdms_total": sum(c["tdms"] for c in cfgs), "chunk": cfgs[0]["chunk"]},
             "cpu_baseline": {"value": value, "unit": "DM-trial*chan*samples/s",
-                             "cores": chain.po.num_threads(), "kind": "port",
-                             "sample": chain.sample + " per step; the reference needs Qt4, Boost, "
+                             "cores": chains[0].po.num_threads(), "kind": "port",
+                             "sample": sample + " per step; the reference needs Qt4, Boost, "
                                        "FFTW3 and pelican, so its algorithm's CPU restatement is "
                                        "timed"},
             "e2e": {"value": value, "unit": "DM-trial*chan*samples/s", "h2d_bytes_per_step": 0,
@@ -388,22 +676,36 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pv", choices=["pv", "reference"])
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "fullband"])
+    ap.add_argument("--beams", type=int, default=64, help="batch64: number of beams")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
     args = ap.parse_args()
-    cfg = fullband_config()
-    if args.tdms or args.chunk or args.nsub:
-        if args.tdms:
-            cfg["tdms"] = args.tdms
-        cfg["chunk"] = args.chunk or cfg["chunk"]
-        cfg["nsub"] = args.nsub or cfg["nsub"]
-        cfg["workload"] += "-reduced(tdms=%d,chunk=%d,nsub=%d)" % (cfg["tdms"], cfg["chunk"], cfg["nsub"])
+    if args.workload == "fullband":
+        cfg = fullband_config()
+        if args.tdms or args.chunk or args.nsub:
+            if args.tdms:
+                cfg["tdms"] = args.tdms
+                cfg["dm_step"] = cfg["dm_max"] / (cfg["tdms"] - 1)
+            cfg["chunk"] = args.chunk or cfg["chunk"]
+            cfg["nsub"] = args.nsub or cfg["nsub"]
+            cfg["workload"] += "-reduced(tdms=%d,chunk=%d,nsub=%d)" % (cfg["tdms"], cfg["chunk"],
+                                                                        cfg["nsub"])
+        if args.impl == "reference":
+            run_reference(args, [cfg], cfg["workload"])
+        else:
+            run_pv(args, cfg)
+        return
+    cfgs = batch_configs(args.beams, chunk=args.chunk or 4096)
+    workload = "batch%d-mixed-beams-4096samp" % args.beams
+    if args.beams != 64 or args.chunk:
+        workload += "-reduced(beams=%d,chunk=%d)" % (args.beams, cfgs[0]["chunk"])
     if args.impl == "reference":
-        run_reference(args, cfg)
+        run_reference(args, cfgs, workload)
     else:
-        run_pv(args, cfg)
+        run_batch(args, cfgs, workload)
 
 
 if __name__ == "__main__":

@@ -302,6 +302,11 @@ typedef struct {
     int zero_dming, rms_from_mean, band_matching, rfi_active;
     int debug_taps;           /* keep the pre-RFI filterbank of the last chunk */
     int timing;               /* record CUDA events at the stage boundaries */
+    int prefilled;            /* the delay ring starts as `lag` chunks of silence (zeros), so
+                                 a window is dedispersed from the first chunk on; logical
+                                 sample 0 is then the start of that silence and the first
+                                 chunk's data starts at lag*chunk.  0: the reference's
+                                 behaviour, the first window waits for lag+1 chunks. */
 } pv_beam_config;
 
 typedef struct pv_beam pv_beam;

@@ -243,7 +243,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         for (int i = 0; i < nbeams; ++i) {
             pv_beam* x = b->beams[i];
             rj[i] = pv::RingJob{x->d_ring, x->row_stride, x->ring_len, x->d_fb, chunk, x->cfg.nsub,
-                                x->nchan_fb, x->inverted, b->ring_blocks};
+                                x->nchan_fb, x->inverted, b->ring_blocks, x->chunks};
             b->ring_blocks += pv::ring_job_blocks(rj[i]);
         }
         if (cudaMalloc(&b->d_ring_jobs, sizeof(pv::RingJob) * nbeams) != cudaSuccess ||
@@ -272,6 +272,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             d.tdms = tdms;
             d.lag = x->lag;
             d.chunk = chunk;
+            d.base = (int)x->chunks;  // lag when the beam starts prefilled, else 0
         }
         const int variant = (flags & PV_BATCH_TUNE) ? -1 : PV_BATCH_VARIANT_OF(flags);
         rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, s0);
@@ -353,7 +354,7 @@ extern "C" int pv_batch_events(pv_batch* b, int beam, pv_event* h_events, long l
         return status;
     }
     pv_beam* x = b->beams[beam];
-    const long long w = b->step - 1 - x->lag;
+    const long long w = b->step + x->chunks - 1 - x->lag;  // x->chunks: prefilled chunks
     if (w < 0) {
         *h_count = 0;
         if (h_first_sample) *h_first_sample = -1;
@@ -376,8 +377,8 @@ extern "C" int pv_batch_info(const pv_batch* b, int beam, long long* h_info8) {
     h_info8[2] = x->lag;
     h_info8[3] = x->ring_len;
     h_info8[4] = x->inverted;
-    h_info8[5] = b->step;
-    h_info8[6] = b->step - 1 - x->lag;
+    h_info8[5] = b->step + x->chunks;
+    h_info8[6] = b->step + x->chunks - 1 - x->lag;
     h_info8[7] = (long long)x->nbins * x->row_stride * (long long)sizeof(float);
     return PV_OK;
 }

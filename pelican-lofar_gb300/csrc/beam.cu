@@ -87,6 +87,7 @@ extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
         return PV_ERR_NOMEM;
     }
     b->d_total = reinterpret_cast<long long*>(static_cast<char*>(b->d_scratch) + scratch);
+    if (c->prefilled) b->chunks = b->lag;  // the ring already holds lag chunks of zeros
     if (c->timing) {
         for (auto& ev : b->ev) {
             if (cudaEventCreate(&ev) != cudaSuccess) {

@@ -48,7 +48,7 @@ __global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride
 }
 
 // The rings of many beams: CTAs are laid out job after job; a job's chunk
-// lands at logical position (*d_step) * nt.
+// lands at logical position (*d_step + base) * nt.
 __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
                                         const long long* __restrict__ d_step) {
     int lo = 0, hi = njobs - 1;
@@ -61,7 +61,7 @@ __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, in
     const int local = (int)(blockIdx.x - J.block_begin);
     const int tiles_t = (J.nt + kTile - 1) / kTile;
     const int bt = local / tiles_t, tt = local - bt * tiles_t;
-    ring_write_tile(J.ring, J.row_stride, J.ring_len, *d_step * J.nt, J.stokes, J.nt, J.nsub, 1,
+    ring_write_tile(J.ring, J.row_stride, J.ring_len, (*d_step + J.base) * J.nt, J.stokes, J.nt, J.nsub, 1,
                     J.nchan, J.inverted, tt * kTile, bt * kTile);
 }
 

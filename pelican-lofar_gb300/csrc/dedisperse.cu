@@ -355,7 +355,8 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
 // delay spread fits the launch's channel slot; warps above it idle on that
 // beam's tiles.  The output window of a beam at device step k is k - lag
 // (its ring then holds every delay of that window); beams with k < lag are
-// skipped.  All waits are bounded as in dedisperse_tma_kernel.
+// skipped.  A beam whose ring started prefilled counts its base chunks of
+// silence in k.  All waits are bounded as in dedisperse_tma_kernel.
 // ---------------------------------------------------------------------------
 template <int R, int CS, int ST>
 __global__ void __launch_bounds__(17 * 32, 1)
@@ -399,7 +400,8 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 if (lane == 0) t = atomicAdd(counter, 1);
                 t = __shfl_sync(0xffffffffu, t, 0);
                 if (t >= ntiles) break;
-                if (step >= jobs[tiles[t].job].lag) {
+                const pv::DdJob& Jt = jobs[tiles[t].job];
+                if (step + Jt.base >= Jt.lag) {
                     tile = t;
                     break;
                 }
@@ -423,7 +425,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             const float dv0 = pv_trial_value(tt.d0, J.start, J.step);
             const float dv_last = pv_trial_value(d_last, J.start, J.step);
             const int valid = min(TT, J.nout - tt.t0);
-            const long long t_base = ((step - J.lag) * J.chunk) % J.ring_len;
+            const long long t_base = ((step + J.base - J.lag) * J.chunk) % J.ring_len;
             const int nst = (J.nchan + CS - 1) / CS;
             for (int st = 0; st < nst; ++st) {
                 const int b = gs % ST;
@@ -776,7 +778,7 @@ int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant)
     for (int i = 0; i < n; ++i) {
         const DdBeam& B = beams[i];
         jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.nchan,
-                        B.nout, B.tdms, B.lag, B.chunk, sh.dms[i], B.start, B.step};
+                        B.nout, B.tdms, B.lag, B.chunk, sh.dms[i], B.base, B.start, B.step};
         max_lag = std::max(max_lag, B.lag);
     }
     (void)max_lag;

@@ -37,6 +37,7 @@ struct DdBeam {
     const float* d_dmshift;
     const float* h_dmshift;
     int nchan, nout, tdms, lag, chunk;
+    int base;           // chunks already in the ring at step 0 (prefilled silence)
     float start, step;  // trial value = start + d*step, in samples per unit delay constant
 };
 struct DdJob {
@@ -45,7 +46,7 @@ struct DdJob {
     const float* ring;
     long long row_stride, ring_len;
     const float* dmshift;
-    int nchan, nout, tdms, lag, chunk, dms;
+    int nchan, nout, tdms, lag, chunk, dms, base;
     float start, step;
 };
 struct DdTile {
@@ -76,6 +77,7 @@ struct RingJob {
     const float* stokes;
     int nt, nsub, nchan, inverted;
     long long block_begin;  // first CTA of this job
+    long long base;         // chunks already in the ring at step 0 (prefilled silence)
 };
 int ring_job_blocks(const RingJob& j);
 int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const long long* d_step,

@@ -55,10 +55,15 @@ def mix_configs(pv, cuda):
     return [calibrated(pv, cuda, beam_kw(**m), rng) for m in MIX]
 
 
-@pytest.mark.parametrize("tune,graph,variant", [(True, True, 0), (False, False, 1), (False, True, 3)])
-def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant):
+@pytest.mark.parametrize("tune,graph,variant,prefilled", [(True, True, 0, False), (False, False, 1, False),
+                                                           (False, True, 3, True)])
+def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled):
     import torch
     cfgs = mix_configs
+    if prefilled:  # rings start as lag chunks of silence: windows from the first chunk on
+        cfgs = [type(c).from_buffer_copy(c) for c in cfgs]
+        for c, o in zip(cfgs, mix_configs):
+            c._bp, c.bp_text, c.prefilled = o._bp, o._bp, 1
     batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant)
     alone = [pv.Beam(c) for c in cfgs]
     lags = [batch.info(i)["lag"] for i in range(len(cfgs))]
@@ -97,6 +102,8 @@ def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant):
                 compared += 1
                 events_seen += na - 1
     assert compared >= len(cfgs) * 3
+    if prefilled:
+        assert compared == len(cfgs) * (max(lags) + 3)
     assert events_seen > 0
 
 
