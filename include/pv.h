@@ -40,6 +40,11 @@ int pv_version(void);
 long long pv_kernel_launches(void);
 /* cudaMemcpyAsync with cudaMemcpyDefault (host or device pointers). */
 int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
+/* Page-locked host memory for input staging (cudaHostAlloc, portable).
+ * write_combined = 1 suits buffers the host only writes and the GPU reads
+ * (voltage chunks): uncached on the host, no cache snooping on transfer. */
+int pv_host_alloc(void** h_ptr, long long bytes, int write_combined);
+void pv_host_free(void* h_ptr);
 
 /* ------------------------------------------------------------------------
  * A7 delay table — DedispersionModule::resize (lib/src/DedispersionModule.cpp:109-190)
@@ -350,20 +355,31 @@ typedef struct pv_batch pv_batch;
 #define PV_BATCH_TUNE 1   /* autotune the dedispersion DM x time tile shape */
 #define PV_BATCH_GRAPH 2  /* capture one step as a CUDA graph, replay it per step */
 #define PV_BATCH_TIMING 4 /* record stage times of every step */
+#define PV_BATCH_PIPELINED 8 /* dedisperse window k-lag-1 while chunk k is channelised and
+                                clipped (rings one chunk longer; events one step later) */
 #define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
 void pv_batch_destroy(pv_batch* batch);
+#define PV_BATCH_HOST_EVENTS 65536 /* events per beam per step kept in host memory */
 /* The device buffer beam's voltages are read from at the next step
- * (pv_beam_input_bytes(.., 1) bytes, [sub][pol][sample] complex int16). */
+ * (pv_beam_input_bytes(.., 1) bytes, [sub][pol][sample] complex int16).
+ * Steps alternate between two buffer sets, so ask again before every step. */
 int pv_batch_input(pv_batch* batch, int beam, void** d_voltages, long long* bytes);
 /* One step of every beam from the input buffers, asynchronously. */
 int pv_batch_run(pv_batch* batch, void* stream);
-/* Copies h_voltages[beam] (host, pinned for speed) to the input buffers, then runs. */
+/* Copies h_voltages[beam] (host, pinned for speed) to the next step's input
+ * buffers on the batch's own copy stream, then runs the step on `stream`
+ * once the copies land.  Returns at once: the copies of step k+1 overlap
+ * the computation of step k. */
 int pv_batch_run_host(pv_batch* batch, const void* const* h_voltages, void* stream);
-/* As pv_beam_events, for one beam of the batch (synchronises the stream). */
-int pv_batch_events(pv_batch* batch, int beam, pv_event* h_events, long long cap,
-                    long long* h_count, long long* h_first_sample, void* stream);
+/* Events of one beam at one of the last two issued steps (step < 0: the
+ * last), as pv_beam_events: total count including the dummy, the window's
+ * first sample (-1 while the ring fills) and up to cap events (at most
+ * PV_BATCH_HOST_EVENTS) copied to h_events.  Waits for that step only, so
+ * the next step may already be running. */
+int pv_batch_events(pv_batch* batch, int beam, long long step, pv_event* h_events, long long cap,
+                    long long* h_count, long long* h_first_sample);
 /* As pv_beam_info, for one beam of the batch. */
 int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
 /* Dedispersion tiling: [variant, time tile, channels per stage, stages,
@@ -373,7 +389,8 @@ int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
 int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tune_ms4,
                    long long* h_graph_kernels);
 /* Device time (ms) of the last step's stages (PV_BATCH_TIMING): channelise,
- * RFI, ring write, dedisperse, analyse. */
+ * RFI, ring write, dedisperse, analyse (pipelined: the last two run
+ * concurrently with the first three). */
 int pv_batch_stage_ms(pv_batch* batch, float* h_ms5);
 int pv_batch_buffers(const pv_batch* batch, int beam, float** d_filterbank, float** d_dedispersed,
                      float** d_ring);

@@ -9,13 +9,24 @@
 //                              DM x time tile shape chosen by the autotuner
 //   K5  analyser               per beam (count, scan, emit)
 //
+// Pipelined mode (PV_BATCH_PIPELINED) splits a step into two concurrent
+// branches after the channeliser: clip and ring-write chunk k, and meanwhile
+// dedisperse and search window k-lag-1 (complete since the previous step).
+// The clippers run one CTA per beam, so the persistent dedispersion launch
+// fills the SMs they leave idle; every ring holds one more chunk so that the
+// branches never touch the same ring positions, and a window's events come
+// one step later.
 // Every launch reads the chunk index from a device step counter that the
 // step's last kernel advances, so one captured CUDA graph replays every
-// step unchanged.  The chain of each beam is the pv_beam chain: the same
+// step unchanged.  Inputs and event outputs are double buffered by step
+// parity: the host copies the next step's voltages (on the batch's copy
+// stream) while the current step computes, and each step's events land in
+// host-mapped pinned memory, readable while the next step runs.  The chain of each beam is the pv_beam chain: the same
 // state layout (tap history, RFI state, delay ring) and the same arithmetic,
 // so a beam's events in the batch equal its events run alone.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "pv_internal.cuh"
@@ -24,13 +35,37 @@ namespace {
 
 __global__ void step_advance_kernel(long long* step) { *step += 1; }
 
+struct ExportJob {
+    const pv_event* d_events;
+    const long long* d_total;
+    long long cap;  // device event capacity of the beam
+};
+
+// Copies every beam's event count and first events of this step into the
+// host-mapped slot of the step's parity, with the dedispersion status word.
+__global__ void event_export_kernel(const ExportJob* __restrict__ jobs, int n,
+                                    const long long* __restrict__ d_step,
+                                    const int* __restrict__ d_status, long long* h_counts,
+                                    pv_event* h_events, long long host_cap, int* h_status) {
+    const int b = blockIdx.x;
+    const int par = (int)(*d_step & 1);
+    const long long total = *jobs[b].d_total;
+    const long long k = min(min(total, jobs[b].cap), host_cap);
+    pv_event* dst = h_events + ((long long)par * n + b) * host_cap;
+    for (long long i = threadIdx.x; i < k; i += blockDim.x) dst[i] = jobs[b].d_events[i];
+    if (threadIdx.x == 0) {
+        h_counts[(long long)par * n + b] = total;
+        if (b == 0) h_status[par] = *d_status;
+    }
+}
+
 }  // namespace
 
 struct pv_batch {
     int n = 0;
     int flags = 0;
     std::vector<pv_beam*> beams;
-    std::vector<void*> d_in;
+    std::vector<void*> d_in;  // [2][n]: inputs of even and odd steps
     std::vector<long long> in_bytes;
     std::vector<float2*> d_hist;  // two per beam
     struct ChanClass {
@@ -44,14 +79,29 @@ struct pv_batch {
     long long ring_blocks = 0;
     pv::DdBatch* dd = nullptr;
     long long* d_step = nullptr;
-    long long* h_totals = nullptr;  // pinned, one per beam
+    ExportJob* d_export = nullptr;
+    void* h_mapped = nullptr;       // host-mapped pinned: counts [2][n], status [2], events [2][n][host_cap]
+    long long* h_counts = nullptr;
+    int* h_status = nullptr;
+    pv_event* h_events = nullptr;
+    long long host_cap = 0;
     long long step = 0;             // steps issued
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t done[2] = {};       // step of each parity finished on the device
+    cudaEvent_t copied[2] = {};     // inputs of each parity copied
+    bool done_valid[2] = {false, false};
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long graph_kernels = 0;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[7] = {};
     bool timed = false;
+    bool pipelined = false;
+    std::vector<int> lag_eff, base;  // steps from a chunk to its window's completion; prefilled chunks
+    cudaStream_t side = nullptr;     // second branch of a pipelined step
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaStream_t rfi_side[3] = {};   // pipelined: one stream per clipper class after the first
+    cudaEvent_t rfi_join[3] = {};
 };
 
 namespace {
@@ -60,6 +110,13 @@ void destroy(pv_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->side) cudaStreamDestroy(b->side);
+    for (int i = 0; i < 3; ++i) {
+        if (b->rfi_side[i]) cudaStreamDestroy(b->rfi_side[i]);
+        if (b->rfi_join[i]) cudaEventDestroy(b->rfi_join[i]);
+    }
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->join_ev) cudaEventDestroy(b->join_ev);
     for (auto e : b->ev)
         if (e) cudaEventDestroy(e);
     if (b->dd) pv::dd_batch_destroy(b->dd);
@@ -68,7 +125,13 @@ void destroy(pv_batch* b) {
         if (c.d_jobs) cudaFree(c.d_jobs);
     if (b->d_ring_jobs) cudaFree(b->d_ring_jobs);
     if (b->d_step) cudaFree(b->d_step);
-    if (b->h_totals) cudaFreeHost(b->h_totals);
+    if (b->d_export) cudaFree(b->d_export);
+    if (b->h_mapped) cudaFreeHost(b->h_mapped);
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        if (b->done[i]) cudaEventDestroy(b->done[i]);
+        if (b->copied[i]) cudaEventDestroy(b->copied[i]);
+    }
     for (void* p : b->d_in)
         if (p) cudaFree(p);
     for (void* p : b->d_hist)
@@ -78,34 +141,69 @@ void destroy(pv_batch* b) {
     delete b;
 }
 
-// Issues one step of every beam on stream s.
+// Issues one step of every beam on stream s.  Pipelined, the channeliser
+// runs first on the whole GPU; then the clippers are launched, and only then
+// the dedispersion branch on the side stream, so that the clippers' CTAs are
+// resident before the persistent dedispersion CTAs take the remaining SMs
+// (and the SMs of every clipper that finishes).  The side stream joins s
+// before the step counter advances.
 int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     const bool timing = (b->flags & PV_BATCH_TIMING) != 0;
-    auto mark = [&](int i) -> int {
+    auto mark = [&](int i, cudaStream_t st) -> int {
         if (!timing) return PV_OK;
-        return pv::cuda_status(capture ? cudaEventRecordWithFlags(b->ev[i], s, cudaEventRecordExternal)
-                                       : cudaEventRecord(b->ev[i], s),
+        return pv::cuda_status(capture ? cudaEventRecordWithFlags(b->ev[i], st, cudaEventRecordExternal)
+                                       : cudaEventRecord(b->ev[i], st),
                                "record stage event");
     };
-    PV_TRY(mark(0));
+    cudaStream_t sd = b->pipelined ? b->side : s;  // stream of the dedispersion branch
+    PV_TRY(mark(0, s));
     for (auto& c : b->chan)
         PV_TRY(pv::launch_chan_fast(c.nchan, 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps, b->d_step, s));
-    PV_TRY(mark(1));
-    if (b->rfi) PV_TRY(pv::rfi_batch_launch(b->rfi, s));
-    PV_TRY(mark(2));
-    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_step, s));
-    PV_TRY(mark(3));
-    PV_TRY(pv::dd_batch_launch(b->dd, b->d_step, s));
-    PV_TRY(mark(4));
-    for (int i = 0; i < b->n; ++i) {
-        pv_beam* x = b->beams[i];
-        const pv_beam_config& c = x->cfg;
-        PV_TRY(pv::analyse_launch(x->d_out, c.chunk, c.tdms, c.chunk, c.threshold, x->rms, c.bin_pow2,
-                                  x->d_events, x->cap, x->d_total, x->d_scratch, s));
-        PV_CUDA(cudaMemcpyAsync(b->h_totals + i, x->d_total, sizeof(long long), cudaMemcpyDeviceToHost, s),
-                "read event count");
+    PV_TRY(mark(1, s));
+    if (b->pipelined) {
+        PV_CUDA(cudaEventRecord(b->fork_ev, s), "fork");
+        PV_CUDA(cudaStreamWaitEvent(sd, b->fork_ev, 0), "fork");
     }
-    PV_TRY(mark(5));
+    if (b->rfi && b->pipelined) {
+        // every clipper class resident at once: class 0 on s, the others on
+        // their own streams, joined back before the ring write
+        const int nk = pv::rfi_batch_launches(b->rfi);
+        for (int k = 1; k < nk; ++k) {
+            PV_CUDA(cudaStreamWaitEvent(b->rfi_side[k - 1], b->fork_ev, 0), "fork clipper");
+            PV_TRY(pv::rfi_batch_launch_one(b->rfi, k, b->rfi_side[k - 1]));
+            PV_CUDA(cudaEventRecord(b->rfi_join[k - 1], b->rfi_side[k - 1]), "join clipper");
+        }
+        if (nk > 0) PV_TRY(pv::rfi_batch_launch_one(b->rfi, 0, s));
+        for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(s, b->rfi_join[k - 1], 0), "join clipper");
+    } else if (b->rfi) {
+        PV_TRY(pv::rfi_batch_launch(b->rfi, s));
+    }
+    PV_TRY(mark(2, s));
+    auto dedisperse_branch = [&]() -> int {
+        PV_TRY(mark(6, sd));
+        PV_TRY(pv::dd_batch_launch(b->dd, b->d_step, sd));
+        PV_TRY(mark(4, sd));
+        for (int i = 0; i < b->n; ++i) {
+            pv_beam* x = b->beams[i];
+            const pv_beam_config& c = x->cfg;
+            PV_TRY(pv::analyse_launch(x->d_out, c.chunk, c.tdms, c.chunk, c.threshold, x->rms,
+                                      c.bin_pow2, x->d_events, x->cap, x->d_total, x->d_scratch, sd));
+        }
+        event_export_kernel<<<b->n, 256, 0, sd>>>(b->d_export, b->n, b->d_step,
+                                                 pv::dd_batch_status_word(b->dd), b->h_counts,
+                                                 b->h_events, b->host_cap, b->h_status);
+        PV_TRY(pv::check_launch("event_export_kernel"));
+        return mark(5, sd);
+    };
+    if (b->pipelined) PV_TRY(dedisperse_branch());
+    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_step, s));
+    PV_TRY(mark(3, s));
+    if (b->pipelined) {
+        PV_CUDA(cudaEventRecord(b->join_ev, sd), "join");
+        PV_CUDA(cudaStreamWaitEvent(s, b->join_ev, 0), "join");
+    } else {
+        PV_TRY(dedisperse_branch());
+    }
     step_advance_kernel<<<1, 1, 0, s>>>(b->d_step);
     return pv::check_launch("step_advance_kernel");
 }
@@ -139,9 +237,12 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
     b->n = nbeams;
     b->flags = flags;
     b->beams.assign(nbeams, nullptr);
-    b->d_in.assign(nbeams, nullptr);
+    b->d_in.assign(2 * nbeams, nullptr);
     b->in_bytes.assign(nbeams, 0);
     b->d_hist.assign(2 * nbeams, nullptr);
+    b->lag_eff.assign(nbeams, 0);
+    b->base.assign(nbeams, 0);
+    b->pipelined = (flags & PV_BATCH_PIPELINED) != 0;
     int rc = PV_OK;
     auto fail = [&](int code) {
         destroy(b);
@@ -164,12 +265,16 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
                           i);
             return fail(PV_ERR_CONFIG);
         }
-        rc = pv_beam_create(&b->beams[i], &c);
+        const int extra = (flags & PV_BATCH_PIPELINED) ? 1 : 0;
+        rc = pv::beam_create(&b->beams[i], &c, extra);
         if (rc != PV_OK) return fail(rc);
         pv_beam* x = b->beams[i];
+        b->lag_eff[i] = x->lag + extra;
+        b->base[i] = (int)x->chunks;  // lag when prefilled, else 0
         b->in_bytes[i] = pv_beam_input_bytes(x, 1);
         const size_t hist = sizeof(float2) * (size_t)c.nsub * 2 * 7 * c.nchan_sub;
         cudaError_t e = cudaMalloc(&b->d_in[i], b->in_bytes[i]);
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_in[nbeams + i], b->in_bytes[i]);
         for (int h = 0; h < 2 && e == cudaSuccess; ++h) {
             e = cudaMalloc(&b->d_hist[2 * i + h], hist);
             if (e == cudaSuccess) e = cudaMemset(b->d_hist[2 * i + h], 0, hist);
@@ -199,6 +304,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         }
         pv::ChanJob j{};
         j.in = b->d_in[i];
+        j.in_odd = b->d_in[nbeams + i];
         j.hist[0] = b->d_hist[2 * i];
         j.hist[1] = b->d_hist[2 * i + 1];
         j.coeffs = coeffs;
@@ -270,21 +376,58 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             d.nchan = nchan;
             d.nout = chunk;
             d.tdms = tdms;
-            d.lag = x->lag;
+            d.lag = b->lag_eff[i];
             d.chunk = chunk;
-            d.base = (int)x->chunks;  // lag when the beam starts prefilled, else 0
+            d.base = b->base[i];
         }
         const int variant = (flags & PV_BATCH_TUNE) ? -1 : PV_BATCH_VARIANT_OF(flags);
         rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, s0);
         if (rc != PV_OK) return fail(rc);
     }
-    if (cudaMalloc(&b->d_step, sizeof(long long)) != cudaSuccess ||
-        cudaMemset(b->d_step, 0, sizeof(long long)) != cudaSuccess ||
-        cudaMallocHost(&b->h_totals, sizeof(long long) * nbeams) != cudaSuccess) {
-        pv::set_error("pv_batch_create: cannot allocate the step counter");
-        return fail(PV_ERR_NOMEM);
+    {
+        long long cap = 0;
+        std::vector<ExportJob> ej(nbeams);
+        for (int i = 0; i < nbeams; ++i) {
+            pv_beam* x = b->beams[i];
+            ej[i] = ExportJob{x->d_events, x->d_total, x->cap};
+            cap = std::max(cap, x->cap);
+        }
+        b->host_cap = std::min<long long>(cap, PV_BATCH_HOST_EVENTS);
+        const size_t counts = sizeof(long long) * 2 * nbeams, status = 16;
+        const size_t bytes = counts + status + sizeof(pv_event) * 2 * (size_t)nbeams * b->host_cap;
+        if (cudaMalloc(&b->d_step, sizeof(long long)) != cudaSuccess ||
+            cudaMemset(b->d_step, 0, sizeof(long long)) != cudaSuccess ||
+            cudaMalloc(&b->d_export, sizeof(ExportJob) * nbeams) != cudaSuccess ||
+            cudaMemcpy(b->d_export, ej.data(), sizeof(ExportJob) * nbeams, cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaHostAlloc(&b->h_mapped, bytes, cudaHostAllocMapped) != cudaSuccess) {
+            pv::set_error("pv_batch_create: cannot allocate the step counter and event slots");
+            return fail(PV_ERR_NOMEM);
+        }
+        std::memset(b->h_mapped, 0, bytes);
+        b->h_counts = static_cast<long long*>(b->h_mapped);
+        b->h_status = reinterpret_cast<int*>(static_cast<char*>(b->h_mapped) + counts);
+        b->h_events = reinterpret_cast<pv_event*>(static_cast<char*>(b->h_mapped) + counts + status);
+        if (cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&b->rfi_side[0], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&b->rfi_side[1], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&b->rfi_side[2], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_join[0], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_join[1], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_join[2], cudaEventDisableTiming) != cudaSuccess) {
+            pv::set_error("pv_batch_create: cannot create streams");
+            return fail(PV_ERR_CUDA);
+        }
+        for (int i = 0; i < 2; ++i)
+            if (cudaEventCreateWithFlags(&b->done[i], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&b->copied[i], cudaEventDisableTiming) != cudaSuccess) {
+                pv::set_error("pv_batch_create: cudaEventCreate failed");
+                return fail(PV_ERR_CUDA);
+            }
     }
-    std::fill(b->h_totals, b->h_totals + nbeams, 0LL);
     if (flags & PV_BATCH_TIMING) {
         for (auto& e : b->ev)
             if (cudaEventCreate(&e) != cudaSuccess) {
@@ -310,62 +453,86 @@ extern "C" void pv_batch_destroy(pv_batch* b) {
 
 extern "C" int pv_batch_input(pv_batch* b, int beam, void** d_voltages, long long* bytes) {
     if (!b || beam < 0 || beam >= b->n) return PV_ERR_ARG;
-    if (d_voltages) *d_voltages = b->d_in[beam];
+    // the buffer the next step reads (steps alternate between two sets)
+    if (d_voltages) *d_voltages = b->d_in[(size_t)(b->step & 1) * b->n + beam];
     if (bytes) *bytes = b->in_bytes[beam];
     return PV_OK;
 }
 
-extern "C" int pv_batch_run(pv_batch* b, void* stream) {
-    if (!b) return PV_ERR_ARG;
-    cudaStream_t s = pv::as_stream(stream);
+namespace {
+
+int launch_step(pv_batch* b, cudaStream_t s) {
+    const int par = (int)(b->step & 1);
     if (b->exec) {
         PV_CUDA(cudaGraphLaunch(b->exec, s), "launch step graph");
         pv::count_launch(b->graph_kernels);
     } else {
         PV_TRY(enqueue_step(b, s, false));
     }
+    PV_CUDA(cudaEventRecord(b->done[par], s), "record step completion");
+    b->done_valid[par] = true;
     b->step += 1;
     b->timed = (b->flags & PV_BATCH_TIMING) != 0;
     return PV_OK;
 }
 
+}  // namespace
+
+extern "C" int pv_batch_run(pv_batch* b, void* stream) {
+    if (!b) return PV_ERR_ARG;
+    return launch_step(b, pv::as_stream(stream));
+}
+
 extern "C" int pv_batch_run_host(pv_batch* b, const void* const* h_voltages, void* stream) {
     if (!b || !h_voltages) return PV_ERR_ARG;
     cudaStream_t s = pv::as_stream(stream);
-    for (int i = 0; i < b->n; ++i) {
+    const int par = (int)(b->step & 1);
+    for (int i = 0; i < b->n; ++i)
         if (!h_voltages[i]) {
             pv::set_error("pv_batch_run_host: no voltages for beam %d", i);
             return PV_ERR_ARG;
         }
-        PV_CUDA(cudaMemcpyAsync(b->d_in[i], h_voltages[i], b->in_bytes[i], cudaMemcpyHostToDevice, s),
+    // the buffers of this parity were last read by the step two back
+    if (b->done_valid[par]) PV_CUDA(cudaStreamWaitEvent(b->copy_stream, b->done[par], 0), "wait");
+    for (int i = 0; i < b->n; ++i)
+        PV_CUDA(cudaMemcpyAsync(b->d_in[(size_t)par * b->n + i], h_voltages[i], b->in_bytes[i],
+                                cudaMemcpyHostToDevice, b->copy_stream),
                 "copy voltages to the device");
-    }
-    return pv_batch_run(b, stream);
+    PV_CUDA(cudaEventRecord(b->copied[par], b->copy_stream), "record copy");
+    PV_CUDA(cudaStreamWaitEvent(s, b->copied[par], 0), "wait for the copy");
+    return launch_step(b, s);
 }
 
-extern "C" int pv_batch_events(pv_batch* b, int beam, pv_event* h_events, long long cap,
-                               long long* h_count, long long* h_first_sample, void* stream) {
+extern "C" int pv_batch_events(pv_batch* b, int beam, long long step, pv_event* h_events,
+                               long long cap, long long* h_count, long long* h_first_sample) {
     if (!b || beam < 0 || beam >= b->n || !h_count) return PV_ERR_ARG;
-    PV_CUDA(cudaStreamSynchronize(pv::as_stream(stream)), "synchronise");
-    int status = PV_OK;
-    PV_TRY(pv::dd_batch_status(b->dd, &status));
+    if (step < 0) step = b->step - 1;
+    if (step < 0 || step >= b->step || step < b->step - 2) {
+        pv::set_error("pv_batch_events: step %lld is not one of the last two issued (%lld)", step,
+                      b->step);
+        return PV_ERR_ARG;
+    }
+    const int par = (int)(step & 1);
+    PV_CUDA(cudaEventSynchronize(b->done[par]), "wait for the step");
+    const int status = ((volatile int*)b->h_status)[par];
     if (status != PV_OK) {
         pv::set_error("pv_batch_events: a dedispersion pipeline wait gave up (status %d)", status);
         return status;
     }
     pv_beam* x = b->beams[beam];
-    const long long w = b->step + x->chunks - 1 - x->lag;  // x->chunks: prefilled chunks
+    const long long w = step + b->base[beam] - b->lag_eff[beam];
     if (w < 0) {
         *h_count = 0;
         if (h_first_sample) *h_first_sample = -1;
         return PV_OK;
     }
-    *h_count = b->h_totals[beam];
+    const long long total = ((volatile long long*)b->h_counts)[(size_t)par * b->n + beam];
+    *h_count = total;
     if (h_first_sample) *h_first_sample = w * x->cfg.chunk;
-    const long long n = std::min(std::min(b->h_totals[beam], x->cap), cap);
+    const long long n = std::min(std::min(total, std::min(x->cap, b->host_cap)), cap);
     if (h_events && n > 0)
-        PV_CUDA(cudaMemcpy(h_events, x->d_events, sizeof(pv_event) * n, cudaMemcpyDeviceToHost),
-                "copy events");
+        std::memcpy(h_events, b->h_events + ((size_t)par * b->n + beam) * b->host_cap,
+                    sizeof(pv_event) * n);
     return PV_OK;
 }
 
@@ -377,8 +544,8 @@ extern "C" int pv_batch_info(const pv_batch* b, int beam, long long* h_info8) {
     h_info8[2] = x->lag;
     h_info8[3] = x->ring_len;
     h_info8[4] = x->inverted;
-    h_info8[5] = b->step + x->chunks;
-    h_info8[6] = b->step + x->chunks - 1 - x->lag;
+    h_info8[5] = b->step + b->base[beam];
+    h_info8[6] = b->step + b->base[beam] - 1 - b->lag_eff[beam];
     h_info8[7] = (long long)x->nbins * x->row_stride * (long long)sizeof(float);
     return PV_OK;
 }
@@ -405,9 +572,10 @@ extern "C" int pv_batch_stage_ms(pv_batch* b, float* h_ms5) {
         pv::set_error("pv_batch_stage_ms: timing is off or no step ran");
         return PV_ERR_STATE;
     }
+    const int from[5] = {0, 1, 2, 6, 4}, to[5] = {1, 2, 3, 4, 5};
     for (int i = 0; i < 5; ++i) {
-        PV_CUDA(cudaEventSynchronize(b->ev[i + 1]), "synchronise stage event");
-        PV_CUDA(cudaEventElapsedTime(&h_ms5[i], b->ev[i], b->ev[i + 1]), "stage time");
+        PV_CUDA(cudaEventSynchronize(b->ev[to[i]]), "synchronise stage event");
+        PV_CUDA(cudaEventElapsedTime(&h_ms5[i], b->ev[from[i]], b->ev[to[i]]), "stage time");
     }
     return PV_OK;
 }

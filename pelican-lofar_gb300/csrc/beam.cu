@@ -35,8 +35,12 @@ void destroy(pv_beam* b) {
 
 }  // namespace
 
-extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
-    if (!out || !c) return PV_ERR_ARG;
+namespace pv {
+
+// pv_beam_create with `extra` more chunks of ring than the delays need (the
+// batch's pipelined mode writes chunk k while window k-lag-1 is read).
+int beam_create(pv_beam** out, const pv_beam_config* c, int extra) {
+    if (!out || !c || extra < 0) return PV_ERR_ARG;
     *out = nullptr;
     if (c->nsub <= 0 || c->nchan_sub <= 0 || c->int_time <= 0 || c->int_chan <= 0 ||
         c->nchan_sub % c->int_chan != 0 || c->chunk <= 0 || c->tdms <= 0 || c->tsamp <= 0.0) {
@@ -63,7 +67,7 @@ extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
     }
     b->max_shift = pv_dedisp_plan_max_shift(b->plan);
     b->lag = (b->max_shift + c->chunk - 1) / c->chunk;
-    b->ring_len = (long long)(b->lag + 1) * c->chunk;
+    b->ring_len = (long long)(b->lag + 1 + extra) * c->chunk;
     b->row_stride = (b->ring_len + 31) / 32 * 32;
     b->cap = c->event_capacity > 0 ? c->event_capacity : (1LL << 20);
     b->rms = std::sqrt((float)b->nchan_fb * (float)c->nsub);  // DedispersionAnalyser.cpp:38
@@ -99,6 +103,12 @@ extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
     }
     *out = b;
     return PV_OK;
+}
+
+}  // namespace pv
+
+extern "C" int pv_beam_create(pv_beam** out, const pv_beam_config* c) {
+    return pv::beam_create(out, c, 0);
 }
 
 extern "C" void pv_beam_destroy(pv_beam* b) {

@@ -244,7 +244,8 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     const int par = d_step ? (int)(*d_step & 1) : 0;
     const float2* hin = J.hist[par];
     float2* hout = J.hist[par ^ 1];
-    const Raw* in = reinterpret_cast<const Raw*>(J.in) + row * nblocks * N + j;
+    const void* src = (par && J.in_odd) ? J.in_odd : J.in;
+    const Raw* in = reinterpret_cast<const Raw*>(src) + row * nblocks * N + j;
 
     float cf[T][M];
 #pragma unroll

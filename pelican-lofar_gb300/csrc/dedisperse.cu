@@ -927,6 +927,7 @@ int dd_batch_shape(const DdBatch* b, int* h8) {
 }
 
 const std::vector<int>& dd_batch_dms(const DdBatch* b) { return b->dms; }
+const int* dd_batch_status_word(const DdBatch* b) { return b->d_status; }
 const std::vector<float>& dd_batch_tune_ms(const DdBatch* b) { return b->tune_ms; }
 
 }  // namespace pv

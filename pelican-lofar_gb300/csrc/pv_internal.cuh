@@ -10,6 +10,7 @@ namespace pv {
 // One beam's share of a Stokes-I channeliser launch (chan_stokes_i_kernel).
 struct ChanJob {
     const void* in;          // [sub][2][nblocks*N] short2 or float2 voltages
+    const void* in_odd;      // read instead of `in` at odd device steps (null: always `in`)
     float2* hist[2];         // [sub][2][7][N]: hist[step & 1] is read (null: zeros), the other written
     const float* coeffs;     // [8][N]
     const float2* twiddle;   // [N/2] exp(-2 pi i k / N)
@@ -59,6 +60,7 @@ int dd_batch_launch(DdBatch* b, const long long* d_step, cudaStream_t s);
 int dd_batch_status(const DdBatch* b, int* h_status);
 int dd_batch_shape(const DdBatch* b, int* h8);
 const std::vector<int>& dd_batch_dms(const DdBatch* b);
+const int* dd_batch_status_word(const DdBatch* b);
 const std::vector<float>& dd_batch_tune_ms(const DdBatch* b);
 void dd_batch_destroy(DdBatch* b);
 
@@ -67,7 +69,8 @@ struct RfiBatch;
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
                      const int* nchan, int n, int nt, cudaStream_t s);
 int rfi_batch_launch(RfiBatch* b, cudaStream_t s);
-int rfi_batch_launches(const RfiBatch* b);
+int rfi_batch_launches(const RfiBatch* b);  // number of CTA-size classes
+int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s);
 void rfi_batch_destroy(RfiBatch* b);
 
 // Batched ring writes (buffer.cu): stokes [nt][nsub][1][nchan] of one beam.
@@ -93,6 +96,10 @@ int analyse_launch(const float* data, long long ld, int tdms, int nsamp, float t
                    cudaStream_t s);
 
 }  // namespace pv
+
+namespace pv {
+int beam_create(pv_beam** out, const pv_beam_config* c, int extra_ring_chunks);
+}
 
 // One beam's device-resident chain state (beam.cu); the batch engine reuses it.
 struct pv_beam {

@@ -1028,10 +1028,13 @@ int rfi_batch_launch(RfiBatch* b, cudaStream_t s) {
     return PV_OK;
 }
 
-int rfi_batch_launches(const RfiBatch* b) {
-    int n = 0;
-    for (auto& c : b->classes) n += c.njobs > 0;
-    return n;
+int rfi_batch_launches(const RfiBatch* b) { return (int)b->classes.size(); }
+
+int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s) {
+    auto& c = b->classes[k];
+    if (c.njobs == 0) return PV_OK;
+    return rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0, Geo{},
+                      nullptr, s);
 }
 
 }  // namespace pv

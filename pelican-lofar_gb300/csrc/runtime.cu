@@ -120,3 +120,22 @@ extern "C" int pv_device_copy(void* dst, const void* src, long long bytes, void*
             "pv_device_copy");
     return PV_OK;
 }
+
+extern "C" int pv_host_alloc(void** h_ptr, long long bytes, int write_combined) {
+    if (!h_ptr || bytes <= 0) {
+        pv::set_error("pv_host_alloc: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const unsigned flags = cudaHostAllocPortable | (write_combined ? cudaHostAllocWriteCombined : 0u);
+    const cudaError_t e = cudaHostAlloc(h_ptr, (size_t)bytes, flags);
+    if (e != cudaSuccess) {
+        *h_ptr = nullptr;
+        pv::set_error("pv_host_alloc: %s (%lld bytes)", cudaGetErrorString(e), bytes);
+        return PV_ERR_NOMEM;
+    }
+    return PV_OK;
+}
+
+extern "C" void pv_host_free(void* h_ptr) {
+    if (h_ptr) cudaFreeHost(h_ptr);
+}

@@ -89,12 +89,14 @@ def _declare(L):
         "pv_beam_info": (i, [vp, P(ll)]),
         "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
         "pv_beam_stage_ms": (i, [vp, P(C.c_float)]),
+        "pv_host_alloc": (i, [P(vp), ll, i]),
+        "pv_host_free": (None, [vp]),
         "pv_batch_create": (i, [P(vp), vp, i, i]),
         "pv_batch_destroy": (None, [vp]),
         "pv_batch_input": (i, [vp, i, P(vp), P(ll)]),
         "pv_batch_run": (i, [vp, vp]),
         "pv_batch_run_host": (i, [vp, P(vp), vp]),
-        "pv_batch_events": (i, [vp, i, vp, ll, P(ll), P(ll), vp]),
+        "pv_batch_events": (i, [vp, i, ll, vp, ll, P(ll), P(ll)]),
         "pv_batch_info": (i, [vp, i, P(ll)]),
         "pv_batch_tiles": (i, [vp, P(i), P(i), P(C.c_float), P(ll)]),
         "pv_batch_stage_ms": (i, [vp, P(C.c_float)]),
@@ -413,17 +415,19 @@ class Beam:
             self.h = C.c_void_p()
 
 
-BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING = 1, 2, 4
+BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
+HOST_EVENTS = 65536  # PV_BATCH_HOST_EVENTS
 
 
 class Batch:
     """Many beams advanced one chunk per step by batched launches (pv_batch)."""
 
-    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0):
+    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0, pipelined=False):
         self.cfgs = list(cfgs)
+        self.pipelined = pipelined
         self._arr = (BeamConfig * len(self.cfgs))(*self.cfgs)
         flags = (BATCH_TUNE if tune else (variant << 8)) | (BATCH_GRAPH if graph else 0) | \
-            (BATCH_TIMING if timing else 0)
+            (BATCH_TIMING if timing else 0) | (BATCH_PIPELINED if pipelined else 0)
         self.h = C.c_void_p()
         check(load().pv_batch_create(C.byref(self.h), self._arr, len(self.cfgs), flags))
 
@@ -449,14 +453,16 @@ class Batch:
             *[C.c_void_p(v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data) for v in h_voltages])
         check(load().pv_batch_run_host(self.h, ptrs, _stream(stream)))
 
-    def events(self, beam, cap=1 << 20, stream=None):
+    def events(self, beam, step=-1, cap=1 << 16):
+        """(events, total count, first sample) of one beam at one of the last
+        two issued steps (-1: the last); waits for that step only."""
         n, first = C.c_longlong(), C.c_longlong()
-        check(load().pv_batch_events(self.h, beam, None, 0, C.byref(n), C.byref(first), _stream(stream)))
-        k = min(n.value, cap)
+        check(load().pv_batch_events(self.h, beam, step, None, 0, C.byref(n), C.byref(first)))
+        k = min(n.value, cap, HOST_EVENTS)
         ev = np.zeros(k, EVENT_DTYPE)
         if k:
-            check(load().pv_batch_events(self.h, beam, C.c_void_p(ev.ctypes.data), k, C.byref(n),
-                                         C.byref(first), _stream(stream)))
+            check(load().pv_batch_events(self.h, beam, step, C.c_void_p(ev.ctypes.data), k, C.byref(n),
+                                         C.byref(first)))
         return ev, n.value, first.value
 
     def info(self, beam):
@@ -490,6 +496,37 @@ class Batch:
         if getattr(self, "h", None) and self.h.value and _lib is not None:
             _lib.pv_batch_destroy(self.h)
             self.h = C.c_void_p()
+
+
+class HostBuffer:
+    """Page-locked host memory from the library (optionally write-combined)."""
+
+    def __init__(self, nbytes, write_combined=False, int16=True):
+        self.nbytes = int(nbytes)
+        self.int16 = int16
+        p = C.c_void_p()
+        check(load().pv_host_alloc(C.byref(p), self.nbytes, int(write_combined)))
+        self.ptr = p.value
+
+    def data_ptr(self):
+        return self.ptr
+
+    @property
+    def dtype(self):
+        import torch
+        return torch.int16 if self.int16 else torch.complex64
+
+    def fill_from(self, tensor, stream=None):
+        """Copies a device (or host) tensor of the same size into the buffer and waits."""
+        assert tensor.numel() * tensor.element_size() == self.nbytes
+        check(load().pv_device_copy(C.c_void_p(self.ptr), _ptr(tensor), self.nbytes, _stream(stream)))
+        import torch
+        torch.cuda.synchronize()
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.pv_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
 
 
 def device_array(ptr, shape, device=None):

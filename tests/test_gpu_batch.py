@@ -55,16 +55,20 @@ def mix_configs(pv, cuda):
     return [calibrated(pv, cuda, beam_kw(**m), rng) for m in MIX]
 
 
-@pytest.mark.parametrize("tune,graph,variant,prefilled", [(True, True, 0, False), (False, False, 1, False),
-                                                           (False, True, 3, True)])
-def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled):
+@pytest.mark.parametrize("tune,graph,variant,prefilled,pipelined",
+                         [(True, True, 0, False, False), (False, False, 1, False, False),
+                          (False, True, 3, True, False), (False, True, 0, False, True),
+                          (True, True, 0, True, True)])
+def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled, pipelined):
+    """Filterbank, event list and dedispersed window of every beam equal the
+    single-beam chain's; pipelined, a window arrives one step later."""
     import torch
     cfgs = mix_configs
     if prefilled:  # rings start as lag chunks of silence: windows from the first chunk on
         cfgs = [type(c).from_buffer_copy(c) for c in cfgs]
         for c, o in zip(cfgs, mix_configs):
             c._bp, c.bp_text, c.prefilled = o._bp, o._bp, 1
-    batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant)
+    batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant, pipelined=pipelined)
     alone = [pv.Beam(c) for c in cfgs]
     lags = [batch.info(i)["lag"] for i in range(len(cfgs))]
     assert lags == [b.info()["lag"] for b in alone]
@@ -74,9 +78,11 @@ def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, p
         assert min(shape["dms"]) < 16  # the wide-spread beam needs a short DM tile
     if graph:
         assert shape["graph_kernels"] >= len(cfgs)
+    delay = 1 if pipelined else 0
     rng = np.random.default_rng(7)
+    history = []  # per step: per beam (events, count, first, dedispersed or None)
     compared = events_seen = 0
-    for step in range(max(lags) + 3):
+    for step in range(max(lags) + 3 + delay):
         ins = []
         for c in cfgs:
             v16, _ = voltages(rng, c.nsub, 2, c.chunk * 4 * c.nchan_sub)
@@ -86,21 +92,28 @@ def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, p
             alone[i].process(x)
         batch.run()
         torch.cuda.synchronize()
+        rec = []
         for i, (c, b) in enumerate(zip(cfgs, alone)):
             nbins = c.nsub * c.nchan_sub
             fb_b, out_b, _ = batch.buffers(i)
             fb_a, _, out_a, _ = b.buffers()
             assert np.array_equal(pv.device_array(fb_b, (c.chunk, nbins)).cpu().numpy(),
                                   pv.device_array(fb_a, (c.chunk, nbins)).cpu().numpy())
-            eb, nb, firstb = batch.events(i)
             ea, na, firsta = b.events()
+            da = pv.device_array(out_a, (c.tdms, c.chunk)).cpu().numpy() if firsta >= 0 else None
+            rec.append((ea, na, firsta, da))
+            eb, nb, firstb = batch.events(i)
+            if step < delay:
+                assert firstb == -1
+                continue
+            ea, na, firsta, da = history[step - delay][i] if delay else rec[i]
             assert (nb, firstb) == (na, firsta)
             assert np.array_equal(eb, ea)
             if firsta >= 0:
-                assert np.array_equal(pv.device_array(out_b, (c.tdms, c.chunk)).cpu().numpy(),
-                                      pv.device_array(out_a, (c.tdms, c.chunk)).cpu().numpy())
+                assert np.array_equal(pv.device_array(out_b, (c.tdms, c.chunk)).cpu().numpy(), da)
                 compared += 1
                 events_seen += na - 1
+        history.append(rec)
     assert compared >= len(cfgs) * 3
     if prefilled:
         assert compared == len(cfgs) * (max(lags) + 3)
@@ -122,3 +135,34 @@ def test_batch_rejects_unsupported_beams(pv, cuda, mix_configs):
     other_chunk = pv.beam_config(**dict(beam_kw(4, 16, 16, 1.0, chunk=256), bp_text=None, rfi_active=0))
     with pytest.raises(pv.PvError, match="same chunk"):
         pv.Batch([mix_configs[0], other_chunk])
+
+
+def test_batch_host_steps_overlap_and_events_of_previous_step(pv, cuda, mix_configs):
+    """run_host returns before its step finishes; the events of step k are read
+    while step k+1 runs and equal those of the beams run alone."""
+    import torch
+    cfgs = mix_configs[:3]
+    batch = pv.Batch(cfgs, tune=False, graph=True)
+    alone = [pv.Beam(c) for c in cfgs]
+    rng = np.random.default_rng(11)
+    want = []
+    nsteps = max(batch.info(i)["lag"] for i in range(len(cfgs))) + 3
+    hosts_prev = None
+    for step in range(nsteps):
+        hosts = []
+        for c in cfgs:
+            v16, _ = voltages(rng, c.nsub, 2, c.chunk * 4 * c.nchan_sub)
+            hosts.append(torch.from_numpy(v16.reshape(c.nsub, 2, -1)).pin_memory())
+        want.append([b.events()[:2] if b.process_host(h) is None else None for b, h in zip(alone, hosts)])
+        batch.run_host(hosts)
+        if step:
+            for i in range(len(cfgs)):
+                ev, n, _ = batch.events(i, step=step - 1)
+                assert n == want[step - 1][i][1] and np.array_equal(ev, want[step - 1][i][0])
+        hosts_prev = hosts  # pinned sources stay alive until their copies are done
+    for i in range(len(cfgs)):
+        ev, n, _ = batch.events(i)
+        assert n == want[-1][i][1] and np.array_equal(ev, want[-1][i][0])
+    with pytest.raises(pv.PvError, match="last two"):
+        batch.events(0, step=0)
+    del hosts_prev
