@@ -55,6 +55,9 @@ import numpy as np
 
 SUB_BW = 0.1953125  # MHz
 RAW_TSAMP = 5.12e-6  # s
+# DRAM bytes per FP32 add of dedisperse_batch_kernel: 1.776 GB for 5.12e10 adds, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the first 3 beams with 1024-sample chunks
+DD_BATCH_BYTES_PER_ADD = 1.776e9 / 5.1204063232e10
 
 
 def beam_dict(nsub, nchan_sub, dm_max, tdms, chunk, **kw):
@@ -494,7 +497,12 @@ def run_batch(args, cfgs, workload):
     chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
     roofline = {"kernel": "dedisperse_batch_kernel", "bound": "fp32",
                 "achieved": achieved / 1e12, "peak": fadd_peak / 1e12, "unit": "Tadd/s",
-                "frac": achieved / fadd_peak, "traffic": None,
+                "frac": achieved / fadd_peak,
+                "smem_bound_frac": achieved / (fadd_peak / 4),
+                "smem_bound": "one 4-byte shared-memory read per add: 32 of 128 lanes per clock",
+                "traffic": DD_BATCH_BYTES_PER_ADD * units_step,
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
+                                  "on the 3-beam, 1024-sample case, scaled by adds",
                 "peak_source": "%d SMs x 128 FP32 lanes x sm_max_mhz of MEASURED_PEAKS.json (%s)"
                                % (nsm, peak_src),
                 "per_unit": "one FP32 add per DM-trial*channel*sample (%d per launch)" % units_step,
