@@ -355,8 +355,9 @@ typedef struct pv_batch pv_batch;
 #define PV_BATCH_TUNE 1   /* autotune the dedispersion DM x time tile shape */
 #define PV_BATCH_GRAPH 2  /* capture one step as a CUDA graph, replay it per step */
 #define PV_BATCH_TIMING 4 /* record stage times of every step */
-#define PV_BATCH_PIPELINED 8 /* dedisperse window k-lag-1 while chunk k is channelised and
-                                clipped (rings one chunk longer; events one step later) */
+#define PV_BATCH_PIPELINED 8 /* dedisperse a beam's window in its step after the chunk that
+                                completes it, beside that step's channeliser and clippers
+                                (rings one chunk longer) */
 #define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
@@ -366,21 +367,30 @@ void pv_batch_destroy(pv_batch* batch);
  * (pv_beam_input_bytes(.., 1) bytes, [sub][pol][sample] complex int16).
  * Steps alternate between two buffer sets, so ask again before every step. */
 int pv_batch_input(pv_batch* batch, int beam, void** d_voltages, long long* bytes);
-/* One step of every beam from the input buffers, asynchronously. */
-int pv_batch_run(pv_batch* batch, void* stream);
-/* Copies h_voltages[beam] (host, pinned for speed) to the next step's input
- * buffers on the batch's own copy stream, then runs the step on `stream`
- * once the copies land.  Returns at once: the copies of step k+1 overlap
- * the computation of step k. */
-int pv_batch_run_host(pv_batch* batch, const void* const* h_voltages, void* stream);
+/* One step from the input buffers, asynchronously.  h_active[beam] != 0
+ * (h_active NULL: every beam) marks the beams that have a chunk this step;
+ * the others keep their state and skip every stage (a serving loop's
+ * continuous batching).  A beam dedisperses a window in the step whose chunk
+ * completes it; pipelined, in the next step (whether or not the beam has a
+ * chunk then).  At most two steps are in flight: issuing a step waits for
+ * the step two back. */
+int pv_batch_run(pv_batch* batch, const unsigned char* h_active, void* stream);
+/* Copies h_voltages[beam] of the active beams (host, page-locked for speed)
+ * to their input buffers on the batch's own copy stream, then runs the step
+ * on `stream` once the copies land.  Returns at once: the copies of step
+ * k+1 overlap the computation of step k. */
+int pv_batch_run_host(pv_batch* batch, const void* const* h_voltages, const unsigned char* h_active,
+                      void* stream);
 /* Events of one beam at one of the last two issued steps (step < 0: the
  * last), as pv_beam_events: total count including the dummy, the window's
- * first sample (-1 while the ring fills) and up to cap events (at most
- * PV_BATCH_HOST_EVENTS) copied to h_events.  Waits for that step only, so
- * the next step may already be running. */
+ * first sample (-1: the beam dedispersed no window in that step) and up to
+ * cap events (at most PV_BATCH_HOST_EVENTS) copied to h_events.  Waits for
+ * that step only, so the next step may already be running. */
 int pv_batch_events(pv_batch* batch, int beam, long long step, pv_event* h_events, long long cap,
                     long long* h_count, long long* h_first_sample);
-/* As pv_beam_info, for one beam of the batch. */
+/* [dedispersion channels, max delay, lag in chunks, ring samples, inverted,
+ *  chunks in the ring (prefilled silence included), last window dedispersed
+ *  (-1: none), ring bytes] after the steps issued. */
 int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
 /* Dedispersion tiling: [variant, time tile, channels per stage, stages,
  * slot floats, tiles, CTAs, shared bytes], the DM tile height of every beam,

@@ -33,7 +33,31 @@
 
 namespace {
 
-__global__ void step_advance_kernel(long long* step) { *step += 1; }
+// First kernel of a step: which beams process a chunk (the host's mask for
+// this step, read from host-mapped memory) and which dedisperse a window.
+// Window w needs ring chunks w..w+lag; pipelined, the chunk written in this
+// step is not yet usable.
+__global__ void plan_kernel(pv::BeamStep* __restrict__ bs, int n, const long long* __restrict__ d_step,
+                            const int* h_mask, int pipelined) {
+    const int par = (int)(*d_step & 1);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        pv::BeamStep& B = bs[b];
+        const int active = ((const volatile int*)h_mask)[par * n + b] != 0;
+        const long long avail = B.written + (pipelined ? 0 : active);
+        B.active = active;
+        B.sel = B.done + B.lag + 1 <= avail;
+        B.window = B.done;
+    }
+}
+
+// Last kernel of a step: advance every beam's counters and the step.
+__global__ void advance_kernel(pv::BeamStep* __restrict__ bs, int n, long long* d_step) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        bs[b].written += bs[b].active;
+        bs[b].done += bs[b].sel;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_step += 1;
+}
 
 struct ExportJob {
     const pv_event* d_events;
@@ -41,20 +65,25 @@ struct ExportJob {
     long long cap;  // device event capacity of the beam
 };
 
-// Copies every beam's event count and first events of this step into the
-// host-mapped slot of the step's parity, with the dedispersion status word.
+// Copies every beam's event count (-1: no window this step), window index and
+// first events of this step into the host-mapped slot of the step's parity,
+// with the dedispersion status word.
 __global__ void event_export_kernel(const ExportJob* __restrict__ jobs, int n,
                                     const long long* __restrict__ d_step,
+                                    const pv::BeamStep* __restrict__ bs,
                                     const int* __restrict__ d_status, long long* h_counts,
-                                    pv_event* h_events, long long host_cap, int* h_status) {
+                                    long long* h_windows, pv_event* h_events, long long host_cap,
+                                    int* h_status) {
     const int b = blockIdx.x;
     const int par = (int)(*d_step & 1);
-    const long long total = *jobs[b].d_total;
-    const long long k = min(min(total, jobs[b].cap), host_cap);
+    const bool sel = bs[b].sel != 0;
+    const long long total = sel ? *jobs[b].d_total : -1;
+    const long long k = sel ? min(min(total, jobs[b].cap), host_cap) : 0;
     pv_event* dst = h_events + ((long long)par * n + b) * host_cap;
     for (long long i = threadIdx.x; i < k; i += blockDim.x) dst[i] = jobs[b].d_events[i];
     if (threadIdx.x == 0) {
         h_counts[(long long)par * n + b] = total;
+        h_windows[(long long)par * n + b] = bs[b].window;
         if (b == 0) h_status[par] = *d_status;
     }
 }
@@ -78,11 +107,16 @@ struct pv_batch {
     pv::RingJob* d_ring_jobs = nullptr;
     long long ring_blocks = 0;
     pv::DdBatch* dd = nullptr;
-    long long* d_step = nullptr;
+    long long* d_step = nullptr;    // steps issued (parity of the host slots)
+    pv::BeamStep* d_bs = nullptr;   // per-beam progress
     ExportJob* d_export = nullptr;
-    void* h_mapped = nullptr;       // host-mapped pinned: counts [2][n], status [2], events [2][n][host_cap]
-    long long* h_counts = nullptr;
-    int* h_status = nullptr;
+    void* h_mapped = nullptr;       // host-mapped pinned: counts, windows, masks, status, events
+    long long* h_counts = nullptr;  // [2][n]
+    long long* h_windows = nullptr; // [2][n]
+    int* h_mask = nullptr;          // [2][n]
+    int* h_status = nullptr;        // [2]
+    std::vector<pv::BeamStep> mirror;  // host copy of the per-beam progress after the last step issued
+    std::vector<long long> processed;  // chunks processed per beam (input parity)
     pv_event* h_events = nullptr;
     long long host_cap = 0;
     long long step = 0;             // steps issued
@@ -97,7 +131,6 @@ struct pv_batch {
     cudaEvent_t ev[7] = {};
     bool timed = false;
     bool pipelined = false;
-    std::vector<int> lag_eff, base;  // steps from a chunk to its window's completion; prefilled chunks
     cudaStream_t side = nullptr;     // second branch of a pipelined step
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     cudaStream_t rfi_side[3] = {};   // pipelined: one stream per clipper class after the first
@@ -125,6 +158,7 @@ void destroy(pv_batch* b) {
         if (c.d_jobs) cudaFree(c.d_jobs);
     if (b->d_ring_jobs) cudaFree(b->d_ring_jobs);
     if (b->d_step) cudaFree(b->d_step);
+    if (b->d_bs) cudaFree(b->d_bs);
     if (b->d_export) cudaFree(b->d_export);
     if (b->h_mapped) cudaFreeHost(b->h_mapped);
     if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
@@ -156,9 +190,11 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
                                "record stage event");
     };
     cudaStream_t sd = b->pipelined ? b->side : s;  // stream of the dedispersion branch
+    plan_kernel<<<1, 256, 0, s>>>(b->d_bs, b->n, b->d_step, b->h_mask, b->pipelined ? 1 : 0);
+    PV_TRY(pv::check_launch("plan_kernel"));
     PV_TRY(mark(0, s));
     for (auto& c : b->chan)
-        PV_TRY(pv::launch_chan_fast(c.nchan, 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps, b->d_step, s));
+        PV_TRY(pv::launch_chan_fast(c.nchan, 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps, b->d_bs, s));
     PV_TRY(mark(1, s));
     if (b->pipelined) {
         PV_CUDA(cudaEventRecord(b->fork_ev, s), "fork");
@@ -181,7 +217,7 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     PV_TRY(mark(2, s));
     auto dedisperse_branch = [&]() -> int {
         PV_TRY(mark(6, sd));
-        PV_TRY(pv::dd_batch_launch(b->dd, b->d_step, sd));
+        PV_TRY(pv::dd_batch_launch(b->dd, b->d_bs, sd));
         PV_TRY(mark(4, sd));
         for (int i = 0; i < b->n; ++i) {
             pv_beam* x = b->beams[i];
@@ -189,14 +225,15 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
             PV_TRY(pv::analyse_launch(x->d_out, c.chunk, c.tdms, c.chunk, c.threshold, x->rms,
                                       c.bin_pow2, x->d_events, x->cap, x->d_total, x->d_scratch, sd));
         }
-        event_export_kernel<<<b->n, 256, 0, sd>>>(b->d_export, b->n, b->d_step,
+        event_export_kernel<<<b->n, 256, 0, sd>>>(b->d_export, b->n, b->d_step, b->d_bs,
                                                  pv::dd_batch_status_word(b->dd), b->h_counts,
-                                                 b->h_events, b->host_cap, b->h_status);
+                                                 b->h_windows, b->h_events, b->host_cap,
+                                                 b->h_status);
         PV_TRY(pv::check_launch("event_export_kernel"));
         return mark(5, sd);
     };
     if (b->pipelined) PV_TRY(dedisperse_branch());
-    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_step, s));
+    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_bs, s));
     PV_TRY(mark(3, s));
     if (b->pipelined) {
         PV_CUDA(cudaEventRecord(b->join_ev, sd), "join");
@@ -204,8 +241,8 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     } else {
         PV_TRY(dedisperse_branch());
     }
-    step_advance_kernel<<<1, 1, 0, s>>>(b->d_step);
-    return pv::check_launch("step_advance_kernel");
+    advance_kernel<<<1, 256, 0, s>>>(b->d_bs, b->n, b->d_step);
+    return pv::check_launch("advance_kernel");
 }
 
 int capture(pv_batch* b) {
@@ -240,8 +277,8 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
     b->d_in.assign(2 * nbeams, nullptr);
     b->in_bytes.assign(nbeams, 0);
     b->d_hist.assign(2 * nbeams, nullptr);
-    b->lag_eff.assign(nbeams, 0);
-    b->base.assign(nbeams, 0);
+    b->mirror.assign(nbeams, pv::BeamStep{});
+    b->processed.assign(nbeams, 0);
     b->pipelined = (flags & PV_BATCH_PIPELINED) != 0;
     int rc = PV_OK;
     auto fail = [&](int code) {
@@ -269,8 +306,10 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         rc = pv::beam_create(&b->beams[i], &c, extra);
         if (rc != PV_OK) return fail(rc);
         pv_beam* x = b->beams[i];
-        b->lag_eff[i] = x->lag + extra;
-        b->base[i] = (int)x->chunks;  // lag when prefilled, else 0
+        pv::BeamStep& m = b->mirror[i];
+        m.base = x->chunks;  // lag when prefilled, else 0
+        m.written = m.base;
+        m.lag = x->lag;
         b->in_bytes[i] = pv_beam_input_bytes(x, 1);
         const size_t hist = sizeof(float2) * (size_t)c.nsub * 2 * 7 * c.nchan_sub;
         cudaError_t e = cudaMalloc(&b->d_in[i], b->in_bytes[i]);
@@ -286,6 +325,12 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         }
     }
     cudaStream_t s0 = nullptr;
+    if (cudaMalloc(&b->d_bs, sizeof(pv::BeamStep) * nbeams) != cudaSuccess ||
+        cudaMemcpy(b->d_bs, b->mirror.data(), sizeof(pv::BeamStep) * nbeams, cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        pv::set_error("pv_batch_create: cannot allocate the beam progress");
+        return fail(PV_ERR_NOMEM);
+    }
     // K1 jobs, one launch per channel count
     std::vector<std::vector<pv::ChanJob>> cj;
     for (int i = 0; i < nbeams; ++i) {
@@ -314,6 +359,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         j.nblocks = x->cfg.chunk * x->cfg.int_time;
         j.window = x->cfg.int_time;
         j.nu = x->cfg.chunk;
+        j.beam = i;
         j.warp_begin = b->chan[k].nwarps;
         b->chan[k].nwarps += pv::chan_job_warps(j);
         cj[k].push_back(j);
@@ -340,7 +386,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             nch[i] = b->beams[i]->nchan_fb;
         }
         rc = pv::rfi_batch_create(&b->rfi, hs.data(), data.data(), nsub.data(), nch.data(), nbeams,
-                                  chunk, s0);
+                                  chunk, b->d_bs, s0);
         if (rc != PV_OK) return fail(rc);
     }
     // A8: ring writes
@@ -349,7 +395,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         for (int i = 0; i < nbeams; ++i) {
             pv_beam* x = b->beams[i];
             rj[i] = pv::RingJob{x->d_ring, x->row_stride, x->ring_len, x->d_fb, chunk, x->cfg.nsub,
-                                x->nchan_fb, x->inverted, b->ring_blocks, x->chunks};
+                                x->nchan_fb, x->inverted, b->ring_blocks, i};
             b->ring_blocks += pv::ring_job_blocks(rj[i]);
         }
         if (cudaMalloc(&b->d_ring_jobs, sizeof(pv::RingJob) * nbeams) != cudaSuccess ||
@@ -376,9 +422,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             d.nchan = nchan;
             d.nout = chunk;
             d.tdms = tdms;
-            d.lag = b->lag_eff[i];
             d.chunk = chunk;
-            d.base = b->base[i];
         }
         const int variant = (flags & PV_BATCH_TUNE) ? -1 : PV_BATCH_VARIANT_OF(flags);
         rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, s0);
@@ -393,8 +437,9 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             cap = std::max(cap, x->cap);
         }
         b->host_cap = std::min<long long>(cap, PV_BATCH_HOST_EVENTS);
-        const size_t counts = sizeof(long long) * 2 * nbeams, status = 16;
-        const size_t bytes = counts + status + sizeof(pv_event) * 2 * (size_t)nbeams * b->host_cap;
+        const size_t counts = sizeof(long long) * 2 * nbeams, masks = sizeof(int) * 2 * nbeams;
+        const size_t status = 16, head = 2 * counts + ((masks + 15) & ~(size_t)15) + status;
+        const size_t bytes = head + sizeof(pv_event) * 2 * (size_t)nbeams * b->host_cap;
         if (cudaMalloc(&b->d_step, sizeof(long long)) != cudaSuccess ||
             cudaMemset(b->d_step, 0, sizeof(long long)) != cudaSuccess ||
             cudaMalloc(&b->d_export, sizeof(ExportJob) * nbeams) != cudaSuccess ||
@@ -405,9 +450,12 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             return fail(PV_ERR_NOMEM);
         }
         std::memset(b->h_mapped, 0, bytes);
-        b->h_counts = static_cast<long long*>(b->h_mapped);
-        b->h_status = reinterpret_cast<int*>(static_cast<char*>(b->h_mapped) + counts);
-        b->h_events = reinterpret_cast<pv_event*>(static_cast<char*>(b->h_mapped) + counts + status);
+        char* h = static_cast<char*>(b->h_mapped);
+        b->h_counts = reinterpret_cast<long long*>(h);
+        b->h_windows = reinterpret_cast<long long*>(h + counts);
+        b->h_mask = reinterpret_cast<int*>(h + 2 * counts);
+        b->h_status = reinterpret_cast<int*>(h + 2 * counts + ((masks + 15) & ~(size_t)15));
+        b->h_events = reinterpret_cast<pv_event*>(h + head);
         if (cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
@@ -453,13 +501,23 @@ extern "C" void pv_batch_destroy(pv_batch* b) {
 
 extern "C" int pv_batch_input(pv_batch* b, int beam, void** d_voltages, long long* bytes) {
     if (!b || beam < 0 || beam >= b->n) return PV_ERR_ARG;
-    // the buffer the next step reads (steps alternate between two sets)
-    if (d_voltages) *d_voltages = b->d_in[(size_t)(b->step & 1) * b->n + beam];
+    // the buffer the beam's next chunk is read from (a beam's chunks alternate between two)
+    if (d_voltages) *d_voltages = b->d_in[(size_t)(b->processed[beam] & 1) * b->n + beam];
     if (bytes) *bytes = b->in_bytes[beam];
     return PV_OK;
 }
 
 namespace {
+
+// Sets this step's mask (all beams when h_active is null) in its host-mapped
+// slot, once the step that last read the slot (two back) has finished.
+int set_mask(pv_batch* b, const unsigned char* h_active) {
+    const int par = (int)(b->step & 1);
+    if (b->done_valid[par]) PV_CUDA(cudaEventSynchronize(b->done[par]), "wait for the step two back");
+    int* m = b->h_mask + (size_t)par * b->n;
+    for (int i = 0; i < b->n; ++i) m[i] = h_active ? (h_active[i] != 0) : 1;
+    return PV_OK;
+}
 
 int launch_step(pv_batch* b, cudaStream_t s) {
     const int par = (int)(b->step & 1);
@@ -471,6 +529,17 @@ int launch_step(pv_batch* b, cudaStream_t s) {
     }
     PV_CUDA(cudaEventRecord(b->done[par], s), "record step completion");
     b->done_valid[par] = true;
+    // the host's mirror of plan_kernel and advance_kernel
+    const int* m = b->h_mask + (size_t)par * b->n;
+    for (int i = 0; i < b->n; ++i) {
+        pv::BeamStep& B = b->mirror[i];
+        B.active = m[i];
+        B.sel = B.done + B.lag + 1 <= B.written + (b->pipelined ? 0 : B.active);
+        B.window = B.done;
+        B.written += B.active;
+        B.done += B.sel;
+        b->processed[i] += B.active;
+    }
     b->step += 1;
     b->timed = (b->flags & PV_BATCH_TIMING) != 0;
     return PV_OK;
@@ -478,26 +547,32 @@ int launch_step(pv_batch* b, cudaStream_t s) {
 
 }  // namespace
 
-extern "C" int pv_batch_run(pv_batch* b, void* stream) {
+extern "C" int pv_batch_run(pv_batch* b, const unsigned char* h_active, void* stream) {
     if (!b) return PV_ERR_ARG;
+    PV_TRY(set_mask(b, h_active));
     return launch_step(b, pv::as_stream(stream));
 }
 
-extern "C" int pv_batch_run_host(pv_batch* b, const void* const* h_voltages, void* stream) {
+extern "C" int pv_batch_run_host(pv_batch* b, const void* const* h_voltages,
+                                 const unsigned char* h_active, void* stream) {
     if (!b || !h_voltages) return PV_ERR_ARG;
     cudaStream_t s = pv::as_stream(stream);
     const int par = (int)(b->step & 1);
     for (int i = 0; i < b->n; ++i)
-        if (!h_voltages[i]) {
+        if ((!h_active || h_active[i]) && !h_voltages[i]) {
             pv::set_error("pv_batch_run_host: no voltages for beam %d", i);
             return PV_ERR_ARG;
         }
-    // the buffers of this parity were last read by the step two back
+    PV_TRY(set_mask(b, h_active));
+    // a beam's input buffer was last read by its step before last, at the
+    // latest the batch step two back
     if (b->done_valid[par]) PV_CUDA(cudaStreamWaitEvent(b->copy_stream, b->done[par], 0), "wait");
-    for (int i = 0; i < b->n; ++i)
-        PV_CUDA(cudaMemcpyAsync(b->d_in[(size_t)par * b->n + i], h_voltages[i], b->in_bytes[i],
-                                cudaMemcpyHostToDevice, b->copy_stream),
+    for (int i = 0; i < b->n; ++i) {
+        if (h_active && !h_active[i]) continue;
+        PV_CUDA(cudaMemcpyAsync(b->d_in[(size_t)(b->processed[i] & 1) * b->n + i], h_voltages[i],
+                                b->in_bytes[i], cudaMemcpyHostToDevice, b->copy_stream),
                 "copy voltages to the device");
+    }
     PV_CUDA(cudaEventRecord(b->copied[par], b->copy_stream), "record copy");
     PV_CUDA(cudaStreamWaitEvent(s, b->copied[par], 0), "wait for the copy");
     return launch_step(b, s);
@@ -519,33 +594,33 @@ extern "C" int pv_batch_events(pv_batch* b, int beam, long long step, pv_event* 
         pv::set_error("pv_batch_events: a dedispersion pipeline wait gave up (status %d)", status);
         return status;
     }
-    pv_beam* x = b->beams[beam];
-    const long long w = step + b->base[beam] - b->lag_eff[beam];
-    if (w < 0) {
+    const size_t slot = (size_t)par * b->n + beam;
+    const long long total = ((volatile long long*)b->h_counts)[slot];
+    if (total < 0) {  // no window of this beam completed in that step
         *h_count = 0;
         if (h_first_sample) *h_first_sample = -1;
         return PV_OK;
     }
-    const long long total = ((volatile long long*)b->h_counts)[(size_t)par * b->n + beam];
+    pv_beam* x = b->beams[beam];
     *h_count = total;
-    if (h_first_sample) *h_first_sample = w * x->cfg.chunk;
+    if (h_first_sample) *h_first_sample = ((volatile long long*)b->h_windows)[slot] * x->cfg.chunk;
     const long long n = std::min(std::min(total, std::min(x->cap, b->host_cap)), cap);
     if (h_events && n > 0)
-        std::memcpy(h_events, b->h_events + ((size_t)par * b->n + beam) * b->host_cap,
-                    sizeof(pv_event) * n);
+        std::memcpy(h_events, b->h_events + slot * b->host_cap, sizeof(pv_event) * n);
     return PV_OK;
 }
 
 extern "C" int pv_batch_info(const pv_batch* b, int beam, long long* h_info8) {
     if (!b || beam < 0 || beam >= b->n || !h_info8) return PV_ERR_ARG;
     const pv_beam* x = b->beams[beam];
+    const pv::BeamStep& B = b->mirror[beam];
     h_info8[0] = x->nbins;
     h_info8[1] = x->max_shift;
     h_info8[2] = x->lag;
     h_info8[3] = x->ring_len;
     h_info8[4] = x->inverted;
-    h_info8[5] = b->step + b->base[beam];
-    h_info8[6] = b->step + b->base[beam] - 1 - b->lag_eff[beam];
+    h_info8[5] = B.written;   // logical chunks in the ring after the steps issued
+    h_info8[6] = B.done - 1;  // last window dedispersed (-1: none yet)
     h_info8[7] = (long long)x->nbins * x->row_stride * (long long)sizeof(float);
     return PV_OK;
 }

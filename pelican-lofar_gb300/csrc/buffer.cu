@@ -47,10 +47,10 @@ __global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride
                     blockIdx.x * kTile, blockIdx.y * kTile);
 }
 
-// The rings of many beams: CTAs are laid out job after job; a job's chunk
-// lands at logical position (*d_step + base) * nt.
+// The rings of many beams: CTAs are laid out job after job; an active beam's
+// chunk lands at logical position written * nt.
 __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
-                                        const long long* __restrict__ d_step) {
+                                        const pv::BeamStep* __restrict__ bs) {
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -58,10 +58,12 @@ __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, in
         else hi = mid - 1;
     }
     const pv::RingJob& J = jobs[lo];
+    const pv::BeamStep& B = bs[J.beam];
+    if (!B.active) return;
     const int local = (int)(blockIdx.x - J.block_begin);
     const int tiles_t = (J.nt + kTile - 1) / kTile;
     const int bt = local / tiles_t, tt = local - bt * tiles_t;
-    ring_write_tile(J.ring, J.row_stride, J.ring_len, (*d_step + J.base) * J.nt, J.stokes, J.nt, J.nsub, 1,
+    ring_write_tile(J.ring, J.row_stride, J.ring_len, B.written * J.nt, J.stokes, J.nt, J.nsub, 1,
                     J.nchan, J.inverted, tt * kTile, bt * kTile);
 }
 
@@ -83,10 +85,10 @@ int ring_job_blocks(const RingJob& j) {
     return ceil_div(j.nt, kTile) * ceil_div(j.nsub * j.nchan, kTile);
 }
 
-int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const long long* d_step,
+int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
                      cudaStream_t s) {
     if (nblocks <= 0) return PV_OK;
-    ring_write_batch_kernel<<<(unsigned)nblocks, dim3(kTile, 8), 0, s>>>(d_jobs, njobs, d_step);
+    ring_write_batch_kernel<<<(unsigned)nblocks, dim3(kTile, 8), 0, s>>>(d_jobs, njobs, bs);
     return check_launch("ring_write_batch_kernel");
 }
 

@@ -220,7 +220,7 @@ struct RawSample<false> {
 template <int N, bool I16>
 __global__ void __launch_bounds__(128)
 chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant__ pv::ChanJob one, int njobs,
-                     long long nwarps, const long long* __restrict__ d_step) {
+                     long long nwarps, const pv::BeamStep* __restrict__ bs) {
     constexpr int M = N / 16, T = kFastTaps, H = T - 1;
     constexpr int LOGN = M == 1 ? 4 : (M == 2 ? 5 : 6);
     using Raw = typename RawSample<I16>::type;
@@ -241,7 +241,12 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     const int B1 = min(B0 + kRangeBlocks, nblocks);
     const int lane = threadIdx.x & 31, pol = lane >> 4, j = lane & 15;
     const long long row = (long long)s * 2 + pol;
-    const int par = d_step ? (int)(*d_step & 1) : 0;
+    int par = 0;  // step parity of this beam: input buffer and history double buffer
+    if (bs) {
+        const pv::BeamStep& B = bs[J.beam];
+        if (!B.active) return;
+        par = (int)((B.written - B.base) & 1);
+    }
     const float2* hin = J.hist[par];
     float2* hout = J.hist[par ^ 1];
     const void* src = (par && J.in_odd) ? J.in_odd : J.in;
@@ -483,13 +488,13 @@ int chan_job_warps(ChanJob& job) {
 }
 
 int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
-                     long long nwarps, const long long* d_step, cudaStream_t s) {
+                     long long nwarps, const BeamStep* bs, cudaStream_t s) {
     if (nwarps <= 0) return PV_OK;
     const unsigned grid = (unsigned)ceil_div<long long>(nwarps, 4);
 #define PV_CHAN_FAST(NN)                                                                         \
     if (nchan == NN) {                                                                           \
-        if (in_int16) chan_stokes_i_kernel<NN, true><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, d_step);  \
-        else chan_stokes_i_kernel<NN, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, d_step);          \
+        if (in_int16) chan_stokes_i_kernel<NN, true><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);  \
+        else chan_stokes_i_kernel<NN, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);          \
         return check_launch("chan_stokes_i_kernel");                                            \
     }
     PV_CHAN_FAST(16)

@@ -353,16 +353,15 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
 // learn the tile from that record when the stage arrives.  A beam's DM tile
 // height (1..16 trials, one warp each) is chosen on the host so that its
 // delay spread fits the launch's channel slot; warps above it idle on that
-// beam's tiles.  The output window of a beam at device step k is k - lag
-// (its ring then holds every delay of that window); beams with k < lag are
-// skipped.  A beam whose ring started prefilled counts its base chunks of
-// silence in k.  All waits are bounded as in dedisperse_tma_kernel.
+// beam's tiles.  Only beams whose BeamStep selects a window this step are
+// dedispersed (window w reads ring columns from w*chunk on).  All waits are
+// bounded as in dedisperse_tma_kernel.
 // ---------------------------------------------------------------------------
 template <int R, int CS, int ST>
 __global__ void __launch_bounds__(17 * 32, 1)
 dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles,
                         int ntiles, int slot, int* __restrict__ counter,
-                        const long long* __restrict__ d_step, int* __restrict__ status) {
+                        const pv::BeamStep* __restrict__ bs, int* __restrict__ status) {
     constexpr int DMS = 16;
     constexpr int TT = 32 * R;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -374,7 +373,6 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     uint64_t* empty = full + ST;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long step = *d_step;
 
     __shared__ int s_abort;
     if (threadIdx.x == 0) {
@@ -400,8 +398,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 if (lane == 0) t = atomicAdd(counter, 1);
                 t = __shfl_sync(0xffffffffu, t, 0);
                 if (t >= ntiles) break;
-                const pv::DdJob& Jt = jobs[tiles[t].job];
-                if (step + Jt.base >= Jt.lag) {
+                if (bs[jobs[tiles[t].job].beam].sel) {
                     tile = t;
                     break;
                 }
@@ -425,7 +422,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             const float dv0 = pv_trial_value(tt.d0, J.start, J.step);
             const float dv_last = pv_trial_value(d_last, J.start, J.step);
             const int valid = min(TT, J.nout - tt.t0);
-            const long long t_base = ((step + J.base - J.lag) * J.chunk) % J.ring_len;
+            const long long t_base = (bs[J.beam].window * J.chunk) % J.ring_len;
             const int nst = (J.nchan + CS - 1) / CS;
             for (int st = 0; st < nst; ++st) {
                 const int b = gs % ST;
@@ -653,7 +650,7 @@ size_t batch_smem(const Variant& v, int slot) {
 
 template <int R, int CS, int ST>
 int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem,
-                   int grid, int* counter, const long long* d_step, int* status, cudaStream_t s,
+                   int grid, int* counter, const pv::BeamStep* bs, int* status, cudaStream_t s,
                    bool set_attr) {
     auto kern = dedisperse_batch_kernel<R, CS, ST>;
     if (set_attr) {
@@ -662,16 +659,16 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
         return PV_OK;
     }
     PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
-    kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, d_step, status);
+    kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status);
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
 int launch_batch(int variant, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot,
-                 size_t smem, int grid, int* counter, const long long* d_step, int* status,
+                 size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
                  cudaStream_t s, bool set_attr) {
     switch (variant) {
 #define PV_VAR(I, R, CS, ST) \
-    case I: return launch_batch_t<R, CS, ST>(jobs, tiles, ntiles, slot, smem, grid, counter, d_step, status, s, set_attr);
+    case I: return launch_batch_t<R, CS, ST>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
         PV_VAR(0, 32, 4, 4)
         PV_VAR(1, 32, 2, 4)
         PV_VAR(2, 16, 4, 4)
@@ -774,14 +771,11 @@ bool build_shape(const Variant& v, const DdBeam* beams, int n, std::vector<std::
 
 int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant) {
     std::vector<DdJob> jobs(n);
-    int max_lag = 0;
     for (int i = 0; i < n; ++i) {
         const DdBeam& B = beams[i];
         jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.nchan,
-                        B.nout, B.tdms, B.lag, B.chunk, sh.dms[i], B.base, B.start, B.step};
-        max_lag = std::max(max_lag, B.lag);
+                        B.nout, B.tdms, B.chunk, sh.dms[i], i, B.start, B.step};
     }
-    (void)max_lag;
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_tiles) cudaFree(b->d_tiles);
     b->d_jobs = nullptr;
@@ -814,7 +808,7 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
         const DdBeam& B = beams[i];
         if (B.ring_len <= 0 || B.ring_len % 4 != 0 || B.row_stride % 4 != 0 || B.ring_len > B.row_stride ||
             (reinterpret_cast<uintptr_t>(B.ring) & 15) != 0 || B.nout <= 0 || B.tdms <= 0 ||
-            B.nchan <= 0 || B.lag < 0 || B.chunk <= 0) {
+            B.nchan <= 0 || B.chunk <= 0) {
             set_error("dedispersion batch: beam %d needs a 16-byte aligned ring of a multiple of 4 "
                       "samples", i);
             return PV_ERR_ARG;
@@ -840,13 +834,17 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
         rc = upload(b, beams, n, sh, variant);
     } else {
         // Autotuner: time every variant that can tile the beams on the rings as
-        // they are, with every beam treated as ready, and keep the fastest.
-        long long* d_tstep = nullptr;
-        long long max_lag = 0;
-        for (int i = 0; i < n; ++i) max_lag = std::max<long long>(max_lag, beams[i].lag);
+        // they are, with every beam dedispersing window 0, and keep the fastest.
+        BeamStep* d_tstep = nullptr;
+        std::vector<BeamStep> all(n);
+        for (auto& x : all) {
+            x = BeamStep{};
+            x.sel = 1;
+        }
         cudaEvent_t e0 = nullptr, e1 = nullptr;
-        PV_CUDA(cudaMalloc(&d_tstep, sizeof(long long)), "allocate tuning step");
-        PV_CUDA(cudaMemcpy(d_tstep, &max_lag, sizeof(long long), cudaMemcpyHostToDevice), "copy tuning step");
+        PV_CUDA(cudaMalloc(&d_tstep, sizeof(BeamStep) * n), "allocate tuning steps");
+        PV_CUDA(cudaMemcpy(d_tstep, all.data(), sizeof(BeamStep) * n, cudaMemcpyHostToDevice),
+                "copy tuning steps");
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         float best = 1e30f;
@@ -903,9 +901,9 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
     return PV_OK;
 }
 
-int dd_batch_launch(DdBatch* b, const long long* d_step, cudaStream_t s) {
+int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s) {
     return launch_batch(b->variant, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
-                        b->d_counter, d_step, b->d_status, s, false);
+                        b->d_counter, bs, b->d_status, s, false);
 }
 
 int dd_batch_status(const DdBatch* b, int* h_status) {

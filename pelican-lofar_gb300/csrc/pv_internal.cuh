@@ -7,6 +7,21 @@
 
 namespace pv {
 
+// A batch beam's progress, device-resident.  The planning kernel at the start
+// of every step sets `active` (a chunk of this beam is processed) and `sel` (a
+// window of this beam is dedispersed, `window` its index); every batched
+// kernel skips the beams it does not concern, and the last kernel of the step
+// advances `written` and `done`.
+struct BeamStep {
+    long long written;  // logical chunks in the ring, prefilled silence included
+    long long done;     // windows dedispersed so far
+    long long base;     // prefilled chunks of silence
+    long long window;   // window dedispersed this step (valid when sel)
+    int lag;            // window w needs ring chunks w..w+lag
+    int active, sel;
+    int pad;
+};
+
 // One beam's share of a Stokes-I channeliser launch (chan_stokes_i_kernel).
 struct ChanJob {
     const void* in;          // [sub][2][nblocks*N] short2 or float2 voltages
@@ -17,11 +32,13 @@ struct ChanJob {
     float* out;              // [nu][sub][N] Stokes I
     long long warp_begin;    // first warp of this job in the launch
     int nsub, nblocks, window, nu, nranges;
+    int beam;                // index into the batch's BeamStep array
 };
 bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window, int bin, int nblocks);
 int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
+// bs == null: one job, always active, input `in`, history hist[0] -> hist[1]
 int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
-                     long long nwarps, const long long* d_step, cudaStream_t s);
+                     long long nwarps, const BeamStep* bs, cudaStream_t s);
 // coefficient [T][N] and twiddle [N/2] tables of a PPF handle
 int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
                int* ntaps);
@@ -37,8 +54,7 @@ struct DdBeam {
     long long row_stride, ring_len;
     const float* d_dmshift;
     const float* h_dmshift;
-    int nchan, nout, tdms, lag, chunk;
-    int base;           // chunks already in the ring at step 0 (prefilled silence)
+    int nchan, nout, tdms, chunk;
     float start, step;  // trial value = start + d*step, in samples per unit delay constant
 };
 struct DdJob {
@@ -47,7 +63,7 @@ struct DdJob {
     const float* ring;
     long long row_stride, ring_len;
     const float* dmshift;
-    int nchan, nout, tdms, lag, chunk, dms, base;
+    int nchan, nout, tdms, chunk, dms, beam;
     float start, step;
 };
 struct DdTile {
@@ -56,7 +72,7 @@ struct DdTile {
 struct DdBatch;
 // variant < 0 runs the autotuner over the DM x time tile variants
 int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cudaStream_t s);
-int dd_batch_launch(DdBatch* b, const long long* d_step, cudaStream_t s);
+int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s);
 int dd_batch_status(const DdBatch* b, int* h_status);
 int dd_batch_shape(const DdBatch* b, int* h8);
 const std::vector<int>& dd_batch_dms(const DdBatch* b);
@@ -66,8 +82,9 @@ void dd_batch_destroy(DdBatch* b);
 
 // Batched RFI clippers (rfi.cu).
 struct RfiBatch;
+// handles[i] null: beam i has no clipper; bs: the batch's BeamStep array (inactive beams skip)
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
-                     const int* nchan, int n, int nt, cudaStream_t s);
+                     const int* nchan, int n, int nt, const BeamStep* bs, cudaStream_t s);
 int rfi_batch_launch(RfiBatch* b, cudaStream_t s);
 int rfi_batch_launches(const RfiBatch* b);  // number of CTA-size classes
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s);
@@ -80,10 +97,10 @@ struct RingJob {
     const float* stokes;
     int nt, nsub, nchan, inverted;
     long long block_begin;  // first CTA of this job
-    long long base;         // chunks already in the ring at step 0 (prefilled silence)
+    int beam;               // index into the BeamStep array: written chunks give the position
 };
 int ring_job_blocks(const RingJob& j);
-int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const long long* d_step,
+int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
                      cudaStream_t s);
 
 int ring_write_device(float* ring, long long row_stride, long long ring_len, long long pos,

@@ -683,12 +683,16 @@ struct RfiJob {
     unsigned char* flags;
     Geo geo;
     int nt;
+    int beam;  // index into the batch's BeamStep array
 };
 
 // The clippers of many beams at once: CTA b runs job b (every job of a launch
-// has the same partial count, the block size).
+// has the same partial count, the block size); beams without a chunk this
+// step return at once.
 template <int MAXT>
-__global__ void __launch_bounds__(MAXT, 1) rfi_batch_kernel(const RfiJob* __restrict__ jobs) {
+__global__ void __launch_bounds__(MAXT, 1) rfi_batch_kernel(const RfiJob* __restrict__ jobs,
+                                                            const pv::BeamStep* __restrict__ bs) {
+    if (bs && !bs[jobs[blockIdx.x].beam].active) return;
     const RfiConfig cfg = jobs[blockIdx.x].cfg;
     const RfiBuffers bufs = jobs[blockIdx.x].bufs;
     const Geo geo = jobs[blockIdx.x].geo;
@@ -702,9 +706,9 @@ size_t rfi_smem_bytes(int nbins) {
 // Sets the shared-memory attribute of both kernels of a block size and
 // launches one of them: jobs != null selects the batched kernel.
 template <int MAXT>
-int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& cfg,
-                 const RfiBuffers& bufs, float* data, int nt, const Geo& geo, unsigned char* flags,
-                 cudaStream_t s) {
+int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamStep* bs,
+                 const RfiConfig& cfg, const RfiBuffers& bufs, float* data, int nt, const Geo& geo,
+                 unsigned char* flags, cudaStream_t s) {
     if (jobs) {
         if (nblocks == 0) {  // set-up call: the attribute only, before any stream capture
             PV_CUDA(cudaFuncSetAttribute(rfi_batch_kernel<MAXT>,
@@ -712,7 +716,7 @@ int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& 
                     "cudaFuncSetAttribute(rfi batch)");
             return PV_OK;
         }
-        rfi_batch_kernel<MAXT><<<nblocks, MAXT, smem, s>>>(jobs);
+        rfi_batch_kernel<MAXT><<<nblocks, MAXT, smem, s>>>(jobs, bs);
         return pv::check_launch("rfi_batch_kernel");
     }
     PV_CUDA(cudaFuncSetAttribute(rfi_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -721,13 +725,13 @@ int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& 
     return pv::check_launch("rfi_kernel");
 }
 
-int rfi_launch(int parts, size_t smem, int nblocks, const RfiJob* jobs, const RfiConfig& cfg,
-               const RfiBuffers& bufs, float* data, int nt, const Geo& geo, unsigned char* flags,
-               cudaStream_t s) {
+int rfi_launch(int parts, size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamStep* bs,
+               const RfiConfig& cfg, const RfiBuffers& bufs, float* data, int nt, const Geo& geo,
+               unsigned char* flags, cudaStream_t s) {
     switch (parts) {
-        case 256: return rfi_launch_t<256>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
-        case 512: return rfi_launch_t<512>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
-        case 1024: return rfi_launch_t<1024>(smem, nblocks, jobs, cfg, bufs, data, nt, geo, flags, s);
+        case 256: return rfi_launch_t<256>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
+        case 512: return rfi_launch_t<512>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
+        case 1024: return rfi_launch_t<1024>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
         default:
             pv::set_error("RFI_Clipper: no kernel for %d partial sums", parts);
             return PV_ERR_ARG;
@@ -903,7 +907,7 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     }
     Geo geo{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1,
             nbins / 8};
-    return rfi_launch(threads, smem, 1, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
+    return rfi_launch(threads, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
 extern "C" int pv_rfi_parts(int nbins) { return nbins <= 1024 ? 256 : (nbins <= 4096 ? 512 : 1024); }
@@ -952,6 +956,7 @@ struct RfiBatch {
         int njobs = 0;
     };
     std::vector<Class> classes;
+    const BeamStep* bs = nullptr;
 };
 
 void rfi_batch_destroy(RfiBatch* b) {
@@ -962,8 +967,9 @@ void rfi_batch_destroy(RfiBatch* b) {
 }
 
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
-                     const int* nchan, int n, int nt, cudaStream_t s) {
+                     const int* nchan, int n, int nt, const BeamStep* bs, cudaStream_t s) {
     auto* b = new RfiBatch;
+    b->bs = bs;
     std::vector<std::vector<RfiJob>> jobs;
     for (int i = 0; i < n; ++i) {
         pv_rfi* h = handles[i];
@@ -996,6 +1002,7 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         j.geo = Geo{nsub[i], 1, nchan[i],
                     (nchan[i] & (nchan[i] - 1)) == 0 ? __builtin_ctz((unsigned)nchan[i]) : -1, nbins / 8};
         j.nt = nt;
+        j.beam = i;
         jobs[k].push_back(j);
     }
     for (size_t k = 0; k < b->classes.size(); ++k) {
@@ -1008,8 +1015,8 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         int rc = e == cudaSuccess ? PV_OK : cuda_status(e, "RFI batch jobs");
         // set the kernel attribute now, outside any stream capture
         if (rc == PV_OK)
-            rc = rfi_launch(c.parts, c.smem, 0, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0, Geo{},
-                            nullptr, s);
+            rc = rfi_launch(c.parts, c.smem, 0, c.d_jobs, nullptr, RfiConfig{}, RfiBuffers{}, nullptr, 0,
+                            Geo{}, nullptr, s);
         if (rc != PV_OK) {
             rfi_batch_destroy(b);
             return rc;
@@ -1022,8 +1029,8 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
 int rfi_batch_launch(RfiBatch* b, cudaStream_t s) {
     for (auto& c : b->classes) {
         if (c.njobs == 0) continue;
-        PV_TRY(rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0,
-                          Geo{}, nullptr, s));
+        PV_TRY(rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, b->bs, RfiConfig{}, RfiBuffers{},
+                          nullptr, 0, Geo{}, nullptr, s));
     }
     return PV_OK;
 }
@@ -1033,8 +1040,8 @@ int rfi_batch_launches(const RfiBatch* b) { return (int)b->classes.size(); }
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s) {
     auto& c = b->classes[k];
     if (c.njobs == 0) return PV_OK;
-    return rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, RfiConfig{}, RfiBuffers{}, nullptr, 0, Geo{},
-                      nullptr, s);
+    return rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, b->bs, RfiConfig{}, RfiBuffers{}, nullptr, 0,
+                      Geo{}, nullptr, s);
 }
 
 }  // namespace pv

@@ -94,8 +94,8 @@ def _declare(L):
         "pv_batch_create": (i, [P(vp), vp, i, i]),
         "pv_batch_destroy": (None, [vp]),
         "pv_batch_input": (i, [vp, i, P(vp), P(ll)]),
-        "pv_batch_run": (i, [vp, vp]),
-        "pv_batch_run_host": (i, [vp, P(vp), vp]),
+        "pv_batch_run": (i, [vp, vp, vp]),
+        "pv_batch_run_host": (i, [vp, P(vp), vp, vp]),
         "pv_batch_events": (i, [vp, i, ll, vp, ll, P(ll), P(ll)]),
         "pv_batch_info": (i, [vp, i, P(ll)]),
         "pv_batch_tiles": (i, [vp, P(i), P(i), P(C.c_float), P(ll)]),
@@ -445,13 +445,26 @@ class Batch:
         assert d_voltages.numel() * d_voltages.element_size() == n
         check(load().pv_device_copy(C.c_void_p(p), _ptr(d_voltages), n, _stream(stream)))
 
-    def run(self, stream=None):
-        check(load().pv_batch_run(self.h, _stream(stream)))
+    def _mask(self, active):
+        if active is None:
+            return None
+        m = np.ascontiguousarray(np.asarray(active, dtype=np.uint8))
+        assert m.shape == (len(self.cfgs),)
+        return m
 
-    def run_host(self, h_voltages, stream=None):
+    def run(self, active=None, stream=None):
+        """One step; active: per-beam flags of the beams that have a chunk (None: all)."""
+        m = self._mask(active)
+        check(load().pv_batch_run(self.h, None if m is None else C.c_void_p(m.ctypes.data),
+                                  _stream(stream)))
+
+    def run_host(self, h_voltages, active=None, stream=None):
+        m = self._mask(active)
         ptrs = (C.c_void_p * len(h_voltages))(
-            *[C.c_void_p(v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data) for v in h_voltages])
-        check(load().pv_batch_run_host(self.h, ptrs, _stream(stream)))
+            *[C.c_void_p(None if v is None else (v.data_ptr() if hasattr(v, "data_ptr") else v.ctypes.data))
+              for v in h_voltages])
+        check(load().pv_batch_run_host(self.h, ptrs, None if m is None else C.c_void_p(m.ctypes.data),
+                                       _stream(stream)))
 
     def events(self, beam, step=-1, cap=1 << 16):
         """(events, total count, first sample) of one beam at one of the last
@@ -468,7 +481,7 @@ class Batch:
     def info(self, beam):
         out = (C.c_longlong * 8)()
         check(load().pv_batch_info(self.h, beam, out))
-        keys = ["nbins", "max_shift", "lag", "ring_len", "inverted", "steps", "window", "ring_bytes"]
+        keys = ["nbins", "max_shift", "lag", "ring_len", "inverted", "written", "window", "ring_bytes"]
         return dict(zip(keys, list(out)))
 
     def tiles(self):

@@ -166,3 +166,49 @@ def test_batch_host_steps_overlap_and_events_of_previous_step(pv, cuda, mix_conf
     with pytest.raises(pv.PvError, match="last two"):
         batch.events(0, step=0)
     del hosts_prev
+
+
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_batch_with_idle_beams_equals_beams_alone(pv, cuda, mix_configs, pipelined):
+    """Continuous batching: in every step only some beams have a chunk.  Each
+    beam's windows (events and dedispersed data) equal those of the beam run
+    alone on its own chunks, whatever the other beams do."""
+    import torch
+    cfgs = mix_configs
+    n = len(cfgs)
+    batch = pv.Batch(cfgs, tune=False, graph=True, pipelined=pipelined)
+    alone = [pv.Beam(c) for c in cfgs]
+    lags = [b.info()["lag"] for b in alone]
+    rng = np.random.default_rng(23)
+    want = [dict() for _ in range(n)]  # window -> (events, count, dedispersed)
+    seen = [0] * n
+    steps = 2 * max(lags) + 8
+    for step in range(steps):
+        active = rng.random(n) < 0.6
+        if step == steps - 1:
+            active[:] = False  # a step with no chunk at all still completes pipelined windows
+        for i, c in enumerate(cfgs):
+            if not active[i]:
+                continue
+            v16, _ = voltages(rng, c.nsub, 2, c.chunk * 4 * c.nchan_sub)
+            x = torch.from_numpy(v16.reshape(c.nsub, 2, -1)).to(cuda)
+            batch.set_input(i, x)
+            alone[i].process(x)
+            ev, cnt, first = alone[i].events()
+            if first >= 0:
+                out = pv.device_array(alone[i].buffers()[2], (c.tdms, c.chunk)).cpu().numpy()
+                want[i][first // c.chunk] = (ev, cnt, out)
+        batch.run(active=active.astype(np.uint8))
+        torch.cuda.synchronize()
+        for i, c in enumerate(cfgs):
+            ev, cnt, first = batch.events(i)
+            if first < 0:
+                continue
+            w = first // c.chunk
+            assert w in want[i], (i, w)
+            wev, wcnt, wout = want[i][w]
+            assert cnt == wcnt and np.array_equal(ev, wev)
+            assert np.array_equal(pv.device_array(batch.buffers(i)[1], (c.tdms, c.chunk)).cpu().numpy(), wout)
+            seen[i] += 1
+    for i in range(n):
+        assert seen[i] == len(want[i]) > 0  # every window the beam completed alone came out once
