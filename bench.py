@@ -556,6 +556,80 @@ def run_batch(args, cfgs, workload):
         dist.destroy_process_group()
 
 
+def serve_beams(nbeams=128, seed=128):
+    """The serving mix: channel counts 512-15616 (32, 61, 122 or 244 subbands of
+    16 or 64 channels), DM ranges 0-250 or 0-1000 in 1024-4096 trials."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nbeams):
+        nsub = int(rng.choice([32, 61, 122, 244]))
+        nch = int(rng.choice([16, 64]))
+        dm_max = float(rng.choice([250.0, 1000.0]))
+        tdms = int(rng.choice([1024, 2048, 4096]))
+        out.append(beam_dict(nsub, nch, dm_max, tdms, 4096))
+    return out
+
+
+def run_serve(args, workload):
+    """The serving loop over 128 streaming beams, batched and plain."""
+    import torch
+    import pv
+    import serve
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    beams = serve_beams(args.beams)
+    cfgs = [pv_config(pv, b) for b in beams]
+    spec = [{"cfg": c, "tsamp": b["tsamp"], "tdms": b["tdms"], "nchan": b["nsub"] * b["nchan_sub"]}
+            for c, b in zip(cfgs, beams)]
+    streams = serve.poisson_streams(spec, args.duration, seed=7)
+    budget = int(args.budget_gb * 1e9)
+
+    def voltages(cfg):
+        g = torch.Generator(device=dev)
+        g.manual_seed(int(cfg.nsub) * 1000 + int(cfg.nchan_sub))
+        n = serve.SUB_CHUNK * cfg.int_time * cfg.nchan_sub
+        v = torch.randn((cfg.nsub, 2, n, 2), generator=g, device=dev) * 16.0
+        return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
+
+    def new_stream():
+        return torch.cuda.Stream(device=dev)
+
+    reports = {}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for name, eng, policy in (("batched", serve.BatchEngine(pv, voltages, new_stream), "batch"),
+                              ("plain", serve.PlainEngine(pv, voltages, new_stream), "fifo1")):
+        launches0 = pv.launches()
+        rep = serve.Server(eng, streams, budget, policy=policy).run(horizon=args.duration + args.grace)
+        rep["gpu_launches"] = pv.launches() - launches0
+        reports[name] = rep
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    clk = clocks.stop()
+    b, p = reports["batched"], reports["plain"]
+    rt_units = sum(s.units_per_spectrum * sum(s.sizes) for s in streams)
+    line = {"metric": "DM-trial*chan*samples/s", "value": b["throughput"],
+            "unit": "DM-trial*chan*samples/s", "n_gpus": 1, "steps": b["chunks_done"],
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded Gaussian int16 voltages, Poisson chunk arrivals",
+            "config": {"workload": workload, "beams": len(streams), "duration_s": args.duration,
+                       "budget_gb": args.budget_gb,
+                       "chunks": b["chunks"], "offered_units": rt_units,
+                       "chunk_spectra": "4096-32768 per beam, Poisson, one chunk per chunk duration",
+                       "nchan_range": [min(x["nchan"] for x in spec), max(x["nchan"] for x in spec)]},
+            "e2e": {"value": b["throughput"], "unit": "DM-trial*chan*samples/s",
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                    "what": "voltages copied from page-locked host memory every step"},
+            "serve": b, "plain": p,
+            "latency_ms": {"p50": b["latency_s"]["p50"] * 1e3, "p99": b["latency_s"]["p99"] * 1e3,
+                           "plain_p50": p["latency_s"]["p50"] * 1e3,
+                           "plain_p99": p["latency_s"]["p99"] * 1e3},
+            "gpu_launches": b["gpu_launches"], "clocks": clk, "cpu_baseline": None}
+    print(json.dumps(line))
+
+
 # ---------------------------------------------------------------------------
 # CPU restatement (baseline / reference arm)
 # ---------------------------------------------------------------------------
@@ -698,8 +772,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pv", choices=["pv", "reference"])
-    ap.add_argument("--workload", default="batch64", choices=["batch64", "fullband"])
-    ap.add_argument("--beams", type=int, default=64, help="batch64: number of beams")
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "fullband", "serve128"])
+    ap.add_argument("--beams", type=int, default=None, help="number of beams (64 / 128)")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve128: seconds of arrivals")
+    ap.add_argument("--grace", type=float, default=30.0, help="serve128: seconds to drain")
+    ap.add_argument("--budget-gb", type=float, default=160.0, help="serve128: HBM budget")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
@@ -720,6 +797,16 @@ def main():
         else:
             run_pv(args, cfg)
         return
+    if args.workload == "serve128":
+        args.beams = args.beams or 128
+        workload = "serve%d-poisson-%gs-%ggb" % (args.beams, args.duration, args.budget_gb)
+        if args.impl == "reference":
+            cfgs = serve_beams(args.beams)
+            run_reference(args, cfgs, workload)
+        else:
+            run_serve(args, workload)
+        return
+    args.beams = args.beams or 64
     cfgs = batch_configs(args.beams, chunk=args.chunk or 4096)
     workload = "batch%d-mixed-beams-4096samp" % args.beams
     if args.beams != 64 or args.chunk:

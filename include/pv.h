@@ -404,6 +404,12 @@ int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tu
 int pv_batch_stage_ms(pv_batch* batch, float* h_ms5);
 int pv_batch_buffers(const pv_batch* batch, int beam, float** d_filterbank, float** d_dedispersed,
                      float** d_ring);
+/* 1 if step `step` (one of the steps issued) has finished on the device, 0 if not. */
+int pv_batch_step_done(const pv_batch* batch, long long step);
+/* Device bytes one beam of this configuration takes in a batch created with
+ * `flags` (ring, input buffers, filterbank, window, events, scratch): the
+ * admission cost of a serving loop under an HBM budget. */
+long long pv_batch_footprint(const pv_beam_config* config, int flags);
 
 #ifdef __cplusplus
 }

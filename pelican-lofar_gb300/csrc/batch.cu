@@ -664,3 +664,44 @@ extern "C" int pv_batch_buffers(const pv_batch* b, int beam, float** d_filterban
     if (d_ring) *d_ring = x->d_ring;
     return PV_OK;
 }
+
+extern "C" int pv_batch_step_done(const pv_batch* b, long long step) {
+    if (!b || step < 0 || step >= b->step) return PV_ERR_ARG;
+    if (step < b->step - 2) return 1;  // older steps finished before the step two back was issued
+    const cudaError_t e = cudaEventQuery(b->done[step & 1]);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return pv::cuda_status(e, "pv_batch_step_done");
+}
+
+extern "C" long long pv_batch_footprint(const pv_beam_config* c, int flags) {
+    if (!c || c->nsub <= 0 || c->nchan_sub <= 0 || c->int_chan <= 0 || c->chunk <= 0 ||
+        c->tdms <= 0 || c->tsamp <= 0.0) {
+        pv::set_error("pv_batch_footprint: invalid beam configuration");
+        return PV_ERR_ARG;
+    }
+    const int nchan_fb = c->nchan_sub / c->int_chan;
+    const int nbins = c->nsub * nchan_fb;
+    std::vector<float> k(nbins);
+    int inverted = 0;
+    if (pv_dm_shifts(c->fch1, c->foff, nbins, k.data(), &inverted) != PV_OK) return PV_ERR_ARG;
+    // the dedispersion plan's maximum delay and the beam's ring
+    const float ts = (float)c->tsamp;
+    const float start = (c->dm_low < 0.0f ? 0.0f : c->dm_low) / ts, step = c->dm_step / ts;
+    const float vmax = std::fmaf((float)(c->tdms - 1), step, start);
+    int max_shift = 0;
+    for (float kc : k) max_shift = std::max(max_shift, (int)(kc * vmax));
+    const long long lag = (max_shift + c->chunk - 1) / c->chunk;
+    const long long ring_len = (lag + 1 + ((flags & PV_BATCH_PIPELINED) ? 1 : 0)) * c->chunk;
+    const long long row_stride = (ring_len + 31) / 32 * 32;
+    const long long cap = c->event_capacity > 0 ? c->event_capacity : (1LL << 20);
+    long long bytes = 4LL * nbins * row_stride;                       // ring
+    bytes += 4LL * c->chunk * nbins;                                   // filterbank
+    bytes += 4LL * c->tdms * c->chunk;                                 // dedispersed window
+    bytes += (long long)sizeof(pv_event) * cap;                        // events
+    bytes += (long long)pv::analyse_scratch_bytes(c->tdms, c->chunk, c->bin_pow2) + 256;
+    bytes += 2LL * c->nsub * 2 * c->chunk * c->int_time * c->nchan_sub * 4;  // two input buffers
+    bytes += 2LL * 2 * (long long)sizeof(float2) * c->nsub * 7 * c->nchan_sub;  // two PPF histories
+    bytes += 16LL * c->history + 12LL * nbins;                        // clipper state, bandpass
+    return bytes;
+}

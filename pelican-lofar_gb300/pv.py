@@ -101,6 +101,8 @@ def _declare(L):
         "pv_batch_tiles": (i, [vp, P(i), P(i), P(C.c_float), P(ll)]),
         "pv_batch_stage_ms": (i, [vp, P(C.c_float)]),
         "pv_batch_buffers": (i, [vp, i, P(vp), P(vp), P(vp)]),
+        "pv_batch_step_done": (i, [vp, ll]),
+        "pv_batch_footprint": (ll, [vp, i]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_ddmod_create": (i, [P(vp), i, i, f, f, d, d]),
         "pv_ddmod_destroy": (None, [vp]),
@@ -419,6 +421,14 @@ BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
 HOST_EVENTS = 65536  # PV_BATCH_HOST_EVENTS
 
 
+def batch_footprint(cfg, pipelined=True):
+    """Device bytes of one beam of this configuration in a batch."""
+    n = load().pv_batch_footprint(C.byref(cfg), BATCH_PIPELINED if pipelined else 0)
+    if n < 0:
+        check(int(n))
+    return int(n)
+
+
 class Batch:
     """Many beams advanced one chunk per step by batched launches (pv_batch)."""
 
@@ -504,6 +514,12 @@ class Batch:
         p = [C.c_void_p() for _ in range(3)]
         check(load().pv_batch_buffers(self.h, beam, *[C.byref(x) for x in p]))
         return [x.value for x in p]
+
+    def step_done(self, step):
+        rc = load().pv_batch_step_done(self.h, step)
+        if rc < 0:
+            check(rc)
+        return rc == 1
 
     def __del__(self):
         if getattr(self, "h", None) and self.h.value and _lib is not None:
