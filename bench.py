@@ -624,8 +624,12 @@ def run_serve(args, workload):
                     "what": "voltages copied from page-locked host memory every step"},
             "serve": b, "plain": p,
             "latency_ms": {"p50": b["latency_s"]["p50"] * 1e3, "p99": b["latency_s"]["p99"] * 1e3,
+                           "p99_after_admission": b["latency_after_admission_s"]["p99"] * 1e3,
+                           "p99_over_chunk_duration": b["latency_over_chunk_duration"]["p99"],
                            "plain_p50": p["latency_s"]["p50"] * 1e3,
-                           "plain_p99": p["latency_s"]["p99"] * 1e3},
+                           "plain_p99": p["latency_s"]["p99"] * 1e3,
+                           "plain_p99_over_chunk_duration": p["latency_over_chunk_duration"]["p99"]},
+            "batched_over_plain_latency_p99": p["latency_s"]["p99"] / b["latency_s"]["p99"],
             "gpu_launches": b["gpu_launches"], "clocks": clk, "cpu_baseline": None}
     print(json.dumps(line))
 

@@ -21,7 +21,8 @@ per beam and one sub-chunk at a time, oldest first, each copied in, processed
 and its events read back before the next (the reference's job-per-buffer
 style).
 
-Engines implement ``footprint(cfg)`` and ``open(cfgs) -> cohort`` with
+Engines implement ``footprint(cfg)``, optionally ``prepare(cfgs)`` (called
+before the clock starts) and ``open(cfgs, ids) -> cohort`` with
 ``step(active) -> id``, ``done(id)``, ``close()``; the tests drive the loop
 with a fake engine on the CPU.
 """
@@ -37,11 +38,12 @@ class Stream:
     """One beam's stream: its configuration, chunk arrival times (s, from the
     start of the run) and chunk sizes (spectra, multiples of SUB_CHUNK)."""
 
-    def __init__(self, cfg, arrivals, sizes, units_per_spectrum):
+    def __init__(self, cfg, arrivals, sizes, units_per_spectrum, tsamp=1.0):
         self.cfg = cfg
         self.arrivals = list(arrivals)
         self.sizes = list(sizes)
         self.units_per_spectrum = units_per_spectrum  # trials x channels
+        self.tsamp = tsamp  # seconds per spectrum
 
     @property
     def end(self):
@@ -69,7 +71,7 @@ def poisson_streams(beams, duration, seed, start_spread=0.5, min_life=0.3):
             arr.append(t)
         if not arr:
             arr = [min(t0 + mean, duration)]
-        out.append(Stream(b["cfg"], arr, [size] * len(arr), b["tdms"] * b["nchan"]))
+        out.append(Stream(b["cfg"], arr, [size] * len(arr), b["tdms"] * b["nchan"], b["tsamp"]))
     return out
 
 
@@ -101,6 +103,9 @@ class Server:
         streams = self.streams
         n = len(streams)
         foot = [self.engine.footprint(s.cfg) for s in streams]
+        prepare = getattr(self.engine, "prepare", None)
+        if prepare:  # receive buffers exist before the streams start
+            prepare([s.cfg for s in streams])
         events = sorted((t, i, k) for i, s in enumerate(streams) for k, t in enumerate(s.arrivals))
         nxt = 0
         queues = [collections.deque() for _ in range(n)]  # (chunk, sub index, last)
@@ -111,7 +116,7 @@ class Server:
         cohorts = []
         used = peak = 0
         last_admit = -1e9
-        lat, waits, units = [], [], 0.0
+        lat, lat_adm, ratio, waits, units = [], [], [], [], 0.0
         left = [len(s.arrivals) for s in streams]  # chunks not yet completed
         sub_left = {}  # (stream, chunk) -> sub-chunks not yet completed
         max_beams = 0
@@ -138,7 +143,7 @@ class Server:
                         used += foot[i]
                         waiting.remove(i)
                 if take:
-                    handle = self.engine.open([streams[i].cfg for i in take])
+                    handle = self.engine.open([streams[i].cfg for i in take], take)
                     c = _Cohort(handle, take, sum(foot[i] for i in take), now)
                     for slot, i in enumerate(take):
                         owner[i] = (c, slot)
@@ -158,7 +163,11 @@ class Server:
                         units += streams[i].units_per_spectrum * SUB_CHUNK
                         sub_left[(i, k)] -= 1
                         if sub_left[(i, k)] == 0:
-                            lat.append(tnow - streams[i].arrivals[k])
+                            a = streams[i].arrivals[k]
+                            lat.append(tnow - a)
+                            if a >= admitted_at[i]:
+                                lat_adm.append(tnow - a)
+                            ratio.append((tnow - a) / (streams[i].sizes[k] * streams[i].tsamp))
                             left[i] -= 1
                     busy = True
             # steps
@@ -210,16 +219,21 @@ class Server:
                     pause = min(max(events[nxt][0] - now, 0.0), 0.001)
                 sleep(pause)
         wall = clock() - t0
-        lat = np.array(lat) if lat else np.zeros(1)
-        waits = np.array(waits) if waits else np.zeros(1)
+
+        def pct(x):
+            x = np.array(x) if x else np.zeros(1)
+            return {"p50": float(np.percentile(x, 50)), "p99": float(np.percentile(x, 99)),
+                    "max": float(x.max())}
+        within = float(np.mean(np.array(ratio) < 1.0)) if ratio else 1.0
         done_chunks = sum(len(s.arrivals) - left[i] for i, s in enumerate(streams))
         return {"policy": self.policy, "beams": n, "chunks": int(sum(len(s.arrivals) for s in streams)),
                 "chunks_done": int(done_chunks), "wall_s": wall,
                 "throughput": units / wall, "units": units,
-                "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                              "max": float(lat.max())},
-                "admission_wait_s": {"p50": float(np.percentile(waits, 50)),
-                                     "p99": float(np.percentile(waits, 99))},
+                "latency_s": pct(lat),
+                "latency_after_admission_s": pct(lat_adm),
+                "latency_over_chunk_duration": pct(ratio),
+                "chunks_within_real_time": within,
+                "admission_wait_s": pct(waits),
                 "max_concurrent_beams": max_beams, "peak_footprint_gb": peak / 1e9,
                 "budget_gb": self.budget / 1e9}
 
@@ -243,22 +257,33 @@ class BatchEngine:
     def footprint(self, cfg):
         return self.pv.batch_footprint(cfg, self.pipelined)
 
-    def open(self, cfgs):
-        return _BatchCohort(self, cfgs)
+    def prepare(self, cfgs):
+        self.staging = _staging(self.pv, self.make_voltages, cfgs)
+
+    def open(self, cfgs, ids):
+        return _BatchCohort(self, cfgs, [self.staging[i] for i in ids])
+
+
+def _staging(pv, make_voltages, cfgs):
+    """One page-locked, write-combined receive buffer per stream, holding a
+    synthetic sub-chunk of voltages."""
+    out = []
+    for c in cfgs:
+        v = make_voltages(c)
+        hb = pv.HostBuffer(v.numel() * v.element_size(), write_combined=True)
+        hb.fill_from(v)
+        out.append(hb)
+        del v
+    return out
 
 
 class _BatchCohort:
-    def __init__(self, eng, cfgs):
+    def __init__(self, eng, cfgs, staging):
         pv = eng.pv
         self.batch = pv.Batch(cfgs, tune=eng.tune, graph=True, variant=eng.variant,
                               pipelined=eng.pipelined)
         self.stream = eng.stream_factory()
-        self.staging = []
-        for c in cfgs:
-            v = eng.make_voltages(c)
-            hb = pv.HostBuffer(v.numel() * v.element_size(), write_combined=True)
-            hb.fill_from(v)
-            self.staging.append(hb)
+        self.staging = staging
         self.steps = 0
 
     def step(self, active):
@@ -287,21 +312,19 @@ class PlainEngine:
     def footprint(self, cfg):
         return self.pv.batch_footprint(cfg, False)
 
-    def open(self, cfgs):
-        return _PlainCohort(self, cfgs)
+    def prepare(self, cfgs):
+        self.staging = _staging(self.pv, self.make_voltages, cfgs)
+
+    def open(self, cfgs, ids):
+        return _PlainCohort(self, cfgs, [self.staging[i] for i in ids])
 
 
 class _PlainCohort:
-    def __init__(self, eng, cfgs):
+    def __init__(self, eng, cfgs, staging):
         pv = eng.pv
         self.beams = [pv.Beam(c) for c in cfgs]
         self.stream = eng.stream_factory()
-        self.staging = []
-        for c in cfgs:
-            v = eng.make_voltages(c)
-            hb = pv.HostBuffer(v.numel() * v.element_size(), write_combined=True)
-            hb.fill_from(v)
-            self.staging.append(hb)
+        self.staging = staging
         self.steps = 0
 
     def step(self, active):

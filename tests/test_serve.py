@@ -28,7 +28,7 @@ class FakeEngine:
     def footprint(self, cfg):
         return cfg["bytes"]
 
-    def open(self, cfgs):
+    def open(self, cfgs, ids):
         eng = self
 
         class Cohort:
