@@ -45,6 +45,11 @@ int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
  * (voltage chunks): uncached on the host, no cache snooping on transfer. */
 int pv_host_alloc(void** h_ptr, long long bytes, int write_combined);
 void pv_host_free(void* h_ptr);
+/* Device memory for callers without CUDA headers (the C++ module shim). */
+int pv_device_alloc(void** d_ptr, long long bytes);
+void pv_device_free(void* d_ptr);
+/* Waits for the work issued on `stream`. */
+int pv_synchronize(void* stream);
 
 /* ------------------------------------------------------------------------
  * A7 delay table — DedispersionModule::resize (lib/src/DedispersionModule.cpp:109-190)

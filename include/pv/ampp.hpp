@@ -1,0 +1,645 @@
+// C++ drop-in for pelican-lofar's beam-processing modules over the libpv C ABI.
+//
+// The classes keep the names, constructor (from the module's XML
+// ConfigNode), run() signatures and data-set layouts of the reference
+// modules, so pipeline code written against them compiles against this
+// header instead:
+//
+//   PPFChanneliser::run(const TimeSeriesDataSetC32*, SpectrumDataSetC32*)      lib/PPFChanneliser.h:68-69
+//   StokesGenerator::run(const SpectrumDataSetC32*, SpectrumDataSetStokes*)   lib/StokesGenerator.h:42-43
+//   StokesIntegrator::run(const SpectrumDataSetStokes*, SpectrumDataSetStokes*) lib/StokesIntegrator.h:46
+//   RFI_Clipper::run(WeightedSpectrumDataSet*), bandPass()                    lib/RFI_Clipper.h:37-38
+//   DedispersionModule::dedisperse(WeightedSpectrumDataSet*), connect(),
+//       unlockCallback(), onChainCompletion(), waitForJobCompletion(),
+//       maxshift(), numberOfSamples()                                          lib/DedispersionModule.h:76-104
+//   DedispersionAnalyser::analyse(DedispersionSpectra*, DedispersionDataAnalysis*) lib/DedispersionAnalyser.h:31
+//
+// XML options are read with the reference's element and attribute names
+// and defaults.  Errors the reference throws as QString (or reports with
+// exit()) are thrown here as std::runtime_error with the same text.  Data
+// sets live in host memory as in the reference; each run() moves its data
+// through device memory.  The DedispersionModule calls its connected
+// functors synchronously, on the thread that completes a buffer, and
+// releases input blobs at once (their samples are copied when added).
+//
+// Qt and the pelican core are absent: ConfigNode here is a small XML reader
+// of one module element, and blobs are plain classes.
+#pragma once
+
+#include <pv.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace pelican {
+
+// ---------------------------------------------------------------------------
+// ConfigNode: one XML element with attributes and child elements.
+// ---------------------------------------------------------------------------
+class ConfigNode {
+  public:
+    ConfigNode() = default;
+
+    // The first element named `tag` in an XML document (any depth).
+    static ConfigNode fromString(const std::string& xml, const std::string& tag) {
+        std::vector<ConfigNode> roots;
+        size_t pos = 0;
+        parse_children(xml, pos, roots, "");
+        const ConfigNode* n = find(roots, tag);
+        if (!n) throw std::runtime_error("ConfigNode: no element <" + tag + ">");
+        return *n;
+    }
+    static ConfigNode fromFile(const std::string& path, const std::string& tag) {
+        std::ifstream f(path);
+        if (!f) throw std::runtime_error("ConfigNode: cannot open " + path);
+        std::stringstream ss;
+        ss << f.rdbuf();
+        ConfigNode n = fromString(ss.str(), tag);
+        const size_t slash = path.find_last_of('/');
+        n.set_search_path(slash == std::string::npos ? "." : path.substr(0, slash));
+        return n;
+    }
+
+    const std::string& name() const { return name_; }
+    bool hasAttribute(const std::string& a) const { return attrs_.count(a) != 0; }
+    std::string getAttribute(const std::string& a) const {
+        auto it = attrs_.find(a);
+        return it == attrs_.end() ? std::string() : it->second;
+    }
+    // The attribute of the first child element `tag` (ConfigNode::getOption).
+    std::string getOption(const std::string& tag, const std::string& attribute,
+                          const std::string& def = "") const {
+        for (const auto& c : children_)
+            if (c.name_ == tag && c.hasAttribute(attribute)) return c.getAttribute(attribute);
+        return def;
+    }
+    // Resolves a file name against the configuration's directory.
+    std::string searchFile(const std::string& file) const {
+        if (file.empty()) throw std::runtime_error("file name empty");
+        if (file[0] == '/' || std::ifstream(file).good()) return file;
+        const std::string p = search_path_ + "/" + file;
+        if (std::ifstream(p).good()) return p;
+        throw std::runtime_error("file \"" + file + "\" not found");
+    }
+    void set_search_path(const std::string& p) {
+        search_path_ = p;
+        for (auto& c : children_) c.set_search_path(p);
+    }
+    const std::vector<ConfigNode>& children() const { return children_; }
+
+  private:
+    std::string name_;
+    std::map<std::string, std::string> attrs_;
+    std::vector<ConfigNode> children_;
+    std::string search_path_ = ".";
+
+    static const ConfigNode* find(const std::vector<ConfigNode>& nodes, const std::string& tag) {
+        for (const auto& n : nodes) {
+            if (n.name_ == tag) return &n;
+            if (const ConfigNode* c = find(n.children_, tag)) return c;
+        }
+        return nullptr;
+    }
+    static void skip_ws(const std::string& s, size_t& p) {
+        while (p < s.size() && std::isspace((unsigned char)s[p])) ++p;
+    }
+    // Parses elements until the closing tag `close` (or the end of the text).
+    static void parse_children(const std::string& s, size_t& p, std::vector<ConfigNode>& out,
+                               const std::string& close) {
+        while (p < s.size()) {
+            const size_t lt = s.find('<', p);
+            if (lt == std::string::npos) { p = s.size(); return; }
+            p = lt;
+            if (s.compare(p, 4, "<!--") == 0) {
+                const size_t e = s.find("-->", p);
+                p = e == std::string::npos ? s.size() : e + 3;
+                continue;
+            }
+            if (s.compare(p, 2, "<?") == 0 || s.compare(p, 2, "<!") == 0) {
+                const size_t e = s.find('>', p);
+                p = e == std::string::npos ? s.size() : e + 1;
+                continue;
+            }
+            if (s.compare(p, 2, "</") == 0) {
+                const size_t e = s.find('>', p);
+                const std::string tag = trim(s.substr(p + 2, e - p - 2));
+                p = e == std::string::npos ? s.size() : e + 1;
+                if (tag != close)
+                    throw std::runtime_error("ConfigNode: </" + tag + "> closes <" + close + ">");
+                return;
+            }
+            ConfigNode n;
+            ++p;
+            const size_t ns = p;
+            while (p < s.size() && !std::isspace((unsigned char)s[p]) && s[p] != '>' && s[p] != '/') ++p;
+            n.name_ = s.substr(ns, p - ns);
+            bool self_closing = false;
+            for (;;) {
+                skip_ws(s, p);
+                if (p >= s.size()) throw std::runtime_error("ConfigNode: unterminated <" + n.name_ + ">");
+                if (s[p] == '/') { self_closing = true; p = s.find('>', p) + 1; break; }
+                if (s[p] == '>') { ++p; break; }
+                const size_t as = p;
+                while (p < s.size() && s[p] != '=' && !std::isspace((unsigned char)s[p])) ++p;
+                const std::string key = s.substr(as, p - as);
+                skip_ws(s, p);
+                if (p >= s.size() || s[p] != '=') throw std::runtime_error("ConfigNode: attribute " + key);
+                ++p;
+                skip_ws(s, p);
+                const char q = s[p];
+                if (q != '"' && q != '\'') throw std::runtime_error("ConfigNode: unquoted " + key);
+                const size_t ve = s.find(q, p + 1);
+                n.attrs_[key] = s.substr(p + 1, ve - p - 1);
+                p = ve + 1;
+            }
+            if (!self_closing) parse_children(s, p, n.children_, n.name_);
+            out.push_back(std::move(n));
+        }
+        if (!close.empty()) throw std::runtime_error("ConfigNode: <" + close + "> not closed");
+    }
+    static std::string trim(const std::string& x) {
+        size_t a = 0, b = x.size();
+        while (a < b && std::isspace((unsigned char)x[a])) ++a;
+        while (b > a && std::isspace((unsigned char)x[b - 1])) --b;
+        return x.substr(a, b - a);
+    }
+};
+
+namespace ampp {
+
+// Throws the library's last error text for a failed call.
+inline void pv_check(int rc) {
+    if (rc != PV_OK) throw std::runtime_error(pv_last_error());
+}
+inline std::string lower(std::string s) {
+    for (auto& c : s) c = (char)std::tolower((unsigned char)c);
+    return s;
+}
+inline unsigned to_uint(const std::string& s) { return s.empty() ? 0u : (unsigned)std::stoul(s); }
+inline float to_float(const std::string& s) { return s.empty() ? 0.0f : std::stof(s); }
+
+// A device buffer owned by a module.
+class DeviceBuffer {
+  public:
+    ~DeviceBuffer() { pv_device_free(p_); }
+    void* get(size_t bytes) {
+        if (bytes > n_) {
+            pv_device_free(p_);
+            p_ = nullptr;
+            n_ = 0;
+            pv_check(pv_device_alloc(&p_, (long long)bytes));
+            n_ = bytes;
+        }
+        return p_;
+    }
+    template <typename T>
+    T* as(size_t count) { return static_cast<T*>(get(count * sizeof(T))); }
+
+  private:
+    void* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Data sets (lib/TimeSeriesDataSet.h, lib/SpectrumDataSet.h)
+// ---------------------------------------------------------------------------
+class DataBlob {
+  public:
+    virtual ~DataBlob() = default;
+    void setBlockRate(double r) { block_rate_ = r; }
+    double getBlockRate() const { return block_rate_; }
+    void setLofarTimestamp(double t) { timestamp_ = t; }
+    double getLofarTimestamp() const { return timestamp_; }
+    double getTime(unsigned sample) const { return timestamp_ + sample * block_rate_; }
+
+  protected:
+    double block_rate_ = 0.0, timestamp_ = 0.0;
+};
+
+// complex<float> [subband][polarisation][block][channel] (TimeSeriesDataSet.h:145-151)
+class TimeSeriesDataSetC32 : public DataBlob {
+  public:
+    void resize(unsigned nBlocks, unsigned nSubbands, unsigned nPols, unsigned nTimesPerBlock) {
+        nb_ = nBlocks; ns_ = nSubbands; np_ = nPols; nt_ = nTimesPerBlock;
+        d_.assign((size_t)nb_ * ns_ * np_ * nt_, {0.0f, 0.0f});
+    }
+    unsigned nTimeBlocks() const { return nb_; }
+    unsigned nSubbands() const { return ns_; }
+    unsigned nPolarisations() const { return np_; }
+    unsigned nTimesPerBlock() const { return nt_; }
+    std::complex<float>* data() { return d_.data(); }
+    const std::complex<float>* data() const { return d_.data(); }
+    std::complex<float>* timeSeriesData(unsigned b, unsigned s, unsigned p) {
+        return d_.data() + ((size_t)nb_ * (s * np_ + p) + b) * nt_;
+    }
+
+  private:
+    unsigned nb_ = 0, ns_ = 0, np_ = 0, nt_ = 0;
+    std::vector<std::complex<float>> d_;
+};
+
+// T [block][subband][polarisation][channel] (SpectrumDataSet.h:229-235)
+template <typename T>
+class SpectrumDataSet : public DataBlob {
+  public:
+    void resize(unsigned nBlocks, unsigned nSubbands, unsigned nPols, unsigned nChannels) {
+        nb_ = nBlocks; ns_ = nSubbands; np_ = nPols; nc_ = nChannels;
+        d_.assign((size_t)nb_ * ns_ * np_ * nc_, T());
+    }
+    unsigned nTimeBlocks() const { return nb_; }
+    unsigned nSubbands() const { return ns_; }
+    unsigned nPolarisations() const { return np_; }
+    unsigned nChannels() const { return nc_; }
+    size_t size() const { return d_.size(); }
+    T* data() { return d_.data(); }
+    const T* data() const { return d_.data(); }
+    long index(unsigned s, unsigned nSub, unsigned p, unsigned nPol, unsigned b, unsigned nChan) const {
+        return (long)nChan * (nPol * ((long)nSub * b + s) + p);
+    }
+    T* spectrumData(unsigned b, unsigned s, unsigned p) {
+        return d_.data() + (size_t)nc_ * (np_ * ((size_t)ns_ * b + s) + p);
+    }
+
+  private:
+    unsigned nb_ = 0, ns_ = 0, np_ = 0, nc_ = 0;
+    std::vector<T> d_;
+};
+using SpectrumDataSetC32 = SpectrumDataSet<std::complex<float>>;
+// float [time][subband][stokes][channel]
+using SpectrumDataSetStokes = SpectrumDataSet<float>;
+
+// The Stokes data and its weights, 1 everywhere (WeightedSpectrumDataSet.h:26-47).
+class WeightedSpectrumDataSet : public DataBlob {
+  public:
+    explicit WeightedSpectrumDataSet(SpectrumDataSetStokes* d = nullptr) { reset(d); }
+    void reset(SpectrumDataSetStokes* d) {
+        data_ = d;
+        if (d) {
+            w_.resize(d->nTimeBlocks(), d->nSubbands(), d->nPolarisations(), d->nChannels());
+            std::fill(w_.data(), w_.data() + w_.size(), 1.0f);
+        }
+    }
+    SpectrumDataSetStokes* stats() const { return data_; }
+    SpectrumDataSetStokes* dataSet() const { return data_; }
+    SpectrumDataSet<float>* weights() { return &w_; }
+
+  private:
+    SpectrumDataSetStokes* data_ = nullptr;
+    SpectrumDataSet<float> w_;
+};
+
+// ---------------------------------------------------------------------------
+// Dedispersion results (lib/DedispersionSpectra.h, DedispersionDataAnalysis.h,
+// DedispersionEvent.h)
+// ---------------------------------------------------------------------------
+class DedispersionSpectra : public DataBlob {
+  public:
+    void resize(unsigned timebins, unsigned dedispersionBins, float start, float width) {
+        t_ = timebins; n_ = dedispersionBins; lower_ = start; width_ = width;
+        d_.assign((size_t)t_ * n_, 0.0f);
+    }
+    std::vector<float>& data() { return d_; }
+    const std::vector<float>& data() const { return d_; }
+    // BinMap::binIndex / binAssignmentNumber (lib/src/BinMap.cpp)
+    int dmIndex(float dm) const { return (int)(0.5 + ((double)dm - lower_) / width_); }
+    float dm(unsigned i) const { return (float)(lower_ + width_ * i); }
+    float dmAmplitude(unsigned t, int dm) const { return d_[t + (size_t)t_ * dm]; }
+    float dmAmplitude(unsigned t, float dm) const { return dmAmplitude(t, dmIndex(dm)); }
+    int dmBins() const { return (int)n_; }
+    int timeSamples() const { return (int)t_; }
+    float dmMax() const { return dm(n_ - 1); }
+    void setFirstSample(unsigned s) { first_ = s; }
+    unsigned firstSample() const { return first_; }
+    // the channel count the analyser's RMS is taken from (inputDataBlobs()[0])
+    void setInputShape(unsigned nChannels, unsigned nSubbands) { nch_ = nChannels; nsub_ = nSubbands; }
+    unsigned inputChannels() const { return nch_; }
+    unsigned inputSubbands() const { return nsub_; }
+    float getRMS() const { return rms_; }
+    void setRMS(float r) { rms_ = r; }
+
+  private:
+    unsigned t_ = 0, n_ = 0, first_ = 0, nch_ = 0, nsub_ = 0;
+    double lower_ = 0.0, width_ = 1.0;
+    float rms_ = 0.0f;
+    std::vector<float> d_;
+};
+
+class DedispersionEvent {
+  public:
+    DedispersionEvent(int dmIndex, unsigned timeIndex, const DedispersionSpectra* d, float factor,
+                      float value)
+        : dm_(dmIndex), t_(timeIndex), d_(d), f_(factor), v_(value) {}
+    unsigned timeBin() const { return t_; }
+    float dm() const { return d_->dm(dm_); }
+    int dmIndex() const { return dm_; }
+    float amplitude() const { return d_->dmAmplitude(t_, dm_); }
+    float mfValue() const { return v_; }
+    float mfBinning() const { return f_; }
+    double getTime() const { return d_->getTime(t_ + d_->firstSample()); }
+
+  private:
+    int dm_;
+    unsigned t_;
+    const DedispersionSpectra* d_;
+    float f_, v_;
+};
+
+class DedispersionDataAnalysis : public DataBlob {
+  public:
+    void reset(const DedispersionSpectra* d) { data_ = d; ev_.clear(); }
+    void addEvent(unsigned dm, unsigned timeBin, float factor, float value) {
+        ev_.emplace_back((int)dm, timeBin, data_, factor, value);
+    }
+    int eventsFound() const { return (int)ev_.size(); }
+    const std::vector<DedispersionEvent>& events() const { return ev_; }
+    const DedispersionSpectra* data() const { return data_; }
+    float getRMS() const { return rms_; }
+    void setRMS(float r) { rms_ = r; }
+
+  private:
+    const DedispersionSpectra* data_ = nullptr;
+    std::vector<DedispersionEvent> ev_;
+    float rms_ = 0.0f;
+};
+
+// ---------------------------------------------------------------------------
+// Modules
+// ---------------------------------------------------------------------------
+
+// lib/src/PPFChanneliser.cpp:29-290
+class PPFChanneliser {
+  public:
+    explicit PPFChanneliser(const ConfigNode& config) {
+        nchan_ = to_uint(config.getOption("outputChannelsPerSubband", "value", "512"));
+        const unsigned taps = to_uint(config.getOption("filter", "nTaps", "8"));
+        const std::string window = lower(config.getOption("filter", "filterWindow", "kaiser"));
+        const int w = pv_window_from_name(window.c_str());
+        if (w < 0) throw std::runtime_error(pv_last_error());
+        pv_check(pv_ppf_create(&h_, (int)nchan_, (int)taps, w, nullptr));
+    }
+    ~PPFChanneliser() { pv_ppf_destroy(h_); }
+    PPFChanneliser(const PPFChanneliser&) = delete;
+    PPFChanneliser& operator=(const PPFChanneliser&) = delete;
+
+    void run(const TimeSeriesDataSetC32* in, SpectrumDataSetC32* out) {
+        if (!in || in->nTimeBlocks() == 0 || in->nSubbands() == 0)
+            throw std::runtime_error("PPFChanneliser: Empty time data blob");
+        if (in->nTimesPerBlock() != nchan_)
+            throw std::runtime_error("PPFChanneliser: Data blob has incorrect number of channels");
+        const unsigned ns = in->nSubbands(), np = in->nPolarisations(), nb = in->nTimeBlocks();
+        const size_t n = (size_t)ns * np * nb * nchan_;
+        float* d_in = din_.as<float>(2 * n);
+        float* d_out = dout_.as<float>(2 * n);
+        pv_check(pv_device_copy(d_in, in->data(), (long long)(8 * n), nullptr));
+        pv_check(pv_ppf_run(h_, d_in, (int)ns, (int)np, (int)nb, d_out, nullptr));
+        out->resize(nb, ns, np, nchan_);
+        pv_check(pv_device_copy(out->data(), d_out, (long long)(8 * n), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        out->setBlockRate(in->getBlockRate() * nchan_);  // PPFChanneliser.cpp:99
+        out->setLofarTimestamp(in->getLofarTimestamp());
+    }
+
+  private:
+    pv_ppf* h_ = nullptr;
+    unsigned nchan_ = 0;
+    DeviceBuffer din_, dout_;
+};
+
+// lib/src/StokesGenerator.cpp:40-108
+class StokesGenerator {
+  public:
+    explicit StokesGenerator(const ConfigNode& config)
+        : nstokes_(to_uint(config.getOption("numberOfStokes", "value", "4"))) {
+        if (nstokes_ != 1 && nstokes_ != 4)
+            throw std::runtime_error("StokesGenerator: You can either generate 1 or 4 Stokes parameters.");
+    }
+    void run(const SpectrumDataSetC32* in, SpectrumDataSetStokes* out) {
+        const unsigned nt = in->nTimeBlocks(), ns = in->nSubbands(), nc = in->nChannels();
+        if (in->nPolarisations() != 2) throw std::runtime_error("StokesGenerator: needs 2 polarisations");
+        const size_t n = (size_t)nt * ns * 2 * nc;
+        float* d_in = din_.as<float>(2 * n);
+        float* d_out = dout_.as<float>((size_t)nt * ns * nstokes_ * nc);
+        pv_check(pv_device_copy(d_in, in->data(), (long long)(8 * n), nullptr));
+        pv_check(pv_stokes(d_in, (int)nt, (int)ns, (int)nc, (int)nstokes_, d_out, nullptr));
+        out->resize(nt, ns, nstokes_, nc);
+        pv_check(pv_device_copy(out->data(), d_out, (long long)(4 * out->size()), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        out->setBlockRate(in->getBlockRate());
+        out->setLofarTimestamp(in->getLofarTimestamp());
+    }
+
+  private:
+    unsigned nstokes_;
+    DeviceBuffer din_, dout_;
+};
+
+// lib/src/StokesIntegrator.cpp:32-119
+class StokesIntegrator {
+  public:
+    explicit StokesIntegrator(const ConfigNode& config)
+        : window_(to_uint(config.getOption("integrateTimeBins", "value", "1"))),
+          bin_(to_uint(config.getOption("integrateFrequencyChannels", "value", "1"))) {}
+    void run(const SpectrumDataSetStokes* in, SpectrumDataSetStokes* out) {
+        const unsigned nt = in->nTimeBlocks(), ns = in->nSubbands(), np = in->nPolarisations(),
+                       nc = in->nChannels();
+        const size_t n = (size_t)nt * ns * np * nc;
+        float* d_in = din_.as<float>(n);
+        float* d_out = dout_.as<float>(n);
+        pv_check(pv_device_copy(d_in, in->data(), (long long)(4 * n), nullptr));
+        int nu = 0;
+        pv_check(pv_integrate(d_in, (int)nt, (int)ns, (int)np, (int)nc, (int)window_, (int)bin_, d_out,
+                              &nu, nullptr));
+        out->resize((unsigned)nu, ns, np, nc / bin_);
+        pv_check(pv_device_copy(out->data(), d_out, (long long)(4 * out->size()), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        const unsigned w = nt < window_ ? (nt ? nt : 1) : window_;
+        out->setBlockRate(in->getBlockRate() * w);  // StokesIntegrator.cpp:53-59
+        out->setLofarTimestamp(in->getLofarTimestamp());
+    }
+
+  private:
+    unsigned window_, bin_;
+    DeviceBuffer din_, dout_;
+};
+
+// lib/src/RFI_Clipper.cpp:22-573 (the BandPassData file is read here and
+// parsed by the library, BandPassAdapter.cpp:30-108)
+class RFI_Clipper {
+  public:
+    explicit RFI_Clipper(const ConfigNode& config) {
+        const bool active = !(config.hasAttribute("active") && lower(config.getAttribute("active")) == "false");
+        std::string text;
+        const std::string file = config.getOption("BandPassData", "file", "");
+        if (!file.empty() && active) {
+            std::string path;
+            try {
+                path = config.searchFile(file);
+            } catch (const std::exception& e) {
+                throw std::runtime_error(std::string("RFI_Clipper: ") + e.what());
+            }
+            std::ifstream f(path);
+            if (!f) throw std::runtime_error("RFI_Clipper: Cannot open File \"" + file + "\"");
+            std::stringstream ss;
+            ss << f.rdbuf();
+            text = ss.str();
+        } else if (active) {
+            throw std::runtime_error("RFI_Clipper: <BandPassData file=?> not defined");
+        }
+        const float cr = config.hasAttribute("channelRejectionRMS")
+                             ? to_float(config.getAttribute("channelRejectionRMS")) : 10.0f;
+        const float sr = config.hasAttribute("spectrumRejectionRMS")
+                             ? to_float(config.getAttribute("spectrumRejectionRMS")) : 4.0f;
+        const int history = std::stoi(config.getOption("History", "maximum", "10"));
+        const int zero_dm = config.getOption("zeroDMing", "active") == "true";
+        const int mor = config.getOption("computeRMSfromMean", "active", "true") == "true";
+        const int matching = config.getOption("Band", "matching") == "true";
+        pv_check(pv_rfi_create(&h_, text.c_str(), cr, sr, history, zero_dm, mor, matching, active ? 1 : 0));
+    }
+    ~RFI_Clipper() { pv_rfi_destroy(h_); }
+    RFI_Clipper(const RFI_Clipper&) = delete;
+    RFI_Clipper& operator=(const RFI_Clipper&) = delete;
+
+    void run(WeightedSpectrumDataSet* weighted) {
+        SpectrumDataSetStokes* d = weighted->stats();
+        const size_t n = d->size();
+        float* dd = dbuf_.as<float>(n);
+        pv_check(pv_device_copy(dd, d->data(), (long long)(4 * n), nullptr));
+        pv_check(pv_rfi_run(h_, dd, (int)d->nTimeBlocks(), (int)d->nSubbands(), (int)d->nPolarisations(),
+                            (int)d->nChannels(), nullptr, nullptr));
+        pv_check(pv_device_copy(d->data(), dd, (long long)(4 * n), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        nbins_ = d->nSubbands() * d->nChannels();
+    }
+    // The rebinned bandpass model in use (BandPass::currentSet).
+    std::vector<float> bandPass() {
+        std::vector<float> bp(nbins_);
+        if (nbins_) pv_check(pv_rfi_bandpass(h_, bp.data(), (int)nbins_));
+        return bp;
+    }
+
+  private:
+    pv_rfi* h_ = nullptr;
+    unsigned nbins_ = 0;
+    DeviceBuffer dbuf_;
+};
+
+// lib/src/DedispersionModule.cpp:45-325 with the reference's buffering
+class DedispersionModule {
+  public:
+    using Functor = std::function<void(DedispersionSpectra*)>;
+    using UnlockCallback = std::function<void(const std::vector<DataBlob*>&)>;
+
+    explicit DedispersionModule(const ConfigNode& config) {
+        const float pow2 = to_float(config.getOption("timeBinsPerBufferPow2", "value", "15"));
+        samples_ = 1u << (unsigned)pow2;
+        tdms_ = to_uint(config.getOption("dedispersionSamples", "value", "1984"));
+        dm_step_ = to_float(config.getOption("dedispersionStepSize", "value", "0.0"));
+        dm_low_ = to_float(config.getOption("dedispersionMinimum", "value", "0.0"));
+        fch1_ = std::stod(config.getOption("frequencyChannel1", "MHz", "0.0"));
+        foff_ = std::stod(config.getOption("channelBandwidth", "MHz", "1.0"));
+        pv_check(pv_ddmod_create(&h_, (int)samples_, (int)tdms_, dm_low_, dm_step_, fch1_, foff_));
+    }
+    ~DedispersionModule() { pv_ddmod_destroy(h_); }
+    DedispersionModule(const DedispersionModule&) = delete;
+    DedispersionModule& operator=(const DedispersionModule&) = delete;
+
+    void connect(const Functor& f) { functors_.push_back(f); }
+    void unlockCallback(const UnlockCallback& f) { unlock_ = f; }
+    void onChainCompletion(const std::function<void()>& f) { chain_.push_back(f); }
+    void waitForJobCompletion() {}
+    unsigned numberOfSamples() const { return samples_; }
+    int maxshift() const {
+        int p[6] = {0};
+        pv_check(pv_ddmod_params(h_, p));
+        return p[0];
+    }
+
+    void dedisperse(WeightedSpectrumDataSet* weighted) { dedisperse_blob(weighted->stats(), weighted); }
+    void dedisperse(DataBlob* blob) {
+        auto* w = dynamic_cast<WeightedSpectrumDataSet*>(blob);
+        if (!w) throw std::runtime_error("DedispersionModule: expecting a WeightedSpectrumDataSet");
+        dedisperse(w);
+    }
+
+  private:
+    void dedisperse_blob(SpectrumDataSetStokes* d, DataBlob* blob) {
+        int done = 0;
+        nch_ = d->nChannels();
+        nsub_ = d->nSubbands();
+        pv_check(pv_ddmod_add(h_, d->data(), (int)d->nTimeBlocks(), (int)d->nSubbands(),
+                              (int)d->nPolarisations(), (int)d->nChannels(), d->getBlockRate(), &done,
+                              nullptr));
+        if (unlock_) unlock_(std::vector<DataBlob*>{blob});  // samples are copied on add
+        for (int i = 0; i < done; ++i) {
+            int p[6] = {0};
+            pv_check(pv_ddmod_params(h_, p));
+            DedispersionSpectra out;
+            out.resize((unsigned)p[2], tdms_, dm_low_ < 0.0f ? 0.0f : dm_low_, dm_step_);
+            int nout = 0;
+            long long first = 0;
+            pv_check(pv_ddmod_pop(h_, out.data().data(), (long long)out.data().size(), &nout, &first, nullptr));
+            out.setFirstSample((unsigned)first);
+            out.setInputShape(nch_, nsub_);
+            out.setBlockRate(d->getBlockRate());
+            out.setLofarTimestamp(d->getLofarTimestamp());
+            for (auto& f : functors_) f(&out);
+            for (auto& f : chain_) f();
+        }
+    }
+
+    pv_ddmod* h_ = nullptr;
+    unsigned samples_ = 0, tdms_ = 0, nch_ = 0, nsub_ = 0;
+    float dm_step_ = 0.0f, dm_low_ = 0.0f;
+    double fch1_ = 0.0, foff_ = 0.0;
+    std::vector<Functor> functors_;
+    std::vector<std::function<void()>> chain_;
+    UnlockCallback unlock_;
+};
+
+// lib/src/DedispersionAnalyser.cpp:30-203
+class DedispersionAnalyser {
+  public:
+    explicit DedispersionAnalyser(const ConfigNode& config)
+        : threshold_(to_float(config.getOption("detectionThreshold", "in_sigma", "6.0"))),
+          bin_pow2_(to_uint(config.getOption("power2ForBinning", "value", "6"))) {}
+
+    int analyse(DedispersionSpectra* data, DedispersionDataAnalysis* result) {
+        result->reset(data);
+        // sigma of the dedispersed sum: sqrt(nChannels * nSubbands) (DedispersionAnalyser.cpp:36-38)
+        const float rms = std::sqrt((float)data->inputChannels() * (float)data->inputSubbands());
+        result->setRMS(rms);
+        const int tdms = data->dmBins(), nsamp = data->timeSamples();
+        const size_t n = (size_t)tdms * nsamp;
+        float* d = dbuf_.as<float>(n ? n : 1);
+        if (n) pv_check(pv_device_copy(d, data->data().data(), (long long)(4 * n), nullptr));
+        long long count = 0;
+        const long long cap = 1 << 20;
+        pv_event* ev = evbuf_.as<pv_event>((size_t)cap);
+        pv_check(pv_analyse(d, nsamp, tdms, nsamp, threshold_, rms, (int)bin_pow2_, ev, cap, &count, nullptr));
+        std::vector<pv_event> h((size_t)std::min(count, cap));
+        if (!h.empty())
+            pv_check(pv_device_copy(h.data(), ev, (long long)(sizeof(pv_event) * h.size()), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        for (const auto& e : h) result->addEvent((unsigned)e.dm, (unsigned)e.t, e.bin_factor, e.value);
+        return result->eventsFound();
+    }
+
+  private:
+    float threshold_;
+    unsigned bin_pow2_;
+    DeviceBuffer dbuf_, evbuf_;
+};
+
+}  // namespace ampp
+}  // namespace pelican

@@ -139,3 +139,28 @@ extern "C" int pv_host_alloc(void** h_ptr, long long bytes, int write_combined) 
 extern "C" void pv_host_free(void* h_ptr) {
     if (h_ptr) cudaFreeHost(h_ptr);
 }
+
+extern "C" int pv_device_alloc(void** d_ptr, long long bytes) {
+    if (!d_ptr || bytes < 0) {
+        pv::set_error("pv_device_alloc: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    *d_ptr = nullptr;
+    if (bytes == 0) return PV_OK;
+    const cudaError_t e = cudaMalloc(d_ptr, (size_t)bytes);
+    if (e != cudaSuccess) {
+        *d_ptr = nullptr;
+        pv::set_error("pv_device_alloc: %s (%lld bytes)", cudaGetErrorString(e), bytes);
+        return PV_ERR_NOMEM;
+    }
+    return PV_OK;
+}
+
+extern "C" void pv_device_free(void* d_ptr) {
+    if (d_ptr) cudaFree(d_ptr);
+}
+
+extern "C" int pv_synchronize(void* stream) {
+    PV_CUDA(cudaStreamSynchronize(pv::as_stream(stream)), "pv_synchronize");
+    return PV_OK;
+}

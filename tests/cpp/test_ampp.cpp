@@ -1,0 +1,178 @@
+// Drives the C++ module shim (include/pv/ampp.hpp) for tests/test_cpp_shim.py.
+//
+//   test_ampp config            XML option parsing (no GPU)
+//   test_ampp chain DIR         PPF -> Stokes -> integrator -> RFI on DIR/volt.bin with
+//                               DIR/config.xml; writes DIR/{ppf,stokes,integ,rfi}.bin
+//   test_ampp ddmod DIR N       DedispersionModule + analyser on DIR/blob.bin (float32
+//                               [nt][nsub][1][nchan], shape in DIR/shape.txt) with
+//                               DIR/config.xml; prints "AMP <dmAmplitude(0, 10.0)>" and
+//                               "EVENTS <count>" per completed buffer
+#include <pv/ampp.hpp>
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+
+using namespace pelican;
+using namespace pelican::ampp;
+
+namespace {
+
+int failures = 0;
+void expect(bool ok, const char* what) {
+    if (!ok) {
+        std::fprintf(stderr, "FAILED: %s\n", what);
+        ++failures;
+    }
+}
+
+template <typename T>
+std::vector<T> read_file(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    std::vector<char> raw((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<T> v(raw.size() / sizeof(T));
+    std::memcpy(v.data(), raw.data(), v.size() * sizeof(T));
+    return v;
+}
+template <typename T>
+void write_file(const std::string& path, const T* p, size_t n) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(p), (std::streamsize)(n * sizeof(T)));
+}
+
+int config_mode() {
+    const std::string xml = R"(<?xml version="1.0"?>
+<!-- a pipeline configuration in the reference's layout -->
+<configuration version="1.0">
+  <pipeline>
+    <modules>
+      <PPFChanneliser>
+        <outputChannelsPerSubband value="16"/>
+        <filter nTaps="8" filterWindow="Kaiser" />
+      </PPFChanneliser>
+      <RFI_Clipper active="true" channelRejectionRMS="5.0" spectrumRejectionRMS="4.5">
+        <zeroDMing active="true" />
+        <BandPassData file="band.bp" />
+        <Band matching="true" />
+        <History maximum="10000" />
+      </RFI_Clipper>
+      <DedispersionModule>
+        <timeBinsPerBufferPow2 value="14"/>
+        <frequencyChannel1 MHz="150.0"/>
+        <channelBandwidth MHz='-0.0029296875'/>
+      </DedispersionModule>
+    </modules>
+  </pipeline>
+</configuration>)";
+    const ConfigNode ppf = ConfigNode::fromString(xml, "PPFChanneliser");
+    expect(ppf.getOption("outputChannelsPerSubband", "value", "512") == "16", "option value");
+    expect(ppf.getOption("filter", "nTaps", "4") == "8", "second attribute");
+    expect(lower(ppf.getOption("filter", "filterWindow")) == "kaiser", "window");
+    expect(ppf.getOption("processingThreads", "value", "2") == "2", "default");
+    const ConfigNode rfi = ConfigNode::fromString(xml, "RFI_Clipper");
+    expect(rfi.hasAttribute("channelRejectionRMS") && rfi.getAttribute("channelRejectionRMS") == "5.0",
+           "element attribute");
+    expect(!rfi.hasAttribute("nothing"), "missing attribute");
+    expect(rfi.getOption("History", "maximum", "10") == "10000", "history");
+    expect(rfi.getOption("zeroDMing", "active") == "true", "zeroDMing");
+    const ConfigNode dd = ConfigNode::fromString(xml, "DedispersionModule");
+    expect(dd.getOption("channelBandwidth", "MHz") == "-0.0029296875", "single quotes");
+    expect(dd.getOption("dedispersionSamples", "value", "1984") == "1984", "dd default");
+    bool threw = false;
+    try {
+        ConfigNode::fromString("<a><b></a>", "a");
+    } catch (const std::runtime_error&) {
+        threw = true;
+    }
+    expect(threw, "mismatched tags throw");
+    threw = false;
+    try {
+        RFI_Clipper r(ConfigNode::fromString("<RFI_Clipper active=\"true\"/>", "RFI_Clipper"));
+    } catch (const std::runtime_error& e) {
+        threw = std::string(e.what()) == "RFI_Clipper: <BandPassData file=?> not defined";
+    }
+    expect(threw, "RFI_Clipper without a bandpass throws the reference message");
+    if (!failures) std::printf("CONFIG OK\n");
+    return failures ? 1 : 0;
+}
+
+int chain_mode(const std::string& dir) {
+    const ConfigNode ppf_cfg = ConfigNode::fromFile(dir + "/config.xml", "PPFChanneliser");
+    const ConfigNode st_cfg = ConfigNode::fromFile(dir + "/config.xml", "StokesGenerator");
+    const ConfigNode in_cfg = ConfigNode::fromFile(dir + "/config.xml", "StokesIntegrator");
+    const ConfigNode rfi_cfg = ConfigNode::fromFile(dir + "/config.xml", "RFI_Clipper");
+    std::ifstream shape(dir + "/shape.txt");
+    unsigned nsub, npol, nblk, nchan;
+    shape >> nsub >> npol >> nblk >> nchan;
+    const auto v = read_file<std::complex<float>>(dir + "/volt.bin");
+    TimeSeriesDataSetC32 ts;
+    ts.resize(nblk, nsub, npol, nchan);
+    std::memcpy(ts.data(), v.data(), v.size() * sizeof(v[0]));
+    ts.setBlockRate(5.12e-6);
+    PPFChanneliser ppf(ppf_cfg);
+    StokesGenerator stokes(st_cfg);
+    StokesIntegrator integ(in_cfg);
+    RFI_Clipper rfi(rfi_cfg);
+    SpectrumDataSetC32 spectra;
+    SpectrumDataSetStokes st, it;
+    ppf.run(&ts, &spectra);
+    stokes.run(&spectra, &st);
+    integ.run(&st, &it);
+    write_file(dir + "/ppf.bin", spectra.data(), spectra.size());
+    write_file(dir + "/stokes.bin", st.data(), st.size());
+    write_file(dir + "/integ.bin", it.data(), it.size());
+    WeightedSpectrumDataSet w(&it);
+    rfi.run(&w);
+    write_file(dir + "/rfi.bin", it.data(), it.size());
+    std::printf("SHAPES %u %u %u %u %g\n", it.nTimeBlocks(), it.nSubbands(), it.nPolarisations(),
+                it.nChannels(), it.getBlockRate());
+    return 0;
+}
+
+int ddmod_mode(const std::string& dir, int nblobs) {
+    const ConfigNode dd_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionModule");
+    const ConfigNode an_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionAnalyser");
+    std::ifstream shape(dir + "/shape.txt");
+    unsigned nt, nsub, nchan;
+    double tsamp;
+    shape >> nt >> nsub >> nchan >> tsamp;
+    const auto blob = read_file<float>(dir + "/blob.bin");
+    DedispersionModule dd(dd_cfg);
+    DedispersionAnalyser an(an_cfg);
+    int unlocked = 0, completed = 0;
+    dd.unlockCallback([&](const std::vector<DataBlob*>& blobs) { unlocked += (int)blobs.size(); });
+    dd.onChainCompletion([&]() { ++completed; });
+    dd.connect([&](DedispersionSpectra* s) {
+        DedispersionDataAnalysis result;
+        const int n = an.analyse(s, &result);
+        std::printf("AMP %g\nEVENTS %d\nFIRST %u\n", s->dmAmplitude(0u, 10.0f), n, s->firstSample());
+    });
+    for (int b = 0; b < nblobs; ++b) {
+        SpectrumDataSetStokes st;
+        st.resize(nt, nsub, 1, nchan);
+        std::memcpy(st.data(), blob.data() + (size_t)b * st.size(), st.size() * sizeof(float));
+        st.setBlockRate(tsamp);
+        WeightedSpectrumDataSet w(&st);
+        dd.dedisperse(&w);
+    }
+    dd.waitForJobCompletion();
+    std::printf("MAXSHIFT %d\nUNLOCKED %d\nCOMPLETED %d\n", dd.maxshift(), unlocked, completed);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2) return 2;
+    const std::string mode = argv[1];
+    try {
+        if (mode == "config") return config_mode();
+        if (mode == "chain" && argc >= 3) return chain_mode(argv[2]);
+        if (mode == "ddmod" && argc >= 4) return ddmod_mode(argv[2], std::atoi(argv[3]));
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "EXCEPTION %s\n", e.what());
+        return 3;
+    }
+    return 2;
+}
