@@ -352,7 +352,7 @@ int pv_beam_buffers(const pv_beam* beam, float** d_filterbank, float** d_filterb
  * few launches (one persistent dedispersion launch over every beam's DM x
  * time tiles), optionally replayed from one captured CUDA graph.  A beam's
  * events equal those of the same beam run alone through pv_beam.
- * Restrictions: every beam has the same chunk (a multiple of 4 spectra), 8
+ * Restrictions: every beam has the same chunk (a multiple of 16 spectra), 8
  * PPF taps, 16, 32 or 64 channels per subband, int_chan = 1 and an int_time
  * dividing 256; input is complex int16.
  * ------------------------------------------------------------------------ */
@@ -363,6 +363,15 @@ typedef struct pv_batch pv_batch;
 #define PV_BATCH_PIPELINED 8 /* dedisperse a beam's window in its step after the chunk that
                                 completes it, beside that step's channeliser and clippers
                                 (rings one chunk longer) */
+#define PV_BATCH_STORE_F16 16 /* delay rings hold FP16 samples (sums stay FP32) */
+#define PV_BATCH_STORE_U8 32  /* delay rings hold uint8 codes q with a per-channel FP32 scale and
+                                 offset: the sample is (q - 128) * scale + offset, scale = 6 sigma
+                                 / 127.  With the clipper and zero-DMing its output has zero
+                                 mean and unit RMS: sigma = 1, offset 0.  Otherwise the offset is
+                                 the median and
+                                 sigma the median absolute deviation x 1.4826 of the first
+                                 chunk in which the channel varies (until then the channel's
+                                 samples are stored as its offset) */
 #define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);

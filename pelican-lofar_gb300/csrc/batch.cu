@@ -105,7 +105,9 @@ struct pv_batch {
     std::vector<ChanClass> chan;
     pv::RfiBatch* rfi = nullptr;
     pv::RingJob* d_ring_jobs = nullptr;
-    long long ring_blocks = 0;
+    long long ring_blocks = 0, cal_blocks = 0;
+    int store = PV_STORE_F32;
+    std::vector<float*> d_scale;  // u8 rings: per beam [scale rows][offset rows][offset sum]
     pv::DdBatch* dd = nullptr;
     long long* d_step = nullptr;    // steps issued (parity of the host slots)
     pv::BeamStep* d_bs = nullptr;   // per-beam progress
@@ -157,6 +159,8 @@ void destroy(pv_batch* b) {
     for (auto& c : b->chan)
         if (c.d_jobs) cudaFree(c.d_jobs);
     if (b->d_ring_jobs) cudaFree(b->d_ring_jobs);
+    for (float* p : b->d_scale)
+        if (p) cudaFree(p);
     if (b->d_step) cudaFree(b->d_step);
     if (b->d_bs) cudaFree(b->d_bs);
     if (b->d_export) cudaFree(b->d_export);
@@ -233,7 +237,9 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
         return mark(5, sd);
     };
     if (b->pipelined) PV_TRY(dedisperse_branch());
-    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_bs, s));
+    if (b->store == PV_STORE_U8)
+        PV_TRY(pv::ring_calibrate_batch(b->d_ring_jobs, b->n, b->cal_blocks, b->d_bs, s));
+    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_bs, b->store, s));
     PV_TRY(mark(3, s));
     if (b->pipelined) {
         PV_CUDA(cudaEventRecord(b->join_ev, sd), "join");
@@ -279,6 +285,10 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
     b->d_hist.assign(2 * nbeams, nullptr);
     b->mirror.assign(nbeams, pv::BeamStep{});
     b->processed.assign(nbeams, 0);
+    b->store = (flags & PV_BATCH_STORE_U8) ? PV_STORE_U8 : ((flags & PV_BATCH_STORE_F16) ? PV_STORE_F16
+                                                                                         : PV_STORE_F32);
+    b->d_scale.assign(nbeams, nullptr);
+    const int elem = b->store == PV_STORE_F32 ? 4 : (b->store == PV_STORE_F16 ? 2 : 1);
     b->pipelined = (flags & PV_BATCH_PIPELINED) != 0;
     int rc = PV_OK;
     auto fail = [&](int code) {
@@ -290,8 +300,8 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         pv_beam_config c = configs[i];
         c.timing = 0;
         c.debug_taps = 0;
-        if (c.chunk != chunk || c.chunk % 4 != 0) {
-            pv::set_error("pv_batch_create: every beam needs the same chunk, a multiple of 4 spectra "
+        if (c.chunk != chunk || c.chunk % 16 != 0) {
+            pv::set_error("pv_batch_create: every beam needs the same chunk, a multiple of 16 spectra "
                           "(beam %d: %d)", i, c.chunk);
             return fail(PV_ERR_CONFIG);
         }
@@ -303,7 +313,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             return fail(PV_ERR_CONFIG);
         }
         const int extra = (flags & PV_BATCH_PIPELINED) ? 1 : 0;
-        rc = pv::beam_create(&b->beams[i], &c, extra);
+        rc = pv::beam_create(&b->beams[i], &c, extra, elem);
         if (rc != PV_OK) return fail(rc);
         pv_beam* x = b->beams[i];
         pv::BeamStep& m = b->mirror[i];
@@ -319,6 +329,16 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             if (e == cudaSuccess) e = cudaMemset(b->d_hist[2 * i + h], 0, hist);
         }
         if (e == cudaSuccess) e = cudaMemset(x->d_out, 0, sizeof(float) * (size_t)c.tdms * c.chunk);
+        if (e == cudaSuccess && b->store == PV_STORE_U8) {
+            // With zero-DMing the clipper leaves every good spectrum at zero mean and unit RMS
+            // (RFI_Clipper.cpp:507-532), so the rows share the scale 6 sigma / 127 = 6/127 and
+            // offset 0; otherwise both come from the data (scale 0: not calibrated yet).
+            std::vector<float> so(2 * (size_t)x->nbins + 1, 0.0f);
+            if (c.rfi_active && c.zero_dming) std::fill(so.begin(), so.begin() + x->nbins, 6.0f / 127.0f);
+            e = cudaMalloc(&b->d_scale[i], sizeof(float) * so.size());
+            if (e == cudaSuccess)
+                e = cudaMemcpy(b->d_scale[i], so.data(), sizeof(float) * so.size(), cudaMemcpyHostToDevice);
+        }
         if (e != cudaSuccess) {
             pv::set_error("pv_batch_create: beam %d: %s", i, cudaGetErrorString(e));
             return fail(PV_ERR_NOMEM);
@@ -394,9 +414,13 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         std::vector<pv::RingJob> rj(nbeams);
         for (int i = 0; i < nbeams; ++i) {
             pv_beam* x = b->beams[i];
+            float* so = b->d_scale[i];
             rj[i] = pv::RingJob{x->d_ring, x->row_stride, x->ring_len, x->d_fb, chunk, x->cfg.nsub,
-                                x->nchan_fb, x->inverted, b->ring_blocks, i};
+                                x->nchan_fb, x->inverted, b->ring_blocks, i, so,
+                                so ? so + x->nbins : nullptr, so ? so + 2 * x->nbins : nullptr,
+                                b->cal_blocks};
             b->ring_blocks += pv::ring_job_blocks(rj[i]);
+            b->cal_blocks += pv::ring_cal_blocks(rj[i]);
         }
         if (cudaMalloc(&b->d_ring_jobs, sizeof(pv::RingJob) * nbeams) != cudaSuccess ||
             cudaMemcpy(b->d_ring_jobs, rj.data(), sizeof(pv::RingJob) * nbeams, cudaMemcpyHostToDevice) !=
@@ -423,9 +447,11 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             d.nout = chunk;
             d.tdms = tdms;
             d.chunk = chunk;
+            d.scale = b->d_scale[i];
+            d.off_sum = b->d_scale[i] ? b->d_scale[i] + 2 * x->nbins : nullptr;
         }
         const int variant = (flags & PV_BATCH_TUNE) ? -1 : PV_BATCH_VARIANT_OF(flags);
-        rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, s0);
+        rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, b->store, s0);
         if (rc != PV_OK) return fail(rc);
     }
     {
@@ -695,7 +721,9 @@ extern "C" long long pv_batch_footprint(const pv_beam_config* c, int flags) {
     const long long ring_len = (lag + 1 + ((flags & PV_BATCH_PIPELINED) ? 1 : 0)) * c->chunk;
     const long long row_stride = (ring_len + 31) / 32 * 32;
     const long long cap = c->event_capacity > 0 ? c->event_capacity : (1LL << 20);
-    long long bytes = 4LL * nbins * row_stride;                       // ring
+    const long long elem = (flags & PV_BATCH_STORE_U8) ? 1 : ((flags & PV_BATCH_STORE_F16) ? 2 : 4);
+    long long bytes = elem * nbins * row_stride;                      // ring
+    if (flags & PV_BATCH_STORE_U8) bytes += 8LL * nbins + 4;          // row scales and offsets
     bytes += 4LL * c->chunk * nbins;                                   // filterbank
     bytes += 4LL * c->tdms * c->chunk;                                 // dedispersed window
     bytes += (long long)sizeof(pv_event) * cap;                        // events

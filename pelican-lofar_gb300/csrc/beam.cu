@@ -39,8 +39,8 @@ namespace pv {
 
 // pv_beam_create with `extra` more chunks of ring than the delays need (the
 // batch's pipelined mode writes chunk k while window k-lag-1 is read).
-int beam_create(pv_beam** out, const pv_beam_config* c, int extra) {
-    if (!out || !c || extra < 0) return PV_ERR_ARG;
+int beam_create(pv_beam** out, const pv_beam_config* c, int extra, int elem) {
+    if (!out || !c || extra < 0 || (elem != 4 && elem != 2 && elem != 1)) return PV_ERR_ARG;
     *out = nullptr;
     if (c->nsub <= 0 || c->nchan_sub <= 0 || c->int_time <= 0 || c->int_chan <= 0 ||
         c->nchan_sub % c->int_chan != 0 || c->chunk <= 0 || c->tdms <= 0 || c->tsamp <= 0.0) {
@@ -76,14 +76,15 @@ int beam_create(pv_beam** out, const pv_beam_config* c, int extra) {
     auto alloc = [&](void** p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
     };
-    alloc((void**)&b->d_ring, sizeof(float) * b->nbins * (size_t)b->row_stride);
+    alloc((void**)&b->d_ring, (size_t)elem * b->nbins * (size_t)b->row_stride);
     alloc((void**)&b->d_fb, sizeof(float) * (size_t)c->chunk * b->nbins);
     if (c->debug_taps) alloc((void**)&b->d_fb_raw, sizeof(float) * (size_t)c->chunk * b->nbins);
     alloc((void**)&b->d_out, sizeof(float) * (size_t)c->tdms * c->chunk);
     alloc((void**)&b->d_events, sizeof(pv_event) * (size_t)b->cap);
     alloc(&b->d_scratch, scratch + 256);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->h_total, sizeof(long long));
-    if (e == cudaSuccess) e = cudaMemset(b->d_ring, 0, sizeof(float) * b->nbins * (size_t)b->row_stride);
+    if (e == cudaSuccess)
+        e = cudaMemset(b->d_ring, elem == 1 ? 0x80 : 0, (size_t)elem * b->nbins * (size_t)b->row_stride);
     if (e != cudaSuccess) {
         pv::set_error("pv_beam_create: %s (ring of %lld x %lld samples)", cudaGetErrorString(e),
                       (long long)b->nbins, b->row_stride);

@@ -7,16 +7,39 @@
 // pos+t lands at physical column (pos+t) mod ring_len.  The noise-template
 // substitution of DedispersionBuffer.cpp:169 is omitted: the reference's
 // weights are always 1, which makes it the identity.
+#include <cuda_fp16.h>
+
 #include "pv_internal.cuh"
 
 namespace {
 
 constexpr int kTile = 32;
 
+// One stored sample: float, half (round to nearest) or the u8 code
+// q = clamp(rint((v - offset) / scale) + 128, 0, 255) of the row (128 while
+// the row has no scale yet).
+template <int STORE>
+__device__ __forceinline__ void ring_store(float* ring, long long i, float v, const float* scale,
+                                           const float* offset, int row) {
+    if (STORE == PV_STORE_F32) {
+        ring[i] = v;
+    } else if (STORE == PV_STORE_F16) {
+        reinterpret_cast<__half*>(ring)[i] = __float2half_rn(v);
+    } else {
+        const float sc = scale[row];
+        float q = sc > 0.0f ? rintf(__fdiv_rn(__fsub_rn(v, offset[row]), sc)) + 128.0f : 128.0f;
+        q = fminf(fmaxf(q, 0.0f), 255.0f);
+        reinterpret_cast<unsigned char*>(ring)[i] = (unsigned char)(int)q;
+    }
+}
+
+template <int STORE = PV_STORE_F32>
 __device__ __forceinline__ void ring_write_tile(float* __restrict__ ring, long long row_stride,
                                                 long long ring_len, long long pos,
                                                 const float* __restrict__ stokes, int nt, int nsub,
-                                                int npol, int nchan, int inverted, int t0, int b0) {
+                                                int npol, int nchan, int inverted, int t0, int b0,
+                                                const float* scale = nullptr,
+                                                const float* offset = nullptr) {
     __shared__ float tile[kTile][kTile + 1];
     const int nbins = nsub * nchan;
     // read: rows of the tile are samples, columns are bins (coalesced in bins)
@@ -35,7 +58,8 @@ __device__ __forceinline__ void ring_write_tile(float* __restrict__ ring, long l
             const int row = inverted ? nbins - 1 - b : b;
             long long col = pos + t;
             if (ring_len > 0) col %= ring_len;
-            ring[(long long)row * row_stride + col] = tile[threadIdx.x][i];
+            ring_store<STORE>(ring, (long long)row * row_stride + col, tile[threadIdx.x][i], scale, offset,
+                              row);
         }
     }
 }
@@ -49,6 +73,7 @@ __global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride
 
 // The rings of many beams: CTAs are laid out job after job; an active beam's
 // chunk lands at logical position written * nt.
+template <int STORE>
 __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
                                         const pv::BeamStep* __restrict__ bs) {
     int lo = 0, hi = njobs - 1;
@@ -63,8 +88,88 @@ __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, in
     const int local = (int)(blockIdx.x - J.block_begin);
     const int tiles_t = (J.nt + kTile - 1) / kTile;
     const int bt = local / tiles_t, tt = local - bt * tiles_t;
-    ring_write_tile(J.ring, J.row_stride, J.ring_len, B.written * J.nt, J.stokes, J.nt, J.nsub, 1,
-                    J.nchan, J.inverted, tt * kTile, bt * kTile);
+    ring_write_tile<STORE>(J.ring, J.row_stride, J.ring_len, B.written * J.nt, J.stokes, J.nt, J.nsub,
+                           1, J.nchan, J.inverted, tt * kTile, bt * kTile, J.scale, J.offset);
+}
+
+// u8 rings of beams without a clipper: each row's offset (the median of its
+// channel) and scale (6 sigma over 127 codes, sigma = 1.4826 times the median
+// absolute deviation), from up to 1024 evenly spaced samples of the chunk.  A
+// row is calibrated by the first chunk whose deviation is not 0 and keeps its
+// scale and offset; until then its samples are stored as the code 128.  Rows
+// with a scale already (every row of a clipped beam) return at once.  One CTA
+// per channel, bitonic sorts in shared memory.
+constexpr int kCalSamples = 1024;
+
+__device__ void bitonic_sort(float* v) {
+    for (int k = 2; k <= kCalSamples; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < kCalSamples; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const float a = v[i], b = v[l];
+                    if ((a > b) == up) {
+                        v[i] = b;
+                        v[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+}
+
+__global__ void ring_calibrate_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
+                                      const pv::BeamStep* __restrict__ bs) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].cal_begin <= (long long)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const pv::RingJob& J = jobs[lo];
+    if (!bs[J.beam].active) return;
+    const int nbins = J.nsub * J.nchan;
+    const int b = (int)(blockIdx.x - J.cal_begin);
+    const int row = J.inverted ? nbins - 1 - b : b;
+    if (J.scale[row] > 0.0f) return;  // calibrated already
+    __shared__ float v[kCalSamples];
+    const int cnt = min(J.nt, kCalSamples);
+    for (int i = threadIdx.x; i < kCalSamples; i += blockDim.x)
+        v[i] = i < cnt ? J.stokes[(long long)((long long)i * J.nt / cnt) * nbins + b] : INFINITY;
+    __syncthreads();
+    bitonic_sort(v);
+    const float med = v[cnt / 2];
+    __syncthreads();
+    for (int i = threadIdx.x; i < kCalSamples; i += blockDim.x)
+        v[i] = i < cnt ? fabsf(v[i] - med) : INFINITY;
+    __syncthreads();
+    bitonic_sort(v);
+    if (threadIdx.x == 0) {
+        const float mad = v[cnt / 2];
+        if (mad > 0.0f && mad < INFINITY) {
+            J.offset[row] = med;
+            J.scale[row] = 6.0f * 1.4826f * mad / 127.0f;
+        }
+    }
+}
+
+// Sum of each active beam's row offsets (added once per dedispersed output).
+__global__ void offset_sum_kernel(const pv::RingJob* __restrict__ jobs, int njobs,
+                                  const pv::BeamStep* __restrict__ bs) {
+    const pv::RingJob& J = jobs[blockIdx.x];
+    if (!bs[J.beam].active) return;
+    __shared__ float part[256];
+    const int nbins = J.nsub * J.nchan;
+    float a = 0.0f;
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) a += J.offset[i];
+    part[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *J.off_sum = part[0];
 }
 
 }  // namespace
@@ -85,11 +190,25 @@ int ring_job_blocks(const RingJob& j) {
     return ceil_div(j.nt, kTile) * ceil_div(j.nsub * j.nchan, kTile);
 }
 
+int ring_cal_blocks(const RingJob& j) { return j.nsub * j.nchan; }
+
 int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
-                     cudaStream_t s) {
+                     int store, cudaStream_t s) {
     if (nblocks <= 0) return PV_OK;
-    ring_write_batch_kernel<<<(unsigned)nblocks, dim3(kTile, 8), 0, s>>>(d_jobs, njobs, bs);
+    const dim3 grid((unsigned)nblocks), block(kTile, 8);
+    if (store == PV_STORE_F16) ring_write_batch_kernel<PV_STORE_F16><<<grid, block, 0, s>>>(d_jobs, njobs, bs);
+    else if (store == PV_STORE_U8) ring_write_batch_kernel<PV_STORE_U8><<<grid, block, 0, s>>>(d_jobs, njobs, bs);
+    else ring_write_batch_kernel<PV_STORE_F32><<<grid, block, 0, s>>>(d_jobs, njobs, bs);
     return check_launch("ring_write_batch_kernel");
+}
+
+int ring_calibrate_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
+                         cudaStream_t s) {
+    if (nblocks <= 0) return PV_OK;
+    ring_calibrate_kernel<<<(unsigned)nblocks, 256, 0, s>>>(d_jobs, njobs, bs);
+    PV_TRY(check_launch("ring_calibrate_kernel"));
+    offset_sum_kernel<<<njobs, 256, 0, s>>>(d_jobs, njobs, bs);
+    return check_launch("offset_sum_kernel");
 }
 
 }  // namespace pv

@@ -21,6 +21,8 @@
 #include <map>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "pv_internal.cuh"
 
 namespace {
@@ -357,18 +359,55 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
 // dedispersed (window w reads ring columns from w*chunk on).  All waits are
 // bounded as in dedisperse_tma_kernel.
 // ---------------------------------------------------------------------------
-template <int R, int CS, int ST>
+// Packed FP32 pairs (Blackwell add/fma .f32x2): two independent IEEE
+// operations, each rounded as the scalar one.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long v) {
+    float2 f;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(v));
+    return f;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// byte i of w as float (q - 128): 0x4B0000qq is 2^23 + q exactly
+__device__ __forceinline__ float u8_centered(unsigned w, int i) {
+    return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | (unsigned)i)) - 8388736.0f;
+}
+
+// Ring storage of the batched kernel: element bytes and TMA alignment unit.
+template <int STORE>
+struct Store {
+    static constexpr int E = STORE == PV_STORE_F32 ? 4 : (STORE == PV_STORE_F16 ? 2 : 1);
+    static constexpr int AU = 16 / E;  // elements per 16 bytes
+};
+
+template <int R, int CS, int ST, int STORE>
 __global__ void __launch_bounds__(17 * 32, 1)
 dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles,
                         int ntiles, int slot, int* __restrict__ counter,
                         const pv::BeamStep* __restrict__ bs, int* __restrict__ status) {
     constexpr int DMS = 16;
     constexpr int TT = 32 * R;
+    constexpr int E = Store<STORE>::E, AU = Store<STORE>::AU;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* slots = reinterpret_cast<float*>(smem_raw);
-    int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * slot);
+    unsigned char* slots = smem_raw;  // [ST*CS][slot] elements of E bytes
+    int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * slot * E);
     float* meta_k = reinterpret_cast<float*>(meta_off + ST * CS);
-    int* s_first = reinterpret_cast<int*>(meta_k + ST * CS);  // [2*ST], ST used
+    float* meta_sc = meta_k + ST * CS;
+    int* s_first = reinterpret_cast<int*>(meta_sc + ST * CS);  // [2*ST], ST used
     uint64_t* full = reinterpret_cast<uint64_t*>(s_first + 2 * ST);
     uint64_t* empty = full + ST;
 
@@ -424,6 +463,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             const int valid = min(TT, J.nout - tt.t0);
             const long long t_base = (bs[J.beam].window * J.chunk) % J.ring_len;
             const int nst = (J.nchan + CS - 1) / CS;
+            const unsigned char* ring = reinterpret_cast<const unsigned char*>(J.ring);
             for (int st = 0; st < nst; ++st) {
                 const int b = gs % ST;
                 if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, kWaitLimitNs)) {
@@ -440,14 +480,15 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                     const int s0 = pv_shift(k, dv0);
                     const int span = valid + pv_shift(k, dv_last) - s0;
                     const long long g0 = (t_base + tt.t0 + s0) % J.ring_len;
-                    g_al = g0 & ~3LL;
+                    g_al = g0 & ~(long long)(AU - 1);
                     const int base = (int)(g0 - g_al);
-                    const unsigned n = (unsigned)((base + span + 3) & ~3);
+                    const unsigned n = (unsigned)((base + span + AU - 1) & ~(AU - 1));
                     piece1 = (unsigned)min((long long)n, J.ring_len - g_al);
                     piece2 = n - piece1;
-                    bytes = n * 4u;
+                    bytes = n * (unsigned)E;
                     meta_off[b * CS + lane] = s0 - base;
                     meta_k[b * CS + lane] = k;
+                    if (STORE == PV_STORE_U8) meta_sc[b * CS + lane] = J.scale[c];
                 }
                 __threadfence_block();
                 unsigned total = bytes;
@@ -457,10 +498,10 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 if (lane == 0) mbar_arrive_expect_tx(&full[b], total);
                 __syncwarp();
                 if (bytes) {
-                    const float* src = J.ring + (long long)c * J.row_stride;
-                    float* dst = slots + (size_t)(b * CS + lane) * slot;
-                    bulk_g2s(dst, src + g_al, piece1 * 4u, &full[b]);
-                    if (piece2) bulk_g2s(dst + piece1, src, piece2 * 4u, &full[b]);
+                    const unsigned char* src = ring + (long long)c * J.row_stride * E;
+                    unsigned char* dst = slots + (size_t)(b * CS + lane) * slot * E;
+                    bulk_g2s(dst, src + g_al * E, piece1 * (unsigned)E, &full[b]);
+                    if (piece2) bulk_g2s(dst + (size_t)piece1 * E, src, piece2 * (unsigned)E, &full[b]);
                 }
                 ++gs;
             }
@@ -475,6 +516,12 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     }
 
     // ---------------- consumers ----------------
+    // FP32 rows: lane l adds samples l + 32r.  FP16 rows: lane l adds samples
+    // 2l, 2l+1 (+64p) from one 4-byte word, or from two when the row offset is
+    // odd.  u8 rows: lane l adds samples 4l..4l+3 (+128q) from one word, or a
+    // funnel shift of two when the offset is not a multiple of 4; a byte q
+    // stands for (q - 128) * scale + offset of its channel, the offsets of all
+    // channels being added once per output.
     unsigned gs = 0;
     for (;;) {
         const int b0 = gs % ST;
@@ -493,8 +540,11 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
         const int nchan = J.nchan;
         const int nst = (nchan + CS - 1) / CS;
         float acc[R];
+        unsigned long long acc2[R / 2];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = 0.0f;
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r) acc2[r] = 0ull;
         for (int st = 0; st < nst; ++st) {
             const int b = gs % ST;
             if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, kWaitLimitNs)) {
@@ -505,10 +555,45 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 const int c_end = min(CS, nchan - st * CS);
                 for (int j = 0; j < c_end; ++j) {
                     const float k = meta_k[b * CS + j];
-                    const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT);
-                    const float* row = slots + (size_t)(b * CS + j) * slot + off + lane;
+                    const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT - 4);
+                    const unsigned char* rowb = slots + (size_t)(b * CS + j) * slot * E;
+                    if (STORE == PV_STORE_F32) {
+                        const float* row = reinterpret_cast<const float*>(rowb) + off + lane;
 #pragma unroll
-                    for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
+                        for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
+                    } else if (STORE == PV_STORE_F16) {
+                        const unsigned* w = reinterpret_cast<const unsigned*>(rowb);
+                        if ((off & 1) == 0) {
+                            const unsigned* wr = w + (off >> 1) + lane;
+#pragma unroll
+                            for (int p = 0; p < R / 2; ++p) {
+                                const unsigned x = wr[32 * p];
+                                const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&x));
+                                acc2[p] = f2_add(acc2[p], f2_pack(f.x, f.y));
+                            }
+                        } else {
+                            const unsigned* wr = w + ((off - 1) >> 1) + lane;
+#pragma unroll
+                            for (int p = 0; p < R / 2; ++p) {
+                                const unsigned x = __byte_perm(wr[32 * p], wr[32 * p + 1], 0x5432u);
+                                const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&x));
+                                acc2[p] = f2_add(acc2[p], f2_pack(f.x, f.y));
+                            }
+                        }
+                    } else {
+                        const unsigned* wr = reinterpret_cast<const unsigned*>(rowb) + (off >> 2) + lane;
+                        const int m = off & 3;
+                        const float sc = meta_sc[b * CS + j];
+                        const unsigned long long sc2 = f2_pack(sc, sc);
+#pragma unroll
+                        for (int q = 0; q < R / 4; ++q) {
+                            unsigned x = wr[32 * q];
+                            if (m) x = __funnelshift_r(x, wr[32 * q + 1], 8 * m);
+                            acc2[2 * q] = f2_fma(f2_pack(u8_centered(x, 0), u8_centered(x, 1)), sc2, acc2[2 * q]);
+                            acc2[2 * q + 1] =
+                                f2_fma(f2_pack(u8_centered(x, 2), u8_centered(x, 3)), sc2, acc2[2 * q + 1]);
+                        }
+                    }
                 }
             }
             __syncwarp();
@@ -517,10 +602,29 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
         }
         if (active) {
             float* o = J.out + (long long)d * J.out_stride;
+            if (STORE == PV_STORE_F32) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const long long t = tt.t0 + lane + 32 * r;
-                if (t < J.nout) o[t] = acc[r];
+                for (int r = 0; r < R; ++r) {
+                    const long long t = tt.t0 + lane + 32 * r;
+                    if (t < J.nout) o[t] = acc[r];
+                }
+            } else if (STORE == PV_STORE_F16) {
+#pragma unroll
+                for (int p = 0; p < R / 2; ++p) {
+                    const long long t = tt.t0 + 64 * p + 2 * lane;
+                    if (t < J.nout) *reinterpret_cast<float2*>(o + t) = f2_unpack(acc2[p]);
+                }
+            } else {
+                const float os = *J.off_sum;
+#pragma unroll
+                for (int q = 0; q < R / 4; ++q) {
+                    const long long t = tt.t0 + 128 * q + 4 * lane;
+                    if (t < J.nout) {
+                        const float2 a = f2_unpack(acc2[2 * q]), c = f2_unpack(acc2[2 * q + 1]);
+                        *reinterpret_cast<float4*>(o + t) =
+                            make_float4(a.x + os, a.y + os, c.x + os, c.y + os);
+                    }
+                }
             }
         }
     }
@@ -644,15 +748,19 @@ constexpr Variant kVariants[] = {{32, 4, 4}, {32, 2, 4}, {16, 4, 4}, {32, 8, 2}}
 constexpr int kNumVariants = 4;
 constexpr size_t kBatchSmemBudget = 220 * 1024;
 
-size_t batch_smem(const Variant& v, int slot) {
-    return (size_t)4 * v.ST * v.CS * slot + (size_t)8 * v.ST * v.CS + (size_t)8 * v.ST + 16 * v.ST;
+int store_bytes(int store) { return store == PV_STORE_F32 ? 4 : (store == PV_STORE_F16 ? 2 : 1); }
+
+// slots, per-channel offsets, delay constants and scales, tile records, barriers
+size_t batch_smem(const Variant& v, int slot, int store) {
+    return (size_t)store_bytes(store) * v.ST * v.CS * slot + (size_t)12 * v.ST * v.CS + (size_t)8 * v.ST +
+           16 * v.ST;
 }
 
-template <int R, int CS, int ST>
+template <int R, int CS, int ST, int STORE>
 int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem,
                    int grid, int* counter, const pv::BeamStep* bs, int* status, cudaStream_t s,
                    bool set_attr) {
-    auto kern = dedisperse_batch_kernel<R, CS, ST>;
+    auto kern = dedisperse_batch_kernel<R, CS, ST, STORE>;
     if (set_attr) {
         PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "cudaFuncSetAttribute(dedisperse_batch)");
@@ -663,16 +771,20 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
-int launch_batch(int variant, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot,
-                 size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
+int launch_batch(int variant, int store, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles,
+                 int slot, size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
                  cudaStream_t s, bool set_attr) {
-    switch (variant) {
-#define PV_VAR(I, R, CS, ST) \
-    case I: return launch_batch_t<R, CS, ST>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
-        PV_VAR(0, 32, 4, 4)
-        PV_VAR(1, 32, 2, 4)
-        PV_VAR(2, 16, 4, 4)
-        PV_VAR(3, 32, 8, 2)
+    switch (variant * 3 + store) {
+#define PV_VAR(I, R, CS, ST, SS)                                                                 \
+    case I * 3 + SS:                                                                            \
+        return launch_batch_t<R, CS, ST, SS>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, \
+                                             status, s, set_attr);
+#define PV_VARS(I, R, CS, ST) PV_VAR(I, R, CS, ST, 0) PV_VAR(I, R, CS, ST, 1) PV_VAR(I, R, CS, ST, 2)
+        PV_VARS(0, 32, 4, 4)
+        PV_VARS(1, 32, 2, 4)
+        PV_VARS(2, 16, 4, 4)
+        PV_VARS(3, 32, 8, 2)
+#undef PV_VARS
 #undef PV_VAR
     }
     pv::set_error("dedispersion: unknown tile variant %d", variant);
@@ -699,7 +811,7 @@ int spread_bound(float kmax, int tdms, int dms, float start, float step) {
 namespace pv {
 
 struct DdBatch {
-    int variant = 0, slot = 0, grid = 0, ntiles = 0;
+    int variant = 0, slot = 0, grid = 0, ntiles = 0, store = PV_STORE_F32;
     size_t smem = 0;
     DdJob* d_jobs = nullptr;
     DdTile* d_tiles = nullptr;
@@ -727,12 +839,17 @@ struct Shape {
 
 // DM tile heights, slot size and tile list of one variant; false if some beam
 // cannot be tiled (its ring is shorter than a tile span).
-bool build_shape(const Variant& v, const DdBeam* beams, int n, std::vector<std::map<int, int>>& exact,
-                 Shape& out) {
+// A slot holds the span (tile + delay spread), up to one alignment unit in
+// front of it and 16 more elements for the reduced-precision readers.
+bool build_shape(const Variant& v, int store, const DdBeam* beams, int n,
+                 std::vector<std::map<int, int>>& exact, Shape& out) {
     const int TT = 32 * v.R;
-    const size_t fixed = batch_smem(v, 0);
-    const int slot_cap = (int)(((kBatchSmemBudget - fixed) / (4 * (size_t)v.ST * v.CS)) & ~(size_t)3);
-    if (slot_cap < TT + 8) return false;
+    const size_t fixed = batch_smem(v, 0, store);
+    const int E = store_bytes(store);
+    const int pad = 16 / E + 16;
+    const int slot_cap =
+        (int)(((kBatchSmemBudget - fixed) / ((size_t)E * v.ST * v.CS)) & ~(size_t)15);
+    if (slot_cap < TT + pad) return false;
     out.dms.assign(n, 1);
     out.slot = 0;
     for (int i = 0; i < n; ++i) {
@@ -741,21 +858,21 @@ bool build_shape(const Variant& v, const DdBeam* beams, int n, std::vector<std::
         for (int c = 0; c < B.nchan; ++c) kmax = std::max(kmax, B.h_dmshift[c]);
         int dms = 16, sp = 0;
         for (; dms >= 1; --dms) {
-            if (TT + spread_bound(kmax, B.tdms, dms, B.start, B.step) + 8 > slot_cap) continue;
+            if (TT + spread_bound(kmax, B.tdms, dms, B.start, B.step) + pad > slot_cap) continue;
             auto it = exact[i].find(dms);
             if (it == exact[i].end()) {
                 std::vector<float> k(B.h_dmshift, B.h_dmshift + B.nchan);
                 it = exact[i].emplace(dms, delay_spread(k, B.tdms, dms, B.start, B.step)).first;
             }
             sp = it->second;
-            if (TT + sp + 8 <= slot_cap) break;
+            if (TT + sp + pad <= slot_cap) break;
         }
         if (dms < 1) return false;
-        if (B.ring_len < (long long)std::min(TT, B.nout) + sp + 8) return false;
+        if (B.ring_len < (long long)std::min(TT, B.nout) + sp + pad) return false;
         out.dms[i] = dms;
-        out.slot = std::max(out.slot, (TT + sp + 8 + 3) & ~3);
+        out.slot = std::max(out.slot, (TT + sp + pad + 15) & ~15);
     }
-    out.smem = batch_smem(v, out.slot);
+    out.smem = batch_smem(v, out.slot, store);
     // tiles, beams with the most work per tile first, time tiles outer
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
@@ -773,8 +890,8 @@ int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant)
     std::vector<DdJob> jobs(n);
     for (int i = 0; i < n; ++i) {
         const DdBeam& B = beams[i];
-        jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.nchan,
-                        B.nout, B.tdms, B.chunk, sh.dms[i], i, B.start, B.step};
+        jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.scale,
+                        B.off_sum, B.nchan, B.nout, B.tdms, B.chunk, sh.dms[i], i, B.start, B.step};
     }
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_tiles) cudaFree(b->d_tiles);
@@ -793,28 +910,35 @@ int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant)
     b->ntiles = (int)sh.tiles.size();
     b->dms = sh.dms;
     b->grid = std::max(1, std::min(b->ntiles, sm_count()));
-    return launch_batch(variant, nullptr, nullptr, 0, 0, b->smem, 0, nullptr, nullptr, nullptr,
-                        nullptr, true);
+    return launch_batch(variant, b->store, nullptr, nullptr, 0, 0, b->smem, 0, nullptr, nullptr,
+                        nullptr, nullptr, true);
 }
 
 }  // namespace
 
-int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cudaStream_t s) {
+int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, int store, cudaStream_t s) {
     if (!out || !beams || n <= 0) {
         set_error("dedispersion batch: no beams");
         return PV_ERR_ARG;
     }
     for (int i = 0; i < n; ++i) {
         const DdBeam& B = beams[i];
-        if (B.ring_len <= 0 || B.ring_len % 4 != 0 || B.row_stride % 4 != 0 || B.ring_len > B.row_stride ||
+        const int au = 16 / store_bytes(store < 0 || store > 2 ? 0 : store);
+        if (B.ring_len <= 0 || B.ring_len % au != 0 || B.row_stride % au != 0 || B.ring_len > B.row_stride ||
+            (store == PV_STORE_U8 && (!B.scale || !B.off_sum)) || B.nout % 4 != 0 ||
             (reinterpret_cast<uintptr_t>(B.ring) & 15) != 0 || B.nout <= 0 || B.tdms <= 0 ||
             B.nchan <= 0 || B.chunk <= 0) {
-            set_error("dedispersion batch: beam %d needs a 16-byte aligned ring of a multiple of 4 "
-                      "samples", i);
+            set_error("dedispersion batch: beam %d needs a 16-byte aligned ring of a multiple of 16 "
+                      "bytes per row and a window of a multiple of 4 samples", i);
             return PV_ERR_ARG;
         }
     }
+    if (store < PV_STORE_F32 || store > PV_STORE_U8) {
+        set_error("dedispersion batch: unknown storage %d", store);
+        return PV_ERR_ARG;
+    }
     auto* b = new DdBatch;
+    b->store = store;
     std::vector<std::map<int, int>> exact(n);
     int rc = PV_OK;
     if (cudaMalloc(&b->d_counter, sizeof(int)) != cudaSuccess ||
@@ -826,7 +950,7 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
     }
     Shape sh;
     if (variant >= 0) {
-        if (variant >= kNumVariants || !build_shape(kVariants[variant], beams, n, exact, sh)) {
+        if (variant >= kNumVariants || !build_shape(kVariants[variant], store, beams, n, exact, sh)) {
             set_error("dedispersion batch: tile variant %d cannot hold these beams", variant);
             dd_batch_destroy(b);
             return PV_ERR_ARG;
@@ -852,13 +976,13 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
         b->tune_ms.assign(kNumVariants, -1.0f);
         for (int v = 0; v < kNumVariants && rc == PV_OK; ++v) {
             Shape cand;
-            if (!build_shape(kVariants[v], beams, n, exact, cand)) continue;
+            if (!build_shape(kVariants[v], store, beams, n, exact, cand)) continue;
             rc = upload(b, beams, n, cand, v);
             if (rc != PV_OK) break;
             float ms = 0.0f;
             for (int it = 0; it < 3 && rc == PV_OK; ++it) {
                 if (it == 1) cudaEventRecord(e0, s);
-                rc = launch_batch(v, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
+                rc = launch_batch(v, store, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
                                   b->d_counter, d_tstep, b->d_status, s, false);
             }
             if (rc != PV_OK) break;
@@ -889,7 +1013,7 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
             rc = PV_ERR_ARG;
         }
         if (rc == PV_OK) {
-            build_shape(kVariants[best_v], beams, n, exact, sh);
+            build_shape(kVariants[best_v], store, beams, n, exact, sh);
             rc = upload(b, beams, n, sh, best_v);
         }
     }
@@ -902,7 +1026,7 @@ int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cuda
 }
 
 int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s) {
-    return launch_batch(b->variant, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
+    return launch_batch(b->variant, b->store, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
                         b->d_counter, bs, b->d_status, s, false);
 }
 

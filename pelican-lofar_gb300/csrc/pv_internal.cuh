@@ -5,6 +5,11 @@
 
 #include "pv_common.cuh"
 
+// Element type of a batch's delay rings.
+#define PV_STORE_F32 0
+#define PV_STORE_F16 1
+#define PV_STORE_U8 2
+
 namespace pv {
 
 // A batch beam's progress, device-resident.  The planning kernel at the start
@@ -50,9 +55,11 @@ int plan_tables(const pv_dedisp_plan* p, const float** d_dmshift, const float** 
 struct DdBeam {
     float* out;
     long long out_stride;
-    const float* ring;
-    long long row_stride, ring_len;
+    const float* ring;               // elements of the batch's storage type
+    long long row_stride, ring_len;  // in elements
     const float* d_dmshift;
+    const float* scale;              // u8 storage: per-row scale (a byte q is (q-128)*scale+offset)
+    const float* off_sum;            // u8 storage: sum of the rows' offsets
     const float* h_dmshift;
     int nchan, nout, tdms, chunk;
     float start, step;  // trial value = start + d*step, in samples per unit delay constant
@@ -63,6 +70,8 @@ struct DdJob {
     const float* ring;
     long long row_stride, ring_len;
     const float* dmshift;
+    const float* scale;
+    const float* off_sum;
     int nchan, nout, tdms, chunk, dms, beam;
     float start, step;
 };
@@ -70,8 +79,8 @@ struct DdTile {
     int job, d0, t0;
 };
 struct DdBatch;
-// variant < 0 runs the autotuner over the DM x time tile variants
-int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, cudaStream_t s);
+// variant < 0 runs the autotuner over the DM x time tile variants; store: PV_STORE_*
+int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, int store, cudaStream_t s);
 int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s);
 int dd_batch_status(const DdBatch* b, int* h_status);
 int dd_batch_shape(const DdBatch* b, int* h8);
@@ -98,10 +107,20 @@ struct RingJob {
     int nt, nsub, nchan, inverted;
     long long block_begin;  // first CTA of this job
     int beam;               // index into the BeamStep array: written chunks give the position
+    float* scale;           // u8 rings: per-row scale (0 until the row is calibrated)
+    float* offset;          // u8 rings: per-row offset
+    float* off_sum;         // u8 rings: sum of the offsets
+    long long cal_begin;    // first CTA of this job in the calibration launch
 };
 int ring_job_blocks(const RingJob& j);
+int ring_cal_blocks(const RingJob& j);
+// store: PV_STORE_* element type of the rings
 int ring_write_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
-                     cudaStream_t s);
+                     int store, cudaStream_t s);
+// u8 rings: scales and offsets of the rows not calibrated yet, from this
+// step's chunk, and every beam's offset sum
+int ring_calibrate_batch(const RingJob* d_jobs, int njobs, long long nblocks, const BeamStep* bs,
+                         cudaStream_t s);
 
 int ring_write_device(float* ring, long long row_stride, long long ring_len, long long pos,
                       const float* stokes, int nt, int nsub, int npol, int nchan, int inverted,
@@ -115,7 +134,8 @@ int analyse_launch(const float* data, long long ld, int tdms, int nsamp, float t
 }  // namespace pv
 
 namespace pv {
-int beam_create(pv_beam** out, const pv_beam_config* c, int extra_ring_chunks);
+// elem_bytes: 4 (float rings), 2 (half) or 1 (u8, cleared to the code 128)
+int beam_create(pv_beam** out, const pv_beam_config* c, int extra_ring_chunks, int elem_bytes = 4);
 }
 
 // One beam's device-resident chain state (beam.cu); the batch engine reuses it.

@@ -418,12 +418,13 @@ class Beam:
 
 
 BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
+BATCH_STORE = {"f32": 0, "f16": 16, "u8": 32}
 HOST_EVENTS = 65536  # PV_BATCH_HOST_EVENTS
 
 
-def batch_footprint(cfg, pipelined=True):
+def batch_footprint(cfg, pipelined=True, store="f32"):
     """Device bytes of one beam of this configuration in a batch."""
-    n = load().pv_batch_footprint(C.byref(cfg), BATCH_PIPELINED if pipelined else 0)
+    n = load().pv_batch_footprint(C.byref(cfg), (BATCH_PIPELINED if pipelined else 0) | BATCH_STORE[store])
     if n < 0:
         check(int(n))
     return int(n)
@@ -432,12 +433,13 @@ def batch_footprint(cfg, pipelined=True):
 class Batch:
     """Many beams advanced one chunk per step by batched launches (pv_batch)."""
 
-    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0, pipelined=False):
+    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0, pipelined=False, store="f32"):
         self.cfgs = list(cfgs)
         self.pipelined = pipelined
+        self.store = store
         self._arr = (BeamConfig * len(self.cfgs))(*self.cfgs)
         flags = (BATCH_TUNE if tune else (variant << 8)) | (BATCH_GRAPH if graph else 0) | \
-            (BATCH_TIMING if timing else 0) | (BATCH_PIPELINED if pipelined else 0)
+            (BATCH_TIMING if timing else 0) | (BATCH_PIPELINED if pipelined else 0) | BATCH_STORE[store]
         self.h = C.c_void_p()
         check(load().pv_batch_create(C.byref(self.h), self._arr, len(self.cfgs), flags))
 
