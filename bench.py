@@ -418,7 +418,7 @@ def run_batch(args, cfgs, workload):
 
     # ---------------- batched engine ----------------
     batch = pv.Batch([pv_config(pv, c, prefilled=1) for c in cfgs], tune=True, graph=True, timing=True,
-                     pipelined=True)
+                     pipelined=True, store=args.store)
     for i, c in enumerate(cfgs):
         v = device_voltages(c, dev, seed(i))
         batch.set_input(i, v, stream=stream)
@@ -476,6 +476,15 @@ def run_batch(args, cfgs, workload):
     d2h = e2e_run(args.steps)
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3
+    in_bytes = sum(batch.input(i)[1] for i in range(nb))
+    ring_gb = sum(x["ring_bytes"] for x in infos) / 1e9
+    precision = None
+    if args.store != "f32":
+        del batch
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        few = sorted(range(nb), key=lambda i: cfgs[i]["dm_max"] * cfgs[i]["nsub"])[:PRECISION_BEAMS]
+        precision = precision_check(pv, [cfgs[i] for i in few], args.store, dev, seed(0))
 
     t = torch.tensor([ms, e2e_ms, plain_ms, plain_e2e_ms], device=dev)
     if world > 1:
@@ -492,7 +501,6 @@ def run_batch(args, cfgs, workload):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     st = {k: float(np.mean([x[k] for x in stage])) for k in stage[0]}
     achieved = units_step / (st["dedisperse"] / 1e3)
-    in_bytes = sum(batch.input(i)[1] for i in range(nb))
     fb_bytes = sum(c["chunk"] * c["nsub"] * c["nchan_sub"] * 4 for c in cfgs)
     chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
     roofline = {"kernel": "dedisperse_batch_kernel", "bound": "fp32",
@@ -513,7 +521,6 @@ def run_batch(args, cfgs, workload):
                                  % (in_bytes, fb_bytes),
                      "kernel_ms": st["channelise"], "peak_source": peak_src}
     chunk_s = [c["chunk"] * c["tsamp"] for c in cfgs]
-    ring_gb = sum(x["ring_bytes"] for x in infos) / 1e9
     cpu = cpu_baseline_mix(cfgs) if (rank == 0 and not args.no_cpu) else None
     line = {"metric": "DM-trial*chan*samples/s", "value": value, "unit": "DM-trial*chan*samples/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -524,6 +531,7 @@ def run_batch(args, cfgs, workload):
             "config": {"workload": workload, "beams": nb, "chunk": cfgs[0]["chunk"],
                        "nchan_total": sum(c["nsub"] * c["nchan_sub"] for c in cfgs),
                        "tdms_total": sum(c["tdms"] for c in cfgs), "ring_gb": ring_gb,
+                       "ring_storage": args.store,
                        "input_gb_per_step": in_bytes / 1e9, "seed": 64,
                        "l2": "inputs larger than L2 (%.0f GB voltages per step, %.0f GB rings)"
                              % (in_bytes / 1e9, ring_gb),
@@ -550,10 +558,53 @@ def run_batch(args, cfgs, workload):
                            "chunk_duration_max": max(chunk_s) * 1e3},
             "events_last_step": n_events,
             "cpu_baseline": cpu}
+    if precision is not None:
+        line["precision"] = precision
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+PRECISION_BEAMS = 6
+
+
+def precision_check(pv, cfgs, store, dev, seed):
+    """The reduced-precision rings against FP32 on a few beams of the workload
+    (the smallest delay spans, so that windows complete within a few steps):
+    both batches start from silence and take identical voltages; the last
+    window's dedispersed power is compared (relative rms) and the events by
+    (DM, sample, binning) key (Jaccard index)."""
+    import torch
+    runs = {st: pv.Batch([pv_config(pv, c) for c in cfgs], tune=False, graph=True, variant=3, store=st)
+            for st in ("f32", store)}
+    steps = max(runs["f32"].info(i)["lag"] for i in range(len(cfgs))) + 2
+    for k in range(steps):
+        for i, c in enumerate(cfgs):
+            v = device_voltages(c, dev, seed + 7919 * k + i)
+            for b in runs.values():
+                b.set_input(i, v)
+            del v
+        for b in runs.values():
+            b.run()
+        torch.cuda.synchronize()
+    errs, inter, union = [], 0, 0
+    for i, c in enumerate(cfgs):
+        outs, keys = [], []
+        for b in (runs["f32"], runs[store]):
+            outs.append(pv.device_array(b.buffers(i)[1], (c["tdms"], c["chunk"])).double().cpu().numpy())
+            ev, _, _ = b.events(i)
+            keys.append(set(zip(ev["dm"].tolist(), ev["t"].tolist(), ev["bin_factor"].tolist())))
+        errs.append(float(np.sqrt(np.mean((outs[1] - outs[0]) ** 2) / np.mean(outs[0] ** 2))))
+        inter += len(keys[0] & keys[1])
+        union += len(keys[0] | keys[1])
+    del runs
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return {"beams": len(cfgs), "steps": steps, "windows_compared": len(cfgs),
+            "rel_rms_vs_f32_max": max(errs), "rel_rms_vs_f32_mean": float(np.mean(errs)),
+            "event_jaccard": inter / union if union else None, "events_union": union,
+            "fp32_vs_fp64": "within 1e-5 relative rms (parity tests)"}
 
 
 def serve_beams(nbeams=128, seed=128):
@@ -782,6 +833,8 @@ def main():
     ap.add_argument("--grace", type=float, default=30.0, help="serve128: seconds to drain")
     ap.add_argument("--budget-gb", type=float, default=160.0, help="serve128: HBM budget")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
+                    help="batch64: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
@@ -813,6 +866,8 @@ def main():
     args.beams = args.beams or 64
     cfgs = batch_configs(args.beams, chunk=args.chunk or 4096)
     workload = "batch%d-mixed-beams-4096samp" % args.beams
+    if args.store != "f32":
+        workload += "-%s-rings" % args.store
     if args.beams != 64 or args.chunk:
         workload += "-reduced(beams=%d,chunk=%d)" % (args.beams, cfgs[0]["chunk"])
     if args.impl == "reference":

@@ -368,10 +368,9 @@ typedef struct pv_batch pv_batch;
                                  offset: the sample is (q - 128) * scale + offset, scale = 6 sigma
                                  / 127.  With the clipper and zero-DMing its output has zero
                                  mean and unit RMS: sigma = 1, offset 0.  Otherwise the offset is
-                                 the median and
-                                 sigma the median absolute deviation x 1.4826 of the first
-                                 chunk in which the channel varies (until then the channel's
-                                 samples are stored as its offset) */
+                                 the median and sigma the median absolute deviation x 1.4826 of
+                                 the first chunk in which the channel varies (until then the
+                                 channel's samples are stored as its offset) */
 #define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
@@ -424,6 +423,39 @@ int pv_batch_step_done(const pv_batch* batch, long long step);
  * `flags` (ring, input buffers, filterbank, window, events, scratch): the
  * admission cost of a serving loop under an HBM budget. */
 long long pv_batch_footprint(const pv_beam_config* config, int flags);
+
+/* ---- LOFAR UDP ingest (AdapterTimeSeriesDataSet) -------------------------
+ * Replaces AdapterTimeSeriesDataSet::deserialise/_checkData/_readData
+ * (lib/src/AdapterTimeSeriesDataSet.cpp:78-282).  Fields are the adapter's
+ * XML options (:37-45).  A chunk is packets_per_chunk packets of a 16-byte
+ * header (lib/LofarUdpHeader.h:25-35) and subband-major data
+ * [subband][time][pol] of complex int8 or int16, padded to 8148 bytes when
+ * fixed_size_packets. */
+typedef struct {
+    int fixed_size_packets; /* <fixedSizePackets value="true"/> */
+    int sample_bits;        /* <dataBitSize value="16"/>: 8 or 16 */
+    int packets_per_chunk;  /* <udpPacketsPerIteration value=.../> */
+    int samples_per_packet; /* <samplesPerPacket value="16"/> */
+    int nchan;              /* <outputChannelsPerSubband value=.../>: samples per time block */
+    int nsub;               /* <subbandsPerPacket value=.../> */
+    int npol;               /* <nRawPolarisations value="2"/> (16-bit data: 2) */
+    int clock_mhz;          /* <clock value="200"/> */
+} pv_udp_config;
+#define PV_UDP_OUT_C32 0 /* complex float [sub][pol][block][nchan]: TimeSeriesDataSetC32 */
+#define PV_UDP_OUT_I16 1 /* complex int16, same order: the station format pv_channelise,
+                            pv_beam_process and pv_batch take with in_int16 = 1 */
+/* _checkData (AdapterTimeSeriesDataSet.cpp:159-199): packet bytes and time
+ * blocks of a chunk of chunk_bytes; PV_ERR_CONFIG with the reference's message. */
+int pv_udp_check(const pv_udp_config* config, long long chunk_bytes, long long* h_packet_bytes,
+                 int* h_nblocks);
+/* _readData (:209-282) for every packet of the device chunk, into d_out
+ * (nsub*npol*packets*samples complex elements of out_type). */
+int pv_udp_unpack(const pv_udp_config* config, const void* d_chunk, long long chunk_bytes,
+                  void* d_out, int out_type, void* stream);
+/* The chunk's LOFAR time stamp (seconds) and block rate (seconds per sample)
+ * from its first packet's header (:107-118). */
+int pv_udp_time(const pv_udp_config* config, const void* h_packet, double* h_timestamp,
+                double* h_block_rate);
 
 #ifdef __cplusplus
 }

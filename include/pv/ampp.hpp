@@ -5,6 +5,7 @@
 // modules, so pipeline code written against them compiles against this
 // header instead:
 //
+//   AdapterTimeSeriesDataSet::config(), deserialise()                         lib/AdapterTimeSeriesDataSet.h
 //   PPFChanneliser::run(const TimeSeriesDataSetC32*, SpectrumDataSetC32*)      lib/PPFChanneliser.h:68-69
 //   StokesGenerator::run(const SpectrumDataSetC32*, SpectrumDataSetStokes*)   lib/StokesGenerator.h:42-43
 //   StokesIntegrator::run(const SpectrumDataSetStokes*, SpectrumDataSetStokes*) lib/StokesIntegrator.h:46
@@ -31,6 +32,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <iostream>
 #include <complex>
 #include <cstring>
 #include <fstream>
@@ -376,6 +378,56 @@ class DedispersionDataAnalysis : public DataBlob {
 // ---------------------------------------------------------------------------
 // Modules
 // ---------------------------------------------------------------------------
+
+// lib/src/AdapterTimeSeriesDataSet.cpp:36-282.  The reference reads one
+// chunk of UDP packets from a QIODevice; deserialise() takes the same bytes
+// from host memory, unpacks them on the GPU and fills the blob given to
+// config(), with the first packet's time stamp and block rate.
+class AdapterTimeSeriesDataSet {
+  public:
+    explicit AdapterTimeSeriesDataSet(const ConfigNode& config) {
+        c_.fixed_size_packets = lower(config.getOption("fixedSizePackets", "value", "true")).rfind("true", 0) == 0;
+        c_.sample_bits = (int)to_uint(config.getOption("dataBitSize", "value", "0"));
+        c_.packets_per_chunk = (int)to_uint(config.getOption("udpPacketsPerIteration", "value", "0"));
+        c_.samples_per_packet = (int)to_uint(config.getOption("samplesPerPacket", "value", "0"));
+        c_.nchan = (int)to_uint(config.getOption("outputChannelsPerSubband", "value", "0"));
+        c_.nsub = (int)to_uint(config.getOption("subbandsPerPacket", "value", "0"));
+        c_.npol = (int)to_uint(config.getOption("nRawPolarisations", "value", "0"));
+        c_.clock_mhz = (int)to_uint(config.getOption("clock", "value", "200"));
+    }
+    // AbstractStreamAdapter::config: the blob to fill and the chunk's bytes.
+    void config(TimeSeriesDataSetC32* data, size_t chunkSize) {
+        data_ = data;
+        chunk_ = chunkSize;
+    }
+    void deserialise(const void* chunk) {
+        long long psize = 0;
+        int nblocks = 0;
+        pv_check(pv_udp_check(&c_, (long long)chunk_, &psize, &nblocks));
+        if (!data_) throw std::runtime_error("AdapterTimeSeriesDataSet: Cannot deserialise into an unallocated blob!.");
+        data_->resize((unsigned)nblocks, (unsigned)c_.nsub, (unsigned)c_.npol, (unsigned)c_.nchan);
+        const size_t n = (size_t)nblocks * c_.nsub * c_.npol * c_.nchan;
+        void* d_in = din_.get(chunk_);
+        void* d_out = dout_.get(8 * n);
+        pv_check(pv_device_copy(d_in, chunk, (long long)chunk_, nullptr));
+        pv_check(pv_udp_unpack(&c_, d_in, (long long)chunk_, d_out, PV_UDP_OUT_C32, nullptr));
+        pv_check(pv_device_copy(data_->data(), d_out, (long long)(8 * n), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        double ts = 0.0, rate = 0.0;
+        pv_check(pv_udp_time(&c_, chunk, &ts, &rate));
+        data_->setLofarTimestamp(ts);
+        data_->setBlockRate(rate);
+        if (ts - last_ > rate) std::cout << "Adapter: data out of sequence -- " << ts - last_ << std::endl;
+        last_ = ts + (double)nblocks * c_.nchan * rate;  // TimeSeriesDataSet::getEndLofarTimestamp
+    }
+
+  private:
+    pv_udp_config c_{};
+    TimeSeriesDataSetC32* data_ = nullptr;
+    size_t chunk_ = 0;
+    double last_ = 0.0;
+    DeviceBuffer din_, dout_;
+};
 
 // lib/src/PPFChanneliser.cpp:29-290
 class PPFChanneliser {

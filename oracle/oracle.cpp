@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
@@ -1206,3 +1207,82 @@ extern "C" void or_ddmod_params(const or_ddmod* m, int* maxshift, int* remaining
 }
 
 extern "C" int or_num_threads(void) { return threads_or_default(0); }
+
+// ===========================================================================
+// F1 LOFAR UDP packets -> TimeSeriesDataSetC32 (AdapterTimeSeriesDataSet)
+// ===========================================================================
+// A packet is the 16-byte header (LofarUdpHeader.h:25-35: version u8,
+// sourceInfo u8, configuration u16, station u16, nrBeamlets u8, nrBlocks u8,
+// timestamp u32, blockSequenceNumber u32; little endian), the data and, for
+// fixed-size packets, padding up to sizeof(UDPPacket) = 8148 bytes (16 + 8130
+// rounded to the struct's 4-byte alignment).
+
+// AdapterTimeSeriesDataSet::_checkData (AdapterTimeSeriesDataSet.cpp:159-199).
+// Returns 0, or the number of the first failing check: 1 sample bits, 2 chunk
+// size, 3 data larger than a packet, 4 time samples not a multiple of the
+// block length.  packet_bytes and nblocks are written when the check passes.
+extern "C" int or_udp_check(int fixed, int bits, int npackets, int spp, int nchan, int nsub,
+                            int npol, long long chunk_bytes, long long* packet_bytes, int* nblocks) {
+    if (bits != 8 && bits != 16) return 1;
+    const long long samples = (long long)nsub * npol * spp;
+    const long long useful_bits = samples * bits * 2;
+    const long long useful_bytes = useful_bits / 8;
+    const long long psize = fixed ? 8148 : 16 + useful_bytes;
+    const long long udp_bits = fixed ? 8130LL * 8 : useful_bits;
+    if (chunk_bytes != psize * npackets) return 2;
+    if (useful_bits > udp_bits) return 3;
+    const long long times = (long long)spp * npackets;
+    if (nchan <= 0 || times % nchan != 0) return 4;
+    if (packet_bytes) *packet_bytes = psize;
+    if (nblocks) *nblocks = (int)(times / nchan);
+    return 0;
+}
+
+// AdapterTimeSeriesDataSet::_readData (AdapterTimeSeriesDataSet.cpp:209-282):
+// each packet's data is read in the order subband, time, polarisation, one
+// complex int8 or int16 per (s, t, p); time t of packet k is sample
+// k*spp + t of the series [s][p] (TimeSeriesDataSet.h:145-151 with blocks of
+// nchan samples: the series is contiguous in time).  The 16-bit reader reads
+// two polarisations per time (:240-258), so 16-bit data needs npol == 2.
+extern "C" int or_udp_unpack(const unsigned char* chunk, long long packet_bytes, int npackets,
+                             int bits, int nsub, int npol, int spp, float* out) {
+    if (bits == 16 && npol != 2) return 1;
+    const long long nt = (long long)npackets * spp;
+    for (int k = 0; k < npackets; ++k) {
+        const unsigned char* d = chunk + (long long)k * packet_bytes + 16;
+        long long ip = 0;
+        for (int s = 0; s < nsub; ++s)
+            for (int t = 0; t < spp; ++t)
+                for (int p = 0; p < npol; ++p) {
+                    float re, im;
+                    if (bits == 8) {
+                        re = (float)(signed char)d[ip];
+                        im = (float)(signed char)d[ip + 1];
+                        ip += 2;
+                    } else {
+                        int16_t v[2];
+                        std::memcpy(v, d + ip, 4);
+                        re = (float)v[0];
+                        im = (float)v[1];
+                        ip += 4;
+                    }
+                    float* o = out + 2 * (((long long)s * npol + p) * nt + (long long)k * spp + t);
+                    o[0] = re;
+                    o[1] = im;
+                }
+    }
+    return 0;
+}
+
+// The chunk's time stamp from its first packet (AdapterTimeSeriesDataSet.cpp:
+// 107-118): blocks per second are 156250 at the 160 MHz clock, else 195313 in
+// even seconds and 195312 in odd ones.
+extern "C" void or_udp_time(const unsigned char* header, int clock_mhz, double* timestamp,
+                            double* block_rate) {
+    uint32_t ts, seq;
+    std::memcpy(&ts, header + 8, 4);
+    std::memcpy(&seq, header + 12, 4);
+    const unsigned tot = clock_mhz == 160 ? 156250u : (ts % 2 == 0 ? 195313u : 195312u);
+    *timestamp = ts + (1.0 * seq) / tot;
+    *block_rate = 1.0 / tot;
+}

@@ -169,6 +169,15 @@ void or_ddmod_params(const or_ddmod*, int* maxshift, int* remaining, int* nout,
 /* ---- Timing helper for the CPU baseline --------------------------------- */
 int or_num_threads(void);
 
+/* ---- F1 LOFAR UDP packets (AdapterTimeSeriesDataSet) --------------------- */
+int or_udp_check(int fixed, int bits, int npackets, int spp, int nchan, int nsub, int npol,
+                 long long chunk_bytes, long long* packet_bytes, int* nblocks);
+/* out: complex float [nsub][npol][npackets*spp] */
+int or_udp_unpack(const unsigned char* chunk, long long packet_bytes, int npackets, int bits,
+                  int nsub, int npol, int spp, float* out);
+void or_udp_time(const unsigned char* header, int clock_mhz, double* timestamp,
+                 double* block_rate);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,9 @@ def lib():
             "or_ddmod_pop": (i, [vp, P(C.c_float), ll, P(ll)]),
             "or_ddmod_params": (None, [vp, P(i), P(i), P(i), P(i), P(i)]),
             "or_num_threads": (i, []),
+            "or_udp_check": (i, [i, i, i, i, i, i, i, ll, P(ll), P(i)]),
+            "or_udp_unpack": (i, [vp, ll, i, i, i, i, i, P(C.c_float)]),
+            "or_udp_time": (None, [vp, i, P(C.c_double), P(C.c_double)]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -292,3 +295,34 @@ def rfi_parts(nbins):
 
 def num_threads():
     return lib().or_num_threads()
+
+
+# --------------------------------------------------------------------------
+# F1 LOFAR UDP packets
+# --------------------------------------------------------------------------
+
+def udp_check(fixed, bits, npackets, spp, nchan, nsub, npol, chunk_bytes):
+    """(code, packet_bytes, nblocks); code 0 when AdapterTimeSeriesDataSet's checks pass."""
+    pb, nb = C.c_longlong(0), C.c_int(0)
+    rc = lib().or_udp_check(int(fixed), bits, npackets, spp, nchan, nsub, npol, chunk_bytes,
+                            C.byref(pb), C.byref(nb))
+    return rc, pb.value, nb.value
+
+
+def udp_unpack(chunk, packet_bytes, npackets, bits, nsub, npol, spp):
+    """complex64 [nsub][npol][npackets*spp] from a chunk of packets (bytes or uint8 array)."""
+    buf = np.frombuffer(chunk, np.uint8) if not isinstance(chunk, np.ndarray) else chunk
+    buf = np.ascontiguousarray(buf, np.uint8)
+    out = np.zeros((nsub, npol, npackets * spp), np.complex64)
+    rc = lib().or_udp_unpack(buf.ctypes.data, packet_bytes, npackets, bits, nsub, npol, spp,
+                             out.ctypes.data_as(C.POINTER(C.c_float)))
+    if rc:
+        raise ValueError("16-bit packets carry two polarisations")
+    return out
+
+
+def udp_time(packet, clock_mhz=200):
+    buf = np.ascontiguousarray(np.frombuffer(bytes(packet[:16]), np.uint8))
+    ts, rate = C.c_double(0), C.c_double(0)
+    lib().or_udp_time(buf.ctypes.data, clock_mhz, C.byref(ts), C.byref(rate))
+    return ts.value, rate.value

@@ -137,6 +137,9 @@ struct pv_batch {
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     cudaStream_t rfi_side[3] = {};   // pipelined: one stream per clipper class after the first
     cudaEvent_t rfi_join[3] = {};
+    cudaEvent_t rfi_tail[3] = {};    // pipelined: end of the dedispersion helper after each class
+    cudaStream_t branch_a = nullptr; // pipelined: clippers and ring write (high priority)
+    cudaEvent_t join_a = nullptr;
 };
 
 namespace {
@@ -149,8 +152,11 @@ void destroy(pv_batch* b) {
     for (int i = 0; i < 3; ++i) {
         if (b->rfi_side[i]) cudaStreamDestroy(b->rfi_side[i]);
         if (b->rfi_join[i]) cudaEventDestroy(b->rfi_join[i]);
+        if (b->rfi_tail[i]) cudaEventDestroy(b->rfi_tail[i]);
     }
     if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    if (b->branch_a) cudaStreamDestroy(b->branch_a);
+    if (b->join_a) cudaEventDestroy(b->join_a);
     if (b->join_ev) cudaEventDestroy(b->join_ev);
     for (auto e : b->ev)
         if (e) cudaEventDestroy(e);
@@ -180,11 +186,12 @@ void destroy(pv_batch* b) {
 }
 
 // Issues one step of every beam on stream s.  Pipelined, the channeliser
-// runs first on the whole GPU; then the clippers are launched, and only then
-// the dedispersion branch on the side stream, so that the clippers' CTAs are
-// resident before the persistent dedispersion CTAs take the remaining SMs
-// (and the SMs of every clipper that finishes).  The side stream joins s
-// before the step counter advances.
+// runs first on the whole GPU.  Then the clippers (one CTA, one SM, per beam)
+// run on high-priority streams beside a persistent dedispersion launch with
+// one CTA for each SM they leave free; as each clipper class ends, a
+// dedispersion launch of as many CTAs joins the same tile queue on its
+// stream, so no SM idles and a dedispersion CTA never holds an SM a clipper
+// needs.  Both branches join s before the step counter advances.
 int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     const bool timing = (b->flags & PV_BATCH_TIMING) != 0;
     auto mark = [&](int i, cudaStream_t st) -> int {
@@ -193,35 +200,50 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
                                        : cudaEventRecord(b->ev[i], st),
                                "record stage event");
     };
-    cudaStream_t sd = b->pipelined ? b->side : s;  // stream of the dedispersion branch
+    cudaStream_t sd = b->pipelined ? b->side : s;      // dedispersion branch (low priority)
+    cudaStream_t sa = b->pipelined ? b->branch_a : s;  // clippers and ring write (high priority)
     plan_kernel<<<1, 256, 0, s>>>(b->d_bs, b->n, b->d_step, b->h_mask, b->pipelined ? 1 : 0);
     PV_TRY(pv::check_launch("plan_kernel"));
     PV_TRY(mark(0, s));
     for (auto& c : b->chan)
         PV_TRY(pv::launch_chan_fast(c.nchan, 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps, b->d_bs, s));
     PV_TRY(mark(1, s));
+    const int nk = b->rfi ? pv::rfi_batch_launches(b->rfi) : 0;
+    int rfi_ctas = 0;
+    for (int k = 0; k < nk; ++k) rfi_ctas += pv::rfi_batch_ctas(b->rfi, k);
     if (b->pipelined) {
+        PV_TRY(pv::dd_batch_reset(b->dd, s));  // one tile queue for every dedispersion launch
         PV_CUDA(cudaEventRecord(b->fork_ev, s), "fork");
+        PV_CUDA(cudaStreamWaitEvent(sa, b->fork_ev, 0), "fork");
         PV_CUDA(cudaStreamWaitEvent(sd, b->fork_ev, 0), "fork");
     }
     if (b->rfi && b->pipelined) {
-        // every clipper class resident at once: class 0 on s, the others on
-        // their own streams, joined back before the ring write
-        const int nk = pv::rfi_batch_launches(b->rfi);
+        // every clipper class resident at once (class 0 on branch A, the
+        // others on their own streams); as a class finishes, a dedispersion
+        // launch of as many CTAs takes its SMs and joins the tile queue
         for (int k = 1; k < nk; ++k) {
-            PV_CUDA(cudaStreamWaitEvent(b->rfi_side[k - 1], b->fork_ev, 0), "fork clipper");
-            PV_TRY(pv::rfi_batch_launch_one(b->rfi, k, b->rfi_side[k - 1]));
-            PV_CUDA(cudaEventRecord(b->rfi_join[k - 1], b->rfi_side[k - 1]), "join clipper");
+            cudaStream_t sk = b->rfi_side[k - 1];
+            PV_CUDA(cudaStreamWaitEvent(sk, b->fork_ev, 0), "fork clipper");
+            PV_TRY(pv::rfi_batch_launch_one(b->rfi, k, sk));
+            PV_CUDA(cudaEventRecord(b->rfi_join[k - 1], sk), "join clipper");
+            PV_TRY(pv::dd_batch_launch_shared(b->dd, b->d_bs, pv::rfi_batch_ctas(b->rfi, k), sk));
+            PV_CUDA(cudaEventRecord(b->rfi_tail[k - 1], sk), "join helper");
         }
-        if (nk > 0) PV_TRY(pv::rfi_batch_launch_one(b->rfi, 0, s));
-        for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(s, b->rfi_join[k - 1], 0), "join clipper");
+        if (nk > 0) PV_TRY(pv::rfi_batch_launch_one(b->rfi, 0, sa));
+        for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(sa, b->rfi_join[k - 1], 0), "join clipper");
     } else if (b->rfi) {
         PV_TRY(pv::rfi_batch_launch(b->rfi, s));
     }
-    PV_TRY(mark(2, s));
+    PV_TRY(mark(2, sa));
     auto dedisperse_branch = [&]() -> int {
         PV_TRY(mark(6, sd));
-        PV_TRY(pv::dd_batch_launch(b->dd, b->d_bs, sd));
+        if (b->pipelined) {
+            // the SMs the clippers leave free; the clippers' SMs join later
+            const int free_sms = std::max(8, pv::sm_count() - rfi_ctas);
+            PV_TRY(pv::dd_batch_launch_shared(b->dd, b->d_bs, std::min(free_sms, pv::dd_batch_grid(b->dd)), sd));
+        } else {
+            PV_TRY(pv::dd_batch_launch(b->dd, b->d_bs, sd));
+        }
         PV_TRY(mark(4, sd));
         for (int i = 0; i < b->n; ++i) {
             pv_beam* x = b->beams[i];
@@ -238,12 +260,16 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     };
     if (b->pipelined) PV_TRY(dedisperse_branch());
     if (b->store == PV_STORE_U8)
-        PV_TRY(pv::ring_calibrate_batch(b->d_ring_jobs, b->n, b->cal_blocks, b->d_bs, s));
-    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_bs, b->store, s));
-    PV_TRY(mark(3, s));
+        PV_TRY(pv::ring_calibrate_batch(b->d_ring_jobs, b->n, b->cal_blocks, b->d_bs, sa));
+    PV_TRY(pv::ring_write_batch(b->d_ring_jobs, b->n, b->ring_blocks, b->d_bs, b->store, sa));
+    PV_TRY(mark(3, sa));
     if (b->pipelined) {
+        if (nk > 0) PV_TRY(pv::dd_batch_launch_shared(b->dd, b->d_bs, pv::rfi_batch_ctas(b->rfi, 0), sa));
+        PV_CUDA(cudaEventRecord(b->join_a, sa), "join");
         PV_CUDA(cudaEventRecord(b->join_ev, sd), "join");
+        PV_CUDA(cudaStreamWaitEvent(s, b->join_a, 0), "join");
         PV_CUDA(cudaStreamWaitEvent(s, b->join_ev, 0), "join");
+        for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(s, b->rfi_tail[k - 1], 0), "join helper");
     } else {
         PV_TRY(dedisperse_branch());
     }
@@ -449,6 +475,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             d.chunk = chunk;
             d.scale = b->d_scale[i];
             d.off_sum = b->d_scale[i] ? b->d_scale[i] + 2 * x->nbins : nullptr;
+            d.uniform = (b->store == PV_STORE_U8 && x->cfg.rfi_active && x->cfg.zero_dming) ? 1 : 0;
         }
         const int variant = (flags & PV_BATCH_TUNE) ? -1 : PV_BATCH_VARIANT_OF(flags);
         rc = pv::dd_batch_create(&b->dd, db.data(), nbeams, variant, b->store, s0);
@@ -482,16 +509,23 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         b->h_mask = reinterpret_cast<int*>(h + 2 * counts);
         b->h_status = reinterpret_cast<int*>(h + 2 * counts + ((masks + 15) & ~(size_t)15));
         b->h_events = reinterpret_cast<pv_event*>(h + head);
+        int lowest = 0, highest = 0;
         if (cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaDeviceGetStreamPriorityRange(&lowest, &highest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, lowest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->branch_a, cudaStreamNonBlocking, highest) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&b->rfi_side[0], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&b->rfi_side[1], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&b->rfi_side[2], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join_a, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->rfi_side[0], cudaStreamNonBlocking, highest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->rfi_side[1], cudaStreamNonBlocking, highest) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->rfi_side[2], cudaStreamNonBlocking, highest) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->rfi_join[0], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->rfi_join[1], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_join[2], cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&b->rfi_join[2], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_tail[0], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_tail[1], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->rfi_tail[2], cudaEventDisableTiming) != cudaSuccess) {
             pv::set_error("pv_batch_create: cannot create streams");
             return fail(PV_ERR_CUDA);
         }
@@ -647,7 +681,8 @@ extern "C" int pv_batch_info(const pv_batch* b, int beam, long long* h_info8) {
     h_info8[4] = x->inverted;
     h_info8[5] = B.written;   // logical chunks in the ring after the steps issued
     h_info8[6] = B.done - 1;  // last window dedispersed (-1: none yet)
-    h_info8[7] = (long long)x->nbins * x->row_stride * (long long)sizeof(float);
+    const long long elem = b->store == PV_STORE_F32 ? 4 : (b->store == PV_STORE_F16 ? 2 : 1);
+    h_info8[7] = (long long)x->nbins * x->row_stride * elem;  // ring bytes
     return PV_OK;
 }
 

@@ -521,7 +521,12 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     // odd.  u8 rows: lane l adds samples 4l..4l+3 (+128q) from one word, or a
     // funnel shift of two when the offset is not a multiple of 4; a byte q
     // stands for (q - 128) * scale + offset of its channel, the offsets of all
-    // channels being added once per output.
+    // channels being added once per output.  When every row of the beam has
+    // the same scale, the codes themselves are summed exactly as integers:
+    // bytes 0 and 2 (1 and 3) of a word go to the two 16-bit halves of one
+    // register, which take 257 codes before a carry could cross, so the
+    // halves move into 32-bit sums every 256 channels; the output is then
+    // scale * (sum - 128 * nchan) + offset sum.
     unsigned gs = 0;
     for (;;) {
         const int b0 = gs % ST;
@@ -539,6 +544,70 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
         const float dv = pv_trial_value(d, J.start, J.step);
         const int nchan = J.nchan;
         const int nst = (nchan + CS - 1) / CS;
+        if (STORE == PV_STORE_U8 && J.uniform) {
+            unsigned pk[R / 2];  // [2q]: samples 4l, 4l+2 of group q; [2q+1]: 4l+1, 4l+3
+            int isum[R];
+#pragma unroll
+            for (int r = 0; r < R / 2; ++r) pk[r] = 0u;
+#pragma unroll
+            for (int r = 0; r < R; ++r) isum[r] = 0;
+            auto flush = [&]() {
+#pragma unroll
+                for (int q = 0; q < R / 4; ++q) {
+                    isum[4 * q + 0] += (int)(pk[2 * q] & 0xffffu);
+                    isum[4 * q + 2] += (int)(pk[2 * q] >> 16);
+                    isum[4 * q + 1] += (int)(pk[2 * q + 1] & 0xffffu);
+                    isum[4 * q + 3] += (int)(pk[2 * q + 1] >> 16);
+                    pk[2 * q] = 0u;
+                    pk[2 * q + 1] = 0u;
+                }
+            };
+            for (int st = 0; st < nst; ++st) {
+                const int b = gs % ST;
+                if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, kWaitLimitNs)) {
+                    if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                    return;
+                }
+                if (active) {
+                    const int c_end = min(CS, nchan - st * CS);
+                    for (int j = 0; j < c_end; ++j) {
+                        const float k = meta_k[b * CS + j];
+                        const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT - 4);
+                        const unsigned* wr =
+                            reinterpret_cast<const unsigned*>(slots + (size_t)(b * CS + j) * slot) + (off >> 2) + lane;
+                        const int m = off & 3;
+#pragma unroll
+                        for (int q = 0; q < R / 4; ++q) {
+                            unsigned x = wr[32 * q];
+                            if (m) x = __funnelshift_r(x, wr[32 * q + 1], 8 * m);
+                            pk[2 * q] += __byte_perm(x, 0u, 0x4240u);
+                            pk[2 * q + 1] += __byte_perm(x, 0u, 0x4341u);
+                        }
+                    }
+                    if ((st + 1) % (256 / CS) == 0) flush();
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&empty[b]);
+                ++gs;
+            }
+            if (active) {
+                flush();
+                float* o = J.out + (long long)d * J.out_stride;
+                const float sc = J.scale[0], os = *J.off_sum;
+                const int bias = 128 * nchan;
+#pragma unroll
+                for (int q = 0; q < R / 4; ++q) {
+                    const long long t = tt.t0 + 128 * q + 4 * lane;
+                    if (t < J.nout)
+                        *reinterpret_cast<float4*>(o + t) =
+                            make_float4(fmaf(sc, (float)(isum[4 * q + 0] - bias), os),
+                                        fmaf(sc, (float)(isum[4 * q + 1] - bias), os),
+                                        fmaf(sc, (float)(isum[4 * q + 2] - bias), os),
+                                        fmaf(sc, (float)(isum[4 * q + 3] - bias), os));
+                }
+            }
+            continue;
+        }
         float acc[R];
         unsigned long long acc2[R / 2];
 #pragma unroll
@@ -766,7 +835,11 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
                 "cudaFuncSetAttribute(dedisperse_batch)");
         return PV_OK;
     }
-    PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
+    if (grid < 0) {  // the counter was reset beforehand: this launch joins the same tile queue
+        grid = -grid;
+    } else {
+        PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
+    }
     kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status);
     return pv::check_launch("dedisperse_batch_kernel");
 }
@@ -891,7 +964,8 @@ int upload(DdBatch* b, const DdBeam* beams, int n, const Shape& sh, int variant)
     for (int i = 0; i < n; ++i) {
         const DdBeam& B = beams[i];
         jobs[i] = DdJob{B.out, B.out_stride, B.ring, B.row_stride, B.ring_len, B.d_dmshift, B.scale,
-                        B.off_sum, B.nchan, B.nout, B.tdms, B.chunk, sh.dms[i], i, B.start, B.step};
+                        B.off_sum, B.nchan, B.nout, B.tdms, B.chunk, sh.dms[i], i, B.start, B.step,
+                        b->store == PV_STORE_U8 ? B.uniform : 0};
     }
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_tiles) cudaFree(b->d_tiles);
@@ -1029,6 +1103,19 @@ int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s) {
     return launch_batch(b->variant, b->store, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem, b->grid,
                         b->d_counter, bs, b->d_status, s, false);
 }
+
+int dd_batch_reset(DdBatch* b, cudaStream_t s) {
+    PV_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s), "reset tile counter");
+    return PV_OK;
+}
+
+int dd_batch_launch_shared(DdBatch* b, const BeamStep* bs, int ctas, cudaStream_t s) {
+    if (ctas <= 0) return PV_OK;
+    return launch_batch(b->variant, b->store, b->d_jobs, b->d_tiles, b->ntiles, b->slot, b->smem,
+                        -std::min(ctas, std::max(b->ntiles, 1)), b->d_counter, bs, b->d_status, s, false);
+}
+
+int dd_batch_grid(const DdBatch* b) { return b->grid; }
 
 int dd_batch_status(const DdBatch* b, int* h_status) {
     PV_CUDA(cudaMemcpy(h_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "read status");

@@ -63,6 +63,7 @@ struct DdBeam {
     const float* h_dmshift;
     int nchan, nout, tdms, chunk;
     float start, step;  // trial value = start + d*step, in samples per unit delay constant
+    int uniform;        // u8 storage: every row has the scale scale[0] (codes summed as integers)
 };
 struct DdJob {
     float* out;
@@ -74,6 +75,7 @@ struct DdJob {
     const float* off_sum;
     int nchan, nout, tdms, chunk, dms, beam;
     float start, step;
+    int uniform;
 };
 struct DdTile {
     int job, d0, t0;
@@ -82,6 +84,11 @@ struct DdBatch;
 // variant < 0 runs the autotuner over the DM x time tile variants; store: PV_STORE_*
 int dd_batch_create(DdBatch** out, const DdBeam* beams, int n, int variant, int store, cudaStream_t s);
 int dd_batch_launch(DdBatch* b, const BeamStep* bs, cudaStream_t s);
+// Launches that share one tile queue: reset the queue once, then launch any
+// number of `ctas`-CTA kernels (possibly on other streams) that drain it.
+int dd_batch_reset(DdBatch* b, cudaStream_t s);
+int dd_batch_launch_shared(DdBatch* b, const BeamStep* bs, int ctas, cudaStream_t s);
+int dd_batch_grid(const DdBatch* b);
 int dd_batch_status(const DdBatch* b, int* h_status);
 int dd_batch_shape(const DdBatch* b, int* h8);
 const std::vector<int>& dd_batch_dms(const DdBatch* b);
@@ -97,6 +104,7 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
 int rfi_batch_launch(RfiBatch* b, cudaStream_t s);
 int rfi_batch_launches(const RfiBatch* b);  // number of CTA-size classes
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s);
+int rfi_batch_ctas(const RfiBatch* b, int k);  // CTAs (beams) of class k
 void rfi_batch_destroy(RfiBatch* b);
 
 // Batched ring writes (buffer.cu): stokes [nt][nsub][1][nchan] of one beam.

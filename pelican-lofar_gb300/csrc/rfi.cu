@@ -1037,6 +1037,8 @@ int rfi_batch_launch(RfiBatch* b, cudaStream_t s) {
 
 int rfi_batch_launches(const RfiBatch* b) { return (int)b->classes.size(); }
 
+int rfi_batch_ctas(const RfiBatch* b, int k) { return b->classes[k].njobs; }
+
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s) {
     auto& c = b->classes[k];
     if (c.njobs == 0) return PV_OK;

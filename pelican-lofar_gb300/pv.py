@@ -103,6 +103,9 @@ def _declare(L):
         "pv_batch_buffers": (i, [vp, i, P(vp), P(vp), P(vp)]),
         "pv_batch_step_done": (i, [vp, ll]),
         "pv_batch_footprint": (ll, [vp, i]),
+        "pv_udp_check": (i, [vp, ll, P(ll), P(i)]),
+        "pv_udp_unpack": (i, [vp, vp, ll, vp, i, vp]),
+        "pv_udp_time": (i, [vp, vp, P(d), P(d)]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_ddmod_create": (i, [P(vp), i, i, f, f, d, d]),
         "pv_ddmod_destroy": (None, [vp]),
@@ -418,6 +421,66 @@ class Beam:
 
 
 BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
+class UdpConfig(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("fixed_size_packets", "sample_bits", "packets_per_chunk",
+                                       "samples_per_packet", "nchan", "nsub", "npol", "clock_mhz")]
+
+
+UDP_OUT = {"c32": 0, "i16": 1}
+
+
+class UdpAdapter:
+    """AdapterTimeSeriesDataSet (lib/src/AdapterTimeSeriesDataSet.cpp:36-282)
+    on the GPU.  Keyword names are the adapter's XML options.  deserialise()
+    takes one chunk of packets (a device uint8 tensor, or host bytes / numpy
+    uint8, copied in first) and returns the TimeSeriesDataSetC32 on the
+    device: complex64 [sub][pol][block][nchan] ("c32"), or the same samples
+    as int16 [sub][pol][block*nchan][2] ("i16", the station format the
+    channeliser takes).  The chunk's LOFAR time stamp and block rate are
+    kept as attributes, and out_of_sequence is set as the reference warns
+    (:113-116)."""
+
+    def __init__(self, fixedSizePackets=True, dataBitSize=0, udpPacketsPerIteration=0,
+                 samplesPerPacket=0, outputChannelsPerSubband=0, subbandsPerPacket=0,
+                 nRawPolarisations=0, clock=200):
+        self.cfg = UdpConfig(int(bool(fixedSizePackets)), dataBitSize, udpPacketsPerIteration,
+                             samplesPerPacket, outputChannelsPerSubband, subbandsPerPacket,
+                             nRawPolarisations, clock)
+        self.timestamp = self.block_rate = None
+        self.out_of_sequence = False
+        self._last = 0.0
+
+    def check(self, chunk_bytes):
+        """(packet_bytes, time blocks) of a chunk; PvError with the reference's message."""
+        pb, nb = C.c_longlong(0), C.c_int(0)
+        check(load().pv_udp_check(C.byref(self.cfg), chunk_bytes, C.byref(pb), C.byref(nb)))
+        return pb.value, nb.value
+
+    def deserialise(self, chunk, out="c32", stream=None):
+        import torch
+        import numpy as np
+        c = self.cfg
+        if isinstance(chunk, torch.Tensor) and chunk.is_cuda:
+            d_chunk, head = chunk, chunk[:16].cpu().numpy()
+        else:
+            host = np.frombuffer(chunk, np.uint8) if not isinstance(chunk, np.ndarray) else chunk
+            head = np.ascontiguousarray(host[:16])
+            d_chunk = torch.from_numpy(np.ascontiguousarray(host, np.uint8)).cuda()
+        nbytes = d_chunk.numel()
+        _, nblocks = self.check(nbytes)
+        if out == "c32":
+            res = torch.empty((c.nsub, c.npol, nblocks, c.nchan), dtype=torch.complex64, device=d_chunk.device)
+        else:
+            res = torch.empty((c.nsub, c.npol, nblocks * c.nchan, 2), dtype=torch.int16, device=d_chunk.device)
+        check(load().pv_udp_unpack(C.byref(c), _ptr(d_chunk), nbytes, _ptr(res), UDP_OUT[out], _stream(stream)))
+        ts, rate = C.c_double(0), C.c_double(0)
+        check(load().pv_udp_time(C.byref(c), head.ctypes.data, C.byref(ts), C.byref(rate)))
+        self.timestamp, self.block_rate = ts.value, rate.value
+        self.out_of_sequence = self.timestamp - self._last > self.block_rate
+        self._last = self.timestamp + nblocks * c.nchan * self.block_rate
+        return res
+
+
 BATCH_STORE = {"f32": 0, "f16": 16, "u8": 32}
 HOST_EVENTS = 65536  # PV_BATCH_HOST_EVENTS
 
@@ -560,11 +623,12 @@ class HostBuffer:
             self.ptr = None
 
 
-def device_array(ptr, shape, device=None):
-    """A float32 torch copy of library-owned device memory."""
+def device_array(ptr, shape, device=None, dtype="float32"):
+    """A torch copy (float32, float16 or uint8) of library-owned device memory."""
     import torch
-    t = torch.empty(shape, dtype=torch.float32, device=device or "cuda")
-    check(load().pv_device_copy(_ptr(t), C.c_void_p(ptr), t.numel() * 4, _stream(None)))
+    tt = {"float32": torch.float32, "float16": torch.float16, "uint8": torch.uint8}[dtype]
+    t = torch.empty(shape, dtype=tt, device=device or "cuda")
+    check(load().pv_device_copy(_ptr(t), C.c_void_p(ptr), t.numel() * t.element_size(), _stream(None)))
     return t
 
 

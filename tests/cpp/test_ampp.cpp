@@ -7,6 +7,8 @@
 //                               [nt][nsub][1][nchan], shape in DIR/shape.txt) with
 //                               DIR/config.xml; prints "AMP <dmAmplitude(0, 10.0)>" and
 //                               "EVENTS <count>" per completed buffer
+//   test_ampp udp DIR           AdapterTimeSeriesDataSet on DIR/chunk.bin with DIR/config.xml;
+//                               writes DIR/ts.bin, prints "SHAPE nb ns np nt" and "TIME ts rate"
 #include <pv/ampp.hpp>
 
 #include <cstdio>
@@ -161,6 +163,20 @@ int ddmod_mode(const std::string& dir, int nblobs) {
     return 0;
 }
 
+int udp_mode(const std::string& dir) {
+    const ConfigNode cfg = ConfigNode::fromFile(dir + "/config.xml", "AdapterTimeSeriesDataSet");
+    const auto chunk = read_file<unsigned char>(dir + "/chunk.bin");
+    AdapterTimeSeriesDataSet adapter(cfg);
+    TimeSeriesDataSetC32 ts;
+    adapter.config(&ts, chunk.size());
+    adapter.deserialise(chunk.data());
+    write_file(dir + "/ts.bin", ts.data(), (size_t)ts.nTimeBlocks() * ts.nSubbands() * ts.nPolarisations() *
+                                               ts.nTimesPerBlock());
+    std::printf("SHAPE %u %u %u %u\nTIME %.17g %.17g\n", ts.nTimeBlocks(), ts.nSubbands(), ts.nPolarisations(),
+                ts.nTimesPerBlock(), ts.getLofarTimestamp(), ts.getBlockRate());
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -170,6 +186,7 @@ int main(int argc, char** argv) {
         if (mode == "config") return config_mode();
         if (mode == "chain" && argc >= 3) return chain_mode(argv[2]);
         if (mode == "ddmod" && argc >= 4) return ddmod_mode(argv[2], std::atoi(argv[3]));
+        if (mode == "udp" && argc >= 3) return udp_mode(argv[2]);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "EXCEPTION %s\n", e.what());
         return 3;

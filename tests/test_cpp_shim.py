@@ -126,3 +126,35 @@ def test_shim_dedispersion_module_known_answer(pv, cuda, shim_exe, tmp_path):
     o = pv.DedispersionModule(8192, 200, 0.0, 0.1, GEN_FCH1, foff)
     o.add(blob, GEN_TSAMP)
     assert int(vals["MAXSHIFT"]) == o.params()["maxshift"]
+
+
+UDP_XML = """<configuration>
+  <AdapterTimeSeriesDataSet>
+    <fixedSizePackets value="true"/>
+    <dataBitSize value="{bits}"/>
+    <udpPacketsPerIteration value="{npk}"/>
+    <samplesPerPacket value="16"/>
+    <outputChannelsPerSubband value="16"/>
+    <subbandsPerPacket value="{nsub}"/>
+    <nRawPolarisations value="2"/>
+    <clock value="200"/>
+  </AdapterTimeSeriesDataSet>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bits", [8, 16])
+def test_shim_udp_adapter_equals_the_oracle(pv, oracle, cuda, shim_exe, tmp_path, bits):
+    from test_udp import FIXED, make_chunk
+    rng = np.random.default_rng(bits)
+    npk, nsub = 64, (61 if bits == 16 else 122)
+    chunk, _ = make_chunk(rng, npk, nsub, 16, 2, bits, True)
+    chunk.tofile(tmp_path / "chunk.bin")
+    (tmp_path / "config.xml").write_text(UDP_XML.format(bits=bits, npk=npk, nsub=nsub))
+    out = _run(shim_exe, "udp", tmp_path).split()
+    assert out[1:5] == [str(npk * 16 // 16), str(nsub), "2", "16"]
+    assert float(out[6]) == 1234567890 + 1000 / 195313 and float(out[7]) == 1.0 / 195313
+    want = oracle.udp_unpack(chunk, FIXED, npk, bits, nsub, 2, 16)
+    got = np.fromfile(tmp_path / "ts.bin", np.complex64).reshape(want.shape)
+    assert np.array_equal(got, want)

@@ -62,11 +62,27 @@ def mix_configs(pv, cuda):
 def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled, pipelined):
     """Filterbank, event list and dedispersed window of every beam equal the
     single-beam chain's; pipelined, a window arrives one step later."""
+    _compare_with_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled, pipelined,
+                              wide_spread=True)
+
+
+@pytest.mark.parametrize("pipelined", [False, True])
+def test_batch_with_two_clipper_classes_equals_beams_alone(pv, cuda, mix_configs, pipelined):
+    """A beam of more than 1024 channels puts its clipper in a second CTA-size
+    class; pipelined, that class runs on its own stream and a dedispersion
+    launch on the same queue follows it."""
+    rng = np.random.default_rng(99)
+    big = calibrated(pv, cuda, beam_kw(40, 32, 24, 0.05), rng)  # 1280 channels
+    assert pv.load().pv_rfi_parts(1280) != pv.load().pv_rfi_parts(256)
+    _compare_with_beams_alone(pv, cuda, mix_configs[:2] + [big], False, True, 0, False, pipelined)
+
+
+def _compare_with_beams_alone(pv, cuda, mix, tune, graph, variant, prefilled, pipelined, wide_spread=False):
     import torch
-    cfgs = mix_configs
+    cfgs = mix
     if prefilled:  # rings start as lag chunks of silence: windows from the first chunk on
         cfgs = [type(c).from_buffer_copy(c) for c in cfgs]
-        for c, o in zip(cfgs, mix_configs):
+        for c, o in zip(cfgs, mix):
             c._bp, c.bp_text, c.prefilled = o._bp, o._bp, 1
     batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant, pipelined=pipelined)
     alone = [pv.Beam(c) for c in cfgs]
@@ -74,7 +90,7 @@ def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, p
     assert lags == [b.info()["lag"] for b in alone]
     shape = batch.tiles()
     assert shape["tiles"] > 0 and all(1 <= d <= 16 for d in shape["dms"])
-    if not tune and variant in (0, 3):  # 16 channel slots of ~3.5k samples
+    if wide_spread and not tune and variant in (0, 3):  # 16 channel slots of ~3.5k samples
         assert min(shape["dms"]) < 16  # the wide-spread beam needs a short DM tile
     if graph:
         assert shape["graph_kernels"] >= len(cfgs)

@@ -48,7 +48,7 @@ def runs(pv, oracle, cuda):
     # the same ring clipped to the u8 code range (+-6 sigma, sigma = 1 after the
     # zero-DMing clipper): spectra the clipper rejects (-0.2 minus the
     # bandpass) saturate there
-    ref, ref_sat = [], []
+    ref, ref_sat, ref_codes = [], [], []
     for i, c in enumerate(cfgs):
         info = batches["f32"].info(i)
         nbins = info["nbins"]
@@ -63,18 +63,24 @@ def runs(pv, oracle, cuda):
         lim = 6.0 / 127.0
         sat = np.clip(ring[:, cols], -128 * lim, 127 * lim)
         ref_sat.append(oracle.dedisperse(sat, c.chunk, c.tdms, k, start, step, f64=True))
-    return cfgs, res, ref, ref_sat
+        # the u8 ring's codes, centred: their FP64 sums are the exact integer sums
+        info8 = batches["u8"].info(i)
+        stride8 = info8["ring_bytes"] // nbins
+        codes = pv.device_array(batches["u8"].buffers(i)[2], (nbins, stride8), dtype="uint8").cpu().numpy()
+        ref_codes.append(oracle.dedisperse(codes[:, cols].astype(np.float32) - 128.0, c.chunk, c.tdms, k,
+                                           start, step, f64=True))
+    return cfgs, res, ref, ref_sat, ref_codes
 
 
 def test_fp32_ring_equals_fp64_within_1e5(runs):
-    cfgs, res, ref, _ = runs
+    cfgs, res, ref, _, _ = runs
     for (ev, n, first, out), r in zip(res["f32"], ref):
         assert first >= 0
         assert _rel_rms(out, r) < 1e-5  # FP32 sums of ~10^2-10^3 channels
 
 
 def test_fp16_ring_dedispersed_power_within_1e3_of_fp64(runs):
-    cfgs, res, ref, _ = runs
+    cfgs, res, ref, _, _ = runs
     for (ev, n, first, out), r in zip(res["f16"], ref):
         assert _rel_rms(out, r) < 1e-3
 
@@ -82,13 +88,23 @@ def test_fp16_ring_dedispersed_power_within_1e3_of_fp64(runs):
 def test_u8_ring_quantisation_error_is_bounded(runs):
     """Against the FP64 sum of the same samples clipped to the code range, the
     u8 error is the quantisation noise: steps of 6/127 sigma."""
-    cfgs, res, ref, ref_sat = runs
+    cfgs, res, ref, ref_sat, _ = runs
     for (ev, n, first, out), r in zip(res["u8"], ref_sat):
         assert _rel_rms(out, r) < 0.05
 
 
+def test_u8_codes_of_uniform_scale_beams_are_summed_exactly(runs):
+    """With the clipper and zero-DMing every row has the scale 6/127: the
+    kernel sums the codes as integers, so each output is the FP32 product of
+    the scale and the exact sum."""
+    cfgs, res, _, _, ref_codes = runs
+    sc = np.float64(np.float32(6.0 / 127.0))
+    for (ev, n, first, out), r in zip(res["u8"], ref_codes):
+        assert np.array_equal(out, (sc * r).astype(np.float32))
+
+
 def test_fp16_events_agree_with_fp32_but_near_the_threshold(runs):
-    cfgs, res, ref, _ = runs
+    cfgs, res, ref, _, _ = runs
     compared = 0
     for c, (e32, n32, f32, _), (e16, n16, f16, _) in zip(cfgs, res["f32"], res["f16"]):
         assert f32 == f16
