@@ -457,6 +457,71 @@ int pv_udp_unpack(const pv_udp_config* config, const void* d_chunk, long long ch
 int pv_udp_time(const pv_udp_config* config, const void* h_packet, double* h_timestamp,
                 double* h_block_rate);
 
+/* ---- Outputs: sigproc filterbank and event text --------------------------
+ * SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:13-293) and
+ * DedispersionDataAnalysisOutput (lib/src/DedispersionDataAnalysisOutput.cpp:
+ * 24-112).  Header values are the writer's members as it writes them
+ * (floats widened to double); the shim's SigprocStokesWriter derives them
+ * from the XML options. */
+typedef struct {
+    int machine_id;        /* <MachineID value="9"/> */
+    int telescope_id;      /* <TelescopeID value="0"/> */
+    int nchans;            /* channels per spectrum written */
+    int nbits;             /* <dataBits value="32"/>: 32 or 8 */
+    int nifs;              /* <params nPolsToWrite="1"/> */
+    double src_raj, src_dej, fch1, foff, tsamp;
+    double tstart;         /* MJD (pv_sigproc_mjd) */
+    char source_name[80];  /* NUL-terminated */
+} pv_sigproc_params;
+/* The header bytes (HEADER_START .. HEADER_END, :118-140) into h_buf;
+ * *h_len is the size needed (PV_ERR_ARG when cap is smaller). */
+int pv_sigproc_header(const pv_sigproc_params* params, char* h_buf, long long cap, long long* h_len);
+/* MJD of a LOFAR (Unix) time stamp: (t - 2011-01-01 00:00 UTC) / 86400 + 55562
+ * (:120-128; the reference's mktime takes the host's time zone). */
+double pv_sigproc_mjd(double lofar_timestamp);
+/* The data block of nt spectra (:195-234) on the device: d_stokes is
+ * SpectrumDataSetStokes float [t][sub][pol][chan]; d_out receives, per t and
+ * written polarisation p < npols_write, subbands then channels in descending
+ * order, as float (nbits 32) or one byte rint((min(x, crop_max) - crop_min) *
+ * 255 / (crop_max - crop_min)), 0 below crop_min (nbits 8, :288-293). */
+int pv_sigproc_pack(const float* d_stokes, int nt, int nsub, int npol, int nchan, int npols_write,
+                    int nbits, float crop_min, float crop_max, void* d_out, void* stream);
+/* The text DedispersionDataAnalysisOutput::sendStream writes for one analysed
+ * buffer (:80-112): a line "mjd,   dm, snr, binFactor" per event after the
+ * first, then "# Written buffer :<dump_index> | MJDstart: ... Done".  Times
+ * are start_timestamp + (t + first_sample) * block_rate of the buffer's first
+ * input blob; dm = dm_low + dm_step * index; snr = value / (rms *
+ * sqrt(binFactor)).  *h_len is the size needed. */
+int pv_events_text(const pv_event* h_events, long long n, double start_timestamp, double block_rate,
+                   long long first_sample, double dm_low, double dm_step, float rms, int dump_index,
+                   char* h_buf, long long cap, long long* h_len);
+/* ---- BandPassRecorder (lib/src/BandPassRecorder.cpp:22-190) ---------------
+ * Options: <requiredSamples value="20000"/>, <fitParmaters coefficients="3"/>,
+ * <Band startFrequency=.. endFrequency=../>.  The integrated Stokes-I
+ * spectrum is summed on the device; the polynomial fit with 2-sigma
+ * trimming of high channels is made on the host once required_samples
+ * spectra have been added (the reference's intent: its own LAPACK call cannot
+ * run). */
+typedef struct pv_bandpass_recorder pv_bandpass_recorder;
+int pv_bandpass_recorder_create(pv_bandpass_recorder** recorder, long long required_samples, int ncoeffs,
+                                float start_freq, float end_freq);
+void pv_bandpass_recorder_destroy(pv_bandpass_recorder* recorder);
+/* BandPassRecorder::run: adds polarisation 0 of d_stokes [t][sub][pol][chan].
+ * Returns 1 when the fit is ready (the stream is synchronised), 0 while
+ * more spectra are needed, or an error.  The next call after a fit starts a
+ * new integration. */
+int pv_bandpass_recorder_add(pv_bandpass_recorder* recorder, const float* d_stokes, int nt, int nsub,
+                             int npol, int nchan, void* stream);
+/* The fit: ncoeffs coefficients of f^0..f^(n-1), the RMS of the cleaned mean
+ * spectrum, the channels trimmed, and the .bp text (BandPassAdapter format,
+ * lib/src/BandPassAdapter.cpp:30-108) that pv_rfi_create loads. */
+int pv_bandpass_recorder_result(const pv_bandpass_recorder* recorder, float* h_coeffs, float* h_rms,
+                                int* h_trimmed, char* h_bp_text, long long cap, long long* h_len);
+
+/* The file header DedispersionDataAnalysisOutput writes when it opens a file (:66-70). */
+#define PV_EVENTS_TEXT_HEADER \
+    "# Generated by DedispersionDataAnalysisOutput\n# Events\n# ------\n# Time|Dm|Amplitude|BinFactor\n# ------\n"
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,9 @@
 //       unlockCallback(), onChainCompletion(), waitForJobCompletion(),
 //       maxshift(), numberOfSamples()                                          lib/DedispersionModule.h:76-104
 //   DedispersionAnalyser::analyse(DedispersionSpectra*, DedispersionDataAnalysis*) lib/DedispersionAnalyser.h:31
+//   SigprocStokesWriter::sendStream(), DedispersionDataAnalysisOutput::sendStream()
+//                                                                              lib/SigprocStokesWriter.h,
+//                                                                              lib/DedispersionDataAnalysisOutput.h
 //
 // XML options are read with the reference's element and attribute names
 // and defaults.  Errors the reference throws as QString (or reports with
@@ -32,6 +35,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <ctime>
 #include <iostream>
 #include <complex>
 #include <cstring>
@@ -321,6 +325,8 @@ class DedispersionSpectra : public DataBlob {
     int dmBins() const { return (int)n_; }
     int timeSamples() const { return (int)t_; }
     float dmMax() const { return dm(n_ - 1); }
+    double dmLow() const { return lower_; }
+    double dmStep() const { return width_; }
     void setFirstSample(unsigned s) { first_ = s; }
     unsigned firstSample() const { return first_; }
     // the channel count the analyser's RMS is taken from (inputDataBlobs()[0])
@@ -633,6 +639,10 @@ class DedispersionModule {
                               (int)d->nPolarisations(), (int)d->nChannels(), d->getBlockRate(), &done,
                               nullptr));
         if (unlock_) unlock_(std::vector<DataBlob*>{blob});  // samples are copied on add
+        if (!have_t0_) {  // sample 0 of the stream: times are t0 + (t + firstSample) * rate
+            t0_ = d->getLofarTimestamp();
+            have_t0_ = true;
+        }
         for (int i = 0; i < done; ++i) {
             int p[6] = {0};
             pv_check(pv_ddmod_params(h_, p));
@@ -644,13 +654,15 @@ class DedispersionModule {
             out.setFirstSample((unsigned)first);
             out.setInputShape(nch_, nsub_);
             out.setBlockRate(d->getBlockRate());
-            out.setLofarTimestamp(d->getLofarTimestamp());
+            out.setLofarTimestamp(t0_);
             for (auto& f : functors_) f(&out);
             for (auto& f : chain_) f();
         }
     }
 
     pv_ddmod* h_ = nullptr;
+    double t0_ = 0.0;
+    bool have_t0_ = false;
     unsigned samples_ = 0, tdms_ = 0, nch_ = 0, nsub_ = 0;
     float dm_step_ = 0.0f, dm_low_ = 0.0f;
     double fch1_ = 0.0, foff_ = 0.0;
@@ -691,6 +703,230 @@ class DedispersionAnalyser {
     float threshold_;
     unsigned bin_pow2_;
     DeviceBuffer dbuf_, evbuf_;
+};
+
+// ---------------------------------------------------------------------------
+// Pipeline driver
+// ---------------------------------------------------------------------------
+
+// pipelines/udpstream/src/DedispersionPipeline.cpp:48-155: per chunk of
+// voltages, PPFChanneliser -> StokesGenerator -> RFI_Clipper ->
+// DedispersionModule (no StokesIntegrator in this pipeline: :101-104); each
+// completed buffer is analysed and goes to the "TriggerInput" output, and
+// to "DedispersionDataAnalysis" when its event count is at least <events
+// min> (min >= max) or within [min, max].  Modules and limits come from one
+// XML file with the reference's element names.  Outputs are callbacks in
+// place of the pelican output manager; input spectra are not kept, so
+// "SignalFoundSpectrum" has no data to send.
+class DedispersionPipeline {
+  public:
+    using Output = std::function<void(const DedispersionDataAnalysis&)>;
+    explicit DedispersionPipeline(const std::string& config_file) {
+        const ConfigNode c = ConfigNode::fromFile(config_file, "DedispersionPipeline");
+        min_ = to_uint(c.getOption("events", "min", "5"));
+        max_ = to_uint(c.getOption("events", "max", "0"));
+        ppf_.reset(new PPFChanneliser(ConfigNode::fromFile(config_file, "PPFChanneliser")));
+        stokes_.reset(new StokesGenerator(ConfigNode::fromFile(config_file, "StokesGenerator")));
+        rfi_.reset(new RFI_Clipper(ConfigNode::fromFile(config_file, "RFI_Clipper")));
+        dd_.reset(new DedispersionModule(ConfigNode::fromFile(config_file, "DedispersionModule")));
+        an_.reset(new DedispersionAnalyser(ConfigNode::fromFile(config_file, "DedispersionAnalyser")));
+        dd_->connect([this](DedispersionSpectra* d) { analysis(d); });
+    }
+    // AbstractPipeline::dataOutput: "TriggerInput" or "DedispersionDataAnalysis"
+    void connectOutput(const std::string& stream, const Output& f) { outputs_.emplace_back(stream, f); }
+
+    void run(TimeSeriesDataSetC32* timeSeries) {
+        ppf_->run(timeSeries, &spectra_);
+        stokes_->run(&spectra_, &stokes_data_);
+        WeightedSpectrumDataSet w(&stokes_data_);
+        rfi_->run(&w);
+        dd_->dedisperse(&w);
+    }
+    unsigned buffers() const { return buffers_; }
+
+  private:
+    void emit(const std::string& stream, const DedispersionDataAnalysis& r) {
+        for (auto& o : outputs_)
+            if (o.first == stream) o.second(r);
+    }
+    void analysis(DedispersionSpectra* d) {
+        ++buffers_;
+        DedispersionDataAnalysis result;
+        if (!an_->analyse(d, &result)) return;
+        emit("TriggerInput", result);
+        const unsigned n = (unsigned)result.eventsFound();
+        if (min_ >= max_ ? n >= min_ : (n >= min_ && n <= max_)) emit("DedispersionDataAnalysis", result);
+    }
+
+    unsigned min_ = 5, max_ = 0, buffers_ = 0;
+    std::unique_ptr<PPFChanneliser> ppf_;
+    std::unique_ptr<StokesGenerator> stokes_;
+    std::unique_ptr<RFI_Clipper> rfi_;
+    std::unique_ptr<DedispersionModule> dd_;
+    std::unique_ptr<DedispersionAnalyser> an_;
+    SpectrumDataSetC32 spectra_;
+    SpectrumDataSetStokes stokes_data_;
+    std::vector<std::pair<std::string, Output>> outputs_;
+};
+
+// ---------------------------------------------------------------------------
+// Output streams
+// ---------------------------------------------------------------------------
+
+// "<path>_D%Y%m%dT%H%M%S<ext>" in local time, as both reference writers name
+// their files (SigprocStokesWriter.cpp:94-101, DedispersionDataAnalysisOutput.cpp:30-37).
+inline std::string stamped_name(const std::string& path, const char* ext) {
+    char ts[22];
+    const time_t now = time(nullptr);
+    struct tm tm_now;
+    localtime_r(&now, &tm_now);
+    strftime(ts, sizeof ts, "D%Y%m%dT%H%M%S", &tm_now);
+    return path + "_" + ts + ext;
+}
+
+// lib/src/SigprocStokesWriter.cpp:13-293: the header values derive from the
+// options with the reference's types (float members, unsigned options, a
+// double 0.5 and 1e6); the data block is reordered and quantised on the GPU.
+class SigprocStokesWriter {
+  public:
+    explicit SigprocStokesWriter(const ConfigNode& c) {
+        nsub_ = to_uint(c.getOption("subbandsPerPacket", "value", "1"));
+        const int n_total = (int)to_uint(c.getOption("totalComplexSubbands", "value", "1"));
+        const float clock = to_float(c.getOption("clock", "value", "200"));
+        const unsigned integ = to_uint(c.getOption("integrateTimeBins", "value", "1"));
+        const unsigned integ_f = to_uint(c.getOption("integrateFrequencyChannels", "value", "1"));
+        const unsigned nchan = to_uint(c.getOption("outputChannelsPerSubband", "value", "128")) / integ_f;
+        const unsigned nraw = to_uint(c.getOption("nRawPolarisations", "value", "2"));
+        nbits_ = to_uint(c.getOption("dataBits", "value", "32"));
+        const float nrange = (float)((int)std::pow(2.0, (double)nbits_) - 1.0);
+        crop_min_ = to_float(c.getOption("scale", "min", "0.0"));
+        const std::string mx = c.getOption("scale", "max", "X");
+        try {
+            size_t used = 0;
+            crop_max_ = std::stof(mx, &used);
+            if (used != mx.size()) crop_max_ = nrange;
+        } catch (const std::exception&) {
+            crop_max_ = nrange;
+        }
+        const std::string path = c.getOption("file", "filepath");
+        const unsigned top = (unsigned)to_float(c.getOption("topSubbandIndex", "value", "150"));
+        const unsigned lbahba = (unsigned)to_float(c.getOption("LBA_0_or_HBA_1", "value", "1"));
+        const float sbw = clock / (float)(nraw * (unsigned)n_total);
+        const float cw = sbw / (float)nchan;
+        float fch1 = 0.0f;
+        if (c.getOption("fch1", "value").empty()) {
+            const float base = sbw * (float)top;
+            if (lbahba == 0)
+                fch1 = (float)((double)base + 0.5 * sbw - 0.5 * cw);
+            else if (clock == 200)
+                fch1 = (float)((double)(100 + base) + 0.5 * sbw - 0.5 * cw);
+            else if (clock == 160)
+                fch1 = (float)((double)(160 + base) + 0.5 * sbw - 0.5 * cw);
+        } else {
+            fch1 = to_float(c.getOption("fch1", "value", "1400.0"));
+        }
+        const float foff = c.getOption("foff", "value").empty() ? -cw : to_float(c.getOption("foff", "value", "1.0"));
+        float tsamp = 0.0f;
+        if (c.getOption("tsamp", "value").empty())
+            tsamp = (float)((float)(nraw * (unsigned)n_total * nchan * integ_f * integ) / clock / 1e6);
+        else
+            tsamp = to_float(c.getOption("tsamp", "value", "1.0"));
+        npols_ = to_uint(c.getOption("params", "nPolsToWrite", "1"));
+        write_header_ = c.hasAttribute("writeHeader") && lower(c.getAttribute("writeHeader")) == "true";
+        const std::string ra = c.getOption("RAJ", "value", "000000.0"), dec = c.getOption("DecJ", "value", "000000.0");
+        const float dec_v = to_float(dec);
+        std::string name = ra.substr(0, 4) + (dec_v > 0.0f ? "+" + dec.substr(0, 4) : dec.substr(0, 5));
+        p_.machine_id = (int)to_uint(c.getOption("MachineID", "value", "9"));
+        p_.telescope_id = (int)to_uint(c.getOption("TelescopeID", "value", "0"));
+        p_.nchans = (int)(nchan * nsub_);
+        p_.nbits = (int)nbits_;
+        p_.nifs = (int)npols_;
+        p_.src_raj = to_float(ra);
+        p_.src_dej = dec_v;
+        p_.fch1 = fch1;
+        p_.foff = foff;
+        p_.tsamp = tsamp;
+        std::snprintf(p_.source_name, sizeof p_.source_name, "%s", name.c_str());
+        file_.open(stamped_name(path, ".fil"), std::ios::out | std::ios::binary);
+    }
+    const pv_sigproc_params& params() const { return p_; }
+
+    void sendStream(const SpectrumDataSetStokes* stokes) {
+        if (!stokes) {
+            std::cerr << "SigprocStokesWriter::send(): Only SpectrumDataSetStokes data can be written by the "
+                         "SigprocWriter" << std::endl;
+            return;
+        }
+        if (write_header_) {
+            write_header_ = false;
+            p_.tstart = pv_sigproc_mjd(stokes->getLofarTimestamp());
+            long long n = 0;
+            pv_sigproc_header(&p_, nullptr, 0, &n);
+            std::vector<char> h((size_t)n);
+            pv_check(pv_sigproc_header(&p_, h.data(), n, &n));
+            file_.write(h.data(), n);
+        }
+        const unsigned nt = stokes->nTimeBlocks(), ns = stokes->nSubbands(), np = stokes->nPolarisations(),
+                       nc = stokes->nChannels();
+        const size_t in_n = (size_t)nt * ns * np * nc;
+        if (nbits_ != 8 && nbits_ != 32) pv_check(pv_sigproc_pack(nullptr, 0, 1, 1, 1, 1, (int)nbits_, 0, 0, nullptr, nullptr));
+        const size_t out_n = (size_t)nt * npols_ * ns * nc * (nbits_ / 8);
+        float* d_in = din_.as<float>(in_n);
+        void* d_out = dout_.get(out_n);
+        std::vector<char> h(out_n);
+        pv_check(pv_device_copy(d_in, stokes->data(), (long long)(4 * in_n), nullptr));
+        pv_check(pv_sigproc_pack(d_in, (int)nt, (int)ns, (int)np, (int)nc, (int)npols_, (int)nbits_, crop_min_,
+                                 crop_max_, d_out, nullptr));
+        pv_check(pv_device_copy(h.data(), d_out, (long long)out_n, nullptr));
+        pv_check(pv_synchronize(nullptr));
+        file_.write(h.data(), (std::streamsize)out_n);
+        file_.flush();
+    }
+
+  private:
+    pv_sigproc_params p_{};
+    unsigned nsub_ = 1, nbits_ = 32, npols_ = 1;
+    float crop_min_ = 0.0f, crop_max_ = 255.0f;
+    bool write_header_ = false;
+    std::ofstream file_;
+    DeviceBuffer din_, dout_;
+};
+
+// lib/src/DedispersionDataAnalysisOutput.cpp:24-112
+class DedispersionDataAnalysisOutput {
+  public:
+    explicit DedispersionDataAnalysisOutput(const ConfigNode& c) {
+        file_.open(stamped_name(c.getOption("file", "name"), ".dat"), std::ios::out | std::ios::binary);
+        if (!file_) {
+            std::cerr << "DedispersionDataAnalysisOutput: unable to open file for writing" << std::endl;
+            return;
+        }
+        file_ << PV_EVENTS_TEXT_HEADER;
+        file_.flush();
+    }
+    void sendStream(const DedispersionDataAnalysis* data) {
+        if (!data || !data->data() || !file_) return;
+        const DedispersionSpectra* d = data->data();
+        std::vector<pv_event> ev;
+        ev.reserve(data->events().size());
+        for (const auto& e : data->events())
+            ev.push_back(pv_event{(int32_t)e.dmIndex(), (int32_t)e.timeBin(), e.mfBinning(), e.mfValue()});
+        ++dump_;
+        long long n = 0;
+        auto call = [&](char* buf, long long cap) {
+            return pv_events_text(ev.data(), (long long)ev.size(), d->getLofarTimestamp(), d->getBlockRate(),
+                                  d->firstSample(), d->dmLow(), d->dmStep(), data->getRMS(), dump_, buf, cap, &n);
+        };
+        call(nullptr, 0);
+        std::vector<char> text((size_t)n);
+        pv_check(call(text.data(), n));
+        file_.write(text.data(), n);
+        file_.flush();
+    }
+
+  private:
+    std::ofstream file_;
+    int dump_ = 0;
 };
 
 }  // namespace ampp

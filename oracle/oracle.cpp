@@ -1286,3 +1286,41 @@ extern "C" void or_udp_time(const unsigned char* header, int clock_mhz, double* 
     *timestamp = ts + (1.0 * seq) / tot;
     *block_rate = 1.0 / tot;
 }
+
+// ===========================================================================
+// F2 SigprocStokesWriter data block (SigprocStokesWriter.cpp:195-234, 288-293)
+// ===========================================================================
+// Per spectrum t, per written polarisation p, subbands s = nsub-1..0 and
+// channels i = nchan-1..0 of the Stokes set (index nchan*(npol*(nsub*t+s)+p),
+// SpectrumDataSet.h:229-235): the float itself (32 bits) or the low byte of
+// (int)rint((min(x, max) - min) * nRange / (max - min)), 0 below min (8
+// bits); nRange = (int)pow(2, nbits) - 1.0 held in a float member, the
+// product and quotient in float, rint on the double.
+extern "C" long long or_sigproc_pack(const float* stokes, int nt, int nsub, int npol, int nchan, int npw,
+                                     int nbits, float cmin, float cmax, unsigned char* out) {
+    const float nrange = (float)((int)std::pow(2.0, (double)nbits) - 1.0);
+    const float delta = cmax - cmin;
+    long long o = 0;
+    for (int t = 0; t < nt; ++t)
+        for (int p = 0; p < npw; ++p)
+            for (int s = nsub - 1; s >= 0; --s) {
+                const long long index = (long long)nchan * (npol * ((long long)nsub * t + s) + p);
+                for (int i = nchan - 1; i >= 0; --i) {
+                    const float x = stokes[index + i];
+                    if (nbits == 32) {
+                        std::memcpy(out + o, &x, 4);
+                        o += 4;
+                    } else {
+                        const float f = (x > cmax) ? cmax : x;
+                        int ci = 0;
+                        if (!(f < cmin)) {
+                            const float q = (f - cmin) * nrange / delta;
+                            const double r = ::rint((double)q);
+                            ci = std::isnan(r) ? 0 : (int)r;  // the conversion of NaN gives a zero low byte
+                        }
+                        out[o++] = (unsigned char)(ci & 0xff);
+                    }
+                }
+            }
+    return o;
+}

@@ -178,6 +178,10 @@ int or_udp_unpack(const unsigned char* chunk, long long packet_bytes, int npacke
 void or_udp_time(const unsigned char* header, int clock_mhz, double* timestamp,
                  double* block_rate);
 
+/* ---- F2 SigprocStokesWriter data block ----------------------------------- */
+long long or_sigproc_pack(const float* stokes, int nt, int nsub, int npol, int nchan, int npw,
+                          int nbits, float cmin, float cmax, unsigned char* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,7 @@ def lib():
             "or_udp_check": (i, [i, i, i, i, i, i, i, ll, P(ll), P(i)]),
             "or_udp_unpack": (i, [vp, ll, i, i, i, i, i, P(C.c_float)]),
             "or_udp_time": (None, [vp, i, P(C.c_double), P(C.c_double)]),
+            "or_sigproc_pack": (ll, [P(C.c_float), i, i, i, i, i, i, f, f, vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -326,3 +327,151 @@ def udp_time(packet, clock_mhz=200):
     ts, rate = C.c_double(0), C.c_double(0)
     lib().or_udp_time(buf.ctypes.data, clock_mhz, C.byref(ts), C.byref(rate))
     return ts.value, rate.value
+
+
+# --------------------------------------------------------------------------
+# F2 outputs: SigprocStokesWriter and DedispersionDataAnalysisOutput
+# --------------------------------------------------------------------------
+
+def sigproc_pack(stokes, npols_write, nbits, crop_min=0.0, crop_max=255.0):
+    """Data block bytes of float32 [t][sub][pol][chan] (SigprocStokesWriter.cpp:195-234)."""
+    x = np.ascontiguousarray(stokes, np.float32)
+    nt, nsub, npol, nchan = x.shape
+    out = np.zeros(nt * npols_write * nsub * nchan * (nbits // 8), np.uint8)
+    n = lib().or_sigproc_pack(_f32p(x), nt, nsub, npol, nchan, npols_write, nbits, crop_min, crop_max,
+                              out.ctypes.data)
+    assert n == out.size
+    return out
+
+
+def sigproc_params(opts):
+    """The header values SigprocStokesWriter's constructor derives from its XML
+    options (SigprocStokesWriter.cpp:13-104), with the C++ expression types:
+    float members, unsigned integer options, a double 0.5 and 1e6."""
+    f32 = np.float32
+    get = opts.get
+    n_total = int(get("totalComplexSubbands", 1))
+    clock = f32(get("clock", 200))
+    integ = int(get("integrateTimeBins", 1))
+    integ_f = int(get("integrateFrequencyChannels", 1))
+    nchan = int(get("outputChannelsPerSubband", 128)) // integ_f
+    nraw = int(get("nRawPolarisations", 2))
+    top = int(f32(get("topSubbandIndex", 150)))      # float option into an unsigned member
+    lbahba = int(f32(get("LBA_0_or_HBA_1", 1)))
+    sbw = f32(clock / f32(nraw * n_total))
+    cw = f32(sbw / f32(nchan))
+    if get("fch1") is None:
+        base = f32(sbw * f32(top))
+        if lbahba == 0:
+            fch1 = f32(float(base) + 0.5 * float(sbw) - 0.5 * float(cw))
+        elif clock == 200:
+            fch1 = f32(float(f32(f32(100) + base)) + 0.5 * float(sbw) - 0.5 * float(cw))
+        else:
+            fch1 = f32(float(f32(f32(160) + base)) + 0.5 * float(sbw) - 0.5 * float(cw))
+    else:
+        fch1 = f32(get("fch1"))
+    foff = -cw if get("foff") is None else f32(get("foff"))
+    if get("tsamp") is None:
+        prod = (nraw * n_total * nchan * integ_f * integ) & 0xFFFFFFFF  # unsigned arithmetic
+        tsamp = f32(float(f32(f32(prod) / clock)) / 1e6)
+    else:
+        tsamp = f32(get("tsamp"))
+    ra_s, dec_s = str(get("RAJ", "000000.0")), str(get("DecJ", "000000.0"))
+    name = ra_s[:4] + ("+" + dec_s[:4] if f32(dec_s) > 0 else dec_s[:5])
+    nsub = int(get("subbandsPerPacket", 1))
+    return dict(machine_id=int(get("MachineID", 9)), telescope_id=int(get("TelescopeID", 0)),
+                nchans=nchan * nsub, nbits=int(get("dataBits", 32)), nifs=int(get("nPolsToWrite", 1)),
+                src_raj=float(f32(ra_s)), src_dej=float(f32(dec_s)), fch1=float(fch1), foff=float(foff),
+                tsamp=float(tsamp), source_name=name)
+
+
+def sigproc_header(p, tstart):
+    """Header bytes (SigprocStokesWriter.cpp:118-181)."""
+    import struct
+
+    def s(x):
+        b = x.encode()
+        return struct.pack("<i", len(b)) + b
+    out = s("HEADER_START") + s("machine_id") + struct.pack("<i", p["machine_id"])
+    out += s("telescope_id") + struct.pack("<i", p["telescope_id"]) + s("data_type") + struct.pack("<i", 1)
+    out += s("source_name") + s(p["source_name"])
+    for k in ("src_raj", "src_dej", "fch1", "foff"):
+        out += s(k) + struct.pack("<d", p[k])
+    out += s("nchans") + struct.pack("<i", p["nchans"]) + s("tsamp") + struct.pack("<d", p["tsamp"])
+    out += s("nbits") + struct.pack("<i", p["nbits"]) + s("tstart") + struct.pack("<d", tstart)
+    out += s("nifs") + struct.pack("<i", p["nifs"]) + s("HEADER_END")
+    return out
+
+
+EVENTS_TEXT_HEADER = ("# Generated by DedispersionDataAnalysisOutput\n# Events\n# ------\n"
+                      "# Time|Dm|Amplitude|BinFactor\n# ------\n")
+
+
+def events_text(events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms, dump_index):
+    """DedispersionDataAnalysisOutput::sendStream for one buffer
+    (DedispersionDataAnalysisOutput.cpp:80-112): QTextStream at precision 14
+    prints reals like %.14g; SNR is value / (rms * sqrt(binFactor)) in double,
+    stored as float."""
+    f32 = np.float32
+    lines, snr_max, dm_best = [], f32(0), f32(0)
+
+    def t_of(t):
+        return start_timestamp + float((int(t) + int(first_sample)) & 0xFFFFFFFF) * block_rate
+    for e in events[1:]:
+        mjd = t_of(e["t"]) / 86400
+        dm = f32(dm_low + dm_step * int(e["dm"]))
+        snr = f32(float(e["value"]) / (float(f32(rms)) * np.sqrt(float(e["bin_factor"]))))
+        if snr > snr_max:
+            dm_best, snr_max = dm, snr
+        lines.append("%.14g,   %.14g, %.14g, %d\n" % (mjd, float(dm), float(snr), int(e["bin_factor"])))
+    mjd0 = t_of(events[0]["t"] if len(events) else 0) / 86400
+    lines.append("# Written buffer :%d | MJDstart: %.14g | Best DM: %.14g | Max SNR: %.14g  Done\n"
+                 % (dump_index, mjd0, float(dm_best), float(snr_max)))
+    return "".join(lines)
+
+
+# --------------------------------------------------------------------------
+# F3 BandPassRecorder
+# --------------------------------------------------------------------------
+
+def bandpass_record(chunks, required, ncoeffs, start, end, seg=256):
+    """BandPassRecorder (BandPassRecorder.cpp:22-190) as it is meant to work:
+    polarisation 0 of each float32 [t][sub][pol][chan] chunk is summed per
+    channel (FP32 in time order within 256-spectrum segments of each call,
+    the segments added in FP64) until `required` spectra; the mean spectrum
+    is fitted by least squares in f^0..f^(n-1) (numpy lstsq), channels more
+    than 2 residual RMS above the fit are set to the fit and the fit is
+    repeated until none is.  Returns (coefficients, rms of the cleaned mean
+    spectrum, channels trimmed) or None while more spectra are needed."""
+    total, acc = 0, None
+    for x in chunks:
+        nt, nsub, npol, nchan = x.shape
+        i = np.ascontiguousarray(x[:, :, 0, :].reshape(nt, nsub * nchan), np.float32)
+        if acc is None:
+            acc = np.zeros(nsub * nchan, np.float64)
+        for t0 in range(0, nt, seg):
+            part = np.cumsum(i[t0:t0 + seg], axis=0, dtype=np.float32)[-1]
+            acc = acc + part.astype(np.float64)
+        total += nt
+        if total >= required and total > 0:
+            break
+    if acc is None or total < required:
+        return None
+    n = acc.size
+    width = (float(np.float32(end)) - float(np.float32(start))) / n
+    f = (float(np.float32(start)) + width * np.arange(n)).astype(np.float32).astype(np.float64)
+    y = acc / total
+    V = np.vander(f, ncoeffs, increasing=True)
+    trimmed = 0
+    for _ in range(1000):
+        coef = np.linalg.lstsq(V, y, rcond=None)[0]
+        res = y - V @ coef
+        margin = 2.0 * np.sqrt(max(0.0, np.mean(res ** 2) - np.mean(res) ** 2))
+        cut = res > margin
+        trimmed += int(cut.sum())
+        if not cut.any():
+            break
+        y = np.where(cut, V @ coef, y)
+    rms = np.sqrt(max(0.0, np.mean(y ** 2) - np.mean(y) ** 2))
+    return coef, float(rms), trimmed
+

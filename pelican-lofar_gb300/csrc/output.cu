@@ -1,0 +1,175 @@
+// Outputs after the path: the sigproc filterbank writer and the event text
+// stream.
+//
+// SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:13-293): a header of
+// length-prefixed keywords with int32 / float64 values (:118-181), then per
+// spectrum, for each written polarisation, the subbands and within them the
+// channels in descending order (:207-234), as float32 or as one byte
+// rint((min(x, max) - min) * 255 / (max - min)), 0 below min (:288-293).
+// The reorder and quantisation run on the device over the filterbank that is
+// already there, so 8-bit output leaves the GPU at a quarter of the bytes.
+//
+// DedispersionDataAnalysisOutput (lib/src/DedispersionDataAnalysisOutput.cpp:
+// 60-112): one text line per event after the first (the time stamp
+// carrier), "mjd,   dm, snr, binFactor", then a summary line per buffer.
+// QTextStream prints reals as %g with 14 significant digits
+// (setRealNumberPrecision(14), default SmartNotation); floats are widened to
+// double first.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "pv_internal.cuh"
+
+namespace {
+
+template <bool U8>
+__global__ void __launch_bounds__(256)
+sigproc_pack_kernel(const float* __restrict__ in, int nt, int nsub, int npol, int nchan, int npw,
+                    float cmin, float cmax, float nrange, float delta, void* __restrict__ out) {
+    const long long per = (long long)npw * nsub * nchan;  // output values per spectrum
+    const long long total = per * nt;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < total;
+         j += (long long)gridDim.x * blockDim.x) {
+        const long long t = j / per;
+        const int r = (int)(j - t * per);
+        const int p = r / (nsub * nchan);
+        const int q = r - p * nsub * nchan;
+        const int s = nsub - 1 - q / nchan;
+        const int i = nchan - 1 - q % nchan;
+        const float x = __ldg(in + (((t * nsub + s) * npol + p) * (long long)nchan + i));
+        if (U8) {
+            const float f = x > cmax ? cmax : x;
+            const int ci = f < cmin ? 0 : __float2int_rn(__fdiv_rn(__fmul_rn(__fsub_rn(f, cmin), nrange), delta));
+            reinterpret_cast<unsigned char*>(out)[j] = (unsigned char)(ci & 0xff);
+        } else {
+            reinterpret_cast<float*>(out)[j] = x;
+        }
+    }
+}
+
+struct Buf {
+    char* p;
+    long long cap, n;
+    void put(const void* src, size_t k) {
+        if (n + (long long)k <= cap && p) std::memcpy(p + n, src, k);
+        n += (long long)k;
+    }
+    void str(const char* s) {
+        const int len = (int)std::strlen(s);
+        put(&len, 4);
+        put(s, (size_t)len);
+    }
+    void i32(const char* name, int v) {
+        str(name);
+        put(&v, 4);
+    }
+    void f64(const char* name, double v) {
+        str(name);
+        put(&v, 8);
+    }
+};
+
+}  // namespace
+
+extern "C" int pv_sigproc_header(const pv_sigproc_params* h, char* h_buf, long long cap, long long* h_len) {
+    if (!h || !h_len || cap < 0) {
+        pv::set_error("pv_sigproc_header: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    char name[sizeof(h->source_name) + 1];
+    std::memcpy(name, h->source_name, sizeof(h->source_name));
+    name[sizeof(h->source_name)] = '\0';
+    Buf b{h_buf, cap, 0};
+    b.str("HEADER_START");
+    b.i32("machine_id", h->machine_id);
+    b.i32("telescope_id", h->telescope_id);
+    b.i32("data_type", 1);
+    b.str("source_name");
+    b.str(name);
+    b.f64("src_raj", h->src_raj);
+    b.f64("src_dej", h->src_dej);
+    b.f64("fch1", h->fch1);
+    b.f64("foff", h->foff);
+    b.i32("nchans", h->nchans);
+    b.f64("tsamp", h->tsamp);
+    b.i32("nbits", h->nbits);
+    b.f64("tstart", h->tstart);
+    b.i32("nifs", h->nifs);
+    b.str("HEADER_END");
+    *h_len = b.n;
+    if (b.n > cap) {
+        pv::set_error("pv_sigproc_header: %lld bytes needed", b.n);
+        return PV_ERR_ARG;
+    }
+    return PV_OK;
+}
+
+extern "C" double pv_sigproc_mjd(double lofar_timestamp) {
+    return (lofar_timestamp - 1293840000.0) / 86400 + 55562.0;  // 2011-01-01 00:00 UTC is MJD 55562
+}
+
+extern "C" int pv_sigproc_pack(const float* d_stokes, int nt, int nsub, int npol, int nchan, int npols_write,
+                               int nbits, float crop_min, float crop_max, void* d_out, void* stream) {
+    if (nbits != 8 && nbits != 32) {
+        pv::set_error("SigprocStokesWriter: %d bit datafiles not yet supported", nbits);
+        return PV_ERR_CONFIG;
+    }
+    if (!d_stokes || !d_out || nt < 0 || nsub <= 0 || npol <= 0 || nchan <= 0 || npols_write <= 0 ||
+        npols_write > npol) {
+        pv::set_error("pv_sigproc_pack: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    const long long total = (long long)nt * npols_write * nsub * nchan;
+    if (total == 0) return PV_OK;
+    const float nrange = 255.0f;  // (int)pow(2, 8) - 1.0 (SigprocStokesWriter.cpp:35)
+    const float delta = crop_max - crop_min;
+    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(total, 256), pv::sm_count() * 16LL);
+    cudaStream_t s = pv::as_stream(stream);
+    if (nbits == 8)
+        sigproc_pack_kernel<true><<<blocks, 256, 0, s>>>(d_stokes, nt, nsub, npol, nchan, npols_write, crop_min,
+                                                         crop_max, nrange, delta, d_out);
+    else
+        sigproc_pack_kernel<false><<<blocks, 256, 0, s>>>(d_stokes, nt, nsub, npol, nchan, npols_write,
+                                                          crop_min, crop_max, nrange, delta, d_out);
+    return pv::check_launch("sigproc_pack_kernel");
+}
+
+extern "C" int pv_events_text(const pv_event* h_events, long long n, double start_timestamp, double block_rate,
+                              long long first_sample, double dm_low, double dm_step, float rms, int dump_index,
+                              char* h_buf, long long cap, long long* h_len) {
+    if ((!h_events && n > 0) || !h_len || cap < 0) {
+        pv::set_error("pv_events_text: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    std::string out;
+    char line[256];
+    auto time_of = [&](long long t) {  // DedispersionSpectra::getTime -> SpectrumDataSet::getTime
+        return start_timestamp + (double)(unsigned)(t + first_sample) * block_rate;
+    };
+    float snr_max = 0.0f, dm_best = 0.0f;
+    for (long long i = 1; i < n; ++i) {
+        const pv_event& e = h_events[i];
+        const double mjd = time_of(e.t) / 86400;
+        const float dm = (float)(dm_low + dm_step * e.dm);  // BinMap::binAssignmentNumber
+        const float snr = (float)(e.value / (rms * std::sqrt((double)e.bin_factor)));
+        if (snr > snr_max) {
+            dm_best = dm;
+            snr_max = snr;
+        }
+        std::snprintf(line, sizeof line, "%.14g,   %.14g, %.14g, %d\n", mjd, (double)dm, (double)snr, (int)e.bin_factor);
+        out += line;
+    }
+    const double mjd0 = (n > 0 ? time_of(h_events[0].t) : time_of(0)) / 86400;
+    std::snprintf(line, sizeof line, "# Written buffer :%d | MJDstart: %.14g | Best DM: %.14g | Max SNR: %.14g  Done\n",
+                  dump_index, mjd0, (double)dm_best, (double)snr_max);
+    out += line;
+    *h_len = (long long)out.size();
+    if (h_buf && (long long)out.size() <= cap) std::memcpy(h_buf, out.data(), out.size());
+    if ((long long)out.size() > cap) {
+        pv::set_error("pv_events_text: %lld bytes needed", (long long)out.size());
+        return PV_ERR_ARG;
+    }
+    return PV_OK;
+}

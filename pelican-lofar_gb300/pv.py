@@ -106,6 +106,14 @@ def _declare(L):
         "pv_udp_check": (i, [vp, ll, P(ll), P(i)]),
         "pv_udp_unpack": (i, [vp, vp, ll, vp, i, vp]),
         "pv_udp_time": (i, [vp, vp, P(d), P(d)]),
+        "pv_sigproc_header": (i, [vp, vp, ll, P(ll)]),
+        "pv_sigproc_mjd": (d, [d]),
+        "pv_sigproc_pack": (i, [vp, i, i, i, i, i, i, f, f, vp, vp]),
+        "pv_events_text": (i, [vp, ll, d, d, ll, d, d, f, i, vp, ll, P(ll)]),
+        "pv_bandpass_recorder_create": (i, [P(vp), ll, i, f, f]),
+        "pv_bandpass_recorder_destroy": (None, [vp]),
+        "pv_bandpass_recorder_add": (i, [vp, vp, i, i, i, i, vp]),
+        "pv_bandpass_recorder_result": (i, [vp, P(f), P(f), P(i), vp, ll, P(ll)]),
         "pv_device_copy": (i, [vp, vp, ll, vp]),
         "pv_ddmod_create": (i, [P(vp), i, i, f, f, d, d]),
         "pv_ddmod_destroy": (None, [vp]),
@@ -479,6 +487,97 @@ class UdpAdapter:
         self.out_of_sequence = self.timestamp - self._last > self.block_rate
         self._last = self.timestamp + nblocks * c.nchan * self.block_rate
         return res
+
+
+class SigprocParams(C.Structure):
+    _fields_ = [("machine_id", C.c_int), ("telescope_id", C.c_int), ("nchans", C.c_int), ("nbits", C.c_int),
+                ("nifs", C.c_int), ("src_raj", C.c_double), ("src_dej", C.c_double), ("fch1", C.c_double),
+                ("foff", C.c_double), ("tsamp", C.c_double), ("tstart", C.c_double),
+                ("source_name", C.c_char * 80)]
+
+
+def sigproc_header(params, tstart):
+    """SigprocStokesWriter's header bytes (lib/src/SigprocStokesWriter.cpp:118-140)
+    from its values (a dict with SigprocParams' fields but tstart)."""
+    p = SigprocParams(**{k: (v.encode() if k == "source_name" else v) for k, v in params.items()})
+    p.tstart = tstart
+    n = C.c_longlong(0)
+    load().pv_sigproc_header(C.byref(p), None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value)
+    check(load().pv_sigproc_header(C.byref(p), buf, n.value, C.byref(n)))
+    return buf.raw[:n.value]
+
+
+def sigproc_mjd(lofar_timestamp):
+    return load().pv_sigproc_mjd(lofar_timestamp)
+
+
+def sigproc_pack(d_stokes, npols_write=1, nbits=32, crop_min=0.0, crop_max=255.0, stream=None):
+    """The filterbank data block of float32 [t][sub][pol][chan] on the device
+    (:195-234, 288-293): a device uint8 tensor of the bytes the writer emits."""
+    import torch
+    nt, nsub, npol, nchan = d_stokes.shape
+    out = torch.empty(nt * npols_write * nsub * nchan * (nbits // 8), dtype=torch.uint8, device=d_stokes.device)
+    check(load().pv_sigproc_pack(_ptr(d_stokes), nt, nsub, npol, nchan, npols_write, nbits, crop_min, crop_max,
+                                 _ptr(out), _stream(stream)))
+    return out
+
+
+EVENTS_TEXT_HEADER = ("# Generated by DedispersionDataAnalysisOutput\n# Events\n# ------\n"
+                      "# Time|Dm|Amplitude|BinFactor\n# ------\n")
+
+
+def events_text(events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms, dump_index):
+    """The text DedispersionDataAnalysisOutput::sendStream writes for one
+    analysed buffer (lib/src/DedispersionDataAnalysisOutput.cpp:80-112)."""
+    import numpy as np
+    ev = np.ascontiguousarray(events)
+    n = C.c_longlong(0)
+    args = (ev.ctypes.data if len(ev) else None, len(ev), start_timestamp, block_rate, first_sample, dm_low,
+            dm_step, rms, dump_index)
+    load().pv_events_text(*args, None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    check(load().pv_events_text(*args, buf, n.value, C.byref(n)))
+    return buf.raw[:n.value].decode()
+
+
+class BandPassRecorder:
+    """BandPassRecorder (lib/src/BandPassRecorder.cpp:22-190): run() adds a
+    device Stokes set [t][sub][pol][chan] and returns True once the fit of
+    requiredSamples spectra is ready; result() gives (coefficients, rms,
+    channels trimmed, .bp text)."""
+
+    def __init__(self, requiredSamples=20000, coefficients=3, startFrequency=None, endFrequency=None):
+        if startFrequency is None:
+            raise PvError("BandPassRecorder: <Band startFrequency=?> not defined")
+        if endFrequency is None:
+            raise PvError("BandPassRecorder: <Band endFrequency=?> not defined")
+        self.n = coefficients
+        self.h = C.c_void_p()
+        check(load().pv_bandpass_recorder_create(C.byref(self.h), requiredSamples, coefficients,
+                                                 startFrequency, endFrequency))
+
+    def run(self, d_stokes, stream=None):
+        nt, nsub, npol, nchan = d_stokes.shape
+        rc = load().pv_bandpass_recorder_add(self.h, _ptr(d_stokes), nt, nsub, npol, nchan, _stream(stream))
+        if rc < 0:
+            check(rc)
+        return rc == 1
+
+    def result(self):
+        import numpy as np
+        co = (C.c_float * self.n)()
+        rms, trimmed, n = C.c_float(0), C.c_int(0), C.c_longlong(0)
+        check(load().pv_bandpass_recorder_result(self.h, co, C.byref(rms), C.byref(trimmed), None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value + 1)
+        check(load().pv_bandpass_recorder_result(self.h, co, C.byref(rms), C.byref(trimmed), buf, n.value,
+                                                 C.byref(n)))
+        return np.array(co[:], np.float32), rms.value, trimmed.value, buf.raw[:n.value].decode()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().pv_bandpass_recorder_destroy(self.h)
+            self.h = None
 
 
 BATCH_STORE = {"f32": 0, "f16": 16, "u8": 32}

@@ -7,6 +7,14 @@
 //                               [nt][nsub][1][nchan], shape in DIR/shape.txt) with
 //                               DIR/config.xml; prints "AMP <dmAmplitude(0, 10.0)>" and
 //                               "EVENTS <count>" per completed buffer
+//   test_ampp ddout DIR N       ddmod with a DedispersionDataAnalysisOutput from DIR/config.xml;
+//                               writes DIR/events.bin (pv_event per event) and prints
+//                               "META start rate first dmlow dmstep rms" per buffer
+//   test_ampp sigproc DIR       SigprocStokesWriter (DIR/config.xml) over DIR/stokes.bin
+//                               (float [t][sub][pol][chan], shape and time stamp in DIR/shape.txt)
+//   test_ampp pipeline DIR N    N chunks of DIR/chunks.bin through AdapterTimeSeriesDataSet and
+//                               DedispersionPipeline into a DedispersionDataAnalysisOutput;
+//                               prints "BUFFERS n"
 //   test_ampp udp DIR           AdapterTimeSeriesDataSet on DIR/chunk.bin with DIR/config.xml;
 //                               writes DIR/ts.bin, prints "SHAPE nb ns np nt" and "TIME ts rate"
 #include <pv/ampp.hpp>
@@ -163,6 +171,81 @@ int ddmod_mode(const std::string& dir, int nblobs) {
     return 0;
 }
 
+int ddout_mode(const std::string& dir, int nblobs) {
+    const ConfigNode dd_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionModule");
+    const ConfigNode an_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionAnalyser");
+    const ConfigNode out_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionDataAnalysisOutput");
+    std::ifstream shape(dir + "/shape.txt");
+    unsigned nt, nsub, nchan;
+    double tsamp, t0;
+    shape >> nt >> nsub >> nchan >> tsamp >> t0;
+    const auto blob = read_file<float>(dir + "/blob.bin");
+    DedispersionModule dd(dd_cfg);
+    DedispersionAnalyser an(an_cfg);
+    DedispersionDataAnalysisOutput out(out_cfg);
+    std::ofstream evf(dir + "/events.bin", std::ios::binary);
+    dd.connect([&](DedispersionSpectra* s) {
+        DedispersionDataAnalysis result;
+        an.analyse(s, &result);
+        out.sendStream(&result);
+        for (const auto& e : result.events()) {
+            const pv_event pe{(int32_t)e.dmIndex(), (int32_t)e.timeBin(), e.mfBinning(), e.mfValue()};
+            evf.write(reinterpret_cast<const char*>(&pe), sizeof pe);
+        }
+        std::printf("META %.17g %.17g %u %.17g %.17g %.9g %d\n", s->getLofarTimestamp(), s->getBlockRate(),
+                    s->firstSample(), s->dmLow(), s->dmStep(), result.getRMS(), result.eventsFound());
+    });
+    for (int b = 0; b < nblobs; ++b) {
+        SpectrumDataSetStokes st;
+        st.resize(nt, nsub, 1, nchan);
+        std::memcpy(st.data(), blob.data() + (size_t)b * st.size(), st.size() * sizeof(float));
+        st.setBlockRate(tsamp);
+        st.setLofarTimestamp(t0 + (double)b * nt * tsamp);
+        WeightedSpectrumDataSet w(&st);
+        dd.dedisperse(&w);
+    }
+    dd.waitForJobCompletion();
+    return 0;
+}
+
+int sigproc_mode(const std::string& dir) {
+    const ConfigNode cfg = ConfigNode::fromFile(dir + "/config.xml", "SigprocStokesWriter");
+    std::ifstream shape(dir + "/shape.txt");
+    unsigned nt, nsub, npol, nchan;
+    double t0;
+    shape >> nt >> nsub >> npol >> nchan >> t0;
+    const auto data = read_file<float>(dir + "/stokes.bin");
+    SigprocStokesWriter w(cfg);
+    for (int half = 0; half < 2; ++half) {  // two blobs: the header precedes the first only
+        SpectrumDataSetStokes st;
+        st.resize(nt / 2, nsub, npol, nchan);
+        std::memcpy(st.data(), data.data() + (size_t)half * st.size(), st.size() * sizeof(float));
+        st.setLofarTimestamp(t0);
+        w.sendStream(&st);
+    }
+    std::printf("NCHANS %d\n", w.params().nchans);
+    return 0;
+}
+
+int pipeline_mode(const std::string& dir, int nchunks) {
+    const std::string xml = dir + "/config.xml";
+    const auto all = read_file<unsigned char>(dir + "/chunks.bin");
+    const size_t chunk = all.size() / (size_t)nchunks;
+    AdapterTimeSeriesDataSet adapter(ConfigNode::fromFile(xml, "AdapterTimeSeriesDataSet"));
+    DedispersionPipeline pipeline(xml);
+    DedispersionDataAnalysisOutput out(ConfigNode::fromFile(xml, "DedispersionDataAnalysisOutput"));
+    pipeline.connectOutput("DedispersionDataAnalysis",
+                           [&](const DedispersionDataAnalysis& r) { out.sendStream(&r); });
+    TimeSeriesDataSetC32 ts;
+    for (int k = 0; k < nchunks; ++k) {
+        adapter.config(&ts, chunk);
+        adapter.deserialise(all.data() + (size_t)k * chunk);
+        pipeline.run(&ts);
+    }
+    std::printf("BUFFERS %u\n", pipeline.buffers());
+    return 0;
+}
+
 int udp_mode(const std::string& dir) {
     const ConfigNode cfg = ConfigNode::fromFile(dir + "/config.xml", "AdapterTimeSeriesDataSet");
     const auto chunk = read_file<unsigned char>(dir + "/chunk.bin");
@@ -187,6 +270,9 @@ int main(int argc, char** argv) {
         if (mode == "chain" && argc >= 3) return chain_mode(argv[2]);
         if (mode == "ddmod" && argc >= 4) return ddmod_mode(argv[2], std::atoi(argv[3]));
         if (mode == "udp" && argc >= 3) return udp_mode(argv[2]);
+        if (mode == "ddout" && argc >= 4) return ddout_mode(argv[2], std::atoi(argv[3]));
+        if (mode == "sigproc" && argc >= 3) return sigproc_mode(argv[2]);
+        if (mode == "pipeline" && argc >= 4) return pipeline_mode(argv[2], std::atoi(argv[3]));
     } catch (const std::exception& e) {
         std::fprintf(stderr, "EXCEPTION %s\n", e.what());
         return 3;

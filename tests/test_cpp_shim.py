@@ -152,9 +152,200 @@ def test_shim_udp_adapter_equals_the_oracle(pv, oracle, cuda, shim_exe, tmp_path
     chunk, _ = make_chunk(rng, npk, nsub, 16, 2, bits, True)
     chunk.tofile(tmp_path / "chunk.bin")
     (tmp_path / "config.xml").write_text(UDP_XML.format(bits=bits, npk=npk, nsub=nsub))
-    out = _run(shim_exe, "udp", tmp_path).split()
-    assert out[1:5] == [str(npk * 16 // 16), str(nsub), "2", "16"]
-    assert float(out[6]) == 1234567890 + 1000 / 195313 and float(out[7]) == 1.0 / 195313
+    lines = {ln.split()[0]: ln.split()[1:] for ln in _run(shim_exe, "udp", tmp_path).splitlines() if ln}
+    assert lines["SHAPE"] == [str(npk * 16 // 16), str(nsub), "2", "16"]
+    assert float(lines["TIME"][0]) == 1234567890 + 1000 / 195313 and float(lines["TIME"][1]) == 1.0 / 195313
+    assert "Adapter:" in lines  # the first chunk follows time 0: the reference's out-of-sequence note
     want = oracle.udp_unpack(chunk, FIXED, npk, bits, nsub, 2, 16)
     got = np.fromfile(tmp_path / "ts.bin", np.complex64).reshape(want.shape)
     assert np.array_equal(got, want)
+
+
+DDOUT_XML = """<configuration>
+  <DedispersionModule>
+    <timeBinsPerBufferPow2 value="13"/>
+    <dedispersionSamples value="200"/>
+    <dedispersionStepSize value="0.1"/>
+    <dedispersionMinimum value="0"/>
+    <frequencyChannel1 MHz="{fch1}"/>
+    <channelBandwidth MHz="{foff}"/>
+  </DedispersionModule>
+  <DedispersionAnalyser>
+    <detectionThreshold in_sigma="6.0"/>
+    <power2ForBinning value="6"/>
+  </DedispersionAnalyser>
+  <DedispersionDataAnalysisOutput>
+    <file name="{path}"/>
+  </DedispersionDataAnalysisOutput>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+def test_shim_event_output_file_equals_the_oracle_text(pv, oracle, cuda, shim_exe, tmp_path):
+    """DedispersionModule -> DedispersionAnalyser -> DedispersionDataAnalysisOutput
+    through the module API: the .dat file is the reference's header and, per
+    buffer, the oracle's formatting of the events the analyser found."""
+    blob = generator_pulse(8192, 10.0)[0]
+    blob.tofile(tmp_path / "blob.bin")
+    t0 = 1.3e9 + 0.25
+    (tmp_path / "shape.txt").write_text("%d %d %d %r %r\n" % (8192, GEN_NSUB, GEN_NCHAN, GEN_TSAMP, t0))
+    foff = -6.0 / (GEN_NSUB * GEN_NCHAN)
+    (tmp_path / "config.xml").write_text(DDOUT_XML.format(fch1=repr(GEN_FCH1), foff=repr(foff),
+                                                          path=str(tmp_path / "events")))
+    out = _run(shim_exe, "ddout", tmp_path, 1)
+    metas = [line.split()[1:] for line in out.splitlines() if line.startswith("META")]
+    assert len(metas) == 1
+    files = list(tmp_path.glob("events_D*.dat"))
+    assert len(files) == 1
+    ev = np.fromfile(tmp_path / "events.bin", pv.EVENT_DTYPE)
+    start, rate, first, dm_low, dm_step, rms, n = metas[0]
+    assert int(n) == len(ev) > 200 and float(start) == t0
+    want = oracle.EVENTS_TEXT_HEADER + oracle.events_text(ev, float(start), float(rate), int(first),
+                                                          float(dm_low), float(dm_step), np.float32(rms), 1)
+    assert files[0].read_text() == want
+
+
+SIGPROC_XML = """<configuration>
+  <SigprocStokesWriter writeHeader="true">
+    <file filepath="{path}"/>
+    <subbandsPerPacket value="{nsub}"/>
+    <totalComplexSubbands value="512"/>
+    <clock value="200"/>
+    <integrateTimeBins value="4"/>
+    <outputChannelsPerSubband value="{nchan}"/>
+    <topSubbandIndex value="180.5"/>
+    <dataBits value="{bits}"/>
+    <scale min="10.0" max="210.0"/>
+    <params nPolsToWrite="{npw}"/>
+    <RAJ value="053432.0"/>
+    <DecJ value="220052.0"/>
+  </SigprocStokesWriter>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bits", [8, 32])
+def test_shim_sigproc_file_equals_the_oracle(pv, oracle, cuda, shim_exe, tmp_path, bits):
+    from test_outputs import _stokes
+    rng = np.random.default_rng(bits)
+    nt, nsub, npol, nchan, npw = 64, 31, 4, 16, 2
+    x = _stokes(rng, nt, nsub, npol, nchan)
+    x.tofile(tmp_path / "stokes.bin")
+    t0 = 1.31e9 + 0.5
+    (tmp_path / "shape.txt").write_text("%d %d %d %d %r\n" % (nt, nsub, npol, nchan, t0))
+    (tmp_path / "config.xml").write_text(SIGPROC_XML.format(path=str(tmp_path / "fb"), nsub=nsub, nchan=nchan,
+                                                            bits=bits, npw=npw))
+    out = _run(shim_exe, "sigproc", tmp_path)
+    assert "NCHANS %d" % (nsub * nchan) in out
+    files = list(tmp_path.glob("fb_D*.fil"))
+    assert len(files) == 1
+    opts = {"subbandsPerPacket": nsub, "totalComplexSubbands": 512, "clock": 200, "integrateTimeBins": 4,
+            "outputChannelsPerSubband": nchan, "topSubbandIndex": 180.5, "dataBits": bits, "nPolsToWrite": npw,
+            "RAJ": "053432.0", "DecJ": "220052.0"}
+    head = oracle.sigproc_header(oracle.sigproc_params(opts), (t0 - 1293840000.0) / 86400 + 55562.0)
+    half = nt // 2
+    data = b"".join(oracle.sigproc_pack(x[k * half:(k + 1) * half], npw, bits, 10.0, 210.0).tobytes()
+                    for k in range(2))
+    assert files[0].read_bytes() == head + data
+
+
+PIPELINE_XML = """<configuration>
+  <AdapterTimeSeriesDataSet>
+    <fixedSizePackets value="true"/>
+    <dataBitSize value="16"/>
+    <udpPacketsPerIteration value="{npk}"/>
+    <samplesPerPacket value="16"/>
+    <outputChannelsPerSubband value="{nchan}"/>
+    <subbandsPerPacket value="{nsub}"/>
+    <nRawPolarisations value="2"/>
+  </AdapterTimeSeriesDataSet>
+  <DedispersionPipeline>
+    <history value="10"/>
+    <events min="{emin}" max="{emax}"/>
+  </DedispersionPipeline>
+  <PPFChanneliser>
+    <outputChannelsPerSubband value="{nchan}"/>
+    <filter nTaps="8" filterWindow="kaiser"/>
+  </PPFChanneliser>
+  <StokesGenerator><numberOfStokes value="1"/></StokesGenerator>
+  <RFI_Clipper active="true" channelRejectionRMS="5.0" spectrumRejectionRMS="4.0">
+    <BandPassData file="band.bp"/>
+    <Band matching="true"/>
+    <History maximum="1000"/>
+    <zeroDMing active="true"/>
+  </RFI_Clipper>
+  <DedispersionModule>
+    <timeBinsPerBufferPow2 value="12"/>
+    <dedispersionSamples value="{tdms}"/>
+    <dedispersionStepSize value="{dm_step}"/>
+    <dedispersionMinimum value="0"/>
+    <frequencyChannel1 MHz="{fch1}"/>
+    <channelBandwidth MHz="{foff}"/>
+  </DedispersionModule>
+  <DedispersionAnalyser>
+    <detectionThreshold in_sigma="{thr}"/>
+    <power2ForBinning value="4"/>
+  </DedispersionAnalyser>
+  <DedispersionDataAnalysisOutput>
+    <file name="{path}"/>
+  </DedispersionDataAnalysisOutput>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("emin,emax", [(1, 0), (10 ** 6, 10 ** 7)])
+def test_shim_pipeline_from_packets_to_event_file(pv, oracle, cuda, shim_exe, tmp_path, emin, emax):
+    """Station packets -> AdapterTimeSeriesDataSet -> DedispersionPipeline
+    (PPF, Stokes, RFI_Clipper, DedispersionModule, analyser; no integrator)
+    -> DedispersionDataAnalysisOutput, against the same chain composed
+    through the Python binding; a window of [min, max] events that no buffer
+    reaches writes no lines."""
+    import torch
+    from test_udp import make_chunk
+    nsub, nchan, npk, nchunks, tdms, dm_step, thr = 8, 16, 2048, 4, 48, 0.5, 4.0
+    rng = np.random.default_rng(17)
+    chunks, ts0 = [], 1300000000
+    for k in range(nchunks):
+        c, _ = make_chunk(rng, npk, nsub, 16, 2, 16, True, ts0=ts0, seq0=1000 + k * npk * 16)
+        chunks.append(c)
+    np.concatenate(chunks).tofile(tmp_path / "chunks.bin")
+    foff = -0.1953125 / nchan
+    fch1 = 150.0
+    ad = pv.UdpAdapter(True, 16, npk, 16, nchan, nsub, 2)
+    ppf = pv.PPF(nchan, 8, window="kaiser")
+    st = []
+    for c in chunks:
+        ts = ad.deserialise(torch.from_numpy(c).to(cuda))
+        st.append(pv.stokes(ppf.run(ts.reshape(nsub, 2, -1)), 1))
+    fb0 = st[0].cpu().numpy()
+    (tmp_path / "band.bp").write_text(make_bp_text(nsub * nchan, fch1 + foff * (nsub * nchan - 1), -foff,
+                                                   float(fb0.mean()), float(fb0.std())))
+    (tmp_path / "config.xml").write_text(PIPELINE_XML.format(
+        npk=npk, nchan=nchan, nsub=nsub, emin=emin, emax=emax, tdms=tdms, dm_step=dm_step, fch1=repr(fch1),
+        foff=repr(foff), thr=thr, path=str(tmp_path / "ev")))
+    out = _run(shim_exe, "pipeline", tmp_path, nchunks)
+    nbuf = int(out.split("BUFFERS")[1].split()[0])
+    # the same chain through the binding
+    rfi = pv.RFI((tmp_path / "band.bp").read_text(), cr=5.0, sr=4.0, history=1000, zero_dming=True)
+    dd = pv.DedispersionModule(1 << 12, tdms, 0.0, dm_step, fch1, foff)
+    tsamp = ad.block_rate * nchan  # the adapter's 1/195313 s (even second) times the PPF length
+    rms = float(np.sqrt(np.float32(nchan) * np.float32(nsub)))
+    text, dump = "", 0
+    t_start = ts0 + 1000 / 195313
+    for x in st:
+        rfi.run(x)
+        for buf, first in dd.add(x.cpu().numpy(), tsamp):
+            ev = pv.analyse(torch.from_numpy(buf).to(cuda), thr, rms, 4)
+            n = len(ev)
+            if (n >= emin) if emin >= emax else (emin <= n <= emax):
+                dump += 1
+                text += pv.events_text(ev, t_start, tsamp, first, 0.0, dm_step, np.float32(rms), dump)
+    assert nbuf >= 2
+    files = list(tmp_path.glob("ev_D*.dat"))
+    assert len(files) == 1
+    assert files[0].read_text() == pv.EVENTS_TEXT_HEADER + text
+    if emin > 1000:
+        assert text == ""  # no buffer has a million events
