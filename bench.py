@@ -337,7 +337,13 @@ def run_pv(args, cfg):
                        "l2": "inputs larger than L2 (2.05 GB voltages per chunk, 4.6 GB ring)",
                        "parallelism": "replicas" if world > 1 else "single beam"},
             "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
-                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h},
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms / args.steps,
+                    "h2d_alone_gbs": h2d_alone_gbs,
+                    "h2d_alone_ms_per_step": in_bytes / h2d_alone_gbs / 1e6,
+                    "what": "voltages copied from write-combined page-locked host buffers on the "
+                            "batch's copy stream while the previous step computes; events of the "
+                            "previous step read meanwhile"},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline,
             "roofline_channeliser": roofline_chan,
             "stage_ms": st,
@@ -418,7 +424,7 @@ def run_batch(args, cfgs, workload):
 
     # ---------------- batched engine ----------------
     batch = pv.Batch([pv_config(pv, c, prefilled=1) for c in cfgs], tune=True, graph=True, timing=True,
-                     pipelined=True, store=args.store)
+                     pipelined=not args.unpipelined, store=args.store)
     for i, c in enumerate(cfgs):
         v = device_voltages(c, dev, seed(i))
         batch.set_input(i, v, stream=stream)
@@ -477,9 +483,21 @@ def run_batch(args, cfgs, workload):
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3
     in_bytes = sum(batch.input(i)[1] for i in range(nb))
+
+    # the same host-to-device copies alone (one scratch buffer, the copy engine idle otherwise):
+    # the rate that bounds the end-to-end number
+    scratch = torch.empty(max(h.nbytes for h in hosts), dtype=torch.uint8, device=dev)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for h in hosts:
+        pv.check(pv.load().pv_device_copy(pv._ptr(scratch), pv.C.c_void_p(h.ptr), h.nbytes, pv._stream(stream)))
+    h1.record(stream)
+    h1.synchronize()
+    h2d_alone_gbs = sum(h.nbytes for h in hosts) / (h0.elapsed_time(h1) / 1e3) / 1e9
+    del scratch
     ring_gb = sum(x["ring_bytes"] for x in infos) / 1e9
     precision = None
-    if args.store != "f32":
+    if args.store != "f32" and args.chunk is None:  # reduced profiling cases start in the clipper's warm-up
         del batch
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
@@ -536,11 +554,19 @@ def run_batch(args, cfgs, workload):
                        "l2": "inputs larger than L2 (%.0f GB voltages per step, %.0f GB rings)"
                              % (in_bytes / 1e9, ring_gb),
                        "start": "prefilled rings (silence before each stream)",
-                       "mode": "pipelined: window k-lag-1 dedispersed while chunk k is channelised "
-                               "and clipped",
+                       "mode": ("unpipelined: each step dedisperses the window its chunk completes, in "
+                                "one launch after the clippers" if args.unpipelined else
+                                "pipelined: window k-lag-1 dedispersed while chunk k is channelised "
+                                "and clipped"),
                        "parallelism": "replicas" if world > 1 else "one GPU, all beams batched"},
             "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
-                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h},
+                    "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms / args.steps,
+                    "h2d_alone_gbs": h2d_alone_gbs,
+                    "h2d_alone_ms_per_step": in_bytes / h2d_alone_gbs / 1e6,
+                    "what": "voltages copied from write-combined page-locked host buffers on the "
+                            "batch's copy stream while the previous step computes; events of the "
+                            "previous step read meanwhile"},
             "plain": {"value": plain_value, "e2e": plain_e2e, "steps": plain_steps,
                       "ms_per_step": plain_ms / plain_steps,
                       "what": "pv_beam per beam, one after another, events read back per beam"},
@@ -626,6 +652,143 @@ def precision_check(pv, cfgs, store, dev, seed):
             "fp32_vs_fp64": "within 1e-5 relative rms (parity tests)"}
 
 
+# ---------------------------------------------------------------------------
+# io workload: the byte-bound kernels before and after the path
+# ---------------------------------------------------------------------------
+
+# the reference adapter test's chunk (AdapterTimeSeriesDataSetTest.cpp setUp): 16384 fixed-size
+# packets of 61 subbands x 16 samples x 2 polarisations of complex int16
+UDP_CHUNK = dict(fixedSizePackets=True, dataBitSize=16, udpPacketsPerIteration=16384, samplesPerPacket=16,
+                 outputChannelsPerSubband=16, subbandsPerPacket=61, nRawPolarisations=2)
+UDP_PACKET = 8148
+
+
+def udp_chunk(rng, npk, nsub, spp):
+    """npk fixed-size packets with counting headers and random int16 samples."""
+    chunk = np.zeros((npk, UDP_PACKET), np.uint8)
+    data = rng.integers(-2048, 2048, size=(npk, nsub * spp * 2 * 2), dtype=np.int16)
+    chunk[:, 16:16 + data.shape[1] * 2] = data.view(np.uint8)
+    hdr = np.zeros((npk, 4), np.uint32)
+    hdr[:, 2] = 1300000000
+    hdr[:, 3] = 1000 + spp * np.arange(npk)
+    chunk[:, :16] = hdr.view(np.uint8)
+    return chunk.reshape(-1)
+
+
+def run_io(args):
+    """HBM-bound kernels around the path, each timed alone with CUDA events over
+    inputs that rotate through more than L2: the UDP unpack of the reference
+    adapter test's chunk (16384 packets, 133 MB) to int16 station order and to
+    TimeSeriesDataSetC32; the sigproc pack of a full-band filterbank chunk
+    (16384 x 3904) to 8- and 32-bit files; the bandpass recorder's integration
+    of the same filterbank."""
+    import torch
+    import pv
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    peaks, peak_src = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    rng = np.random.default_rng(11)
+    nrot = 8  # rotating inputs: 8 x 133 MB of packets, 8 x 256 MB of filterbank
+    ad = pv.UdpAdapter(**UDP_CHUNK)
+    chunk_bytes = UDP_PACKET * UDP_CHUNK["udpPacketsPerIteration"]
+    host_chunk = udp_chunk(rng, UDP_CHUNK["udpPacketsPerIteration"], 61, 16)
+    chunks = [torch.from_numpy(host_chunk).to(dev) for _ in range(nrot)]
+    nt, nsub, nchan = 16384, 244, 16
+    fbs = [torch.randn((nt, nsub, 1, nchan), device=dev) * 50 + 120 for _ in range(nrot)]
+    launches0 = pv.launches()
+    clocks = ClockSampler(0)
+    clocks.start()
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            for k in range(args.warmup):
+                fn(k % nrot)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for k in range(args.steps * nrot):
+                fn(k % nrot)
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / (args.steps * nrot)  # ms per launch
+
+    out_c32 = torch.empty((61, 2, 16384, 16), dtype=torch.complex64, device=dev)
+    out_i16 = torch.empty((61, 2, 16384 * 16, 2), dtype=torch.int16, device=dev)
+    cfg = ad.cfg
+    res = {}
+
+    def udp(out, kind):
+        def fn(k):
+            pv.check(pv.load().pv_udp_unpack(pv.C.byref(cfg), pv._ptr(chunks[k]), chunk_bytes, pv._ptr(out),
+                                             pv.UDP_OUT[kind], pv._stream(stream)))
+        return fn
+    for kind, out in (("i16", out_i16), ("c32", out_c32)):
+        ms = timed(udp(out, kind))
+        byts = chunk_bytes + out.numel() * out.element_size()
+        res["udp_unpack_" + kind] = {"ms": ms, "bytes": byts, "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    for nbits in (8, 32):
+        out = torch.empty(nt * nsub * nchan * nbits // 8, dtype=torch.uint8, device=dev)
+
+        def fn(k, out=out, nbits=nbits):
+            pv.check(pv.load().pv_sigproc_pack(pv._ptr(fbs[k]), nt, nsub, 1, nchan, 1, nbits, 0.0, 255.0,
+                                               pv._ptr(out), pv._stream(stream)))
+        ms = timed(fn)
+        byts = fbs[0].numel() * 4 + out.numel()
+        res["sigproc_pack_%d" % nbits] = {"ms": ms, "bytes": byts, "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    rec = pv.BandPassRecorder(requiredSamples=1 << 62, coefficients=3, startFrequency=110.0, endFrequency=157.65625)
+
+    def bp(k):
+        pv.check(min(0, pv.load().pv_bandpass_recorder_add(rec.h, pv._ptr(fbs[k]), nt, nsub, 1, nchan,
+                                                           pv._stream(stream))))
+    ms = timed(bp)
+    byts = fbs[0].numel() * 4
+    res["bandpass_integrate"] = {"ms": ms, "bytes": byts, "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    clk = clocks.stop()
+    launches = pv.launches() - launches0
+
+    # end to end: the chunk from page-locked host memory, unpacked, the voltages read back
+    hb = pv.HostBuffer(chunk_bytes, write_combined=True)
+    hb.fill_from(chunks[0])
+    back = torch.empty(out_i16.shape, dtype=torch.int16).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            pv.check(pv.load().pv_device_copy(pv._ptr(chunks[0]), pv.C.c_void_p(hb.ptr), chunk_bytes,
+                                              pv._stream(stream)))
+            udp(out_i16, "i16")(0)
+            back.copy_(out_i16, non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    u = res["udp_unpack_i16"]
+    cpu = None
+    if not args.no_cpu:
+        from oracle import pyoracle as po
+        t0 = time.perf_counter()
+        po.udp_unpack(host_chunk, UDP_PACKET, UDP_CHUNK["udpPacketsPerIteration"], 16, 61, 2, 16)
+        cs = time.perf_counter() - t0
+        cpu = {"value": chunk_bytes / cs / 1e9, "unit": "GB/s of packets", "cores": 1, "kind": "port",
+               "sample": "one 16384-packet chunk through the oracle's scalar _readData restatement"}
+    line = {"metric": "UDP chunk bytes unpacked per second", "value": chunk_bytes / u["ms"] / 1e6,
+            "unit": "GB/s of packets", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": u["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16", "data": "synthetic: seeded int16 samples in LOFAR packets; seeded Gaussian filterbank",
+            "config": {"workload": "io-udp-16384x61sub-sigproc-bandpass-16384x3904",
+                       "udp": UDP_CHUNK, "chunk_bytes": chunk_bytes,
+                       "l2": "inputs rotate through 8 buffers (1.07 GB of packets, 2.05 GB of filterbank)"},
+            "e2e": {"value": chunk_bytes / e2e_s / 1e9, "unit": "GB/s of packets",
+                    "h2d_bytes_per_step": chunk_bytes, "d2h_bytes_per_step": out_i16.numel() * 2},
+            "gpu_launches": launches, "clocks": clk,
+            "roofline": {"kernel": "udp_unpack_kernel<16, false>", "bound": "hbm", "achieved": u["gbs"],
+                         "peak": hbm, "unit": "GB/s", "frac": u["frac"], "traffic": None,
+                         "per_unit": "chunk bytes read + int16 voltages written per launch",
+                         "peak_source": peak_src},
+            "kernels": res, "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def serve_beams(nbeams=128, seed=128):
     """The serving mix: channel counts 512-15616 (32, 61, 122 or 244 subbands of
     16 or 64 channels), DM ranges 0-250 or 0-1000 in 1024-4096 trials."""
@@ -668,7 +831,7 @@ def run_serve(args, workload):
     reports = {}
     clocks = ClockSampler(0)
     clocks.start()
-    for name, eng, policy in (("batched", serve.BatchEngine(pv, voltages, new_stream), "batch"),
+    for name, eng, policy in (("batched", serve.BatchEngine(pv, voltages, new_stream, store=args.store), "batch"),
                               ("plain", serve.PlainEngine(pv, voltages, new_stream), "fifo1")):
         launches0 = pv.launches()
         rep = serve.Server(eng, streams, budget, policy=policy).run(horizon=args.duration + args.grace)
@@ -685,6 +848,7 @@ def run_serve(args, workload):
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded Gaussian int16 voltages, Poisson chunk arrivals",
             "config": {"workload": workload, "beams": len(streams), "duration_s": args.duration,
+                       "ring_storage": args.store,
                        "budget_gb": args.budget_gb,
                        "chunks": b["chunks"], "offered_units": rt_units,
                        "chunk_spectra": "4096-32768 per beam, Poisson, one chunk per chunk duration",
@@ -846,18 +1010,27 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pv", choices=["pv", "reference"])
-    ap.add_argument("--workload", default="batch64", choices=["batch64", "fullband", "serve128"])
+    ap.add_argument("--workload", default="batch64", choices=["batch64", "fullband", "serve128", "io"])
     ap.add_argument("--beams", type=int, default=None, help="number of beams (64 / 128)")
     ap.add_argument("--duration", type=float, default=60.0, help="serve128: seconds of arrivals")
     ap.add_argument("--grace", type=float, default=30.0, help="serve128: seconds to drain")
     ap.add_argument("--budget-gb", type=float, default=160.0, help="serve128: HBM budget")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--unpipelined", action="store_true",
+                    help="batch64: one dedispersion launch per step after the clippers (the same work)")
     ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
-                    help="batch64: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
+                    help="batch64, serve128: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
     args = ap.parse_args()
+    if args.workload == "io":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the io workload times device kernels only; "
+                              "its cpu_baseline key holds the CPU restatement's rate"}))
+            return
+        run_io(args)
+        return
     if args.workload == "fullband":
         cfg = fullband_config()
         if args.tdms or args.chunk or args.nsub:
@@ -876,6 +1049,8 @@ def main():
     if args.workload == "serve128":
         args.beams = args.beams or 128
         workload = "serve%d-poisson-%gs-%ggb" % (args.beams, args.duration, args.budget_gb)
+        if args.store != "f32":
+            workload += "-%s-rings" % args.store
         if args.impl == "reference":
             cfgs = serve_beams(args.beams)
             run_reference(args, cfgs, workload)

@@ -394,8 +394,8 @@ int pv_batch_run(pv_batch* batch, const unsigned char* h_active, void* stream);
  * k+1 overlap the computation of step k. */
 int pv_batch_run_host(pv_batch* batch, const void* const* h_voltages, const unsigned char* h_active,
                       void* stream);
-/* Events of one beam at one of the last two issued steps (step < 0: the
- * last), as pv_beam_events: total count including the dummy, the window's
+/* Events of one beam at one of the last two issued steps (step >= 0: that
+ * step; -1: the last issued, -2: the one before), as pv_beam_events: total count including the dummy, the window's
  * first sample (-1: the beam dedispersed no window in that step) and up to
  * cap events (at most PV_BATCH_HOST_EVENTS) copied to h_events.  Waits for
  * that step only, so the next step may already be running. */
@@ -426,7 +426,7 @@ long long pv_batch_footprint(const pv_beam_config* config, int flags);
 
 /* ---- LOFAR UDP ingest (AdapterTimeSeriesDataSet) -------------------------
  * Replaces AdapterTimeSeriesDataSet::deserialise/_checkData/_readData
- * (lib/src/AdapterTimeSeriesDataSet.cpp:78-282).  Fields are the adapter's
+ * (lib/src/AdapterTimeSeriesDataSet.cpp:78-293).  Fields are the adapter's
  * XML options (:37-45).  A chunk is packets_per_chunk packets of a 16-byte
  * header (lib/LofarUdpHeader.h:25-35) and subband-major data
  * [subband][time][pol] of complex int8 or int16, padded to 8148 bytes when
@@ -444,7 +444,7 @@ typedef struct {
 #define PV_UDP_OUT_C32 0 /* complex float [sub][pol][block][nchan]: TimeSeriesDataSetC32 */
 #define PV_UDP_OUT_I16 1 /* complex int16, same order: the station format pv_channelise,
                             pv_beam_process and pv_batch take with in_int16 = 1 */
-/* _checkData (AdapterTimeSeriesDataSet.cpp:159-199): packet bytes and time
+/* _checkData (AdapterTimeSeriesDataSet.cpp:152-191): packet bytes and time
  * blocks of a chunk of chunk_bytes; PV_ERR_CONFIG with the reference's message. */
 int pv_udp_check(const pv_udp_config* config, long long chunk_bytes, long long* h_packet_bytes,
                  int* h_nblocks);
@@ -458,9 +458,9 @@ int pv_udp_time(const pv_udp_config* config, const void* h_packet, double* h_tim
                 double* h_block_rate);
 
 /* ---- Outputs: sigproc filterbank and event text --------------------------
- * SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:13-293) and
+ * SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:15-293) and
  * DedispersionDataAnalysisOutput (lib/src/DedispersionDataAnalysisOutput.cpp:
- * 24-112).  Header values are the writer's members as it writes them
+ * 18-112).  Header values are the writer's members as it writes them
  * (floats widened to double); the shim's SigprocStokesWriter derives them
  * from the XML options. */
 typedef struct {

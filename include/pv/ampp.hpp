@@ -385,7 +385,7 @@ class DedispersionDataAnalysis : public DataBlob {
 // Modules
 // ---------------------------------------------------------------------------
 
-// lib/src/AdapterTimeSeriesDataSet.cpp:36-282.  The reference reads one
+// lib/src/AdapterTimeSeriesDataSet.cpp:35-293.  The reference reads one
 // chunk of UDP packets from a QIODevice; deserialise() takes the same bytes
 // from host memory, unpacks them on the GPU and fills the blob given to
 // config(), with the first packet's time stamp and block rate.
@@ -774,7 +774,7 @@ class DedispersionPipeline {
 // ---------------------------------------------------------------------------
 
 // "<path>_D%Y%m%dT%H%M%S<ext>" in local time, as both reference writers name
-// their files (SigprocStokesWriter.cpp:94-101, DedispersionDataAnalysisOutput.cpp:30-37).
+// their files (SigprocStokesWriter.cpp:104-111, DedispersionDataAnalysisOutput.cpp:20-28).
 inline std::string stamped_name(const std::string& path, const char* ext) {
     char ts[22];
     const time_t now = time(nullptr);
@@ -784,7 +784,7 @@ inline std::string stamped_name(const std::string& path, const char* ext) {
     return path + "_" + ts + ext;
 }
 
-// lib/src/SigprocStokesWriter.cpp:13-293: the header values derive from the
+// lib/src/SigprocStokesWriter.cpp:15-293: the header values derive from the
 // options with the reference's types (float members, unsigned options, a
 // double 0.5 and 1e6); the data block is reordered and quantised on the GPU.
 class SigprocStokesWriter {
@@ -892,7 +892,7 @@ class SigprocStokesWriter {
     DeviceBuffer din_, dout_;
 };
 
-// lib/src/DedispersionDataAnalysisOutput.cpp:24-112
+// lib/src/DedispersionDataAnalysisOutput.cpp:18-112
 class DedispersionDataAnalysisOutput {
   public:
     explicit DedispersionDataAnalysisOutput(const ConfigNode& c) {

@@ -1217,7 +1217,7 @@ extern "C" int or_num_threads(void) { return threads_or_default(0); }
 // fixed-size packets, padding up to sizeof(UDPPacket) = 8148 bytes (16 + 8130
 // rounded to the struct's 4-byte alignment).
 
-// AdapterTimeSeriesDataSet::_checkData (AdapterTimeSeriesDataSet.cpp:159-199).
+// AdapterTimeSeriesDataSet::_checkData (AdapterTimeSeriesDataSet.cpp:152-191).
 // Returns 0, or the number of the first failing check: 1 sample bits, 2 chunk
 // size, 3 data larger than a packet, 4 time samples not a multiple of the
 // block length.  packet_bytes and nblocks are written when the check passes.
@@ -1238,7 +1238,7 @@ extern "C" int or_udp_check(int fixed, int bits, int npackets, int spp, int ncha
     return 0;
 }
 
-// AdapterTimeSeriesDataSet::_readData (AdapterTimeSeriesDataSet.cpp:209-282):
+// AdapterTimeSeriesDataSet::_readData (AdapterTimeSeriesDataSet.cpp:217-293):
 // each packet's data is read in the order subband, time, polarisation, one
 // complex int8 or int16 per (s, t, p); time t of packet k is sample
 // k*spp + t of the series [s][p] (TimeSeriesDataSet.h:145-151 with blocks of
@@ -1275,7 +1275,7 @@ extern "C" int or_udp_unpack(const unsigned char* chunk, long long packet_bytes,
 }
 
 // The chunk's time stamp from its first packet (AdapterTimeSeriesDataSet.cpp:
-// 107-118): blocks per second are 156250 at the 160 MHz clock, else 195313 in
+// 108-120): blocks per second are 156250 at the 160 MHz clock, else 195313 in
 // even seconds and 195312 in odd ones.
 extern "C" void or_udp_time(const unsigned char* header, int clock_mhz, double* timestamp,
                             double* block_rate) {
@@ -1288,7 +1288,7 @@ extern "C" void or_udp_time(const unsigned char* header, int clock_mhz, double* 
 }
 
 // ===========================================================================
-// F2 SigprocStokesWriter data block (SigprocStokesWriter.cpp:195-234, 288-293)
+// F2 SigprocStokesWriter data block (SigprocStokesWriter.cpp:187-236, 288-293)
 // ===========================================================================
 // Per spectrum t, per written polarisation p, subbands s = nsub-1..0 and
 // channels i = nchan-1..0 of the Stokes set (index nchan*(npol*(nsub*t+s)+p),

@@ -334,7 +334,7 @@ def udp_time(packet, clock_mhz=200):
 # --------------------------------------------------------------------------
 
 def sigproc_pack(stokes, npols_write, nbits, crop_min=0.0, crop_max=255.0):
-    """Data block bytes of float32 [t][sub][pol][chan] (SigprocStokesWriter.cpp:195-234)."""
+    """Data block bytes of float32 [t][sub][pol][chan] (SigprocStokesWriter.cpp:187-236)."""
     x = np.ascontiguousarray(stokes, np.float32)
     nt, nsub, npol, nchan = x.shape
     out = np.zeros(nt * npols_write * nsub * nchan * (nbits // 8), np.uint8)
@@ -346,7 +346,7 @@ def sigproc_pack(stokes, npols_write, nbits, crop_min=0.0, crop_max=255.0):
 
 def sigproc_params(opts):
     """The header values SigprocStokesWriter's constructor derives from its XML
-    options (SigprocStokesWriter.cpp:13-104), with the C++ expression types:
+    options (SigprocStokesWriter.cpp:15-111), with the C++ expression types:
     float members, unsigned integer options, a double 0.5 and 1e6."""
     f32 = np.float32
     get = opts.get
@@ -386,7 +386,7 @@ def sigproc_params(opts):
 
 
 def sigproc_header(p, tstart):
-    """Header bytes (SigprocStokesWriter.cpp:118-181)."""
+    """Header bytes (SigprocStokesWriter.cpp:115-146)."""
     import struct
 
     def s(x):

@@ -641,7 +641,7 @@ extern "C" int pv_batch_run_host(pv_batch* b, const void* const* h_voltages,
 extern "C" int pv_batch_events(pv_batch* b, int beam, long long step, pv_event* h_events,
                                long long cap, long long* h_count, long long* h_first_sample) {
     if (!b || beam < 0 || beam >= b->n || !h_count) return PV_ERR_ARG;
-    if (step < 0) step = b->step - 1;
+    if (step < 0) step = b->step + step;  // -1: the last step issued, -2: the one before
     if (step < 0 || step >= b->step || step < b->step - 2) {
         pv::set_error("pv_batch_events: step %lld is not one of the last two issued (%lld)", step,
                       b->step);

@@ -9,10 +9,11 @@
 // of the residuals above the fit are replaced by the fit and the fit is
 // repeated until none is; the bandpass RMS is that of the cleaned mean
 // spectrum across channels.  The reference's own code cannot run (its
-// LAPACK call takes the character 'N' as a pointer, the right-hand side
-// holds ncoeffs of nBins values, the matrix is row-major under a
-// column-major leading dimension, and the trim loop never clears its
-// count), so this is a restatement of the intent, not of those lines.
+// LAPACK call takes the character 'N' as a pointer (:18), the right-hand
+// side holds ncoeffs of nBins values (:53, :155), the matrix is row-major
+// under a column-major leading dimension (:60), and the trim loop never
+// clears its count (:106-129)), so this is a restatement of the intent, not
+// of those lines.
 //
 // The sum over time is the only heavy part (every filterbank byte read
 // once): each CTA owns 256 channels of a 256-spectrum segment and sums it in

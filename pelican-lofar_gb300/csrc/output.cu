@@ -1,7 +1,7 @@
 // Outputs after the path: the sigproc filterbank writer and the event text
 // stream.
 //
-// SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:13-293): a header of
+// SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:15-293): a header of
 // length-prefixed keywords with int32 / float64 values (:118-181), then per
 // spectrum, for each written polarisation, the subbands and within them the
 // channels in descending order (:207-234), as float32 or as one byte
@@ -10,7 +10,7 @@
 // already there, so 8-bit output leaves the GPU at a quarter of the bytes.
 //
 // DedispersionDataAnalysisOutput (lib/src/DedispersionDataAnalysisOutput.cpp:
-// 60-112): one text line per event after the first (the time stamp
+// 58-112): one text line per event after the first (the time stamp
 // carrier), "mjd,   dm, snr, binFactor", then a summary line per buffer.
 // QTextStream prints reals as %g with 14 significant digits
 // (setRealNumberPrecision(14), default SmartNotation); floats are widened to
@@ -123,7 +123,7 @@ extern "C" int pv_sigproc_pack(const float* d_stokes, int nt, int nsub, int npol
     }
     const long long total = (long long)nt * npols_write * nsub * nchan;
     if (total == 0) return PV_OK;
-    const float nrange = 255.0f;  // (int)pow(2, 8) - 1.0 (SigprocStokesWriter.cpp:35)
+    const float nrange = 255.0f;  // (int)pow(2, 8) - 1.0 (SigprocStokesWriter.cpp:27)
     const float delta = crop_max - crop_min;
     const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(total, 256), pv::sm_count() * 16LL);
     cudaStream_t s = pv::as_stream(stream);

@@ -1,14 +1,14 @@
 // LOFAR UDP ingest: chunks of station packets -> TimeSeriesDataSetC32.
 //
 // Replaces AdapterTimeSeriesDataSet::deserialise/_readData
-// (lib/src/AdapterTimeSeriesDataSet.cpp:78-282).  The reference copies each
+// (lib/src/AdapterTimeSeriesDataSet.cpp:78-293).  The reference copies each
 // packet through a temporary buffer and scatters it element by element on
 // one host thread; here the chunk of packets is one device buffer (copied in
 // once) and the scatter is a byte transpose on the GPU.
 //
 // A packet is a 16-byte header (lib/LofarUdpHeader.h:25-35), then the data,
 // subband-major: for each subband, each time, each polarisation one complex
-// int8 or int16 (AdapterTimeSeriesDataSet.cpp:215-262), then, for fixed-size
+// int8 or int16 (AdapterTimeSeriesDataSet.cpp:229-288), then, for fixed-size
 // packets, padding up to sizeof(UDPPacket) = 8148 bytes.  Time t of packet k
 // is sample k*spp + t of the series [subband][pol], and a series is
 // contiguous in time in TimeSeriesDataSetC32 (lib/TimeSeriesDataSet.h:145-151).

@@ -438,7 +438,7 @@ UDP_OUT = {"c32": 0, "i16": 1}
 
 
 class UdpAdapter:
-    """AdapterTimeSeriesDataSet (lib/src/AdapterTimeSeriesDataSet.cpp:36-282)
+    """AdapterTimeSeriesDataSet (lib/src/AdapterTimeSeriesDataSet.cpp:35-293)
     on the GPU.  Keyword names are the adapter's XML options.  deserialise()
     takes one chunk of packets (a device uint8 tensor, or host bytes / numpy
     uint8, copied in first) and returns the TimeSeriesDataSetC32 on the
@@ -497,7 +497,7 @@ class SigprocParams(C.Structure):
 
 
 def sigproc_header(params, tstart):
-    """SigprocStokesWriter's header bytes (lib/src/SigprocStokesWriter.cpp:118-140)
+    """SigprocStokesWriter's header bytes (lib/src/SigprocStokesWriter.cpp:129-146)
     from its values (a dict with SigprocParams' fields but tstart)."""
     p = SigprocParams(**{k: (v.encode() if k == "source_name" else v) for k, v in params.items()})
     p.tstart = tstart
@@ -642,7 +642,8 @@ class Batch:
 
     def events(self, beam, step=-1, cap=1 << 16):
         """(events, total count, first sample) of one beam at one of the last
-        two issued steps (-1: the last); waits for that step only."""
+        two issued steps (-1: the last, -2: the one before, or the step's
+        index); waits for that step only."""
         n, first = C.c_longlong(), C.c_longlong()
         check(load().pv_batch_events(self.h, beam, step, None, 0, C.byref(n), C.byref(first)))
         k = min(n.value, cap, HOST_EVENTS)

@@ -246,16 +246,17 @@ class BatchEngine:
     """Cohorts are pv.Batch objects (graph, pipelined) fed from page-locked,
     write-combined staging buffers holding one synthetic sub-chunk per beam."""
 
-    def __init__(self, pv, make_voltages, stream_factory, pipelined=True, tune=False, variant=3):
+    def __init__(self, pv, make_voltages, stream_factory, pipelined=True, tune=False, variant=3, store="f32"):
         self.pv = pv
         self.make_voltages = make_voltages  # cfg -> int16 device tensor of one sub-chunk
         self.stream_factory = stream_factory
         self.pipelined = pipelined
         self.tune = tune
         self.variant = variant
+        self.store = store  # delay-ring storage: "f32", "f16" or "u8"
 
     def footprint(self, cfg):
-        return self.pv.batch_footprint(cfg, self.pipelined)
+        return self.pv.batch_footprint(cfg, self.pipelined, self.store)
 
     def prepare(self, cfgs):
         self.staging = _staging(self.pv, self.make_voltages, cfgs)
@@ -281,7 +282,7 @@ class _BatchCohort:
     def __init__(self, eng, cfgs, staging):
         pv = eng.pv
         self.batch = pv.Batch(cfgs, tune=eng.tune, graph=True, variant=eng.variant,
-                              pipelined=eng.pipelined)
+                              pipelined=eng.pipelined, store=eng.store)
         self.stream = eng.stream_factory()
         self.staging = staging
         self.steps = 0

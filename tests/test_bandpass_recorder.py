@@ -24,7 +24,7 @@ def _filterbank(rng, nt, nsub=31, npol=1, nchan=16, start=110.0, end=116.0546875
 def test_recorder_fit_equals_the_oracle(pv, oracle, cuda, npol):
     import torch
     rng = np.random.default_rng(npol)
-    chunks = [_filterbank(rng, nt, npol=npol, spikes=(7, 100, 300)) for nt in (700, 1300, 517)]
+    chunks = [_filterbank(rng, nt, npol=npol, spikes=(7, 100, 300)) for nt in (700, 1200, 517)]
     rec = pv.BandPassRecorder(requiredSamples=2000, coefficients=3, startFrequency=110.0,
                               endFrequency=116.0546875)
     ready = [rec.run(torch.from_numpy(c).to(cuda)) for c in chunks]

@@ -338,8 +338,8 @@ def test_shim_pipeline_from_packets_to_event_file(pv, oracle, cuda, shim_exe, tm
     for x in st:
         rfi.run(x)
         for buf, first in dd.add(x.cpu().numpy(), tsamp):
-            ev = pv.analyse(torch.from_numpy(buf).to(cuda), thr, rms, 4)
-            n = len(ev)
+            ev, n = pv.analyse(torch.from_numpy(buf).to(cuda), thr, rms, 4)
+            assert n == len(ev)
             if (n >= emin) if emin >= emax else (emin <= n <= emax):
                 dump += 1
                 text += pv.events_text(ev, t_start, tsamp, first, 0.0, dm_step, np.float32(rms), dump)

@@ -175,6 +175,8 @@ def test_batch_host_steps_overlap_and_events_of_previous_step(pv, cuda, mix_conf
             for i in range(len(cfgs)):
                 ev, n, _ = batch.events(i, step=step - 1)
                 assert n == want[step - 1][i][1] and np.array_equal(ev, want[step - 1][i][0])
+                ev2, n2, _ = batch.events(i, step=-2)  # counted back from the last issued step
+                assert n2 == n and np.array_equal(ev2, ev)
         hosts_prev = hosts  # pinned sources stay alive until their copies are done
     for i in range(len(cfgs)):
         ev, n, _ = batch.events(i)
