@@ -44,6 +44,7 @@ spectrum_partial_kernel(const float* __restrict__ in, int nt, int npol, int ncha
     const long long base = ((long long)s * npol) * nchan + c;           // polarisation 0
     const int t0 = seg * kSeg, t1 = min(nt, t0 + kSeg);
     float acc = 0.0f;
+#pragma unroll 8
     for (int t = t0; t < t1; ++t) acc = __fadd_rn(acc, __ldg(in + base + (long long)t * stride));
     part[(long long)seg * nbins + bin] = acc;
 }

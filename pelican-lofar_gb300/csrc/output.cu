@@ -15,6 +15,7 @@
 // QTextStream prints reals as %g with 14 significant digits
 // (setRealNumberPrecision(14), default SmartNotation); floats are widened to
 // double first.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +46,45 @@ sigproc_pack_kernel(const float* __restrict__ in, int nt, int nsub, int npol, in
             reinterpret_cast<unsigned char*>(out)[j] = (unsigned char)(ci & 0xff);
         } else {
             reinterpret_cast<float*>(out)[j] = x;
+        }
+    }
+}
+
+// The same order, four outputs per thread when nchan % 4 == 0: outputs q..q+3
+// of a row (spectrum t, written polarisation p) are channels i..i-3 of one
+// subband, one aligned float4 read backwards.  blockIdx.y is the row group,
+// blockIdx.x the position in the row.
+template <bool U8>
+__device__ __forceinline__ unsigned char quantise(float x, float cmin, float cmax, float nrange, float delta) {
+    const float f = x > cmax ? cmax : x;
+    const int ci = f < cmin ? 0 : __float2int_rn(__fdiv_rn(__fmul_rn(__fsub_rn(f, cmin), nrange), delta));
+    return (unsigned char)(ci & 0xff);
+}
+
+template <bool U8>
+__global__ void __launch_bounds__(256)
+sigproc_pack4_kernel(const float* __restrict__ in, int nrows, int nsub, int npol, int nchan, int npw, float cmin,
+                     float cmax, float nrange, float delta, void* __restrict__ out) {
+    const int per = nsub * nchan;  // outputs per row
+    const int q = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (q >= per) return;
+    for (long long row = blockIdx.y; row < nrows; row += gridDim.y) {
+        const long long t = row / npw;
+        const int p = (int)(row - t * npw);
+        const int sr = q / nchan, ir = q - sr * nchan;
+        const int s = nsub - 1 - sr, i = nchan - 1 - ir;  // channels i, i-1, i-2, i-3
+        const float4 v =
+            __ldg(reinterpret_cast<const float4*>(in + ((t * nsub + s) * npol + p) * (long long)nchan + i - 3));
+        const long long o = row * per + q;
+        if (U8) {
+            uchar4 b;
+            b.x = quantise<true>(v.w, cmin, cmax, nrange, delta);
+            b.y = quantise<true>(v.z, cmin, cmax, nrange, delta);
+            b.z = quantise<true>(v.y, cmin, cmax, nrange, delta);
+            b.w = quantise<true>(v.x, cmin, cmax, nrange, delta);
+            reinterpret_cast<uchar4*>(out)[o >> 2] = b;
+        } else {
+            reinterpret_cast<float4*>(out)[o >> 2] = make_float4(v.w, v.z, v.y, v.x);
         }
     }
 }
@@ -125,8 +165,22 @@ extern "C" int pv_sigproc_pack(const float* d_stokes, int nt, int nsub, int npol
     if (total == 0) return PV_OK;
     const float nrange = 255.0f;  // (int)pow(2, 8) - 1.0 (SigprocStokesWriter.cpp:27)
     const float delta = crop_max - crop_min;
-    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(total, 256), pv::sm_count() * 16LL);
     cudaStream_t s = pv::as_stream(stream);
+    const uintptr_t align = reinterpret_cast<uintptr_t>(d_stokes) | reinterpret_cast<uintptr_t>(d_out);
+    if (nchan % 4 == 0 && align % 16 == 0) {
+        const int per = nsub * nchan;
+        const long long rows = (long long)nt * npols_write;
+        const dim3 grid((unsigned)pv::ceil_div(per / 4, 256),
+                        (unsigned)std::min<long long>(rows, std::max(1LL, pv::sm_count() * 64LL / pv::ceil_div(per / 4, 256))));
+        if (nbits == 8)
+            sigproc_pack4_kernel<true><<<grid, 256, 0, s>>>(d_stokes, (int)rows, nsub, npol, nchan, npols_write,
+                                                            crop_min, crop_max, nrange, delta, d_out);
+        else
+            sigproc_pack4_kernel<false><<<grid, 256, 0, s>>>(d_stokes, (int)rows, nsub, npol, nchan, npols_write,
+                                                             crop_min, crop_max, nrange, delta, d_out);
+        return pv::check_launch("sigproc_pack4_kernel");
+    }
+    const int blocks = (int)std::min<long long>(pv::ceil_div<long long>(total, 256), pv::sm_count() * 16LL);
     if (nbits == 8)
         sigproc_pack_kernel<true><<<blocks, 256, 0, s>>>(d_stokes, nt, nsub, npol, nchan, npols_write, crop_min,
                                                          crop_max, nrange, delta, d_out);

@@ -70,17 +70,19 @@ def _stokes(rng, nt, nsub, npol, nchan):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nbits,npol,npw,crop", [(8, 1, 1, (0.0, 255.0)), (8, 4, 2, (10.0, 210.0)),
-                                                  (32, 4, 4, (0.0, 255.0)), (32, 1, 1, (0.0, 255.0))])
-def test_gpu_sigproc_pack_equals_the_oracle(pv, oracle, cuda, nbits, npol, npw, crop):
+@pytest.mark.parametrize("nbits,npol,npw,crop,nchan", [(8, 1, 1, (0.0, 255.0), 16), (8, 4, 2, (10.0, 210.0), 16),
+                                                        (32, 4, 4, (0.0, 255.0), 16), (32, 1, 1, (0.0, 255.0), 16),
+                                                        (8, 2, 1, (0.0, 255.0), 6), (32, 1, 1, (0.0, 255.0), 6)])
+def test_gpu_sigproc_pack_equals_the_oracle(pv, oracle, cuda, nbits, npol, npw, crop, nchan):
+    """Four outputs per thread when nchan % 4 == 0, one otherwise."""
     import torch
-    rng = np.random.default_rng(nbits + npol)
-    x = _stokes(rng, 37, 31, npol, 16)
+    rng = np.random.default_rng(nbits + npol + nchan)
+    x = _stokes(rng, 37, 31, npol, nchan)
     got = pv.sigproc_pack(torch.from_numpy(x).to(cuda), npw, nbits, *crop).cpu().numpy()
     want = oracle.sigproc_pack(x, npw, nbits, *crop)
     assert got.size == want.size and np.array_equal(got, want)
     if nbits == 32:  # the floats themselves, channels and subbands descending
-        first = got[: 4 * 16].view(np.float32)
+        first = got[: 4 * nchan].view(np.float32)
         assert np.array_equal(first, x[0, -1, 0, ::-1], equal_nan=True)
 
 
