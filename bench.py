@@ -341,7 +341,7 @@ def run_pv(args, cfg):
                     "ms_per_step": e2e_ms / args.steps,
                     "h2d_alone_gbs": h2d_alone_gbs,
                     "h2d_alone_ms_per_step": in_bytes / h2d_alone_gbs / 1e6,
-                    "what": "voltages copied from write-combined page-locked host buffers on the "
+                    "what": "voltages copied from page-locked host buffers on the "
                             "batch's copy stream while the previous step computes; events of the "
                             "previous step read meanwhile"},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline,
@@ -387,9 +387,9 @@ def run_batch(args, cfgs, workload):
     # ---------------- plain per-beam chain ----------------
     # every beam's chunk resident on the device; host copies for the end-to-end pass
     volts = [device_voltages(c, dev, seed(i)) for i, c in enumerate(cfgs)]
-    hosts = []  # write-combined page-locked staging: the host writes, the GPU reads
+    hosts = []  # page-locked staging (write-combined memory reads at less than half the rate here)
     for v in volts:
-        hosts.append(pv.HostBuffer(v.numel() * v.element_size(), write_combined=True))
+        hosts.append(pv.HostBuffer(v.numel() * v.element_size()))
         hosts[-1].fill_from(v)
     beams = [pv.Beam(pv_config(pv, c, prefilled=1)) for c in cfgs]
 
@@ -564,7 +564,7 @@ def run_batch(args, cfgs, workload):
                     "ms_per_step": e2e_ms / args.steps,
                     "h2d_alone_gbs": h2d_alone_gbs,
                     "h2d_alone_ms_per_step": in_bytes / h2d_alone_gbs / 1e6,
-                    "what": "voltages copied from write-combined page-locked host buffers on the "
+                    "what": "voltages copied from page-locked host buffers on the "
                             "batch's copy stream while the previous step computes; events of the "
                             "previous step read meanwhile"},
             "plain": {"value": plain_value, "e2e": plain_e2e, "steps": plain_steps,
@@ -749,7 +749,7 @@ def run_io(args):
     launches = pv.launches() - launches0
 
     # end to end: the chunk from page-locked host memory, unpacked, the voltages read back
-    hb = pv.HostBuffer(chunk_bytes, write_combined=True)
+    hb = pv.HostBuffer(chunk_bytes)
     hb.fill_from(chunks[0])
     back = torch.empty(out_i16.shape, dtype=torch.int16).pin_memory()
     torch.cuda.synchronize()

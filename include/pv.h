@@ -41,8 +41,9 @@ long long pv_kernel_launches(void);
 /* cudaMemcpyAsync with cudaMemcpyDefault (host or device pointers). */
 int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
 /* Page-locked host memory for input staging (cudaHostAlloc, portable).
- * write_combined = 1 suits buffers the host only writes and the GPU reads
- * (voltage chunks): uncached on the host, no cache snooping on transfer. */
+ * write_combined = 1 makes it write-combined (uncached on the host).  On
+ * GB300 (Grace host) the copy engine reads ordinary page-locked memory at
+ * 211 GB/s and write-combined memory at 91 GB/s: stage with 0. */
 int pv_host_alloc(void** h_ptr, long long bytes, int write_combined);
 void pv_host_free(void* h_ptr);
 /* Device memory for callers without CUDA headers (the C++ module shim). */

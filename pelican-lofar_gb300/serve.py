@@ -244,7 +244,7 @@ class Server:
 
 class BatchEngine:
     """Cohorts are pv.Batch objects (graph, pipelined) fed from page-locked,
-    write-combined staging buffers holding one synthetic sub-chunk per beam."""
+    page-locked staging buffers holding one synthetic sub-chunk per beam."""
 
     def __init__(self, pv, make_voltages, stream_factory, pipelined=True, tune=False, variant=3, store="f32"):
         self.pv = pv
@@ -266,12 +266,12 @@ class BatchEngine:
 
 
 def _staging(pv, make_voltages, cfgs):
-    """One page-locked, write-combined receive buffer per stream, holding a
+    """One page-locked receive buffer per stream, holding a
     synthetic sub-chunk of voltages."""
     out = []
     for c in cfgs:
         v = make_voltages(c)
-        hb = pv.HostBuffer(v.numel() * v.element_size(), write_combined=True)
+        hb = pv.HostBuffer(v.numel() * v.element_size())
         hb.fill_from(v)
         out.append(hb)
         del v
