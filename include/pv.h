@@ -42,8 +42,10 @@ long long pv_kernel_launches(void);
 int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
 /* Page-locked host memory for input staging (cudaHostAlloc, portable).
  * write_combined = 1 makes it write-combined (uncached on the host).  On
- * GB300 (Grace host) the copy engine reads ordinary page-locked memory at
- * 211 GB/s and write-combined memory at 91 GB/s: stage with 0. */
+ * GB300 (Grace host) the copy engine read write-combined staging at 91 GB/s
+ * and ordinary page-locked staging at up to 211 GB/s, but at 60-165 GB/s
+ * when it was allocated before the engine's device memory: stage with 0,
+ * allocated after pv_batch_create. */
 int pv_host_alloc(void** h_ptr, long long bytes, int write_combined);
 void pv_host_free(void* h_ptr);
 /* Device memory for callers without CUDA headers (the C++ module shim). */
