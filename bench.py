@@ -165,6 +165,21 @@ class ClockSampler:
 # synthetic voltages
 # ---------------------------------------------------------------------------
 
+def max_over_ranks(times_ms, device, world):
+    """Each time (ms) as the maximum over the ranks: the job ends with its slowest replica."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x) for x in times_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def job_rate(units_per_rank_step, steps, world, ms):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return units_per_rank_step * steps * world / (ms / 1e3)
+
+
 def device_voltages(cfg, dev, seed):
     """int16 [sub][pol][n][2] on the device: noise, narrowband RFI, bursts."""
     import torch
@@ -293,14 +308,11 @@ def run_pv(args, cfg):
     barrier()
     e2e_ms = e_start.elapsed_time(e_stop)
 
-    t = torch.tensor([ms, e2e_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms = float(t[0]), float(t[1])
+    ms, e2e_ms = max_over_ranks([ms, e2e_ms], dev, world)
     nbins = info["nbins"]
     units_step = cfg["tdms"] * nbins * cfg["chunk"]
-    value = units_step * args.steps * world / (ms / 1e3)
-    e2e_value = units_step * args.steps * world / (e2e_ms / 1e3)
+    value = job_rate(units_step, args.steps, world, ms)
+    e2e_value = job_rate(units_step, args.steps, world, e2e_ms)
 
     peaks, peak_src = measured_peaks()
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -511,14 +523,11 @@ def run_batch(args, cfgs, workload):
         few = sorted(range(nb), key=lambda i: cfgs[i]["dm_max"] * cfgs[i]["nsub"])[:PRECISION_BEAMS]
         precision = precision_check(pv, [cfgs[i] for i in few], args.store, dev, seed(0))
 
-    t = torch.tensor([ms, e2e_ms, plain_ms, plain_e2e_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, e2e_ms, plain_ms, plain_e2e_ms = [float(x) for x in t]
-    value = units_step * args.steps * world / (ms / 1e3)
-    e2e_value = units_step * args.steps * world / (e2e_ms / 1e3)
-    plain_value = units_step * plain_steps * world / (plain_ms / 1e3)
-    plain_e2e = units_step * plain_steps * world / (plain_e2e_ms / 1e3)
+    ms, e2e_ms, plain_ms, plain_e2e_ms = max_over_ranks([ms, e2e_ms, plain_ms, plain_e2e_ms], dev, world)
+    value = job_rate(units_step, args.steps, world, ms)
+    e2e_value = job_rate(units_step, args.steps, world, e2e_ms)
+    plain_value = job_rate(units_step, plain_steps, world, plain_ms)
+    plain_e2e = job_rate(units_step, plain_steps, world, plain_e2e_ms)
 
     peaks, peak_src = measured_peaks()
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count

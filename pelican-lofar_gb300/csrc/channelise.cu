@@ -217,6 +217,84 @@ struct RawSample<false> {
     static __device__ __forceinline__ float2 f2(float2 v) { return v; }
 };
 
+// Packed FP32 pairs for the FIR (Blackwell mul/fma .f32x2): each half is
+// rounded as the scalar operation, so the sums are bit-identical.  ptxas
+// contracts a packed multiply feeding a packed add into one fused
+// multiply-add even with .rn and --fmad false (measured on sm_103a: every
+// 8-tap sum equal to the fused chain), so the product is added as
+// fma(product, one, sum) with `one` a 1.0 the compiler cannot see: exactly
+// round(product + sum), with no multiply-add pair left to fuse.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(unsigned long long v) {
+    float2 f;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(v));
+    return f;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// round(p + s) for p, s pairs, written as fma(p, one, s) (one == 1.0)
+__device__ __forceinline__ unsigned long long add_product2(unsigned long long p, unsigned long long one,
+                                                           unsigned long long s) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(p), "l"(one), "l"(s));
+    return r;
+}
+
+// The FIR window of one lane as packed pairs.  M == 1: (re, im) of the lane's
+// channel, coefficients duplicated.  M >= 2: channels 2k and 2k+1 (strided
+// by 16) side by side, real parts and imaginary parts in separate pairs, so
+// coefficient pairs are two distinct taps' values of the same slot.
+template <int M, int T>
+struct FirWindow {
+    static constexpr int K = M == 1 ? 1 : M / 2;
+    unsigned long long re[T][K], im[T][M == 1 ? 1 : K], cf[T][K], one;
+    __device__ __forceinline__ void coeffs(const float (&c)[T][M], float unit) {
+        one = pk2(unit, unit);
+#pragma unroll
+        for (int t = 0; t < T; ++t)
+#pragma unroll
+            for (int k = 0; k < K; ++k) cf[t][k] = M == 1 ? pk2(c[t][0], c[t][0]) : pk2(c[t][2 * k], c[t][2 * k + 1]);
+    }
+    __device__ __forceinline__ void set(int q, const float2 (&v)[M]) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (M == 1) {
+                re[q][0] = pk2(v[0].x, v[0].y);
+            } else {
+                re[q][k] = pk2(v[2 * k].x, v[2 * k + 1].x);
+                im[q][k] = pk2(v[2 * k].y, v[2 * k + 1].y);
+            }
+        }
+    }
+    // y[m] = sum over taps t (oldest first: slot (q + 1 + t) & (T - 1)) of x * coeff[t]
+    __device__ __forceinline__ void fir(int q, float2 (&y)[M]) const {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            unsigned long long ar = 0ull, ai = 0ull;  // +0.0f pairs
+#pragma unroll
+            for (int t = 0; t < T; ++t) {
+                const int slot = (q + 1 + t) & (T - 1);
+                ar = add_product2(mul2(re[slot][k], cf[t][k]), one, ar);
+                if (M != 1) ai = add_product2(mul2(im[slot][k], cf[t][k]), one, ai);
+            }
+            if (M == 1) {
+                y[0] = upk2(ar);
+            } else {
+                const float2 r = upk2(ar), i = upk2(ai);
+                y[2 * k] = make_float2(r.x, i.x);
+                y[2 * k + 1] = make_float2(r.y, i.y);
+            }
+        }
+    }
+};
+
 template <int N, bool I16>
 __global__ void __launch_bounds__(128)
 chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant__ pv::ChanJob one, int njobs,
@@ -274,15 +352,18 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     }
 
     // FIR window: slot b & 7 holds block b (B0 is a multiple of 8)
-    float2 ring[T][M];
+    FirWindow<M, T> win;
+    win.coeffs(cf, J.unit);
 #pragma unroll
     for (int q = 1; q < T; ++q) {
         const int b = B0 - T + q;
+        float2 v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            if (b >= 0) ring[q][m] = RawSample<I16>::f2(in[(long long)b * N + 16 * m]);
-            else ring[q][m] = hin ? hin[(row * H + (H + b)) * N + j + 16 * m] : make_float2(0.0f, 0.0f);
+            if (b >= 0) v[m] = RawSample<I16>::f2(in[(long long)b * N + 16 * m]);
+            else v[m] = hin ? hin[(row * H + (H + b)) * N + j + 16 * m] : make_float2(0.0f, 0.0f);
         }
+        win.set(q, v);
     }
     Raw cur[T][M];
 #pragma unroll
@@ -301,25 +382,19 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
         for (int q = 0; q < T; ++q) {
             const int b = g0 + q;
             if (b >= B1) break;
+            {
+                float2 v[M];
 #pragma unroll
-            for (int m = 0; m < M; ++m) ring[q][m] = RawSample<I16>::f2(cur[q][m]);
+                for (int m = 0; m < M; ++m) v[m] = RawSample<I16>::f2(cur[q][m]);
+                win.set(q, v);
+            }
             if (b + T < B1) {
 #pragma unroll
                 for (int m = 0; m < M; ++m) cur[q][m] = in[(long long)(b + T) * N + 16 * m];
             }
-            // FIR, oldest tap (block b-7, slot q+1) first
+            // FIR, oldest tap (block b-7, slot q+1) first, in packed pairs
             float2 y[M];
-#pragma unroll
-            for (int m = 0; m < M; ++m) {
-                float re = 0.0f, im = 0.0f;
-#pragma unroll
-                for (int t = 0; t < T; ++t) {
-                    const float2 v = ring[(q + 1 + t) & (T - 1)][m];
-                    re = __fadd_rn(re, __fmul_rn(v.x, cf[t][m]));
-                    im = __fadd_rn(im, __fmul_rn(v.y, cf[t][m]));
-                }
-                y[m] = make_float2(re, im);
-            }
+            win.fir(q, y);
             // FFT stages of stride 16*hm inside the lane
 #pragma unroll
             for (int hm = M / 2; hm >= 1; hm >>= 1)
@@ -484,6 +559,7 @@ bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window
 
 int chan_job_warps(ChanJob& job) {
     job.nranges = ceil_div(job.nblocks, kRangeBlocks);
+    job.unit = 1.0f;
     return job.nsub * job.nranges;
 }
 

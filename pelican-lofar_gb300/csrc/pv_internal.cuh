@@ -38,6 +38,7 @@ struct ChanJob {
     long long warp_begin;    // first warp of this job in the launch
     int nsub, nblocks, window, nu, nranges;
     int beam;                // index into the batch's BeamStep array
+    float unit;              // 1.0f, unknown to the compiler (set by chan_job_warps): see FirWindow
 };
 bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window, int bin, int nblocks);
 int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
