@@ -324,9 +324,12 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         }
         if (active) {
             const int c_end = min(CS, a.nchan - st * CS);
+            // lane j computes channel j's row offset once per stage; the warp
+            // takes it by shuffle (no shared-memory wavefront per channel)
+            const int my_off =
+                lane < c_end ? min(pv_shift(meta_k[b * CS + lane], dv) - meta_off[b * CS + lane], a.slot - TT) : 0;
             for (int j = 0; j < c_end; ++j) {
-                const float k = meta_k[b * CS + j];
-                const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], a.slot - TT);
+                const int off = __shfl_sync(0xffffffffu, my_off, j);
                 const float* row = slots + (size_t)(b * CS + j) * a.slot + off + lane;
 #pragma unroll
                 for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
@@ -570,9 +573,11 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 }
                 if (active) {
                     const int c_end = min(CS, nchan - st * CS);
+                    const int my_off =
+                        lane < c_end ? min(pv_shift(meta_k[b * CS + lane], dv) - meta_off[b * CS + lane], slot - TT - 4)
+                                     : 0;
                     for (int j = 0; j < c_end; ++j) {
-                        const float k = meta_k[b * CS + j];
-                        const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT - 4);
+                        const int off = __shfl_sync(0xffffffffu, my_off, j);
                         const unsigned* wr =
                             reinterpret_cast<const unsigned*>(slots + (size_t)(b * CS + j) * slot) + (off >> 2) + lane;
                         const int m = off & 3;
@@ -622,9 +627,11 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             }
             if (active) {
                 const int c_end = min(CS, nchan - st * CS);
+                // lane j computes channel j's row offset once per stage (see the single-beam kernel)
+                const int my_off =
+                    lane < c_end ? min(pv_shift(meta_k[b * CS + lane], dv) - meta_off[b * CS + lane], slot - TT - 4) : 0;
                 for (int j = 0; j < c_end; ++j) {
-                    const float k = meta_k[b * CS + j];
-                    const int off = min(pv_shift(k, dv) - meta_off[b * CS + j], slot - TT - 4);
+                    const int off = __shfl_sync(0xffffffffu, my_off, j);
                     const unsigned char* rowb = slots + (size_t)(b * CS + j) * slot * E;
                     if (STORE == PV_STORE_F32) {
                         const float* row = reinterpret_cast<const float*>(rowb) + off + lane;
