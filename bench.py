@@ -165,6 +165,25 @@ class ClockSampler:
 # synthetic voltages
 # ---------------------------------------------------------------------------
 
+def udp_subbands(cfg):
+    """Subbands per LOFAR packet stream for a beam: 61 for 16-bit beamlets, or all of a narrower beam."""
+    return 61 if cfg["nsub"] % 61 == 0 else cfg["nsub"]
+
+
+def to_packets(v, per_packet, ts0=1300000000):
+    """int16 voltages [sub][pol][n][2] on the device -> the nsub/per_packet streams of variable-size
+    LOFAR packets (16-byte header, [subband][16 samples][pol] complex int16), one after another."""
+    import torch
+    nsub, _, n, _ = v.shape
+    streams, npk = nsub // per_packet, n // 16
+    body = v.view(streams, per_packet, 2, npk, 16, 2).permute(0, 3, 1, 4, 2, 5).contiguous()
+    body = body.view(torch.uint8).view(streams, npk, per_packet * 16 * 2 * 4)
+    hdr = torch.zeros((streams, npk, 4), dtype=torch.int32, device=v.device)
+    hdr[:, :, 2] = ts0
+    hdr[:, :, 3] = 16 * torch.arange(npk, device=v.device, dtype=torch.int32)
+    return torch.cat([hdr.view(torch.uint8).view(streams, npk, 16), body], dim=2).reshape(-1)
+
+
 def max_over_ranks(times_ms, device, world):
     """Each time (ms) as the maximum over the ranks: the job ends with its slowest replica."""
     import torch
@@ -398,8 +417,20 @@ def run_batch(args, cfgs, workload):
 
     # ---------------- plain per-beam chain ----------------
     # every beam's chunk resident on the device; host copies for the end-to-end pass
-    volts = [device_voltages(c, dev, seed(i)) for i, c in enumerate(cfgs)]
-    beams = [pv.Beam(pv_config(pv, c, prefilled=1)) for c in cfgs]
+    udp = args.ingest == "udp"
+
+    def beam_cfg(c):
+        if not udp:
+            return pv_config(pv, c, prefilled=1)
+        p = udp_subbands(c)
+        return pv_config(pv, c, prefilled=1, udp_packet_bytes=16 + p * 16 * 2 * 4, udp_subbands=p)
+
+    def chunk_input(i, c):  # one step's input of beam i: int16 voltages, or the same as packets
+        v = device_voltages(c, dev, seed(i))
+        return to_packets(v, udp_subbands(c)) if udp else v
+
+    volts = [chunk_input(i, c) for i, c in enumerate(cfgs)]
+    beams = [pv.Beam(beam_cfg(c)) for c in cfgs]
     # page-locked staging, allocated after the arm's device memory: on this host the copy engine
     # read staging allocated first at 60-70 GB/s and staging allocated after the engine at
     # 211 GB/s (write-combined staging: 91 GB/s)
@@ -438,11 +469,11 @@ def run_batch(args, cfgs, workload):
     torch.cuda.empty_cache()
 
     # ---------------- batched engine ----------------
-    batch = pv.Batch([pv_config(pv, c, prefilled=1) for c in cfgs], tune=True, graph=True, timing=True,
+    batch = pv.Batch([beam_cfg(c) for c in cfgs], tune=True, graph=True, timing=True,
                      pipelined=not args.unpipelined, store=args.store)
     bhosts = []  # the batch's staging, allocated after the batch (see the plain arm's)
     for i, c in enumerate(cfgs):
-        v = device_voltages(c, dev, seed(i))
+        v = chunk_input(i, c)
         batch.set_input(i, v, stream=stream)
         bhosts.append(pv.HostBuffer(v.numel() * v.element_size()))
         bhosts[-1].fill_from(v, stream=stream)
@@ -563,6 +594,8 @@ def run_batch(args, cfgs, workload):
             "data": "synthetic: seeded Gaussian int16 voltages with narrowband and burst RFI and "
                     "dispersed pulses",
             "config": {"workload": workload, "beams": nb, "chunk": cfgs[0]["chunk"],
+                       "ingest": ("LOFAR UDP packets (variable size, 61 or all subbands per stream) "
+                                  "read by the channeliser" if udp else "int16 voltages [sub][pol][t]"),
                        "nchan_total": sum(c["nsub"] * c["nchan_sub"] for c in cfgs),
                        "tdms_total": sum(c["tdms"] for c in cfgs), "ring_gb": ring_gb,
                        "ring_storage": args.store,
@@ -1032,6 +1065,8 @@ def main():
     ap.add_argument("--grace", type=float, default=30.0, help="serve128: seconds to drain")
     ap.add_argument("--budget-gb", type=float, default=160.0, help="serve128: HBM budget")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ingest", default="voltages", choices=["voltages", "udp"],
+                    help="batch64: each step's input as int16 voltages or as LOFAR UDP packet streams")
     ap.add_argument("--unpipelined", action="store_true",
                     help="batch64: one dedispersion launch per step after the clippers (the same work)")
     ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
@@ -1078,6 +1113,8 @@ def main():
     workload = "batch%d-mixed-beams-4096samp" % args.beams
     if args.store != "f32":
         workload += "-%s-rings" % args.store
+    if args.ingest == "udp":
+        workload += "-udp-packets"
     if args.beams != 64 or args.chunk:
         workload += "-reduced(beams=%d,chunk=%d)" % (args.beams, cfgs[0]["chunk"])
     if args.impl == "reference":

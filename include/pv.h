@@ -320,6 +320,16 @@ typedef struct {
                                  sample 0 is then the start of that silence and the first
                                  chunk's data starts at lag*chunk.  0: the reference's
                                  behaviour, the first window waits for lag+1 chunks. */
+    int udp_packet_bytes;     /* > 0: a chunk is LOFAR UDP packets (pv_udp_config layout:
+                                 16-byte header, [subband][16 samples][2 pols] complex int16,
+                                 padded to this size; 16 + udp_subbands*128 for variable-size
+                                 packets, 8148 for fixed), read by the channeliser in place
+                                 of pv_udp_unpack's int16 voltages.  Needs 16, 32 or 64
+                                 channels per subband and 8 taps. */
+    int udp_subbands;         /* subbands per packet; the nsub / udp_subbands packet streams
+                                 of a chunk follow each other, each chunk*int_time*nchan_sub/16
+                                 packets long.  pv_beam_input_bytes is then the packet bytes
+                                 of a chunk, and the in_int16 arguments do not apply. */
 } pv_beam_config;
 
 typedef struct pv_beam pv_beam;

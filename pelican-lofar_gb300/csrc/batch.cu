@@ -406,6 +406,8 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         j.window = x->cfg.int_time;
         j.nu = x->cfg.chunk;
         j.beam = i;
+        j.pkt_bytes = x->cfg.udp_packet_bytes;
+        j.pkt_nsub = x->cfg.udp_subbands;
         j.warp_begin = b->chan[k].nwarps;
         b->chan[k].nwarps += pv::chan_job_warps(j);
         cj[k].push_back(j);
@@ -763,7 +765,11 @@ extern "C" long long pv_batch_footprint(const pv_beam_config* c, int flags) {
     bytes += 4LL * c->tdms * c->chunk;                                 // dedispersed window
     bytes += (long long)sizeof(pv_event) * cap;                        // events
     bytes += (long long)pv::analyse_scratch_bytes(c->tdms, c->chunk, c->bin_pow2) + 256;
-    bytes += 2LL * c->nsub * 2 * c->chunk * c->int_time * c->nchan_sub * 4;  // two input buffers
+    if (c->udp_packet_bytes > 0 && c->udp_subbands > 0)  // two input buffers of packet streams
+        bytes += 2LL * (c->nsub / c->udp_subbands) * c->chunk * c->int_time * (c->nchan_sub / 16) *
+                 c->udp_packet_bytes;
+    else
+        bytes += 2LL * c->nsub * 2 * c->chunk * c->int_time * c->nchan_sub * 4;  // two input buffers
     bytes += 2LL * 2 * (long long)sizeof(float2) * c->nsub * 7 * c->nchan_sub;  // two PPF histories
     bytes += 16LL * c->history + 12LL * nbins;                        // clipper state, bandpass
     return bytes;

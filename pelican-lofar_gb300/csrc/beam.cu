@@ -47,6 +47,14 @@ int beam_create(pv_beam** out, const pv_beam_config* c, int extra, int elem) {
         pv::set_error("pv_beam_create: invalid beam configuration");
         return PV_ERR_CONFIG;
     }
+    if (c->udp_packet_bytes > 0 &&
+        (c->udp_subbands <= 0 || c->nsub % c->udp_subbands != 0 || c->udp_packet_bytes % 4 != 0 ||
+         c->udp_packet_bytes < 16 + c->udp_subbands * 16 * 2 * 4 ||
+         (c->nchan_sub != 16 && c->nchan_sub != 32 && c->nchan_sub != 64) || c->ntaps != 8)) {
+        pv::set_error("pv_beam_create: packet input needs 16, 32 or 64 channels, 8 taps, subbands per packet "
+                      "dividing nsub and a packet size that is a multiple of 4 holding them");
+        return PV_ERR_CONFIG;
+    }
     auto* b = new pv_beam;
     b->cfg = *c;
     b->cfg.bp_text = nullptr;
@@ -131,8 +139,11 @@ extern "C" int pv_beam_info(const pv_beam* b, long long* h_info8) {
 
 extern "C" long long pv_beam_input_bytes(const pv_beam* b, int in_int16) {
     if (!b) return -1;
-    return (long long)b->cfg.nsub * 2 * b->cfg.chunk * b->cfg.int_time * b->cfg.nchan_sub *
-           (in_int16 ? 4 : 8);
+    const pv_beam_config& c = b->cfg;
+    if (c.udp_packet_bytes > 0)  // the packet streams of one chunk
+        return (long long)(c.nsub / c.udp_subbands) * c.chunk * c.int_time * (c.nchan_sub / 16) *
+               c.udp_packet_bytes;
+    return (long long)c.nsub * 2 * c.chunk * c.int_time * c.nchan_sub * (in_int16 ? 4 : 8);
 }
 
 extern "C" int pv_beam_process(pv_beam* b, const void* d_voltages, int in_int16, void* stream) {
@@ -148,8 +159,13 @@ extern "C" int pv_beam_process(pv_beam* b, const void* d_voltages, int in_int16,
     };
     int nu = 0;
     mark(0);
-    PV_TRY(pv_channelise(b->ppf, d_voltages, in_int16, c.nsub, nblocks, 1, c.int_time, c.int_chan,
-                         b->d_fb, &nu, stream));
+    if (c.udp_packet_bytes > 0) {  // the chunk is packets: in_int16 does not apply
+        PV_TRY(pv::channelise_stokes_i(b->ppf, d_voltages, c.nsub, nblocks, c.int_time, c.int_chan, b->d_fb, &nu,
+                                       c.udp_packet_bytes, c.udp_subbands, s));
+    } else {
+        PV_TRY(pv_channelise(b->ppf, d_voltages, in_int16, c.nsub, nblocks, 1, c.int_time, c.int_chan,
+                             b->d_fb, &nu, stream));
+    }
     if (nu != c.chunk) {
         pv::set_error("pv_beam_process: integration produced %d of %d samples", nu, c.chunk);
         return PV_ERR_STATE;

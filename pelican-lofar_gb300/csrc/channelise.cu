@@ -328,7 +328,24 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     const float2* hin = J.hist[par];
     float2* hout = J.hist[par ^ 1];
     const void* src = (par && J.in_odd) ? J.in_odd : J.in;
-    const Raw* in = reinterpret_cast<const Raw*>(src) + row * nblocks * N + j;
+    // Raw element (block b, channel-lane m) at in[b * sb + m * sm].  Voltages: the row
+    // [sub][pol][t] with t = b*N + j + 16m.  Packets (int16, 16 samples per packet, subband-major
+    // [subband][t][pol] after a 16-byte header; AdapterTimeSeriesDataSet.cpp:246-288): sample t is
+    // time j of packet b*(N/16) + m of the subband's stream.
+    const Raw* in;
+    long long sb, sm;
+    if (I16 && J.pkt_bytes > 0) {
+        const long long pw = J.pkt_bytes / 4;  // 4-byte words per packet
+        const long long npk = (long long)nblocks * (N / 16);
+        const int stream = s / J.pkt_nsub, ls = s - stream * J.pkt_nsub;
+        in = reinterpret_cast<const Raw*>(src) + stream * npk * pw + 4 + (ls * 16 + j) * 2 + pol;
+        sb = (N / 16) * pw;
+        sm = pw;
+    } else {
+        in = reinterpret_cast<const Raw*>(src) + row * nblocks * N + j;
+        sb = N;
+        sm = 16;
+    }
 
     float cf[T][M];
 #pragma unroll
@@ -360,7 +377,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
         float2 v[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            if (b >= 0) v[m] = RawSample<I16>::f2(in[(long long)b * N + 16 * m]);
+            if (b >= 0) v[m] = RawSample<I16>::f2(in[(long long)b * sb + m * sm]);
             else v[m] = hin ? hin[(row * H + (H + b)) * N + j + 16 * m] : make_float2(0.0f, 0.0f);
         }
         win.set(q, v);
@@ -370,7 +387,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     for (int q = 0; q < T; ++q)
 #pragma unroll
         for (int m = 0; m < M; ++m)
-            if (B0 + q < B1) cur[q][m] = in[(long long)(B0 + q) * N + 16 * m];
+            if (B0 + q < B1) cur[q][m] = in[(long long)(B0 + q) * sb + m * sm];
 
     float acc[M];
 #pragma unroll
@@ -390,7 +407,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
             }
             if (b + T < B1) {
 #pragma unroll
-                for (int m = 0; m < M; ++m) cur[q][m] = in[(long long)(b + T) * N + 16 * m];
+                for (int m = 0; m < M; ++m) cur[q][m] = in[(long long)(b + T) * sb + m * sm];
             }
             // FIR, oldest tap (block b-7, slot q+1) first, in packed pairs
             float2 y[M];
@@ -445,7 +462,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
 #pragma unroll
             for (int m = 0; m < M; ++m)
                 hout[(row * H + q) * N + j + 16 * m] =
-                    RawSample<I16>::f2(in[(long long)(nblocks - H + q) * N + 16 * m]);
+                    RawSample<I16>::f2(in[(long long)(nblocks - H + q) * sb + m * sm]);
     }
 }
 
@@ -587,7 +604,7 @@ namespace {
 
 int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol, int nblocks,
                    int mode, float2* d_spectra, float* d_stokes, int nstokes, int window, int bin,
-                   int* nu_out, cudaStream_t s) {
+                   int* nu_out, cudaStream_t s, long long pkt_bytes = 0, int pkt_nsub = 0) {
     if (!h || !d_in || nsub <= 0 || npol <= 0 || nblocks <= 0) {
         pv::set_error("PPFChanneliser: Empty time data blob");
         return PV_ERR_ARG;
@@ -608,8 +625,12 @@ int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol
     PV_TRY(prepare_history(h, nsub, npol, s));
     const int w = mode == 1 ? std::min(window, nblocks) : 1;  // StokesIntegrator.cpp:53-59
     const int nu = mode == 1 ? nblocks / w : 0;
-    if (mode == 1 && pv::chan_fast_supported(h->nchan, h->ntaps, npol, nstokes, w, bin, nblocks) &&
-        getenv("PV_CHAN_GENERIC") == nullptr) {
+    const bool fast = mode == 1 && pv::chan_fast_supported(h->nchan, h->ntaps, npol, nstokes, w, bin, nblocks);
+    if (pkt_bytes > 0 && (!fast || !in_int16)) {
+        pv::set_error("channelise: packet input needs int16 samples, 16/32/64 channels, 8 taps, Stokes I");
+        return PV_ERR_ARG;
+    }
+    if (fast && (pkt_bytes > 0 || getenv("PV_CHAN_GENERIC") == nullptr)) {
         pv::ChanJob job{};
         job.in = d_in;
         job.hist[0] = h->have_hist ? h->d_hist[h->cur] : nullptr;
@@ -621,6 +642,8 @@ int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol
         job.nblocks = nblocks;
         job.window = w;
         job.nu = nu;
+        job.pkt_bytes = pkt_bytes;
+        job.pkt_nsub = pkt_nsub;
         const long long nwarps = pv::chan_job_warps(job);
         PV_TRY(pv::launch_chan_fast(h->nchan, in_int16, nullptr, job, 1, nwarps, nullptr, s));
         h->cur ^= 1;
@@ -739,6 +762,12 @@ extern "C" int pv_ppf_run(pv_ppf* h, const float* d_in, int nsub, int npol, int 
                           float* d_out, void* stream) {
     return run_channelise(h, d_in, 0, nsub, npol, nblocks, 0, reinterpret_cast<float2*>(d_out),
                           nullptr, 1, 1, 1, nullptr, pv::as_stream(stream));
+}
+
+int pv::channelise_stokes_i(pv_ppf* h, const void* d_in, int nsub, int nblocks, int window, int bin, float* d_stokes,
+                            int* nu_out, long long pkt_bytes, int pkt_nsub, cudaStream_t s) {
+    return run_channelise(h, d_in, 1, nsub, 2, nblocks, 1, nullptr, d_stokes, 1, window, bin, nu_out, s, pkt_bytes,
+                          pkt_nsub);
 }
 
 extern "C" int pv_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int nblocks,

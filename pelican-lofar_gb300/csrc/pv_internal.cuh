@@ -39,8 +39,14 @@ struct ChanJob {
     int nsub, nblocks, window, nu, nranges;
     int beam;                // index into the batch's BeamStep array
     float unit;              // 1.0f, unknown to the compiler (set by chan_job_warps): see FirWindow
+    long long pkt_bytes;     // > 0: `in` holds LOFAR packets of this size (int16, 16 samples each)
+    int pkt_nsub;            // subbands per packet; the nsub/pkt_nsub streams follow each other
 };
 bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window, int bin, int nblocks);
+// pv_channelise (Stokes I, int16 input) with the input in the LOFAR packet layout when
+// pkt_bytes > 0 (the register channeliser only)
+int channelise_stokes_i(pv_ppf* h, const void* d_in, int nsub, int nblocks, int window, int bin, float* d_stokes,
+                        int* nu_out, long long pkt_bytes, int pkt_nsub, cudaStream_t s);
 int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
 // bs == null: one job, always active, input `in`, history hist[0] -> hist[1]
 int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,

@@ -354,13 +354,15 @@ class BeamConfig(C.Structure):
                 ("bp_text", C.c_char_p), ("cr", C.c_float), ("sr", C.c_float),
                 ("history", C.c_int), ("zero_dming", C.c_int), ("rms_from_mean", C.c_int),
                 ("band_matching", C.c_int), ("rfi_active", C.c_int), ("debug_taps", C.c_int),
-                ("timing", C.c_int), ("prefilled", C.c_int)]
+                ("timing", C.c_int), ("prefilled", C.c_int), ("udp_packet_bytes", C.c_int),
+                ("udp_subbands", C.c_int)]
 
 
 def beam_config(**kw):
     d = dict(ntaps=8, window=WINDOWS["kaiser"], int_time=4, int_chan=1, dm_low=0.0, threshold=6.0,
              bin_pow2=6, event_capacity=0, cr=10.0, sr=4.0, history=10, zero_dming=0,
-             rms_from_mean=1, band_matching=1, rfi_active=1, debug_taps=0, timing=0, prefilled=0)
+             rms_from_mean=1, band_matching=1, rfi_active=1, debug_taps=0, timing=0, prefilled=0,
+             udp_packet_bytes=0, udp_subbands=0)
     d.update(kw)
     if isinstance(d.get("window"), str):
         d["window"] = WINDOWS[d["window"]]

@@ -141,3 +141,79 @@ def test_gpu_unpacked_packets_feed_the_beam_chain(pv, cuda):
         torch.cuda.synchronize()
         outs.append(pv.device_array(b.buffers()[0], (chunk_len, nsub * nch)).cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def _beam_packets(rng, nsub, per_packet, npk, fixed):
+    """One chunk of a beam as packet streams (nsub / per_packet of them, one after another) and the
+    same samples as int16 voltages [sub][pol][t][2]."""
+    chunks, volts = [], []
+    for _ in range(nsub // per_packet):
+        c, data = make_chunk(rng, npk, per_packet, 16, 2, 16, fixed)
+        chunks.append(c)
+        volts.append(data.transpose(1, 3, 0, 2, 4).reshape(per_packet, 2, npk * 16, 2))
+    return np.concatenate(chunks), np.ascontiguousarray(np.concatenate(volts))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nch,fixed", [(16, True), (32, False), (64, True)])
+def test_gpu_packet_fed_beam_equals_voltage_fed_beam(pv, cuda, nch, fixed):
+    """The channeliser reads the packets in place: filterbank, dedispersed window and events
+    equal those of the same beam given the unpacked voltages, chunk after chunk."""
+    import torch
+    from test_gpu_batch import beam_kw
+    rng = np.random.default_rng(nch)
+    nsub, per_packet, chunk = 6, 3, 256
+    npk = chunk * 4 * nch // 16
+    psize = FIXED if fixed else HEADER + per_packet * 16 * 2 * 4
+    kw = dict(beam_kw(nsub, nch, 24, 1.0, chunk=chunk), rfi_active=0, bp_text=None, prefilled=1)
+    b_pkt = pv.Beam(pv.beam_config(**dict(kw, udp_packet_bytes=psize, udp_subbands=per_packet)))
+    b_vol = pv.Beam(pv.beam_config(**kw))
+    assert b_pkt.input_bytes() == (nsub // per_packet) * npk * psize
+    for _ in range(3):
+        pk, v = _beam_packets(rng, nsub, per_packet, npk, fixed)
+        b_pkt.process(torch.from_numpy(pk).to(cuda))
+        b_vol.process(torch.from_numpy(v.reshape(nsub, 2, -1)).to(cuda))
+        torch.cuda.synchronize()
+        fa, _, oa, _ = b_pkt.buffers()
+        fb, _, ob, _ = b_vol.buffers()
+        nbins = nsub * nch
+        assert np.array_equal(pv.device_array(fa, (chunk, nbins)).cpu().numpy(),
+                              pv.device_array(fb, (chunk, nbins)).cpu().numpy())
+        ea, na, firsta = b_pkt.events()
+        eb, nb, firstb = b_vol.events()
+        assert (na, firsta) == (nb, firstb) and np.array_equal(ea, eb)
+        assert np.array_equal(pv.device_array(oa, (24, chunk)).cpu().numpy(),
+                              pv.device_array(ob, (24, chunk)).cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_gpu_batch_with_packet_fed_beam_equals_beams_alone(pv, cuda):
+    import torch
+    from test_gpu_batch import beam_kw
+    rng = np.random.default_rng(31)
+    chunk = 256
+    kw_a = dict(beam_kw(4, 16, 24, 1.0, chunk=chunk), rfi_active=0, bp_text=None, prefilled=1,
+                udp_packet_bytes=FIXED, udp_subbands=2)
+    kw_b = dict(beam_kw(3, 32, 16, 0.7, chunk=chunk), rfi_active=0, bp_text=None, prefilled=1)
+    cfgs = [pv.beam_config(**kw_a), pv.beam_config(**kw_b)]
+    batch = pv.Batch(cfgs, tune=False, graph=True, pipelined=True)
+    alone = [pv.Beam(c) for c in cfgs]
+    hist = []
+    for step in range(4):
+        pk, _ = _beam_packets(rng, 4, 2, chunk * 4 * 16 // 16, True)
+        v = rng.normal(0.0, 16.0, (3, 2, chunk * 4 * 32 * 2))
+        ins = [torch.from_numpy(pk).to(cuda), torch.from_numpy(np.rint(v).astype(np.int16)).to(cuda)]
+        rec = []
+        for i, x in enumerate(ins):
+            batch.set_input(i, x)
+            alone[i].process(x)
+        batch.run()
+        torch.cuda.synchronize()
+        for i, b in enumerate(alone):
+            rec.append(b.events())
+        hist.append(rec)
+        if step >= 1:  # pipelined: a window's events come one step later
+            for i in range(2):
+                ev, n, first = batch.events(i)
+                ea, na, firsta = hist[step - 1][i]
+                assert (n, first) == (na, firsta) and np.array_equal(ev, ea)
