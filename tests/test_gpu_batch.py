@@ -230,3 +230,17 @@ def test_batch_with_idle_beams_equals_beams_alone(pv, cuda, mix_configs, pipelin
             seen[i] += 1
     for i in range(n):
         assert seen[i] == len(want[i]) > 0  # every window the beam completed alone came out once
+
+
+def test_batch_of_twelve_beams_in_three_clipper_classes_equals_beams_alone(pv, cuda):
+    """Twelve beams whose clippers fall in all three CTA-size classes (up to 1024, 4096 and more
+    channels), pipelined under one graph: every window and event list equals the beam's alone."""
+    rng = np.random.default_rng(121)
+    shapes = [(4, 16), (6, 32), (3, 64), (8, 16),       # 256-thread class
+              (40, 32), (20, 64), (96, 16), (50, 32),   # 512-thread class
+              (70, 64), (300, 16), (140, 32), (80, 64)]  # 1024-thread class
+    mix = [calibrated(pv, cuda, beam_kw(ns, nc, 16 + 4 * i, 0.05 + 0.02 * i, chunk=256), rng)
+           for i, (ns, nc) in enumerate(shapes)]
+    parts = {pv.load().pv_rfi_parts(ns * nc) for ns, nc in shapes}
+    assert len(parts) == 3
+    _compare_with_beams_alone(pv, cuda, mix, False, True, 0, True, True)
