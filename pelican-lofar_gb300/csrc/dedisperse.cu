@@ -385,6 +385,15 @@ __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsig
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
+// Mixed-precision add (sm_100+): float(h) + a with one rounding, h an FP16 bit pattern
+__device__ __forceinline__ float add_f16(unsigned short h, float a) {
+    float r;
+    asm("add.rn.f32.f16 %0, %1, %2;" : "=f"(r) : "h"(h), "f"(a));
+    return r;
+}
+__device__ __forceinline__ void f16_halves(unsigned w, unsigned short& lo, unsigned short& hi) {
+    asm("mov.b32 {%0, %1}, %2;" : "=h"(lo), "=h"(hi) : "r"(w));
+}
 // byte i of w as float (q - 128): 0x4B0000qq is 2^23 + q exactly
 __device__ __forceinline__ float u8_centered(unsigned w, int i) {
     return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u | (unsigned)i)) - 8388736.0f;
@@ -638,22 +647,28 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
 #pragma unroll
                         for (int r = 0; r < R; ++r) acc[r] = __fadd_rn(acc[r], row[32 * r]);
                     } else if (STORE == PV_STORE_F16) {
+                        // each half is added to its FP32 sum by one mixed-precision add
+                        // (exactly fadd(float(h), sum)); odd offsets take the high half of
+                        // one word and the low half of the next
                         const unsigned* w = reinterpret_cast<const unsigned*>(rowb);
                         if ((off & 1) == 0) {
                             const unsigned* wr = w + (off >> 1) + lane;
 #pragma unroll
                             for (int p = 0; p < R / 2; ++p) {
-                                const unsigned x = wr[32 * p];
-                                const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&x));
-                                acc2[p] = f2_add(acc2[p], f2_pack(f.x, f.y));
+                                unsigned short lo, hi;
+                                f16_halves(wr[32 * p], lo, hi);
+                                acc[2 * p] = add_f16(lo, acc[2 * p]);
+                                acc[2 * p + 1] = add_f16(hi, acc[2 * p + 1]);
                             }
                         } else {
                             const unsigned* wr = w + ((off - 1) >> 1) + lane;
 #pragma unroll
                             for (int p = 0; p < R / 2; ++p) {
-                                const unsigned x = __byte_perm(wr[32 * p], wr[32 * p + 1], 0x5432u);
-                                const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&x));
-                                acc2[p] = f2_add(acc2[p], f2_pack(f.x, f.y));
+                                unsigned short lo0, hi0, lo1, hi1;
+                                f16_halves(wr[32 * p], lo0, hi0);
+                                f16_halves(wr[32 * p + 1], lo1, hi1);
+                                acc[2 * p] = add_f16(hi0, acc[2 * p]);
+                                acc[2 * p + 1] = add_f16(lo1, acc[2 * p + 1]);
                             }
                         }
                     } else {
@@ -688,7 +703,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
 #pragma unroll
                 for (int p = 0; p < R / 2; ++p) {
                     const long long t = tt.t0 + 64 * p + 2 * lane;
-                    if (t < J.nout) *reinterpret_cast<float2*>(o + t) = f2_unpack(acc2[p]);
+                    if (t < J.nout) *reinterpret_cast<float2*>(o + t) = make_float2(acc[2 * p], acc[2 * p + 1]);
                 }
             } else {
                 const float os = *J.off_sum;
