@@ -362,7 +362,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
 // dedispersed (window w reads ring columns from w*chunk on).  All waits are
 // bounded as in dedisperse_tma_kernel.
 // ---------------------------------------------------------------------------
-// Packed FP32 pairs (Blackwell add/fma .f32x2): two independent IEEE
+// Packed FP32 pairs (Blackwell fma .f32x2): two independent IEEE
 // operations, each rounded as the scalar one.
 __device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
     unsigned long long r;
@@ -373,11 +373,6 @@ __device__ __forceinline__ float2 f2_unpack(unsigned long long v) {
     float2 f;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(v));
     return f;
-}
-__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
 }
 __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
                                                      unsigned long long c) {
