@@ -99,6 +99,7 @@ struct pv_batch {
     std::vector<float2*> d_hist;  // two per beam
     struct ChanClass {
         int nchan = 0, njobs = 0;
+        int packets = 0;  // the class's beams take LOFAR packets (one kernel per input layout)
         long long nwarps = 0;
         pv::ChanJob* d_jobs = nullptr;
     };
@@ -206,7 +207,8 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
     PV_TRY(pv::check_launch("plan_kernel"));
     PV_TRY(mark(0, s));
     for (auto& c : b->chan)
-        PV_TRY(pv::launch_chan_fast(c.nchan, 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps, b->d_bs, s));
+        PV_TRY(pv::launch_chan_fast(c.nchan, c.packets ? 2 : 1, c.d_jobs, pv::ChanJob{}, c.njobs, c.nwarps,
+                                    b->d_bs, s));
     PV_TRY(mark(1, s));
     const int nk = b->rfi ? pv::rfi_batch_launches(b->rfi) : 0;
     int rfi_ctas = 0;
@@ -386,11 +388,13 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
         int nchan = 0, ntaps = 0;
         rc = pv::ppf_tables(x->ppf, &coeffs, &tw, &nchan, &ntaps);
         if (rc != PV_OK) return fail(rc);
+        const int packets = x->cfg.udp_packet_bytes > 0 ? 1 : 0;
         size_t k = 0;
-        while (k < b->chan.size() && b->chan[k].nchan != nchan) ++k;
+        while (k < b->chan.size() && (b->chan[k].nchan != nchan || b->chan[k].packets != packets)) ++k;
         if (k == b->chan.size()) {
             b->chan.emplace_back();
             b->chan[k].nchan = nchan;
+            b->chan[k].packets = packets;
             cj.emplace_back();
         }
         pv::ChanJob j{};

@@ -295,7 +295,7 @@ struct FirWindow {
     }
 };
 
-template <int N, bool I16>
+template <int N, bool I16, bool PKT>
 __global__ void __launch_bounds__(128)
 chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant__ pv::ChanJob one, int njobs,
                      long long nwarps, const pv::BeamStep* __restrict__ bs) {
@@ -334,7 +334,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     // time j of packet b*(N/16) + m of the subband's stream.
     const Raw* in;
     long long sb, sm;
-    if (I16 && J.pkt_bytes > 0) {
+    if (PKT) {
         const long long pw = J.pkt_bytes / 4;  // 4-byte words per packet
         const long long npk = (long long)nblocks * (N / 16);
         const int stream = s / J.pkt_nsub, ls = s - stream * J.pkt_nsub;
@@ -580,14 +580,18 @@ int chan_job_warps(ChanJob& job) {
     return job.nsub * job.nranges;
 }
 
-int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
+int launch_chan_fast(int nchan, int input, const ChanJob* d_jobs, const ChanJob& one, int njobs,
                      long long nwarps, const BeamStep* bs, cudaStream_t s) {
     if (nwarps <= 0) return PV_OK;
     const unsigned grid = (unsigned)ceil_div<long long>(nwarps, 4);
 #define PV_CHAN_FAST(NN)                                                                         \
     if (nchan == NN) {                                                                           \
-        if (in_int16) chan_stokes_i_kernel<NN, true><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);  \
-        else chan_stokes_i_kernel<NN, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);          \
+        if (input == 2)                                                                          \
+            chan_stokes_i_kernel<NN, true, true><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);  \
+        else if (input == 1)                                                                     \
+            chan_stokes_i_kernel<NN, true, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs); \
+        else                                                                                     \
+            chan_stokes_i_kernel<NN, false, false><<<grid, 128, 0, s>>>(d_jobs, one, njobs, nwarps, bs);\
         return check_launch("chan_stokes_i_kernel");                                            \
     }
     PV_CHAN_FAST(16)
@@ -645,7 +649,8 @@ int run_channelise(pv_ppf* h, const void* d_in, int in_int16, int nsub, int npol
         job.pkt_bytes = pkt_bytes;
         job.pkt_nsub = pkt_nsub;
         const long long nwarps = pv::chan_job_warps(job);
-        PV_TRY(pv::launch_chan_fast(h->nchan, in_int16, nullptr, job, 1, nwarps, nullptr, s));
+        PV_TRY(pv::launch_chan_fast(h->nchan, pkt_bytes > 0 ? 2 : (in_int16 ? 1 : 0), nullptr, job, 1, nwarps,
+                                    nullptr, s));
         h->cur ^= 1;
         h->have_hist = true;
         if (nu_out) *nu_out = nu;

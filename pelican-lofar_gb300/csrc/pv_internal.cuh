@@ -48,8 +48,9 @@ bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window
 int channelise_stokes_i(pv_ppf* h, const void* d_in, int nsub, int nblocks, int window, int bin, float* d_stokes,
                         int* nu_out, long long pkt_bytes, int pkt_nsub, cudaStream_t s);
 int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
-// bs == null: one job, always active, input `in`, history hist[0] -> hist[1]
-int launch_chan_fast(int nchan, int in_int16, const ChanJob* d_jobs, const ChanJob& one, int njobs,
+// bs == null: one job, always active, input `in`, history hist[0] -> hist[1].
+// input: 0 complex float voltages, 1 int16 voltages, 2 int16 LOFAR packets (pkt_bytes of every job)
+int launch_chan_fast(int nchan, int input, const ChanJob* d_jobs, const ChanJob& one, int njobs,
                      long long nwarps, const BeamStep* bs, cudaStream_t s);
 // coefficient [T][N] and twiddle [N/2] tables of a PPF handle
 int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
