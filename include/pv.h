@@ -508,6 +508,23 @@ int pv_sigproc_pack(const float* d_stokes, int nt, int nsub, int npol, int nchan
 int pv_events_text(const pv_event* h_events, long long n, double start_timestamp, double block_rate,
                    long long first_sample, double dm_low, double dm_step, float rms, int dump_index,
                    char* h_buf, long long cap, long long* h_len);
+/* The FRATS trigger TriggerOutput::_convertToTrigger_FRATS sends for one
+ * analysed buffer (lib/src/TriggerOutput.cpp:151-183).  When the buffer holds
+ * at least min_events events (the analyser's first event counts), the event of
+ * largest snr = value / (rms * sqrt(binFactor)) in float (above 0; the first
+ * of equals) gives, if snr >= snr_threshold, the message
+ *   artemis:<station>##ID:<id_root><message_number>##cFreqMHz:<cfreq_mhz>
+ *   ##beamRA:<beam_ra>##beamDec:<beam_dec>##eTime:<time %.9f>##eDM:<dm %.3f>
+ *   ##eSNR:<snr %.2f>
+ * (one line; fields left-padded with '0' to 4, 10, 10, 9, 20, 9 and 6
+ * characters, never cut).  Time and dm as in pv_events_text.  *h_len is the
+ * message size, 0 when the buffer raises no trigger; h_buf may be null for a
+ * size query. */
+int pv_trigger_message(const pv_event* h_events, long long n, double start_timestamp, double block_rate,
+                       long long first_sample, double dm_low, double dm_step, float rms, int min_events,
+                       float snr_threshold, const char* station, const char* id_root, int message_number,
+                       const char* cfreq_mhz, const char* beam_ra, const char* beam_dec, char* h_buf,
+                       long long cap, long long* h_len);
 /* ---- BandPassRecorder (lib/src/BandPassRecorder.cpp:22-190) ---------------
  * Options: <requiredSamples value="20000"/>, <fitParmaters coefficients="3"/>,
  * <Band startFrequency=.. endFrequency=../>.  The integrated Stokes-I

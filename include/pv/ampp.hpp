@@ -32,6 +32,11 @@
 
 #include <pv.h>
 
+#include <arpa/inet.h>
+#include <netinet/in.h>
+#include <sys/socket.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -927,6 +932,109 @@ class DedispersionDataAnalysisOutput {
   private:
     std::ofstream file_;
     int dump_ = 0;
+};
+
+// lib/src/TriggerOutput.cpp:33-204.  Options <Receiver host port/>, <Trigger
+// format/>, <Logfile name/>, <Telescope stationID beamID/>, <RADec rajd
+// decjd/>, <frequencyChannel1 MHz/>, <Threshold snr events/>.  Each buffer
+// that raises a FRATS trigger (pv_trigger_message) goes as one UDP datagram to
+// every receiver and as one line appended to the log file.  The receiver host
+// is an IPv4 address, as QHostAddress(host) takes it; the identifier root is
+// the construction time (yyyyMMddhhmm, local) and the beam id to two digits.
+class TriggerOutput {
+  public:
+    explicit TriggerOutput(const ConfigNode& c) {
+        const std::string host = c.getOption("Receiver", "host");
+        const int port = std::atoi(c.getOption("Receiver", "port", "0").c_str());
+        if (!host.empty() && port != 0) addReceiver(host, (uint16_t)port);
+        format_ = c.getOption("Trigger", "format");
+        const std::string log = c.getOption("Logfile", "name");
+        if (!log.empty()) addFile(log);
+        station_ = c.getOption("Telescope", "stationID");
+        char ts[16];
+        const time_t now = time(nullptr);
+        struct tm tm_now;
+        localtime_r(&now, &tm_now);
+        strftime(ts, sizeof ts, "%Y%m%d%H%M", &tm_now);
+        std::string beam = c.getOption("Telescope", "beamID");
+        if (beam.size() < 2) beam.insert(0, 2 - beam.size(), '0');
+        id_root_ = std::string(ts) + "-" + beam;
+        ra_ = c.getOption("RADec", "rajd");
+        dec_ = c.getOption("RADec", "decjd");
+        cfreq_ = c.getOption("frequencyChannel1", "MHz");
+        snr_ = to_float(c.getOption("Threshold", "snr"));
+        min_events_ = std::atoi(c.getOption("Threshold", "events", "0").c_str());
+    }
+    ~TriggerOutput() {
+        for (auto& r : receivers_) close(r.first);
+    }
+    TriggerOutput(const TriggerOutput&) = delete;
+    TriggerOutput& operator=(const TriggerOutput&) = delete;
+
+    void addReceiver(const std::string& host, uint16_t port) {
+        sockaddr_in a{};
+        a.sin_family = AF_INET;
+        a.sin_port = htons(port);
+        if (inet_pton(AF_INET, host.c_str(), &a.sin_addr) != 1) {
+            std::cerr << "TriggerOutput: not an IPv4 address: " << host << std::endl;
+            return;
+        }
+        const int s = socket(AF_INET, SOCK_DGRAM, 0);
+        if (s < 0) {
+            std::cerr << "TriggerOutput: no UDP socket" << std::endl;
+            return;
+        }
+        receivers_.emplace_back(s, a);
+    }
+    void addFile(const std::string& name) {
+        auto f = std::make_unique<std::ofstream>(name, std::ios::out | std::ios::app | std::ios::binary);
+        if (!*f) {
+            std::cerr << "unable to open file for writing: " << name << std::endl;
+            return;
+        }
+        files_.push_back(std::move(f));
+    }
+    // The message sent for this buffer, or "" when it raised none.
+    std::string sendStream(const DedispersionDataAnalysis* data) {
+        if (format_ != "FRATS") {
+            std::cerr << "Trigger format not recognized / implemented";
+            return "";
+        }
+        if (!data || !data->data()) return "";
+        const DedispersionSpectra* d = data->data();
+        std::vector<pv_event> ev;
+        ev.reserve(data->events().size());
+        for (const auto& e : data->events())
+            ev.push_back(pv_event{(int32_t)e.dmIndex(), (int32_t)e.timeBin(), e.mfBinning(), e.mfValue()});
+        long long n = 0;
+        auto call = [&](char* buf, long long cap) {
+            return pv_trigger_message(ev.data(), (long long)ev.size(), d->getLofarTimestamp(), d->getBlockRate(),
+                                      d->firstSample(), d->dmLow(), d->dmStep(), data->getRMS(), min_events_, snr_,
+                                      station_.c_str(), id_root_.c_str(), counter_ + 1, cfreq_.c_str(), ra_.c_str(),
+                                      dec_.c_str(), buf, cap, &n);
+        };
+        pv_check(call(nullptr, 0));
+        if (n == 0) return "";
+        std::string msg((size_t)n, '\0');
+        pv_check(call(&msg[0], n));
+        ++counter_;
+        if (ra_.empty()) std::cerr << "No RA/Dec found, conversion not yet implemented";
+        for (auto& r : receivers_)
+            sendto(r.first, msg.data(), msg.size(), 0, reinterpret_cast<const sockaddr*>(&r.second), sizeof r.second);
+        for (auto& f : files_) {
+            *f << msg << '\n';
+            f->flush();
+        }
+        return msg;
+    }
+    int messages() const { return counter_; }
+
+  private:
+    std::vector<std::pair<int, sockaddr_in>> receivers_;
+    std::vector<std::unique_ptr<std::ofstream>> files_;
+    std::string format_, station_, id_root_, ra_, dec_, cfreq_;
+    float snr_ = 0.0f;
+    int min_events_ = 0, counter_ = 0;
 };
 
 }  // namespace ampp

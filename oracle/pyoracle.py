@@ -430,6 +430,32 @@ def events_text(events, start_timestamp, block_rate, first_sample, dm_low, dm_st
     return "".join(lines)
 
 
+def trigger_message(events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms, min_events,
+                    snr_threshold, station, id_root, message_number, cfreq_mhz, beam_ra, beam_dec):
+    """TriggerOutput::_convertToTrigger_FRATS (TriggerOutput.cpp:151-183):
+    with at least min_events events (the first, dummy one counts), the event
+    of largest float SNR value / (rms * sqrt(binFactor)) wins (the running
+    maximum starts at 0 with no event, since the reference leaves it unset;
+    ties keep the first); at SNR >= threshold the message is built field by
+    field with QString::arg(s, width, '0'), i.e. left-padded with '0'."""
+    f32 = np.float32
+    if len(events) < min_events:
+        return None
+    best, snr_max = None, f32(0)
+    for e in events:
+        snr = f32(e["value"]) / (f32(rms) * np.sqrt(f32(e["bin_factor"])))
+        if snr > snr_max:
+            best, snr_max = e, snr
+    if best is None or not snr_max >= f32(snr_threshold):
+        return None
+    t = start_timestamp + float((int(best["t"]) + int(first_sample)) & 0xFFFFFFFF) * block_rate
+    dm = f32(dm_low + dm_step * int(best["dm"]))
+    return ("artemis:%s##ID:%s%s##cFreqMHz:%s##beamRA:%s##beamDec:%s##eTime:%s##eDM:%s##eSNR:%s"
+            % (station, id_root, str(message_number).rjust(4, "0"), cfreq_mhz.rjust(10, "0"),
+               beam_ra.rjust(10, "0"), beam_dec.rjust(9, "0"), ("%.9f" % t).rjust(20, "0"),
+               ("%.3f" % float(dm)).rjust(9, "0"), ("%.2f" % float(snr_max)).rjust(6, "0")))
+
+
 # --------------------------------------------------------------------------
 # F3 BandPassRecorder
 # --------------------------------------------------------------------------

@@ -227,3 +227,56 @@ extern "C" int pv_events_text(const pv_event* h_events, long long n, double star
     }
     return PV_OK;
 }
+
+namespace {
+// QString::arg(a, width, '0'): right-aligned, padded on the left, never cut.
+std::string zero_pad(const std::string& s, size_t width) {
+    return s.size() >= width ? s : std::string(width - s.size(), '0') + s;
+}
+std::string fixed(double v, int digits) {  // QString::number(v, 'f', digits)
+    char b[64];
+    std::snprintf(b, sizeof b, "%.*f", digits, v);
+    return b;
+}
+}  // namespace
+
+extern "C" int pv_trigger_message(const pv_event* h_events, long long n, double start_timestamp, double block_rate,
+                                  long long first_sample, double dm_low, double dm_step, float rms, int min_events,
+                                  float snr_threshold, const char* station, const char* id_root, int message_number,
+                                  const char* cfreq_mhz, const char* beam_ra, const char* beam_dec, char* h_buf,
+                                  long long cap, long long* h_len) {
+    if ((!h_events && n > 0) || !h_len || cap < 0 || !station || !id_root || !cfreq_mhz || !beam_ra || !beam_dec) {
+        pv::set_error("pv_trigger_message: invalid arguments");
+        return PV_ERR_ARG;
+    }
+    *h_len = 0;
+    if (n < (long long)min_events) return PV_OK;  // eventsFound() counts the analyser's first event
+    // The reference declares the running maximum and its event without a value; they start at
+    // "no event" here, so only an SNR above 0 can win.  The first of equal SNRs is kept.
+    long long best = -1;
+    float snr_max = 0.0f;
+    for (long long i = 0; i < n; ++i) {
+        const float snr = h_events[i].value / (rms * std::sqrt(h_events[i].bin_factor));
+        if (snr > snr_max) {
+            snr_max = snr;
+            best = i;
+        }
+    }
+    if (best < 0 || !(snr_max >= snr_threshold)) return PV_OK;
+    const pv_event& e = h_events[best];
+    const double t = start_timestamp + (double)(unsigned)(e.t + first_sample) * block_rate;
+    const float dm = (float)(dm_low + dm_step * e.dm);
+    const std::string msg = std::string("artemis:") + station + "##ID:" + id_root +
+                            zero_pad(std::to_string(message_number), 4) + "##cFreqMHz:" + zero_pad(cfreq_mhz, 10) +
+                            "##beamRA:" + zero_pad(beam_ra, 10) + "##beamDec:" + zero_pad(beam_dec, 9) +
+                            "##eTime:" + zero_pad(fixed(t, 9), 20) + "##eDM:" + zero_pad(fixed(dm, 3), 9) +
+                            "##eSNR:" + zero_pad(fixed(snr_max, 2), 6);
+    *h_len = (long long)msg.size();
+    if ((long long)msg.size() > cap) {
+        if (!h_buf) return PV_OK;  // size query
+        pv::set_error("pv_trigger_message: %lld bytes needed", (long long)msg.size());
+        return PV_ERR_ARG;
+    }
+    if (h_buf) std::memcpy(h_buf, msg.data(), msg.size());
+    return PV_OK;
+}

@@ -8,6 +8,7 @@ be built (``build.py``); nothing here falls back to a CPU path.
 import ctypes as C
 import os
 import re
+import sys
 
 import numpy as np
 
@@ -110,6 +111,8 @@ def _declare(L):
         "pv_sigproc_mjd": (d, [d]),
         "pv_sigproc_pack": (i, [vp, i, i, i, i, i, i, f, f, vp, vp]),
         "pv_events_text": (i, [vp, ll, d, d, ll, d, d, f, i, vp, ll, P(ll)]),
+        "pv_trigger_message": (i, [vp, ll, d, d, ll, d, d, f, i, f, C.c_char_p, C.c_char_p, i, C.c_char_p,
+                                   C.c_char_p, C.c_char_p, vp, ll, P(ll)]),
         "pv_bandpass_recorder_create": (i, [P(vp), ll, i, f, f]),
         "pv_bandpass_recorder_destroy": (None, [vp]),
         "pv_bandpass_recorder_add": (i, [vp, vp, i, i, i, i, vp]),
@@ -541,6 +544,79 @@ def events_text(events, start_timestamp, block_rate, first_sample, dm_low, dm_st
     buf = C.create_string_buffer(n.value + 1)
     check(load().pv_events_text(*args, buf, n.value, C.byref(n)))
     return buf.raw[:n.value].decode()
+
+
+def trigger_message(events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms, min_events,
+                    snr_threshold, station, id_root, message_number, cfreq_mhz, beam_ra, beam_dec):
+    """The FRATS trigger TriggerOutput sends for one analysed buffer
+    (lib/src/TriggerOutput.cpp:151-183), or None when the buffer raises none."""
+    import numpy as np
+    ev = np.ascontiguousarray(events)
+    n = C.c_longlong(0)
+    args = (ev.ctypes.data if len(ev) else None, len(ev), start_timestamp, block_rate, first_sample, dm_low,
+            dm_step, rms, min_events, snr_threshold, station.encode(), id_root.encode(), message_number,
+            cfreq_mhz.encode(), beam_ra.encode(), beam_dec.encode())
+    check(load().pv_trigger_message(*args, None, 0, C.byref(n)))
+    if n.value == 0:
+        return None
+    buf = C.create_string_buffer(n.value + 1)
+    check(load().pv_trigger_message(*args, buf, n.value, C.byref(n)))
+    return buf.raw[:n.value].decode()
+
+
+class TriggerOutput:
+    """TriggerOutput (lib/src/TriggerOutput.cpp:33-204): each analysed buffer
+    that raises a FRATS trigger sends it as one UDP datagram to every receiver
+    and appends it, with a newline, to the log file.  The identifier root is
+    the construction time (yyyyMMddhhmm, local) and the beam id to two digits."""
+
+    def __init__(self, station="", beamID="", rajd="", decjd="", cfreq_mhz="", snr=0.0, events=0,
+                 receiver=None, logfile=None, format="FRATS"):
+        import socket
+        import time
+        self.format = format
+        self.station, self.ra, self.dec, self.cfreq = station, rajd, decjd, cfreq_mhz
+        self.snr, self.min_events = float(snr), int(events)
+        self.id_root = "%s-%s" % (time.strftime("%Y%m%d%H%M"), beamID.rjust(2, "0"))
+        self.counter = 0
+        self.receivers = []
+        if receiver and receiver[0] and receiver[1]:
+            s = socket.socket(socket.AF_INET, socket.SOCK_DGRAM)
+            self.receivers.append((s, (receiver[0], int(receiver[1]))))
+        self.log = None
+        if logfile:
+            try:
+                self.log = open(logfile, "ab")
+            except OSError:
+                print("unable to open file for writing: " + logfile, file=sys.stderr)
+
+    def send_stream(self, events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms):
+        """Returns the message sent, or None."""
+        if self.format != "FRATS":
+            print("Trigger format not recognized / implemented", file=sys.stderr)
+            return None
+        msg = trigger_message(events, start_timestamp, block_rate, first_sample, dm_low, dm_step, rms,
+                              self.min_events, self.snr, self.station, self.id_root, self.counter + 1,
+                              self.cfreq, self.ra, self.dec)
+        if msg is None:
+            return None
+        self.counter += 1
+        if not self.ra:
+            print("No RA/Dec found, conversion not yet implemented", file=sys.stderr)
+        for s, addr in self.receivers:
+            s.sendto(msg.encode(), addr)
+        if self.log:
+            self.log.write(msg.encode() + b"\n")
+            self.log.flush()
+        return msg
+
+    def close(self):
+        for s, _ in self.receivers:
+            s.close()
+        self.receivers = []
+        if self.log:
+            self.log.close()
+            self.log = None
 
 
 class BandPassRecorder:

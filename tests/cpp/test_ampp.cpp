@@ -9,7 +9,8 @@
 //                               "EVENTS <count>" per completed buffer
 //   test_ampp ddout DIR N       ddmod with a DedispersionDataAnalysisOutput from DIR/config.xml;
 //                               writes DIR/events.bin (pv_event per event) and prints
-//                               "META start rate first dmlow dmstep rms" per buffer
+//                               "META start rate first dmlow dmstep rms" per buffer; with a
+//                               TriggerOutput element also "TRIGGER <message>" per trigger sent
 //   test_ampp sigproc DIR       SigprocStokesWriter (DIR/config.xml) over DIR/stokes.bin
 //                               (float [t][sub][pol][chan], shape and time stamp in DIR/shape.txt)
 //   test_ampp pipeline DIR N    N chunks of DIR/chunks.bin through AdapterTimeSeriesDataSet and
@@ -183,11 +184,20 @@ int ddout_mode(const std::string& dir, int nblobs) {
     DedispersionModule dd(dd_cfg);
     DedispersionAnalyser an(an_cfg);
     DedispersionDataAnalysisOutput out(out_cfg);
+    std::unique_ptr<TriggerOutput> trigger;
+    try {
+        trigger.reset(new TriggerOutput(ConfigNode::fromFile(dir + "/config.xml", "TriggerOutput")));
+    } catch (const std::runtime_error&) {
+    }
     std::ofstream evf(dir + "/events.bin", std::ios::binary);
     dd.connect([&](DedispersionSpectra* s) {
         DedispersionDataAnalysis result;
         an.analyse(s, &result);
         out.sendStream(&result);
+        if (trigger) {
+            const std::string m = trigger->sendStream(&result);
+            if (!m.empty()) std::printf("TRIGGER %s\n", m.c_str());
+        }
         for (const auto& e : result.events()) {
             const pv_event pe{(int32_t)e.dmIndex(), (int32_t)e.timeBin(), e.mfBinning(), e.mfValue()};
             evf.write(reinterpret_cast<const char*>(&pe), sizeof pe);

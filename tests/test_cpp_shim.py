@@ -206,6 +206,61 @@ def test_shim_event_output_file_equals_the_oracle_text(pv, oracle, cuda, shim_ex
     assert files[0].read_text() == want
 
 
+TRIGGER_XML = """  <TriggerOutput>
+    <Receiver host="127.0.0.1" port="{port}"/>
+    <Trigger format="FRATS"/>
+    <Logfile name="{log}"/>
+    <Telescope stationID="CS302" beamID="7"/>
+    <RADec rajd="83.633" decjd="22.014"/>
+    <frequencyChannel1 MHz="150.0"/>
+    <Threshold snr="{snr}" events="2"/>
+  </TriggerOutput>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("snr", [8.0, 1e9])
+def test_shim_trigger_output_sends_the_oracle_message(pv, oracle, cuda, shim_exe, tmp_path, snr):
+    """DedispersionModule -> DedispersionAnalyser -> TriggerOutput through the
+    module API: the datagram received on the loopback port and the log line are
+    the oracle's FRATS message for the events the analyser found; a threshold
+    no event reaches sends nothing."""
+    import re
+    import socket
+    rx = socket.socket(socket.AF_INET, socket.SOCK_DGRAM)
+    rx.bind(("127.0.0.1", 0))
+    rx.settimeout(5.0)
+    blob = generator_pulse(8192, 10.0)[0]
+    blob.tofile(tmp_path / "blob.bin")
+    t0 = 1.3e9 + 0.25
+    (tmp_path / "shape.txt").write_text("%d %d %d %r %r\n" % (8192, GEN_NSUB, GEN_NCHAN, GEN_TSAMP, t0))
+    foff = -6.0 / (GEN_NSUB * GEN_NCHAN)
+    xml = DDOUT_XML.format(fch1=repr(GEN_FCH1), foff=repr(foff), path=str(tmp_path / "events"))
+    xml = xml.replace("</configuration>\n", TRIGGER_XML.format(port=rx.getsockname()[1], log=tmp_path / "trig.log",
+                                                                snr=snr))
+    (tmp_path / "config.xml").write_text(xml)
+    out = _run(shim_exe, "ddout", tmp_path, 1)
+    metas = [line.split()[1:] for line in out.splitlines() if line.startswith("META")]
+    sent = [line[len("TRIGGER "):] for line in out.splitlines() if line.startswith("TRIGGER ")]
+    ev = np.fromfile(tmp_path / "events.bin", pv.EVENT_DTYPE)
+    start, rate, first, dm_low, dm_step, rms, n = metas[0]
+    if snr > 1e6:
+        assert sent == []
+        assert not (tmp_path / "trig.log").exists() or (tmp_path / "trig.log").read_text() == ""
+        rx.close()
+        return
+    assert len(sent) == 1
+    m = re.fullmatch(r"artemis:CS302##ID:(\d{12}-07)0001##.*", sent[0])
+    assert m, sent[0]
+    want = oracle.trigger_message(ev, float(start), float(rate), int(first), float(dm_low), float(dm_step),
+                                  np.float32(rms), 2, snr, "CS302", m.group(1), 1, "150.0", "83.633", "22.014")
+    assert sent[0] == want
+    assert rx.recv(4096).decode() == want
+    assert (tmp_path / "trig.log").read_text() == want + "\n"
+    rx.close()
+
+
 SIGPROC_XML = """<configuration>
   <SigprocStokesWriter writeHeader="true">
     <file filepath="{path}"/>

@@ -35,6 +35,50 @@ def test_event_text_equals_the_oracle(pv, oracle, n):
     assert pv.EVENTS_TEXT_HEADER == oracle.EVENTS_TEXT_HEADER
 
 
+@pytest.mark.parametrize("n,min_events,snr", [(1, 0, 0.0), (2, 2, 5.0), (50, 10, 20.0), (50, 51, 5.0),
+                                             (50, 0, 1e6), (3, 0, 0.0)])
+def test_trigger_message_equals_the_oracle(pv, oracle, n, min_events, snr):
+    rng = np.random.default_rng(100 + n)
+    ev = _events(rng, n)
+    if n == 3:
+        ev["value"][1:] = ev["value"][1]  # equal SNRs: the first is kept
+        ev["bin_factor"][1:] = 1.0
+    args = (1.3e9 + 0.123456789, 327.68e-6, 16384, float(np.float32(0.0)), float(np.float32(0.1)),
+            np.float32(45.254834), min_events, snr, "CS302", "202612031200-07", 12, "150.0", "", "-22.014")
+    got = pv.trigger_message(ev, *args)
+    assert got == oracle.trigger_message(ev, *args)
+    raises = n > 1 and n >= min_events and snr < 1e6
+    assert (got is not None) == raises
+    if raises:
+        f = dict(kv.split(":", 1) for kv in got.split("##"))
+        assert f["artemis"] == "CS302" and f["ID"] == "202612031200-070012"
+        assert f["cFreqMHz"] == "00000150.0" and f["beamRA"] == "0000000000" and f["beamDec"] == "00-22.014"
+        assert len(f["eTime"]) == 20 and len(f["eDM"]) == 9 and len(f["eSNR"]) == 6
+        snr_all = ev["value"][1:] / (np.float32(45.254834) * np.sqrt(ev["bin_factor"][1:]))
+        i = 1 + int(np.argmax(snr_all))
+        assert float(f["eDM"]) == pytest.approx(0.1 * int(ev["dm"][i]), abs=1e-3)
+
+
+def test_trigger_output_sends_one_datagram_and_log_line(pv, tmp_path):
+    import socket
+    rx = socket.socket(socket.AF_INET, socket.SOCK_DGRAM)
+    rx.bind(("127.0.0.1", 0))
+    rx.settimeout(5.0)
+    out = pv.TriggerOutput(station="CS302", beamID="7", rajd="83.6", decjd="22.0", cfreq_mhz="150", snr=5.0,
+                           events=2, receiver=("127.0.0.1", rx.getsockname()[1]), logfile=str(tmp_path / "t.log"))
+    ev = _events(np.random.default_rng(5), 20)
+    args = (1.3e9, 327.68e-6, 0, 0.0, 0.1, 45.254834)
+    first = out.send_stream(ev, *args)
+    second = out.send_stream(ev, *args)
+    assert out.send_stream(ev[:1], *args) is None  # fewer events than the threshold count
+    out.close()
+    assert first.split("##")[1].endswith("0001") and second.split("##")[1].endswith("0002")
+    assert first.split("##")[1][3:] == out.id_root + "0001"
+    assert rx.recv(4096).decode() == first and rx.recv(4096).decode() == second
+    assert (tmp_path / "t.log").read_text() == first + "\n" + second + "\n"
+    rx.close()
+
+
 OPTIONS = [
     {},  # every default
     {"subbandsPerPacket": 31, "totalComplexSubbands": 512, "clock": 200, "integrateTimeBins": 4,
