@@ -8,9 +8,9 @@
 // samples each) of both polarisations.  It stages the tile plus the T-1
 // preceding blocks (from the previous call's history where the tile starts
 // the chunk) in shared memory, applies the T-tap polyphase FIR per channel
-// (oldest tap first, FP32 products and sums in the reference's order),
-// transforms every block with a shared-memory radix-2 Stockham FFT (forward,
-// unnormalised, natural order, as FFTW_FORWARD) and then either writes the
+// (oldest tap first in the reference's order, each product added by one FP32
+// fused multiply-add), transforms every block with a shared-memory radix-2
+// decimation-in-frequency FFT (forward, unnormalised, as FFTW_FORWARD) and then either writes the
 // complex spectra (SpectrumDataSetC32 layout) or forms Stokes parameters and
 // integrates them over `window` blocks and `bin` channels (the
 // SpectrumDataSetStokes layout), so the channelised voltages never reach
@@ -54,13 +54,16 @@ __device__ __forceinline__ float2 load_sample(const ChanArgs& a, long long idx) 
 // The upper output of a radix-2 decimation-in-frequency butterfly,
 // (u - v) * w, with the rounding every channeliser kernel uses: the lower
 // output is u + v.  Both kernels evaluate each butterfly identically, so their
-// spectra agree bit for bit.
+// spectra agree bit for bit.  The last two stages (spans 1 and 2) only meet
+// the twiddles 1 and -i (held exactly in the table): d and (d.y, -d.x), with
+// no multiplication.
 __device__ __forceinline__ float2 twiddle_mul(float2 d, float2 w) {
     return make_float2(fmaf(d.x, w.x, __fmul_rn(-d.y, w.y)), fmaf(d.x, w.y, __fmul_rn(d.y, w.x)));
 }
 __device__ __forceinline__ float2 dif_upper(float2 u, float2 v, float2 w) {
     return twiddle_mul(make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y)), w);
 }
+__device__ __forceinline__ float2 times_minus_i(float2 d) { return make_float2(d.y, -d.x); }
 
 __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
     extern __shared__ float2 sm[];
@@ -114,8 +117,8 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
         for (int t = 0; t < T; ++t) {
             const float k = cf[t * N + c];
             const float2 v = xs[(size_t)t * N];
-            re = __fadd_rn(re, __fmul_rn(v.x, k));
-            im = __fadd_rn(im, __fmul_rn(v.y, k));
+            re = __fmaf_rn(v.x, k, re);
+            im = __fmaf_rn(v.y, k, im);
         }
         y[((size_t)p * BT + b) * N + c] = make_float2(re, im);
     }
@@ -133,7 +136,10 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
             const int lo = ((j >> lh) << (lh + 1)) + (j & (h - 1));
             const float2 u = r[lo], v = r[lo + h];
             r[lo] = make_float2(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y));
-            r[lo + h] = dif_upper(u, v, tw[(j & (h - 1)) << (lg - 1 - lh)]);
+            const float2 d = make_float2(__fsub_rn(u.x, v.x), __fsub_rn(u.y, v.y));
+            if (lh == 0) r[lo + h] = d;                                   // twiddle 1
+            else if (lh == 1) r[lo + h] = (j & 1) ? times_minus_i(d) : d;  // 1 or -i
+            else r[lo + h] = twiddle_mul(d, tw[(j & (h - 1)) << (lg - 1 - lh)]);
         }
         __syncthreads();
     }
@@ -193,7 +199,9 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
 // I = |X|^2 + |Y|^2.  Every FIR product and sum, FFT butterfly, Stokes and
 // integration step is evaluated exactly as channelise_kernel evaluates it, so
 // the two kernels' outputs are bit-identical.  Inputs are read once (plus 7
-// warm-up blocks per range); raw loads run 8 blocks ahead of the arithmetic.
+// warm-up blocks per range); raw loads run 8 blocks ahead of the arithmetic
+// (4 for 64 channels, whose int16 kernel is held to 168 registers so that
+// three CTAs share an SM).
 //
 // Jobs (one per beam) are laid out one after another in warp space, so one
 // launch channelises any number of beams with the same N.
@@ -217,13 +225,8 @@ struct RawSample<false> {
     static __device__ __forceinline__ float2 f2(float2 v) { return v; }
 };
 
-// Packed FP32 pairs for the FIR (Blackwell mul/fma .f32x2): each half is
-// rounded as the scalar operation, so the sums are bit-identical.  ptxas
-// contracts a packed multiply feeding a packed add into one fused
-// multiply-add even with .rn and --fmad false (measured on sm_103a: every
-// 8-tap sum equal to the fused chain), so the product is added as
-// fma(product, one, sum) with `one` a 1.0 the compiler cannot see: exactly
-// round(product + sum), with no multiply-add pair left to fuse.
+// Packed FP32 pairs for the FIR (Blackwell fma .f32x2): each half is rounded
+// as the scalar __fmaf_rn, so the sums are bit-identical to channelise_kernel's.
 __device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
     unsigned long long r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
@@ -234,16 +237,11 @@ __device__ __forceinline__ float2 upk2(unsigned long long v) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(v));
     return f;
 }
-__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+// round(a * b + s) per half
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long s) {
     unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-// round(p + s) for p, s pairs, written as fma(p, one, s) (one == 1.0)
-__device__ __forceinline__ unsigned long long add_product2(unsigned long long p, unsigned long long one,
-                                                           unsigned long long s) {
-    unsigned long long r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(p), "l"(one), "l"(s));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(s));
     return r;
 }
 
@@ -254,9 +252,8 @@ __device__ __forceinline__ unsigned long long add_product2(unsigned long long p,
 template <int M, int T>
 struct FirWindow {
     static constexpr int K = M == 1 ? 1 : M / 2;
-    unsigned long long re[T][K], im[T][M == 1 ? 1 : K], cf[T][K], one;
-    __device__ __forceinline__ void coeffs(const float (&c)[T][M], float unit) {
-        one = pk2(unit, unit);
+    unsigned long long re[T][K], im[T][M == 1 ? 1 : K], cf[T][K];
+    __device__ __forceinline__ void coeffs(const float (&c)[T][M]) {
 #pragma unroll
         for (int t = 0; t < T; ++t)
 #pragma unroll
@@ -281,8 +278,8 @@ struct FirWindow {
 #pragma unroll
             for (int t = 0; t < T; ++t) {
                 const int slot = (q + 1 + t) & (T - 1);
-                ar = add_product2(mul2(re[slot][k], cf[t][k]), one, ar);
-                if (M != 1) ai = add_product2(mul2(im[slot][k], cf[t][k]), one, ai);
+                ar = fma2(re[slot][k], cf[t][k], ar);
+                if (M != 1) ai = fma2(im[slot][k], cf[t][k], ai);
             }
             if (M == 1) {
                 y[0] = upk2(ar);
@@ -296,7 +293,7 @@ struct FirWindow {
 };
 
 template <int N, bool I16, bool PKT>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, N == 64 && I16 ? 3 : 1)  // 3 CTAs of 168 registers
 chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant__ pv::ChanJob one, int njobs,
                      long long nwarps, const pv::BeamStep* __restrict__ bs) {
     constexpr int M = N / 16, T = kFastTaps, H = T - 1;
@@ -360,6 +357,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
         for (int q = 0; q < hm; ++q) twr[M - 2 * hm + q] = J.twiddle[(j + 16 * q) * (M / (2 * hm))];
     float2 tws[4];
     float sgn[4];
+    const bool rot = (j & 3) == 3;  // upper lane of the stride-2 stage with twiddle -i
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int h = 8 >> q;
@@ -370,7 +368,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
 
     // FIR window: slot b & 7 holds block b (B0 is a multiple of 8)
     FirWindow<M, T> win;
-    win.coeffs(cf, J.unit);
+    win.coeffs(cf);
 #pragma unroll
     for (int q = 1; q < T; ++q) {
         const int b = B0 - T + q;
@@ -382,9 +380,10 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
         }
         win.set(q, v);
     }
-    Raw cur[T][M];
+    constexpr int PF = M == 4 ? 4 : T;  // raw loads run PF blocks ahead
+    Raw cur[PF][M];
 #pragma unroll
-    for (int q = 0; q < T; ++q)
+    for (int q = 0; q < PF; ++q)
 #pragma unroll
         for (int m = 0; m < M; ++m)
             if (B0 + q < B1) cur[q][m] = in[(long long)(B0 + q) * sb + m * sm];
@@ -402,12 +401,12 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
             {
                 float2 v[M];
 #pragma unroll
-                for (int m = 0; m < M; ++m) v[m] = RawSample<I16>::f2(cur[q][m]);
+                for (int m = 0; m < M; ++m) v[m] = RawSample<I16>::f2(cur[q % PF][m]);
                 win.set(q, v);
             }
-            if (b + T < B1) {
+            if (b + PF < B1) {
 #pragma unroll
-                for (int m = 0; m < M; ++m) cur[q][m] = in[(long long)(b + T) * sb + m * sm];
+                for (int m = 0; m < M; ++m) cur[q % PF][m] = in[(long long)(b + PF) * sb + m * sm];
             }
             // FIR, oldest tap (block b-7, slot q+1) first, in packed pairs
             float2 y[M];
@@ -423,7 +422,8 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
                         y[m + hm] = dif_upper(a, c, twr[M - 2 * hm + (m & (hm - 1))]);
                     }
             // stages of stride 8..1 across lanes: d = a + b (lower lane) or
-            // a - b (upper lane) -- exact sign flips -- then (d * w), w = 1 below
+            // a - b (upper lane) -- exact sign flips -- then (d * w), w = 1 below;
+            // stride 2 meets only w = 1 and -i, stride 1 only w = 1
 #pragma unroll
             for (int q2 = 0; q2 < 4; ++q2) {
                 const int h = 8 >> q2;
@@ -432,7 +432,9 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
                     const float ox = __shfl_xor_sync(0xffffffffu, y[m].x, h);
                     const float oy = __shfl_xor_sync(0xffffffffu, y[m].y, h);
                     const float2 d = make_float2(fmaf(sgn[q2], y[m].x, ox), fmaf(sgn[q2], y[m].y, oy));
-                    y[m] = twiddle_mul(d, tws[q2]);
+                    if (h == 1) y[m] = d;
+                    else if (h == 2) y[m] = rot ? times_minus_i(d) : d;
+                    else y[m] = twiddle_mul(d, tws[q2]);
                 }
             }
             // Stokes I = |X|^2 + |Y|^2 and integration
@@ -576,7 +578,6 @@ bool chan_fast_supported(int nchan, int ntaps, int npol, int nstokes, int window
 
 int chan_job_warps(ChanJob& job) {
     job.nranges = ceil_div(job.nblocks, kRangeBlocks);
-    job.unit = 1.0f;
     return job.nsub * job.nranges;
 }
 
@@ -722,6 +723,7 @@ extern "C" int pv_ppf_create(pv_ppf** out, int nchan, int ntaps, int window,
         const double ang = -2.0 * M_PI * k / nchan;
         tw[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
+    if (nchan >= 4) tw[nchan / 4] = make_float2(0.0f, -1.0f);  // exactly -i (cos(pi/2) is not 0 in FP64)
     cudaError_t e = cudaMalloc(&h->d_coeffs, sizeof(float) * h->h_coeffs.size());
     if (e == cudaSuccess) e = cudaMalloc(&h->d_twiddle, sizeof(float2) * tw.size());
     if (e == cudaSuccess)

@@ -38,7 +38,6 @@ struct ChanJob {
     long long warp_begin;    // first warp of this job in the launch
     int nsub, nblocks, window, nu, nranges;
     int beam;                // index into the batch's BeamStep array
-    float unit;              // 1.0f, unknown to the compiler (set by chan_job_warps): see FirWindow
     long long pkt_bytes;     // > 0: `in` holds LOFAR packets of this size (int16, 16 samples each)
     int pkt_nsub;            // subbands per packet; the nsub/pkt_nsub streams follow each other
 };
