@@ -330,14 +330,15 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
     // [subband][t][pol] after a 16-byte header; AdapterTimeSeriesDataSet.cpp:246-288): sample t is
     // time j of packet b*(N/16) + m of the subband's stream.
     const Raw* in;
-    long long sb, sm;
+    long long sb;
+    int sm;  // channel-group stride (a packet: under 64 KiB of words)
     if (PKT) {
         const long long pw = J.pkt_bytes / 4;  // 4-byte words per packet
         const long long npk = (long long)nblocks * (N / 16);
         const int stream = s / J.pkt_nsub, ls = s - stream * J.pkt_nsub;
         in = reinterpret_cast<const Raw*>(src) + stream * npk * pw + 4 + (ls * 16 + j) * 2 + pol;
         sb = (N / 16) * pw;
-        sm = pw;
+        sm = (int)pw;
     } else {
         in = reinterpret_cast<const Raw*>(src) + row * nblocks * N + j;
         sb = N;
@@ -387,6 +388,7 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
 #pragma unroll
         for (int m = 0; m < M; ++m)
             if (B0 + q < B1) cur[q][m] = in[(long long)(B0 + q) * sb + m * sm];
+    const Raw* nxt = in + (long long)(B0 + PF) * sb;  // packets: block b + PF, advanced by sb per block
 
     float acc[M];
 #pragma unroll
@@ -406,8 +408,10 @@ chan_stokes_i_kernel(const pv::ChanJob* __restrict__ jobs, const __grid_constant
             }
             if (b + PF < B1) {
 #pragma unroll
-                for (int m = 0; m < M; ++m) cur[q % PF][m] = in[(long long)(b + PF) * sb + m * sm];
+                for (int m = 0; m < M; ++m)
+                    cur[q % PF][m] = PKT ? nxt[m * sm] : in[(long long)(b + PF) * sb + m * sm];
             }
+            if (PKT) nxt += sb;
             // FIR, oldest tap (block b-7, slot q+1) first, in packed pairs
             float2 y[M];
             win.fir(q, y);
