@@ -3,7 +3,7 @@
 // each stage of all beams in as few launches as the kernels allow:
 //
 //   K1  chan_stokes_i_kernel   one launch per channels-per-subband class
-//   K2  rfi_batch_kernel       one CTA per beam, one launch per CTA size
+//   K2  rfi_batch_kernel       one CTA per beam, one launch per channel count
 //   A8  ring_write_batch_kernel one launch
 //   K4  dedisperse_batch_kernel one persistent launch over every beam's tiles,
 //                              DM x time tile shape chosen by the autotuner
@@ -136,9 +136,9 @@ struct pv_batch {
     bool pipelined = false;
     cudaStream_t side = nullptr;     // second branch of a pipelined step
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-    cudaStream_t rfi_side[3] = {};   // pipelined: one stream per clipper class after the first
-    cudaEvent_t rfi_join[3] = {};
-    cudaEvent_t rfi_tail[3] = {};    // pipelined: end of the dedispersion helper after each class
+    std::vector<cudaStream_t> rfi_side;  // pipelined: one stream per clipper class after the first
+    std::vector<cudaEvent_t> rfi_join;
+    std::vector<cudaEvent_t> rfi_tail;   // pipelined: end of the dedispersion helper after each class
     cudaStream_t branch_a = nullptr; // pipelined: clippers and ring write (high priority)
     cudaEvent_t join_a = nullptr;
 };
@@ -150,11 +150,12 @@ void destroy(pv_batch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     if (b->side) cudaStreamDestroy(b->side);
-    for (int i = 0; i < 3; ++i) {
-        if (b->rfi_side[i]) cudaStreamDestroy(b->rfi_side[i]);
-        if (b->rfi_join[i]) cudaEventDestroy(b->rfi_join[i]);
-        if (b->rfi_tail[i]) cudaEventDestroy(b->rfi_tail[i]);
-    }
+    for (cudaStream_t x : b->rfi_side)
+        if (x) cudaStreamDestroy(x);
+    for (cudaEvent_t x : b->rfi_join)
+        if (x) cudaEventDestroy(x);
+    for (cudaEvent_t x : b->rfi_tail)
+        if (x) cudaEventDestroy(x);
     if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->branch_a) cudaStreamDestroy(b->branch_a);
     if (b->join_a) cudaEventDestroy(b->join_a);
@@ -234,7 +235,15 @@ int enqueue_step(pv_batch* b, cudaStream_t s, bool capture) {
         if (nk > 0) PV_TRY(pv::rfi_batch_launch_one(b->rfi, 0, sa));
         for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(sa, b->rfi_join[k - 1], 0), "join clipper");
     } else if (b->rfi) {
-        PV_TRY(pv::rfi_batch_launch(b->rfi, s));
+        // the classes side by side, joined before the dedispersion
+        if (nk > 1) PV_CUDA(cudaEventRecord(b->fork_ev, s), "fork");
+        for (int k = 1; k < nk; ++k) {
+            PV_CUDA(cudaStreamWaitEvent(b->rfi_side[k - 1], b->fork_ev, 0), "fork clipper");
+            PV_TRY(pv::rfi_batch_launch_one(b->rfi, k, b->rfi_side[k - 1]));
+            PV_CUDA(cudaEventRecord(b->rfi_join[k - 1], b->rfi_side[k - 1]), "join clipper");
+        }
+        if (nk > 0) PV_TRY(pv::rfi_batch_launch_one(b->rfi, 0, s));
+        for (int k = 1; k < nk; ++k) PV_CUDA(cudaStreamWaitEvent(s, b->rfi_join[k - 1], 0), "join clipper");
     }
     PV_TRY(mark(2, sa));
     auto dedisperse_branch = [&]() -> int {
@@ -522,18 +531,21 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             cudaStreamCreateWithPriority(&b->branch_a, cudaStreamNonBlocking, highest) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->join_a, cudaEventDisableTiming) != cudaSuccess ||
-            cudaStreamCreateWithPriority(&b->rfi_side[0], cudaStreamNonBlocking, highest) != cudaSuccess ||
-            cudaStreamCreateWithPriority(&b->rfi_side[1], cudaStreamNonBlocking, highest) != cudaSuccess ||
-            cudaStreamCreateWithPriority(&b->rfi_side[2], cudaStreamNonBlocking, highest) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_join[0], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_join[1], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_join[2], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_tail[0], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_tail[1], cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->rfi_tail[2], cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&b->join_a, cudaEventDisableTiming) != cudaSuccess) {
             pv::set_error("pv_batch_create: cannot create streams");
             return fail(PV_ERR_CUDA);
+        }
+        const int nk = b->rfi ? pv::rfi_batch_launches(b->rfi) : 0;
+        for (int k = 1; k < nk; ++k) {
+            b->rfi_side.push_back(nullptr);
+            b->rfi_join.push_back(nullptr);
+            b->rfi_tail.push_back(nullptr);
+            if (cudaStreamCreateWithPriority(&b->rfi_side.back(), cudaStreamNonBlocking, highest) != cudaSuccess ||
+                cudaEventCreateWithFlags(&b->rfi_join.back(), cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&b->rfi_tail.back(), cudaEventDisableTiming) != cudaSuccess) {
+                pv::set_error("pv_batch_create: cannot create streams");
+                return fail(PV_ERR_CUDA);
+            }
         }
         for (int i = 0; i < 2; ++i)
             if (cudaEventCreateWithFlags(&b->done[i], cudaEventDisableTiming) != cudaSuccess ||

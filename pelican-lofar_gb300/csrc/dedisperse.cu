@@ -848,8 +848,12 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
                    bool set_attr) {
     auto kern = dedisperse_batch_kernel<R, CS, ST, STORE>;
     if (set_attr) {
-        PV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                "cudaFuncSetAttribute(dedisperse_batch)");
+        size_t limit = 0;
+        PV_CUDA(pv::allow_max_dynamic_smem(kern, &limit), "cudaFuncSetAttribute(dedisperse_batch)");
+        if (smem > limit) {
+            pv::set_error("dedisperse_batch: %zu bytes of shared memory exceed one CTA's %zu", smem, limit);
+            return PV_ERR_ARG;
+        }
         return PV_OK;
     }
     if (grid < 0) {  // the counter was reset beforehand: this launch joins the same tile queue

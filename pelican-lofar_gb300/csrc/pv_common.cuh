@@ -41,6 +41,22 @@ inline T ceil_div(T a, T b) { return (a + b - 1) / b; }
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
+// Largest dynamic shared memory a CTA may opt into on the current device.  The
+// batched kernels set their attribute to it once: the attribute is global to
+// the process, and launches captured into a graph for one batch must not
+// depend on the shared memory another batch asked for afterwards.
+int smem_optin();
+// Sets kern's dynamic shared-memory limit to smem_optin() less its static
+// shared memory; *limit (if given) receives that limit.
+template <typename Kernel>
+cudaError_t allow_max_dynamic_smem(Kernel kern, size_t* limit = nullptr) {
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaFuncGetAttributes(&a, kern);
+    if (e != cudaSuccess) return e;
+    const int dyn = smem_optin() - (int)a.sharedSizeBytes;
+    if (limit) *limit = (size_t)dyn;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+}
 
 // Stream-ordered scratch allocation (cudaMallocAsync / cudaFreeAsync).
 int scratch_alloc(void** p, size_t bytes, cudaStream_t s);

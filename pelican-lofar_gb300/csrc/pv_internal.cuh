@@ -108,8 +108,7 @@ struct RfiBatch;
 // handles[i] null: beam i has no clipper; bs: the batch's BeamStep array (inactive beams skip)
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
                      const int* nchan, int n, int nt, const BeamStep* bs, cudaStream_t s);
-int rfi_batch_launch(RfiBatch* b, cudaStream_t s);
-int rfi_batch_launches(const RfiBatch* b);  // number of CTA-size classes
+int rfi_batch_launches(const RfiBatch* b);  // number of classes (beams with one channel count), largest first
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s);
 int rfi_batch_ctas(const RfiBatch* b, int k);  // CTAs (beams) of class k
 void rfi_batch_destroy(RfiBatch* b);

@@ -711,9 +711,12 @@ int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamSte
                  unsigned char* flags, cudaStream_t s) {
     if (jobs) {
         if (nblocks == 0) {  // set-up call: the attribute only, before any stream capture
-            PV_CUDA(cudaFuncSetAttribute(rfi_batch_kernel<MAXT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "cudaFuncSetAttribute(rfi batch)");
+            size_t limit = 0;
+            PV_CUDA(pv::allow_max_dynamic_smem(rfi_batch_kernel<MAXT>, &limit), "cudaFuncSetAttribute(rfi batch)");
+            if (smem > limit) {
+                pv::set_error("RFI_Clipper: %zu bytes of shared memory exceed one CTA's %zu", smem, limit);
+                return PV_ERR_ARG;
+            }
             return PV_OK;
         }
         rfi_batch_kernel<MAXT><<<nblocks, MAXT, smem, s>>>(jobs, bs);
@@ -944,13 +947,16 @@ extern "C" int pv_rfi_bandpass(pv_rfi* h, float* out, int nbins) {
 
 // ---------------------------------------------------------------------------
 // Batched clippers: the RFI_Clipper of every beam of a batch, one CTA per
-// beam, one launch per partial-count class.
+// beam, one launch per class of beams with the same channel count (so the
+// same partial-sum count and about the same time per spectrum): the SMs of a
+// class are free for other work as soon as its own beams are done.  Classes
+// run largest channel count first.
 // ---------------------------------------------------------------------------
 namespace pv {
 
 struct RfiBatch {
     struct Class {
-        int parts = 0;
+        int parts = 0, nbins = 0;
         size_t smem = 0;
         RfiJob* d_jobs = nullptr;
         int njobs = 0;
@@ -987,10 +993,11 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         }
         const int parts = pv_rfi_parts(nbins);
         size_t k = 0;
-        while (k < b->classes.size() && b->classes[k].parts != parts) ++k;
+        while (k < b->classes.size() && b->classes[k].nbins != nbins) ++k;
         if (k == b->classes.size()) {
             b->classes.emplace_back();
             b->classes[k].parts = parts;
+            b->classes[k].nbins = nbins;
             jobs.emplace_back();
         }
         b->classes[k].smem = std::max(b->classes[k].smem, smem);
@@ -1004,6 +1011,20 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         j.nt = nt;
         j.beam = i;
         jobs[k].push_back(j);
+    }
+    {  // largest channel count first
+        std::vector<size_t> order(b->classes.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](size_t x, size_t y) { return b->classes[x].nbins > b->classes[y].nbins; });
+        std::vector<RfiBatch::Class> cs;
+        std::vector<std::vector<RfiJob>> js;
+        for (size_t k : order) {
+            cs.push_back(b->classes[k]);
+            js.push_back(std::move(jobs[k]));
+        }
+        b->classes.swap(cs);
+        jobs.swap(js);
     }
     for (size_t k = 0; k < b->classes.size(); ++k) {
         auto& c = b->classes[k];
@@ -1023,15 +1044,6 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         }
     }
     *out = b;
-    return PV_OK;
-}
-
-int rfi_batch_launch(RfiBatch* b, cudaStream_t s) {
-    for (auto& c : b->classes) {
-        if (c.njobs == 0) continue;
-        PV_TRY(rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, b->bs, RfiConfig{}, RfiBuffers{},
-                          nullptr, 0, Geo{}, nullptr, s));
-    }
     return PV_OK;
 }
 

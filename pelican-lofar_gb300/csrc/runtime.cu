@@ -40,6 +40,14 @@ int sm_count() {
     return g_sm_counts[dev];
 }
 
+int smem_optin() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n <= 0)
+        return 227 * 1024;
+    return n;
+}
+
 int scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
     *p = nullptr;
     if (bytes == 0) return PV_OK;
