@@ -186,6 +186,24 @@ def test_batch_host_steps_overlap_and_events_of_previous_step(pv, cuda, mix_conf
     del hosts_prev
 
 
+def test_a_later_batch_with_smaller_beams_leaves_an_earlier_batch_runnable(pv, cuda, mix_configs):
+    """Kernel attributes are global to the process: a batch created after
+    another, with smaller beams, must not shrink the shared memory that the
+    first batch's captured launches use."""
+    import torch
+    big = pv.Batch(mix_configs, tune=False, graph=True)
+    small = pv.Batch(mix_configs[:1], tune=False, graph=True)
+    rng = np.random.default_rng(5)
+    for b, cfgs in ((big, mix_configs), (small, mix_configs[:1]), (big, mix_configs)):
+        for i, c in enumerate(cfgs):
+            v16, _ = voltages(rng, c.nsub, 2, c.chunk * 4 * c.nchan_sub)
+            b.set_input(i, torch.from_numpy(v16.reshape(c.nsub, 2, -1)).to(cuda))
+        b.run()
+        for i in range(len(cfgs)):
+            b.events(i)  # waits for the step and raises if it failed
+    torch.cuda.synchronize()
+
+
 @pytest.mark.parametrize("pipelined", [False, True])
 def test_batch_with_idle_beams_equals_beams_alone(pv, cuda, mix_configs, pipelined):
     """Continuous batching: in every step only some beams have a chunk.  Each
@@ -233,8 +251,9 @@ def test_batch_with_idle_beams_equals_beams_alone(pv, cuda, mix_configs, pipelin
 
 
 def test_batch_of_twelve_beams_in_three_clipper_classes_equals_beams_alone(pv, cuda):
-    """Twelve beams whose clippers fall in all three CTA-size classes (up to 1024, 4096 and more
-    channels), pipelined under one graph: every window and event list equals the beam's alone."""
+    """Twelve beams whose clippers use all three CTA sizes (up to 1024, 4096 and more channels;
+    one launch per channel count, several sharing a CTA size), pipelined under one graph: every
+    window and event list equals the beam's alone."""
     rng = np.random.default_rng(121)
     shapes = [(4, 16), (6, 32), (3, 64), (8, 16),       # 256-thread class
               (40, 32), (20, 64), (96, 16), (50, 32),   # 512-thread class
