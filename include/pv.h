@@ -470,6 +470,43 @@ int pv_udp_unpack(const pv_udp_config* config, const void* d_chunk, long long ch
 int pv_udp_time(const pv_udp_config* config, const void* h_packet, double* h_timestamp,
                 double* h_block_rate);
 
+/* ---- ALFABURST spectrometer packets: ABDataAdapter ------------------------
+ * ABDataAdapter::deserialise (lib/src/ABDataAdapter.cpp:14-173), the input of
+ * ABPipeline (pipelines/udpstream/src/ABPipeline.cpp:56-140).  A packet is an
+ * 8-byte header (bytes 0-5: the integration count, most significant byte
+ * first; byte 6: the spectral quarter; byte 7: the beam) and `channels`
+ * records of four big-endian 16-bit pseudo-Stokes values (XX, YY, XY re,
+ * XY im): 8 + 8 * channels bytes. */
+typedef struct pv_ab_config {
+    int packets_per_spectrum; /* <spectrum packets> */
+    int channels;             /* <packet channels> */
+    int samples_per_packet;   /* <packet samples>; 0 (absent) counts as 1 */
+    float tsamp;              /* <samplingTime seconds> */
+} pv_ab_config;
+/* What the adapter carries from chunk to chunk; zero it before the first. */
+typedef struct pv_ab_state {
+    long long seen;              /* packets read so far */
+    unsigned long long count0;   /* the first packet's integration count */
+    double last_time;            /* the previous packet's time */
+} pv_ab_state;
+/* The header pass over one chunk in host memory (:68-150).  The chunk holds
+ * bytes / packet size packets and the blob (packets / packets_per_spectrum) *
+ * samples_per_packet spectra (*h_nblocks).  Each packet whose spectral
+ * quarter is packets_per_spectrum - 3 fills the next spectrum: h_index
+ * receives the packets' indices (at most min(cap, *h_nblocks); *h_nspectra of
+ * them).  A packet's time is (count - count0) * tsamp, count0 being 0 for the
+ * very first packet and that packet's count afterwards; *h_timestamp is the
+ * chunk's last packet's time and *h_gaps counts the packets more than tsamp
+ * after the previous one (the reference's "FATAL!" lines). */
+int pv_ab_headers(const pv_ab_config* config, pv_ab_state* state, const void* h_chunk, long long bytes,
+                  int* h_index, long long cap, long long* h_nspectra, long long* h_nblocks,
+                  double* h_timestamp, long long* h_gaps);
+/* The data pass on the device: spectrum k of d_out [nblocks][channels] float
+ * is XX + YY (unsigned 16-bit) of packet d_index[k] for k < nspectra, and 0
+ * for the rest. */
+int pv_ab_unpack(const pv_ab_config* config, const void* d_chunk, long long bytes, const int* d_index,
+                 long long nspectra, long long nblocks, float* d_out, void* stream);
+
 /* ---- Outputs: sigproc filterbank and event text --------------------------
  * SigprocStokesWriter (lib/src/SigprocStokesWriter.cpp:15-293) and
  * DedispersionDataAnalysisOutput (lib/src/DedispersionDataAnalysisOutput.cpp:

@@ -440,6 +440,58 @@ class AdapterTimeSeriesDataSet {
     DeviceBuffer din_, dout_;
 };
 
+// lib/src/ABDataAdapter.cpp:14-173: options <spectrum packets>, <packet
+// channels>, <packet samples>, <samplingTime seconds>.  deserialise() takes
+// the chunk's bytes from host memory: the headers are read on the host
+// (pv_ab_headers) and the Stokes-I spectra are assembled on the GPU
+// (pv_ab_unpack) into the one-subband, one-polarisation blob given to
+// config(), with the chunk's last packet's time and the sampling time.
+class ABDataAdapter {
+  public:
+    explicit ABDataAdapter(const ConfigNode& config) {
+        c_.packets_per_spectrum = (int)to_uint(config.getOption("spectrum", "packets"));
+        c_.channels = (int)to_uint(config.getOption("packet", "channels"));
+        c_.samples_per_packet = (int)to_uint(config.getOption("packet", "samples"));
+        c_.tsamp = to_float(config.getOption("samplingTime", "seconds"));
+    }
+    // AbstractStreamAdapter::config: the blob to fill and the chunk's bytes.
+    void config(SpectrumDataSetStokes* data, size_t chunkSize) {
+        data_ = data;
+        chunk_ = chunkSize;
+    }
+    void deserialise(const void* chunk) {
+        if (!data_) throw std::runtime_error("ABDataAdapter: Cannot deserialise into an unallocated blob!.");
+        const long long npk = c_.channels > 0 ? (long long)chunk_ / (8 + 8LL * c_.channels) : 0;
+        std::vector<int> index((size_t)std::max<long long>(1, npk));
+        long long nsp = 0, nbl = 0, gaps = 0;
+        double ts = 0.0;
+        pv_check(pv_ab_headers(&c_, &st_, chunk, (long long)chunk_, index.data(), (long long)index.size(), &nsp,
+                               &nbl, &ts, &gaps));
+        if (gaps) std::cerr << "FATAL! " << gaps << " packet(s) more than one sample after the previous" << std::endl;
+        gaps_ += gaps;
+        data_->resize((unsigned)nbl, 1, 1, (unsigned)c_.channels);
+        void* d_in = din_.get(chunk_);
+        int* d_index = dindex_.as<int>(index.size());
+        float* d_out = dout_.as<float>(std::max<size_t>(1, data_->size()));
+        pv_check(pv_device_copy(d_in, chunk, (long long)chunk_, nullptr));
+        if (nsp) pv_check(pv_device_copy(d_index, index.data(), 4 * nsp, nullptr));
+        pv_check(pv_ab_unpack(&c_, d_in, (long long)chunk_, d_index, nsp, nbl, d_out, nullptr));
+        if (data_->size()) pv_check(pv_device_copy(data_->data(), d_out, (long long)(4 * data_->size()), nullptr));
+        pv_check(pv_synchronize(nullptr));
+        data_->setLofarTimestamp(ts);
+        data_->setBlockRate(c_.tsamp);
+    }
+    long long gaps() const { return gaps_; }
+
+  private:
+    pv_ab_config c_{};
+    pv_ab_state st_{};
+    SpectrumDataSetStokes* data_ = nullptr;
+    size_t chunk_ = 0;
+    long long gaps_ = 0;
+    DeviceBuffer din_, dindex_, dout_;
+};
+
 // lib/src/PPFChanneliser.cpp:29-290
 class PPFChanneliser {
   public:
@@ -723,33 +775,26 @@ class DedispersionAnalyser {
 // XML file with the reference's element names.  Outputs are callbacks in
 // place of the pelican output manager; input spectra are not kept, so
 // "SignalFoundSpectrum" has no data to send.
-class DedispersionPipeline {
+// What both pipeline drivers do with a dedispersed buffer
+// (DedispersionPipeline.cpp:111-150, ABPipeline.cpp:142-170): analyse it,
+// send the result to the "TriggerInput" outputs, and to the
+// "DedispersionDataAnalysis" outputs when the event count lies in
+// <events min max> (at least min when min >= max).
+class PipelineAnalysis {
   public:
     using Output = std::function<void(const DedispersionDataAnalysis&)>;
-    explicit DedispersionPipeline(const std::string& config_file) {
-        const ConfigNode c = ConfigNode::fromFile(config_file, "DedispersionPipeline");
-        min_ = to_uint(c.getOption("events", "min", "5"));
-        max_ = to_uint(c.getOption("events", "max", "0"));
-        ppf_.reset(new PPFChanneliser(ConfigNode::fromFile(config_file, "PPFChanneliser")));
-        stokes_.reset(new StokesGenerator(ConfigNode::fromFile(config_file, "StokesGenerator")));
+    // AbstractPipeline::dataOutput: "TriggerInput" or "DedispersionDataAnalysis"
+    void connectOutput(const std::string& stream, const Output& f) { outputs_.emplace_back(stream, f); }
+    unsigned buffers() const { return buffers_; }
+
+  protected:
+    // the modules after the first stages: RFI_Clipper, DedispersionModule, DedispersionAnalyser
+    void setup(const std::string& config_file) {
         rfi_.reset(new RFI_Clipper(ConfigNode::fromFile(config_file, "RFI_Clipper")));
         dd_.reset(new DedispersionModule(ConfigNode::fromFile(config_file, "DedispersionModule")));
         an_.reset(new DedispersionAnalyser(ConfigNode::fromFile(config_file, "DedispersionAnalyser")));
         dd_->connect([this](DedispersionSpectra* d) { analysis(d); });
     }
-    // AbstractPipeline::dataOutput: "TriggerInput" or "DedispersionDataAnalysis"
-    void connectOutput(const std::string& stream, const Output& f) { outputs_.emplace_back(stream, f); }
-
-    void run(TimeSeriesDataSetC32* timeSeries) {
-        ppf_->run(timeSeries, &spectra_);
-        stokes_->run(&spectra_, &stokes_data_);
-        WeightedSpectrumDataSet w(&stokes_data_);
-        rfi_->run(&w);
-        dd_->dedisperse(&w);
-    }
-    unsigned buffers() const { return buffers_; }
-
-  private:
     void emit(const std::string& stream, const DedispersionDataAnalysis& r) {
         for (auto& o : outputs_)
             if (o.first == stream) o.second(r);
@@ -764,14 +809,71 @@ class DedispersionPipeline {
     }
 
     unsigned min_ = 5, max_ = 0, buffers_ = 0;
-    std::unique_ptr<PPFChanneliser> ppf_;
-    std::unique_ptr<StokesGenerator> stokes_;
     std::unique_ptr<RFI_Clipper> rfi_;
     std::unique_ptr<DedispersionModule> dd_;
     std::unique_ptr<DedispersionAnalyser> an_;
+    std::vector<std::pair<std::string, Output>> outputs_;
+};
+
+class DedispersionPipeline : public PipelineAnalysis {
+  public:
+    explicit DedispersionPipeline(const std::string& config_file) {
+        const ConfigNode c = ConfigNode::fromFile(config_file, "DedispersionPipeline");
+        min_ = to_uint(c.getOption("events", "min", "5"));
+        max_ = to_uint(c.getOption("events", "max", "0"));
+        ppf_.reset(new PPFChanneliser(ConfigNode::fromFile(config_file, "PPFChanneliser")));
+        stokes_.reset(new StokesGenerator(ConfigNode::fromFile(config_file, "StokesGenerator")));
+        setup(config_file);
+    }
+    void run(TimeSeriesDataSetC32* timeSeries) {
+        ppf_->run(timeSeries, &spectra_);
+        stokes_->run(&spectra_, &stokes_data_);
+        WeightedSpectrumDataSet w(&stokes_data_);
+        rfi_->run(&w);
+        dd_->dedisperse(&w);
+    }
+
+  private:
+    std::unique_ptr<PPFChanneliser> ppf_;
+    std::unique_ptr<StokesGenerator> stokes_;
     SpectrumDataSetC32 spectra_;
     SpectrumDataSetStokes stokes_data_;
-    std::vector<std::pair<std::string, Output>> outputs_;
+};
+
+// pipelines/udpstream/src/ABPipeline.cpp:56-140: the ALFABURST driver.  Each
+// chunk's spectra (ABDataAdapter) go through the StokesIntegrator (its
+// element is optional: 1 and 1 when absent, as createModule gives), the
+// RFI_Clipper, the DedispersionModule and the analyser; <events min max>
+// default to 5 and 5.  <history> sizes the reference's lock ring of input
+// blobs, which the module here does not need: it copies the data it keeps.
+class ABPipeline : public PipelineAnalysis {
+  public:
+    explicit ABPipeline(const std::string& config_file) {
+        const ConfigNode c = ConfigNode::fromFile(config_file, "ABPipeline");
+        history_ = to_uint(c.getOption("history", "value", "10"));
+        min_ = to_uint(c.getOption("events", "min", "5"));
+        max_ = to_uint(c.getOption("events", "max", "5"));
+        ConfigNode integ;
+        try {
+            integ = ConfigNode::fromFile(config_file, "StokesIntegrator");
+        } catch (const std::runtime_error&) {
+        }
+        integrator_.reset(new StokesIntegrator(integ));
+        setup(config_file);
+    }
+    void run(SpectrumDataSetStokes* stokes) {
+        if (!stokes) throw std::runtime_error("No stokes!");
+        integrator_->run(stokes, &integrated_);
+        WeightedSpectrumDataSet w(&integrated_);
+        rfi_->run(&w);
+        dd_->dedisperse(&w);
+    }
+    unsigned history() const { return history_; }
+
+  private:
+    unsigned history_ = 10;
+    std::unique_ptr<StokesIntegrator> integrator_;
+    SpectrumDataSetStokes integrated_;
 };
 
 // ---------------------------------------------------------------------------

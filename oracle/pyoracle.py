@@ -329,6 +329,46 @@ def udp_time(packet, clock_mhz=200):
     return ts.value, rate.value
 
 
+def ab_deserialise(chunk, packets_per_spectrum, channels, samples_per_packet, tsamp, state):
+    """ABDataAdapter::deserialise (ABDataAdapter.cpp:44-173), packet by packet
+    in Python.  Header bytes 0-5 are the integration count, most significant
+    first (the reference reads 8 bytes little-endian, masks 48 bits and swaps
+    them back); a packet's time is (count - start) * tsamp in double with
+    tsamp a float, start being 0 for the very first packet and that packet's
+    count afterwards; a time more than tsamp after the previous packet's is a
+    gap.  Packets of quarter packets_per_spectrum - 3 (compared as unsigned)
+    fill the next block with float(ntohs(XX) + ntohs(YY)) per channel.  The
+    blob has (packets // packets_per_spectrum) * samples blocks (samples 0
+    counts as 1); spectra past it are dropped, blocks not filled are 0.
+    state: dict with seen, count0, last_time, updated in place.  Returns
+    (spectra float32 [blocks][channels], timestamp, gaps, blocks filled)."""
+    psize = 8 + 8 * channels
+    raw = np.frombuffer(bytes(chunk), np.uint8)
+    npk = len(raw) // psize
+    nblocks = npk // packets_per_spectrum * (samples_per_packet if samples_per_packet > 0 else 1)
+    out = np.zeros((nblocks, channels), np.float32)
+    keep = (packets_per_spectrum - 3) & 0xFFFFFFFF
+    ts = float(np.float32(tsamp))
+    block, gaps, t = 0, 0, 0.0
+    for p in range(npk):
+        h = raw[p * psize:p * psize + 8]
+        count = int.from_bytes(bytes(h[:6]), "big")
+        start = state["count0"] if state["seen"] else 0
+        t = float((count - start) & 0xFFFFFFFFFFFFFFFF) * ts
+        if state["seen"]:
+            if t - state["last_time"] > ts:
+                gaps += 1
+        else:
+            state["count0"] = count
+        if int(h[6]) == keep and block < nblocks:
+            rec = raw[p * psize + 8:(p + 1) * psize].view(">u2").reshape(channels, 4)
+            out[block] = (rec[:, 0].astype(np.int64) + rec[:, 1].astype(np.int64)).astype(np.float32)
+            block += 1
+        state["last_time"] = t
+        state["seen"] += 1
+    return out, t, gaps, block
+
+
 # --------------------------------------------------------------------------
 # F2 outputs: SigprocStokesWriter and DedispersionDataAnalysisOutput
 # --------------------------------------------------------------------------

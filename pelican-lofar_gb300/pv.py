@@ -107,6 +107,8 @@ def _declare(L):
         "pv_udp_check": (i, [vp, ll, P(ll), P(i)]),
         "pv_udp_unpack": (i, [vp, vp, ll, vp, i, vp]),
         "pv_udp_time": (i, [vp, vp, P(d), P(d)]),
+        "pv_ab_headers": (i, [vp, vp, vp, ll, vp, ll, P(ll), P(ll), P(d), P(ll)]),
+        "pv_ab_unpack": (i, [vp, vp, ll, vp, ll, ll, vp, vp]),
         "pv_sigproc_header": (i, [vp, vp, ll, P(ll)]),
         "pv_sigproc_mjd": (d, [d]),
         "pv_sigproc_pack": (i, [vp, i, i, i, i, i, i, f, f, vp, vp]),
@@ -492,6 +494,48 @@ class UdpAdapter:
         self.out_of_sequence = self.timestamp - self._last > self.block_rate
         self._last = self.timestamp + nblocks * c.nchan * self.block_rate
         return res
+
+
+class AbConfig(C.Structure):
+    _fields_ = [("packets_per_spectrum", C.c_int), ("channels", C.c_int), ("samples_per_packet", C.c_int),
+                ("tsamp", C.c_float)]
+
+
+class AbState(C.Structure):
+    _fields_ = [("seen", C.c_longlong), ("count0", C.c_ulonglong), ("last_time", C.c_double)]
+
+
+class ABDataAdapter:
+    """ABDataAdapter (lib/src/ABDataAdapter.cpp:14-173), the input of
+    ABPipeline: chunks of ALFABURST spectrometer packets -> a device
+    SpectrumDataSetStokes float32 [block][1][1][channels] of Stokes I.
+    Keyword names follow the XML options (<spectrum packets>, <packet
+    channels>, <packet samples>, <samplingTime seconds>).  The headers are
+    read on the host; timestamp (the chunk's last packet), block_rate and gaps
+    (the reference's "FATAL!" packets) are kept as attributes."""
+
+    def __init__(self, packets=4, channels=1024, samples=0, seconds=0.0):
+        self.cfg = AbConfig(packets, channels, samples, seconds)
+        self.state = AbState()
+        self.timestamp, self.block_rate, self.gaps = 0.0, float(np.float32(seconds)), 0
+
+    def deserialise(self, chunk, stream=None):
+        import torch
+        host = np.ascontiguousarray(np.frombuffer(chunk, np.uint8) if not isinstance(chunk, np.ndarray)
+                                    else chunk.view(np.uint8).reshape(-1))
+        npk = len(host) // (8 + 8 * self.cfg.channels)
+        idx = np.zeros(max(1, npk), np.int32)
+        nsp, nbl, ts, gaps = C.c_longlong(0), C.c_longlong(0), C.c_double(0), C.c_longlong(0)
+        check(load().pv_ab_headers(C.byref(self.cfg), C.byref(self.state), host.ctypes.data, len(host),
+                                   idx.ctypes.data, len(idx), C.byref(nsp), C.byref(nbl), C.byref(ts),
+                                   C.byref(gaps)))
+        d_chunk = torch.from_numpy(host).cuda()
+        d_idx = torch.from_numpy(idx[:max(1, nsp.value)]).cuda()
+        out = torch.empty((nbl.value, 1, 1, self.cfg.channels), dtype=torch.float32, device=d_chunk.device)
+        check(load().pv_ab_unpack(C.byref(self.cfg), _ptr(d_chunk), len(host), _ptr(d_idx), nsp.value,
+                                  nbl.value, _ptr(out), _stream(stream)))
+        self.timestamp, self.gaps = ts.value, gaps.value
+        return out
 
 
 class SigprocParams(C.Structure):

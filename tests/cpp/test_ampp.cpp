@@ -16,6 +16,9 @@
 //   test_ampp pipeline DIR N    N chunks of DIR/chunks.bin through AdapterTimeSeriesDataSet and
 //                               DedispersionPipeline into a DedispersionDataAnalysisOutput;
 //                               prints "BUFFERS n"
+//   test_ampp ab DIR N          N chunks of DIR/chunks.bin through ABDataAdapter and ABPipeline into a
+//                               DedispersionDataAnalysisOutput; writes DIR/spectra.bin (the adapter's
+//                               blobs) and prints "BUFFERS n", "GAPS g", "TIME t rate" per chunk
 //   test_ampp udp DIR           AdapterTimeSeriesDataSet on DIR/chunk.bin with DIR/config.xml;
 //                               writes DIR/ts.bin, prints "SHAPE nb ns np nt" and "TIME ts rate"
 #include <pv/ampp.hpp>
@@ -256,6 +259,28 @@ int pipeline_mode(const std::string& dir, int nchunks) {
     return 0;
 }
 
+int ab_mode(const std::string& dir, int nchunks) {
+    const std::string xml = dir + "/config.xml";
+    const auto all = read_file<unsigned char>(dir + "/chunks.bin");
+    const size_t chunk = all.size() / (size_t)nchunks;
+    ABDataAdapter adapter(ConfigNode::fromFile(xml, "ABDataAdapter"));
+    ABPipeline pipeline(xml);
+    DedispersionDataAnalysisOutput out(ConfigNode::fromFile(xml, "DedispersionDataAnalysisOutput"));
+    pipeline.connectOutput("DedispersionDataAnalysis",
+                           [&](const DedispersionDataAnalysis& r) { out.sendStream(&r); });
+    std::ofstream sp(dir + "/spectra.bin", std::ios::binary);
+    SpectrumDataSetStokes stokes;
+    for (int k = 0; k < nchunks; ++k) {
+        adapter.config(&stokes, chunk);
+        adapter.deserialise(all.data() + (size_t)k * chunk);
+        sp.write(reinterpret_cast<const char*>(stokes.data()), (std::streamsize)(stokes.size() * sizeof(float)));
+        std::printf("TIME %.17g %.17g\n", stokes.getLofarTimestamp(), stokes.getBlockRate());
+        pipeline.run(&stokes);
+    }
+    std::printf("BUFFERS %u\nGAPS %lld\n", pipeline.buffers(), adapter.gaps());
+    return 0;
+}
+
 int udp_mode(const std::string& dir) {
     const ConfigNode cfg = ConfigNode::fromFile(dir + "/config.xml", "AdapterTimeSeriesDataSet");
     const auto chunk = read_file<unsigned char>(dir + "/chunk.bin");
@@ -283,6 +308,7 @@ int main(int argc, char** argv) {
         if (mode == "ddout" && argc >= 4) return ddout_mode(argv[2], std::atoi(argv[3]));
         if (mode == "sigproc" && argc >= 3) return sigproc_mode(argv[2]);
         if (mode == "pipeline" && argc >= 4) return pipeline_mode(argv[2], std::atoi(argv[3]));
+        if (mode == "ab" && argc >= 4) return ab_mode(argv[2], std::atoi(argv[3]));
     } catch (const std::exception& e) {
         std::fprintf(stderr, "EXCEPTION %s\n", e.what());
         return 3;

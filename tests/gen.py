@@ -127,3 +127,28 @@ def inject_dispersed_pulse(vc, sub_freq0, sub_bw, tsamp_raw, dm, t0, width, snr_
             lo, hi = max(start, 0), min(start + L, n)
             vc[s, p, lo:hi] += disp[lo - start:hi - start].astype(np.complex64)
     return vc
+
+
+def ab_emulator_packets(npackets, channels, counter0=0, quarter0=0, beam=0, records=None, skip=()):
+    """Packets as the reference's ABEmulator writes them (lib/test/src/ABEmulator.cpp:
+    49-98): the header counter big-endian in bytes 0-5, the spectral quarter in
+    byte 6 (0..3, the counter advancing after quarter 3), the beam in byte 7,
+    then per channel four 16-bit values in host (little-endian) order: 42, 43,
+    44, 45.  records (uint16 [npackets][channels][4]) replaces those values,
+    written big-endian as the spectrometer sends them; packets whose index is
+    in skip are left out (lost packets)."""
+    psize = 8 + 8 * channels
+    chunks = []
+    counter, quarter = counter0, quarter0
+    emu = np.tile(np.array((42, 43, 44, 45), "<i2"), channels).view(np.uint8)
+    for p in range(npackets):
+        if p not in skip:
+            pk = np.zeros(psize, np.uint8)
+            pk[:6] = np.frombuffer(counter.to_bytes(6, "big"), np.uint8)
+            pk[6], pk[7] = quarter, beam
+            pk[8:] = emu if records is None else np.asarray(records[p], ">u2").reshape(-1).view(np.uint8)
+            chunks.append(pk)
+        quarter = (quarter + 1) % 4
+        if quarter == 0:
+            counter += 1
+    return np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)

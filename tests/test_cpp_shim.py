@@ -261,6 +261,111 @@ def test_shim_trigger_output_sends_the_oracle_message(pv, oracle, cuda, shim_exe
     rx.close()
 
 
+AB_XML = """<configuration>
+  <ABDataAdapter>
+    <spectrum packets="4"/>
+    <packet channels="{nch}"/>
+    <samplingTime seconds="{tsamp}"/>
+  </ABDataAdapter>
+  <ABPipeline>
+    <history value="2048"/>
+    <events min="{emin}" max="{emax}"/>
+  </ABPipeline>
+  <RFI_Clipper active="true" channelRejectionRMS="3.5" spectrumRejectionRMS="6.0">
+    <zeroDMing active="true"/>
+    <BandPassData file="band.bp"/>
+    <Band matching="true"/>
+    <History maximum="1000"/>
+  </RFI_Clipper>
+  <DedispersionModule>
+    <timeBinsPerBufferPow2 value="12"/>
+    <frequencyChannel1 MHz="{fch1}"/>
+    <sampleTime seconds="{tsamp}"/>
+    <channelBandwidth MHz="{foff}"/>
+    <dedispersionSamples value="{tdms}"/>
+    <dedispersionStepSize value="{dm_step}"/>
+    <dedispersionMinimum value="0"/>
+  </DedispersionModule>
+  <DedispersionAnalyser>
+    <detectionThreshold in_sigma="{thr}"/>
+    <power2ForBinning value="4"/>
+  </DedispersionAnalyser>
+  <DedispersionDataAnalysisOutput>
+    <file name="{path}"/>
+  </DedispersionDataAnalysisOutput>
+</configuration>
+"""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("emin,emax", [(1, 0), (10 ** 6, 10 ** 7)])
+def test_shim_ab_pipeline_from_spectrometer_packets_to_event_file(pv, oracle, cuda, shim_exe, tmp_path, emin,
+                                                                  emax):
+    """ALFABURST packets -> ABDataAdapter -> ABPipeline (StokesIntegrator with
+    its defaults, RFI_Clipper, DedispersionModule, analyser) ->
+    DedispersionDataAnalysisOutput, with 8 packets lost in the fourth chunk:
+    the adapter's blobs equal the oracle's, and the event file equals the same
+    chain composed through the Python binding."""
+    import torch
+    from gen import ab_emulator_packets
+    nch, npk, nchunks, tdms, dm_step, thr = 64, 4096, 10, 32, 1.0, 3.0
+    fch1, foff, tsamp = 1500.0, -0.1, 0.000128
+    rng = np.random.default_rng(23)
+    total = nchunks * npk + 8
+    lost = tuple(range(3 * npk + 100, 3 * npk + 108))
+    stream = ab_emulator_packets(total, nch, counter0=5000, records=rng.integers(0, 65536, (total, nch, 4)),
+                                 skip=lost)
+    stream.tofile(tmp_path / "chunks.bin")
+    chunk_bytes = len(stream) // nchunks
+    chunks = [stream[k * chunk_bytes:(k + 1) * chunk_bytes] for k in range(nchunks)]
+    ad = pv.ABDataAdapter(packets=4, channels=nch, seconds=tsamp)
+    spectra, times, ost = [], [], {"seen": 0, "count0": 0, "last_time": 0.0}
+    for c in chunks:
+        x = ad.deserialise(c)
+        want, t, _, _ = oracle.ab_deserialise(c, 4, nch, 0, tsamp, ost)
+        assert np.array_equal(x.cpu().numpy().reshape(want.shape), want) and ad.timestamp == t
+        spectra.append(x)
+        times.append(t)
+    fb0 = spectra[0].cpu().numpy()
+    (tmp_path / "band.bp").write_text(make_bp_text(nch, fch1 + foff * (nch - 1), -foff, float(fb0.mean()),
+                                                   float(fb0.std())))
+    (tmp_path / "config.xml").write_text(AB_XML.format(nch=nch, tsamp=repr(tsamp), emin=emin, emax=emax,
+                                                       fch1=repr(fch1), foff=repr(foff), tdms=tdms,
+                                                       dm_step=dm_step, thr=thr, path=str(tmp_path / "ev")))
+    out = _run(shim_exe, "ab", tmp_path, nchunks)
+    lines = out.splitlines()
+    got_times = [float(ln.split()[1]) for ln in lines if ln.startswith("TIME")]
+    assert got_times == times
+    assert all(float(ln.split()[2]) == float(np.float32(tsamp)) for ln in lines if ln.startswith("TIME"))
+    assert int(out.split("GAPS")[1].split()[0]) == 1
+    got_sp = np.fromfile(tmp_path / "spectra.bin", np.float32)
+    assert np.array_equal(got_sp, torch.cat([s.reshape(-1) for s in spectra]).cpu().numpy())
+    nbuf = int(out.split("BUFFERS")[1].split()[0])
+    # the same chain through the binding
+    rfi = pv.RFI((tmp_path / "band.bp").read_text(), cr=3.5, sr=6.0, history=1000, zero_dming=True)
+    dd = pv.DedispersionModule(1 << 12, tdms, 0.0, dm_step, fch1, foff)
+    rate = float(np.float32(tsamp))
+    rms = float(np.sqrt(np.float32(nch) * np.float32(1)))
+    text, dump, nbuf_want = "", 0, 0
+    for x in spectra:
+        xi = pv.integrate(x, 1, 1)
+        rfi.run(xi)
+        for buf, first in dd.add(xi.cpu().numpy(), rate):
+            nbuf_want += 1
+            ev, n = pv.analyse(torch.from_numpy(buf).to(cuda), thr, rms, 4)
+            if (n >= emin) if emin >= emax else (emin <= n <= emax):
+                dump += 1
+                text += pv.events_text(ev, times[0], rate, first, 0.0, dm_step, np.float32(rms), dump)
+    assert nbuf == nbuf_want >= 2
+    files = list(tmp_path.glob("ev_D*.dat"))
+    assert len(files) == 1
+    assert files[0].read_text() == pv.EVENTS_TEXT_HEADER + text
+    if emin > 1000:
+        assert text == ""
+    else:
+        assert text.count("\n") > 2
+
+
 SIGPROC_XML = """<configuration>
   <SigprocStokesWriter writeHeader="true">
     <file filepath="{path}"/>
