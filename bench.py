@@ -982,12 +982,33 @@ class CpuChain:
         return (t1 - t0) * self.sub_scale + (t3 - t2) + (t4 - t3) * self.trial_scale
 
 
+def host_cpu():
+    """The host's CPU model and logical CPU count, for the CPU baselines."""
+    model, impl, part = None, None, None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key, _, val = line.partition(":")
+                key, val = key.strip(), val.strip()
+                if key == "model name" and model is None:
+                    model = val
+                elif key == "CPU implementer" and impl is None:
+                    impl = val
+                elif key == "CPU part" and part is None:
+                    part = val
+    except OSError:
+        pass
+    if model is None and part is not None:
+        model = {"0xd4f": "Arm Neoverse V2"}.get(part.lower(), "Arm implementer %s part %s" % (impl, part))
+    return {"cpu_model": model or "unknown", "nproc": os.cpu_count()}
+
+
 def cpu_baseline(cfg, args, repeats=1):
     chain = CpuChain(cfg)
     secs = [chain.chunk_seconds() for _ in range(repeats)]
     units = cfg["tdms"] * cfg["nsub"] * cfg["nchan_sub"] * cfg["chunk"]
     return {"value": units / float(np.median(secs)), "unit": "DM-trial*chan*samples/s",
-            "cores": chain.po.num_threads(), "kind": "port",
+            "cores": chain.po.num_threads(), "kind": "port", **host_cpu(),
             "sample": chain.sample + "; %.1f s per chunk extrapolated" % float(np.median(secs))}
 
 
@@ -1012,7 +1033,7 @@ def cpu_baseline_mix(cfgs):
     secs = cpu_mix_seconds(chains, cfgs)
     units = sum(c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs)
     return {"value": units / secs, "unit": "DM-trial*chan*samples/s",
-            "cores": chains[0].po.num_threads(), "kind": "port",
+            "cores": chains[0].po.num_threads(), "kind": "port", **host_cpu(),
             "sample": "first %d beams of the mix, each: %s; scaled to the %d-beam step by work "
                       "(%.1f s per step)" % (len(chains), "; ".join(ch.sample for ch in chains),
                                              len(cfgs), secs)}
@@ -1049,7 +1070,7 @@ def run_reference(args, cfgs, workload):
                        "nchan_total": sum(c["nsub"] * c["nchan_sub"] for c in cfgs),
                        "tdms_total": sum(c["tdms"] for c in cfgs), "chunk": cfgs[0]["chunk"]},
             "cpu_baseline": {"value": value, "unit": "DM-trial*chan*samples/s",
-                             "cores": chains[0].po.num_threads(), "kind": "port",
+                             "cores": chains[0].po.num_threads(), "kind": "port", **host_cpu(),
                              "sample": sample + " per step; the reference needs Qt4, Boost, "
                                        "FFTW3 and pelican, so its algorithm's CPU restatement is "
                                        "timed"},
