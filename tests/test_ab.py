@@ -91,3 +91,25 @@ def test_gpu_emulator_packets_decode_to_the_known_answer(pv, cuda):
     ad = pv.ABDataAdapter(packets=4, channels=1024, seconds=0.000128)
     got = ad.deserialise(ab_emulator_packets(1024, 1024)).cpu().numpy()  # the reference XML's chunk
     assert got.shape == (256, 1, 1, 1024) and np.all(got == 21760.0)
+
+
+@pytest.mark.parametrize("pps,tail", [(2, 0), (1, 0), (4, 100), (5, 7)])
+def test_header_pass_edge_cases_equal_the_oracle(pv, oracle, pps, tail):
+    """Fewer than 3 packets per spectrum (the quarter to keep, pps - 3, wraps
+    as an unsigned number, so no packet fills a spectrum) and chunks ending in
+    part of a packet (ignored)."""
+    import ctypes as C
+    rng = np.random.default_rng(pps * 100 + tail)
+    pk = ab_emulator_packets(24, NCH, counter0=3, records=rng.integers(0, 65536, (24, NCH, 4)))
+    chunk = np.concatenate([pk, rng.integers(0, 256, tail).astype(np.uint8)])
+    want, t, gaps, n = oracle.ab_deserialise(chunk, pps, NCH, 0, 0.001, _state())
+    cfg = pv.AbConfig(pps, NCH, 0, 0.001)
+    idx = np.zeros(32, np.int32)
+    nsp, nbl, ts, g = C.c_longlong(0), C.c_longlong(0), C.c_double(0), C.c_longlong(0)
+    pv.check(pv.load().pv_ab_headers(C.byref(cfg), C.byref(pv.AbState()), chunk.ctypes.data, len(chunk),
+                                     idx.ctypes.data, len(idx), C.byref(nsp), C.byref(nbl), C.byref(ts),
+                                     C.byref(g)))
+    assert (nsp.value, nbl.value, ts.value, g.value) == (n, len(want), t, gaps)
+    assert nbl.value == 24 // pps
+    if pps < 3:
+        assert n == 0
