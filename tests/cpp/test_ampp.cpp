@@ -16,6 +16,10 @@
 //   test_ampp pipeline DIR N    N chunks of DIR/chunks.bin through AdapterTimeSeriesDataSet and
 //                               DedispersionPipeline into a DedispersionDataAnalysisOutput;
 //                               prints "BUFFERS n"
+//   test_ampp outputs DIR       (no GPU) DIR/events.bin and DIR/meta.txt (start rate first dmlow
+//                               dmstep rms ntime ndm) as one analysed buffer, sent twice through a
+//                               DedispersionDataAnalysisOutput and a TriggerOutput from
+//                               DIR/config.xml; prints "TRIGGER <message>" per trigger sent
 //   test_ampp ab DIR N          N chunks of DIR/chunks.bin through ABDataAdapter and ABPipeline into a
 //                               DedispersionDataAnalysisOutput; writes DIR/spectra.bin (the adapter's
 //                               blobs) and prints "BUFFERS n", "GAPS g", "TIME t rate" per chunk
@@ -259,6 +263,33 @@ int pipeline_mode(const std::string& dir, int nchunks) {
     return 0;
 }
 
+int outputs_mode(const std::string& dir) {
+    const std::string xml = dir + "/config.xml";
+    std::ifstream meta(dir + "/meta.txt");
+    double start, rate, dmlow, dmstep;
+    unsigned first, ntime, ndm;
+    float rms;
+    meta >> start >> rate >> first >> dmlow >> dmstep >> rms >> ntime >> ndm;
+    const auto ev = read_file<pv_event>(dir + "/events.bin");
+    DedispersionSpectra spectra;
+    spectra.resize(ntime, ndm, (float)dmlow, (float)dmstep);
+    spectra.setFirstSample(first);
+    spectra.setLofarTimestamp(start);
+    spectra.setBlockRate(rate);
+    DedispersionDataAnalysis result;
+    result.reset(&spectra);
+    result.setRMS(rms);
+    for (const pv_event& e : ev) result.addEvent((unsigned)e.dm, (unsigned)e.t, e.bin_factor, e.value);
+    DedispersionDataAnalysisOutput out(ConfigNode::fromFile(xml, "DedispersionDataAnalysisOutput"));
+    TriggerOutput trigger(ConfigNode::fromFile(xml, "TriggerOutput"));
+    for (int k = 0; k < 2; ++k) {
+        out.sendStream(&result);
+        const std::string m = trigger.sendStream(&result);
+        if (!m.empty()) std::printf("TRIGGER %s\n", m.c_str());
+    }
+    return 0;
+}
+
 int ab_mode(const std::string& dir, int nchunks) {
     const std::string xml = dir + "/config.xml";
     const auto all = read_file<unsigned char>(dir + "/chunks.bin");
@@ -309,6 +340,7 @@ int main(int argc, char** argv) {
         if (mode == "sigproc" && argc >= 3) return sigproc_mode(argv[2]);
         if (mode == "pipeline" && argc >= 4) return pipeline_mode(argv[2], std::atoi(argv[3]));
         if (mode == "ab" && argc >= 4) return ab_mode(argv[2], std::atoi(argv[3]));
+        if (mode == "outputs" && argc >= 3) return outputs_mode(argv[2]);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "EXCEPTION %s\n", e.what());
         return 3;

@@ -219,6 +219,46 @@ TRIGGER_XML = """  <TriggerOutput>
 """
 
 
+OUTPUTS_XML = """<configuration>
+  <DedispersionDataAnalysisOutput>
+    <file name="{path}"/>
+  </DedispersionDataAnalysisOutput>
+""" + TRIGGER_XML
+
+
+def test_shim_outputs_of_an_analysed_buffer_equal_the_oracle(pv, oracle, shim_exe, tmp_path):
+    """No GPU: one analysed buffer, sent twice, through the shim's
+    DedispersionDataAnalysisOutput (the .dat text) and TriggerOutput (the
+    datagrams, numbered 0001 and 0002, and the log lines)."""
+    import re
+    import socket
+    from test_outputs import _events
+    ev = _events(np.random.default_rng(41), 30)
+    ev.tofile(tmp_path / "events.bin")
+    start, rate, first, rms = 1.31e9 + 0.5, 327.68e-6, 8192, np.float32(45.254834)
+    (tmp_path / "meta.txt").write_text("%r %r %d %r %r %r %d %d\n" % (start, rate, first, 0.0, 0.25,
+                                                                       float(rms), 4096, 200))
+    rx = socket.socket(socket.AF_INET, socket.SOCK_DGRAM)
+    rx.bind(("127.0.0.1", 0))
+    rx.settimeout(5.0)
+    (tmp_path / "config.xml").write_text(OUTPUTS_XML.format(path=tmp_path / "ev", port=rx.getsockname()[1],
+                                                            log=tmp_path / "trig.log", snr=5.0))
+    out = _run(shim_exe, "outputs", tmp_path)
+    sent = [ln[len("TRIGGER "):] for ln in out.splitlines() if ln.startswith("TRIGGER ")]
+    assert len(sent) == 2
+    root = re.fullmatch(r"artemis:CS302##ID:(\d{12}-07)0001##.*", sent[0]).group(1)
+    want = [oracle.trigger_message(ev, start, rate, first, 0.0, float(np.float32(0.25)), rms, 2, 5.0, "CS302", root,
+                                   k, "150.0", "83.633", "22.014") for k in (1, 2)]
+    assert sent == want
+    assert [rx.recv(4096).decode() for _ in range(2)] == want
+    assert (tmp_path / "trig.log").read_text() == want[0] + "\n" + want[1] + "\n"
+    files = list(tmp_path.glob("ev_D*.dat"))
+    assert len(files) == 1
+    text = "".join(oracle.events_text(ev, start, rate, first, 0.0, float(np.float32(0.25)), rms, k) for k in (1, 2))
+    assert files[0].read_text() == oracle.EVENTS_TEXT_HEADER + text
+    rx.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("snr", [8.0, 1e9])
 def test_shim_trigger_output_sends_the_oracle_message(pv, oracle, cuda, shim_exe, tmp_path, snr):
