@@ -44,6 +44,7 @@
 #include <iostream>
 #include <complex>
 #include <cstring>
+#include <deque>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -340,12 +341,18 @@ class DedispersionSpectra : public DataBlob {
     unsigned inputSubbands() const { return nsub_; }
     float getRMS() const { return rms_; }
     void setRMS(float r) { rms_ = r; }
+    // The Stokes blobs whose samples the buffer holds, oldest first
+    // (DedispersionSpectra::inputDataBlobs, filled by DedispersionBuffer::copy
+    // and addSamples); valid while the functors run.
+    const std::vector<const SpectrumDataSetStokes*>& inputDataBlobs() const { return inputs_; }
+    void setInputDataBlobs(const std::vector<const SpectrumDataSetStokes*>& b) { inputs_ = b; }
 
   private:
     unsigned t_ = 0, n_ = 0, first_ = 0, nch_ = 0, nsub_ = 0;
     double lower_ = 0.0, width_ = 1.0;
     float rms_ = 0.0f;
     std::vector<float> d_;
+    std::vector<const SpectrumDataSetStokes*> inputs_;
 };
 
 class DedispersionEvent {
@@ -700,6 +707,9 @@ class DedispersionModule {
             t0_ = d->getLofarTimestamp();
             have_t0_ = true;
         }
+        // a copy of the blob for the buffers that will hold its samples
+        held_.push_back(Held{received_, std::make_shared<SpectrumDataSetStokes>(*d)});
+        received_ += d->nTimeBlocks();
         for (int i = 0; i < done; ++i) {
             int p[6] = {0};
             pv_check(pv_ddmod_params(h_, p));
@@ -712,10 +722,24 @@ class DedispersionModule {
             out.setInputShape(nch_, nsub_);
             out.setBlockRate(d->getBlockRate());
             out.setLofarTimestamp(t0_);
+            std::vector<const SpectrumDataSetStokes*> inputs;
+            for (const Held& h : held_)
+                if (h.start < first + (long long)samples_ && h.start + h.blob->nTimeBlocks() > first)
+                    inputs.push_back(h.blob.get());
+            out.setInputDataBlobs(inputs);
             for (auto& f : functors_) f(&out);
             for (auto& f : chain_) f();
+            // later buffers start after this one: blobs wholly before it are not needed again
+            while (!held_.empty() && held_.front().start + held_.front().blob->nTimeBlocks() <= first)
+                held_.pop_front();
         }
     }
+    struct Held {
+        long long start;  // the blob's first sample in the stream
+        std::shared_ptr<SpectrumDataSetStokes> blob;
+    };
+    std::deque<Held> held_;
+    long long received_ = 0;
 
     pv_ddmod* h_ = nullptr;
     double t0_ = 0.0;
@@ -783,8 +807,14 @@ class DedispersionAnalyser {
 class PipelineAnalysis {
   public:
     using Output = std::function<void(const DedispersionDataAnalysis&)>;
+    using SpectrumOutput = std::function<void(const SpectrumDataSetStokes&)>;
     // AbstractPipeline::dataOutput: "TriggerInput" or "DedispersionDataAnalysis"
     void connectOutput(const std::string& stream, const Output& f) { outputs_.emplace_back(stream, f); }
+    // "SignalFoundSpectrum": each input blob of a buffer that reaches the
+    // "DedispersionDataAnalysis" outputs (for a SigprocStokesWriter)
+    void connectSpectrumOutput(const std::string& stream, const SpectrumOutput& f) {
+        spectrum_outputs_.emplace_back(stream, f);
+    }
     unsigned buffers() const { return buffers_; }
 
   protected:
@@ -805,7 +835,12 @@ class PipelineAnalysis {
         if (!an_->analyse(d, &result)) return;
         emit("TriggerInput", result);
         const unsigned n = (unsigned)result.eventsFound();
-        if (min_ >= max_ ? n >= min_ : (n >= min_ && n <= max_)) emit("DedispersionDataAnalysis", result);
+        if (min_ >= max_ ? n >= min_ : (n >= min_ && n <= max_)) {
+            emit("DedispersionDataAnalysis", result);
+            for (const SpectrumDataSetStokes* b : d->inputDataBlobs())
+                for (auto& o : spectrum_outputs_)
+                    if (o.first == "SignalFoundSpectrum") o.second(*b);
+        }
     }
 
     unsigned min_ = 5, max_ = 0, buffers_ = 0;
@@ -813,6 +848,7 @@ class PipelineAnalysis {
     std::unique_ptr<DedispersionModule> dd_;
     std::unique_ptr<DedispersionAnalyser> an_;
     std::vector<std::pair<std::string, Output>> outputs_;
+    std::vector<std::pair<std::string, SpectrumOutput>> spectrum_outputs_;
 };
 
 class DedispersionPipeline : public PipelineAnalysis {

@@ -22,7 +22,8 @@
 //                               DIR/config.xml; prints "TRIGGER <message>" per trigger sent
 //   test_ampp ab DIR N          N chunks of DIR/chunks.bin through ABDataAdapter and ABPipeline into a
 //                               DedispersionDataAnalysisOutput; writes DIR/spectra.bin (the adapter's
-//                               blobs) and prints "BUFFERS n", "GAPS g", "TIME t rate" per chunk
+//                               blobs) and prints "BUFFERS n", "GAPS g", "TIME t rate" per chunk and
+//                               "SIGNAL dump t blocks" per SignalFoundSpectrum blob
 //   test_ampp udp DIR           AdapterTimeSeriesDataSet on DIR/chunk.bin with DIR/config.xml;
 //                               writes DIR/ts.bin, prints "SHAPE nb ns np nt" and "TIME ts rate"
 #include <pv/ampp.hpp>
@@ -297,8 +298,14 @@ int ab_mode(const std::string& dir, int nchunks) {
     ABDataAdapter adapter(ConfigNode::fromFile(xml, "ABDataAdapter"));
     ABPipeline pipeline(xml);
     DedispersionDataAnalysisOutput out(ConfigNode::fromFile(xml, "DedispersionDataAnalysisOutput"));
-    pipeline.connectOutput("DedispersionDataAnalysis",
-                           [&](const DedispersionDataAnalysis& r) { out.sendStream(&r); });
+    int dumps = 0;
+    pipeline.connectOutput("DedispersionDataAnalysis", [&](const DedispersionDataAnalysis& r) {
+        out.sendStream(&r);
+        ++dumps;
+    });
+    pipeline.connectSpectrumOutput("SignalFoundSpectrum", [&](const SpectrumDataSetStokes& s) {
+        std::printf("SIGNAL %d %.17g %u\n", dumps, s.getLofarTimestamp(), s.nTimeBlocks());
+    });
     std::ofstream sp(dir + "/spectra.bin", std::ios::binary);
     SpectrumDataSetStokes stokes;
     for (int k = 0; k < nchunks; ++k) {

@@ -386,7 +386,8 @@ def test_shim_ab_pipeline_from_spectrometer_packets_to_event_file(pv, oracle, cu
     dd = pv.DedispersionModule(1 << 12, tdms, 0.0, dm_step, fch1, foff)
     rate = float(np.float32(tsamp))
     rms = float(np.sqrt(np.float32(nch) * np.float32(1)))
-    text, dump, nbuf_want = "", 0, 0
+    text, dump, nbuf_want, signal = "", 0, 0, []
+    nblk = npk // 4
     for x in spectra:
         xi = pv.integrate(x, 1, 1)
         rfi.run(xi)
@@ -396,7 +397,13 @@ def test_shim_ab_pipeline_from_spectrometer_packets_to_event_file(pv, oracle, cu
             if (n >= emin) if emin >= emax else (emin <= n <= emax):
                 dump += 1
                 text += pv.events_text(ev, times[0], rate, first, 0.0, dm_step, np.float32(rms), dump)
+                # SignalFoundSpectrum: the chunks whose samples the 4096-sample buffer holds
+                signal += [(dump, times[k], nblk) for k in range(nchunks)
+                           if k * nblk < first + 4096 and (k + 1) * nblk > first]
     assert nbuf == nbuf_want >= 2
+    got_signal = [(int(ln.split()[1]), float(ln.split()[2]), int(ln.split()[3])) for ln in lines
+                  if ln.startswith("SIGNAL")]
+    assert got_signal == signal and (emin > 1000) == (signal == [])
     files = list(tmp_path.glob("ev_D*.dat"))
     assert len(files) == 1
     assert files[0].read_text() == pv.EVENTS_TEXT_HEADER + text
