@@ -176,7 +176,7 @@ int parse_bandpass(const char* text, Bandpass& bp) {
     bp.set_rms(rms);
     for (unsigned idx : kills) {
         // The reference reads the kill line's index as its frequency too
-        // (BandPassAdapter.cpp:555), so the check below rejects it unless the
+        // (BandPassAdapter.cpp:67), so the check below rejects it unless the
         // index happens to name its own bin.
         if (m.index((double)idx) != (int)idx) {
             pv::set_error("BandPassAdapter:  Frequency kill mismatch: index %u does not match "

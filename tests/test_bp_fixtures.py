@@ -34,3 +34,18 @@ def test_broken_bandpass_files_fail_with_the_reference_messages(pv, oracle, path
             pv.RFI(text, history=10)
         with pytest.raises(ValueError):
             oracle.RFI(text, history=10)
+
+
+def test_kill_lines_are_checked_as_the_reference_reads_them(pv, oracle):
+    """BandPassAdapter reads a kill line's index as its frequency too (:60-70),
+    so 'K index frequency' passes its bin check only when the index names its
+    own bin: with start 0 and width 1 it does, elsewhere it fails."""
+    body = open(FILES[0]).read().splitlines()
+    own = "\n".join(["# start 0, width 1", "64", "0", "64", "1", "2.0", "10.0", "K 5 5.0"]) + "\n"
+    pv.RFI(own, history=10)
+    oracle.RFI(own, history=10)
+    other = "\n".join(body + ["K 5 131.25"]) + "\n"
+    with pytest.raises(pv.PvError, match="Frequency kill mismatch"):
+        pv.RFI(other, history=10)
+    with pytest.raises(ValueError, match="Frequency kill mismatch"):
+        oracle.RFI(other, history=10)
