@@ -735,7 +735,8 @@ def run_io(args):
     adapter test's chunk (16384 packets, 133 MB) to int16 station order and to
     TimeSeriesDataSetC32; the sigproc pack of a full-band filterbank chunk
     (16384 x 3904) to 8- and 32-bit files; the bandpass recorder's integration
-    of the same filterbank."""
+    of the same filterbank; the ALFABURST assembly of 16384 spectrometer
+    packets of 1024 channels (134 MB, one packet in four kept)."""
     import torch
     import pv
 
@@ -799,6 +800,27 @@ def run_io(args):
     ms = timed(bp)
     byts = fbs[0].numel() * 4
     res["bandpass_integrate"] = {"ms": ms, "bytes": byts, "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    # ALFABURST spectrometer packets: 8-byte header, 1024 records of four big-endian 16-bit values
+    npk_ab, nch_ab = 16384, 1024
+    psize = 8 + 8 * nch_ab
+    ab_host = np.zeros((npk_ab, psize), np.uint8)
+    counts = np.arange(npk_ab, dtype=np.uint64) // 4
+    for b in range(6):
+        ab_host[:, b] = (counts >> np.uint64(8 * (5 - b))) & np.uint64(0xFF)
+    ab_host[:, 6] = np.arange(npk_ab) % 4
+    ab_host[:, 8:] = rng.integers(0, 256, (npk_ab, 8 * nch_ab), dtype=np.uint8)
+    ab_host = ab_host.reshape(-1)
+    abc = pv.AbConfig(4, nch_ab, 0, 0.000128)
+    ab_chunks = [torch.from_numpy(ab_host).to(dev) for _ in range(nrot)]
+    ab_idx = torch.arange(1, npk_ab, 4, dtype=torch.int32, device=dev)  # the quarter-1 packets
+    ab_out = torch.empty((npk_ab // 4, nch_ab), dtype=torch.float32, device=dev)
+
+    def ab(k):
+        pv.check(pv.load().pv_ab_unpack(pv.C.byref(abc), pv._ptr(ab_chunks[k]), len(ab_host), pv._ptr(ab_idx),
+                                        npk_ab // 4, npk_ab // 4, pv._ptr(ab_out), pv._stream(stream)))
+    ms = timed(ab)
+    byts = ab_out.numel() * 8 + ab_out.numel() * 4 + ab_idx.numel() * 4  # kept records in, spectra out
+    res["ab_unpack"] = {"ms": ms, "bytes": byts, "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
     clk = clocks.stop()
     launches = pv.launches() - launches0
 
