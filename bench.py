@@ -223,21 +223,25 @@ def device_voltages(cfg, dev, seed):
         v[:, :, int(b0):int(b0) + 16, :] *= 3.0
     # dispersed pulses (dm, width s, position as a fraction of the chunk):
     # Gaussian amplitude envelopes delayed per subband by the cold-plasma
-    # delay at the subband centre frequency
+    # delay at the subband centre frequency.  Every step feeds the same
+    # chunk, so the stream is periodic in the chunk duration and each
+    # subband's envelope sits at its delay modulo the chunk: the whole
+    # dispersed track is in the stream, a pulse once per chunk.  The peak
+    # raises a channel's power by 49 %, about 1.4 sigma of one integrated
+    # sample, under the 5-sigma channel clip; dedispersed over ~1000
+    # channels and a few samples the pulse stands far above 6 sigma.
     f_top = cfg["f_sub0"] + (nsub - 1) * SUB_BW
     for dm, width, pos in cfg.get("pulses", []):
         sig = max(width / 2.355 / RAW_TSAMP, 1.0)
         for s in range(nsub):
             f = cfg["f_sub0"] + s * SUB_BW
             delay = 4148.741601 * dm * (1.0 / f ** 2 - 1.0 / f_top ** 2) / RAW_TSAMP
-            c0 = pos * n + delay
+            c0 = (pos * n + delay) % n
             lo, hi = int(c0 - 4 * sig), int(c0 + 4 * sig) + 1
-            if hi <= 0 or lo >= n:
-                continue
-            lo, hi = max(lo, 0), min(hi, n)
             tt = torch.arange(lo, hi, device=dev, dtype=torch.float32)
-            env = 1.0 + 1.5 * torch.exp(-0.5 * ((tt - c0) / sig) ** 2)
-            v[s, :, lo:hi, :] *= env[None, :, None]
+            env = 1.0 + 0.22 * torch.exp(-0.5 * ((tt - c0) / sig) ** 2)
+            idx = torch.remainder(torch.arange(lo, hi, device=dev), n)
+            v[s, :, idx, :] *= env[None, :, None]
     return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
 
 
@@ -439,20 +443,28 @@ def run_batch(args, cfgs, workload):
         hosts.append(pv.HostBuffer(v.numel() * v.element_size()))
         hosts[-1].fill_from(v)
 
-    def plain_step(e2e=False):
+    plain_rec = [dict() for _ in range(nb)]  # window index -> (digest, events) of the untimed steps
+
+    def plain_step(e2e=False, record=False):
         d2h = 0
         for i, b in enumerate(beams):
             if e2e:
                 b.process_host(hosts[i], stream=stream)
             else:
                 b.process(volts[i], stream=stream)
-            ev, n, _ = b.events(cap=1 << 16, stream=stream)  # synchronises: job per buffer
+            ev, n, first = b.events(cap=1 << 16, stream=stream)  # synchronises: job per buffer
             d2h += 8 + ev.nbytes
+            if record and first >= 0:
+                c = cfgs[i]
+                plain_rec[i][first // c["chunk"]] = (
+                    window_digest(pv, b.buffers()[2], c["tdms"] * c["chunk"], stream), ev[:n].tobytes())
         return d2h
 
     plain_steps = max(2, args.steps // 2)
-    for _ in range(args.warmup):
-        plain_step()
+    # the warm-up steps are also the parity steps: every window they give is
+    # compared with the batched engine's window of the same index
+    for _ in range(max(args.warmup, PARITY_STEPS)):
+        plain_step(record=True)
     barrier()
     t0 = time.perf_counter()
     for _ in range(plain_steps):
@@ -483,8 +495,32 @@ def run_batch(args, cfgs, workload):
     torch.cuda.empty_cache()
     infos = [batch.info(i) for i in range(nb)]
     tiles = batch.tiles()
-    for _ in range(args.warmup):
+    parity = {"windows_compared": 0, "identical": 0, "events_identical": 0, "events": 0,
+              "beams_with_events": 0, "steps": 0}
+    with_events = set()
+    for _ in range(max(args.warmup, PARITY_STEPS + (0 if args.unpipelined else 1))):
         batch.run(stream=stream)
+        stream.synchronize()
+        parity["steps"] += 1
+        for i in range(nb):
+            ev, n, first = batch.events(i, step=-1)
+            if first < 0:
+                continue
+            w = first // cfgs[i]["chunk"]
+            if w not in plain_rec[i]:
+                continue
+            digest = window_digest(pv, batch.buffers(i)[1], cfgs[i]["tdms"] * cfgs[i]["chunk"], stream)
+            want_digest, want_ev = plain_rec[i][w]
+            parity["windows_compared"] += 1
+            parity["identical"] += int(digest == want_digest)
+            parity["events_identical"] += int(ev[:n].tobytes() == want_ev)
+            parity["events"] += max(0, n - 1)
+            if n > 1:
+                with_events.add(i)
+    parity["beams_with_events"] = len(with_events)
+    parity["what"] = ("every beam's dedispersed window (exact digest of its FP32 bits) and event list from the "
+                      "batched engine's untimed warm-up steps against the plain per-beam chain's window of "
+                      "the same index; events exclude each window's dummy event")
     barrier()
     launches0 = pv.launches()
     lat_ms, stage = [], []
@@ -624,7 +660,15 @@ def run_batch(args, cfgs, workload):
             "batched_over_plain": value / plain_value,
             "batched_over_plain_e2e": e2e_value / plain_e2e,
             "gpu_launches": launches, "clocks": clk, "roofline": roofline,
-            "roofline_channeliser": roofline_chan, "stage_ms": st,
+            "roofline_channeliser": roofline_chan,
+            "stage_wall_ms": {"channelise": st["channelise"], "rfi_wall": st["rfi"],
+                              "ring_write_wall": st["ring_write"], "dedisperse": st["dedisperse"],
+                              "analyse": st["analyse"],
+                              "what": "mean over the timed steps of the CUDA-event intervals at the stage "
+                                      "boundaries on each stage's stream; pipelined, rfi_wall and "
+                                      "ring_write_wall include the waits of those streams for SMs the "
+                                      "concurrent dedispersion holds (the kernels alone: the launch list "
+                                      "in profiles/)"},
             "tiles": {k: tiles[k] for k in ("variant", "time_tile", "chan_per_stage", "stages",
                                              "slot", "tiles", "ctas", "tune_ms", "graph_kernels")},
             "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
@@ -634,6 +678,7 @@ def run_batch(args, cfgs, workload):
                            "chunk_duration_min": min(chunk_s) * 1e3,
                            "chunk_duration_max": max(chunk_s) * 1e3},
             "events_last_step": n_events,
+            "parity": parity,
             "cpu_baseline": cpu}
     if precision is not None:
         line["precision"] = precision
@@ -644,6 +689,21 @@ def run_batch(args, cfgs, workload):
 
 
 PRECISION_BEAMS = 6
+# Untimed steps of both arms whose windows and events are compared bit for bit.
+PARITY_STEPS = 8
+
+
+def window_digest(pv, ptr, n, stream):
+    """Exact digest of n float32 values at a device pointer: the sums of the
+    values' bit patterns and of the bit patterns weighted by odd position
+    numbers (wrapping 64-bit integer arithmetic)."""
+    import torch
+    stream.synchronize()
+    x = pv.device_array(ptr, (n,))  # copied on the legacy default stream
+    torch.cuda.synchronize()
+    x = x.view(torch.int32).to(torch.int64)
+    w = torch.arange(1, 2 * n, 2, device=x.device, dtype=torch.int64)
+    return int(x.sum().item()), int((x * w).sum().item())
 # The batched end-to-end run starts from an idle GPU, so its first copy overlaps no compute;
 # at least this many steps amortise that fill.
 E2E_MIN_STEPS = 30

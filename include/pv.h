@@ -38,6 +38,15 @@ const char* pv_last_error(void);
 int pv_version(void);
 /* Number of kernels this library launched since load (all entry points). */
 long long pv_kernel_launches(void);
+/* Limit (ns) of each bounded device-side wait of the pipelined dedispersion
+ * kernels launched from now on (ns <= 0: the default, 0.5 s).  A wait that
+ * runs out makes the kernel record PV_ERR_TIMEOUT, wait for its own copies
+ * in flight (up to 0.5 s) and return; the launch's other CTAs stop, and the
+ * status reaches the caller through pv_dedisp_plan_status, pv_beam_events or
+ * pv_batch_events.  A CUDA graph keeps the limit it was captured with.
+ * Returns the previous limit.  No counterpart in the reference, whose
+ * GPU_Job reports failures as GPU_Job::Failed (lib/src/GPU_Manager.cpp). */
+long long pv_set_wait_limit(long long ns);
 /* cudaMemcpyAsync with cudaMemcpyDefault (host or device pointers). */
 int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
 /* Page-locked host memory for input staging (cudaHostAlloc, portable).
@@ -112,6 +121,9 @@ int pv_dedisp_plan_max_shift(const pv_dedisp_plan* plan);
 /* PV_OK, or PV_ERR_TIMEOUT if a pipelined launch's bounded wait gave up
  * (synchronous read of the plan's device status word). */
 int pv_dedisp_plan_status(const pv_dedisp_plan* plan, int* h_status);
+/* Clears a recorded PV_ERR_TIMEOUT so that the plan's next launch runs
+ * (launches stop at their start while the status word holds an error). */
+int pv_dedisp_plan_clear_status(pv_dedisp_plan* plan, void* stream);
 /* Dedisperses nout samples.  Linear mode (ring_len == 0): rows of row_stride
  * floats, samples at or beyond row_len read as 0 (row_len == row_stride reads
  * on into the next row, as the reference's contiguous buffer does).  Ring

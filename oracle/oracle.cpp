@@ -744,6 +744,41 @@ struct Rfi : RfiBase {
     int bad_spectra = 0, num = 0, remaining_zeros = 0;
     std::vector<float> last_good;
 
+    // Guided run (test infrastructure for the "bit-exact except within eps of
+    // threshold" bar): hint holds another implementation's flags [t][nbins]
+    // (bit 0 channel, bit 1 spectrum).  Where this run's decision differs
+    // from the hint and its decision statistic lies within eps of the
+    // threshold, the hint is taken (an allowed near-threshold difference);
+    // any other difference is counted as a mismatch and the hint is taken
+    // too, so that both runs keep the same state and every later decision is
+    // still compared.  Channel statistic: (I - dataModel - bp) - margin in
+    // units of rmsRunAve; spectrum statistic: (mean - meanRunAve) - tolerance
+    // in units of bandpass rms / sqrt(nBins) (RFI_Clipper.cpp:315,415-419).
+    const uint8_t* hint = nullptr;
+    double eps_c = 0.0, eps_s = 0.0;
+    double rep[12] = {0};
+    void guide_reset() {
+        for (double& r : rep) r = 0.0;
+        rep[8] = rep[9] = 1e300;
+        rep[10] = -1.0;
+    }
+    bool guide(bool own, bool want, double stat, double scale, long long t, bool spectrum,
+               bool integral) {
+        const int base = spectrum ? 4 : 0;
+        const double z = scale > 0.0 ? std::fabs(stat) / scale : std::fabs(stat);
+        rep[base] += 1.0;
+        if (!integral && z < rep[spectrum ? 9 : 8]) rep[spectrum ? 9 : 8] = z;
+        if (own == want) return own;
+        if (!integral && z <= (spectrum ? eps_s : eps_c)) {
+            rep[base + 1] += 1.0;
+            if (z > rep[base + 3]) rep[base + 3] = z;
+        } else {
+            rep[base + 2] += 1.0;
+        }
+        if (rep[10] < 0.0) rep[10] = (double)t;
+        return want;
+    }
+
     // mode 0: one sequential FP32 sum; mode 1: canonical partials + tree
     template <typename F>
     float channel_sum(int n, F f) const {
@@ -870,7 +905,11 @@ struct Rfi : RfiBase {
             int good_per_band[8] = {0};
             for (unsigned bin = 0; bin < nbins; ++bin) {
                 float v = at(bin);
-                const bool clip = (float)((float)(v - data_model) - bandpass[bin]) > margin;
+                const float x = (float)((float)(v - data_model) - bandpass[bin]);
+                bool clip = x > margin;
+                if (hint)
+                    clip = guide(clip, (hint[(long long)t * nbins + bin] & 1) != 0,
+                                 (double)x - (double)margin, std::fabs(rms_run), t, false, false);
                 if (clip) {
                     clipped[bin] = 1;
                     unsigned s = bin / nchan, c = bin % nchan;
@@ -919,14 +958,33 @@ struct Rfi : RfiBase {
                 mean_buf.push_back(spectrum_sum);
             }
             bool reject;
+            double reject_stat;
             if (!f64) {
                 const float tol = (float)((double)(sr * bp.rms()) / ::sqrt((double)nbins));
-                reject = (float)(spectrum_sum - (float)mean_run) > tol;
+                const float dev = (float)(spectrum_sum - (float)mean_run);
+                reject = dev > tol;
+                reject_stat = (double)dev - (double)tol;
             } else {
                 const float tol = (float)((double)(sr * bp.rms()) * inv_sqrt_nbins);
                 reject = (double)spectrum_sum - mean_run > (double)tol;
+                reject_stat = ((double)spectrum_sum - mean_run) - (double)tol;
             }
             bool spectrum_clip = false;
+            if (hint) {
+                // the 1000-spectrum gate and the bad-band count are integer
+                // decisions: any difference there is a mismatch
+                const bool want = (hint[(long long)t * nbins] & 2) != 0;
+                const bool gate = mean_buf.size() < 1000;
+                const bool integral = gate || bad_bands >= 4;
+                const bool own = gate || reject || bad_bands >= 4;
+                const bool take = guide(own, want, reject_stat,
+                                        std::fabs((double)bp.rms()) * inv_sqrt_nbins, t, true, integral);
+                // follow the hint past the gate (inside the gate it cannot be followed)
+                if (!gate && take != own) {
+                    reject = take;
+                    if (!take) bad_bands = 0;
+                }
+            }
             if (mean_buf.size() < 1000) {
                 spectrum_clip = true;
             } else if (reject || bad_bands >= 4) {
@@ -1058,6 +1116,20 @@ extern "C" void or_rfi_destroy(or_rfi* r) {
 extern "C" int or_rfi_run(or_rfi* r, float* data, float* weights, int nt, int nsub, int npol,
                           int nchan, uint8_t* flags) {
     return r->impl->run(data, weights, nt, nsub, npol, nchan, flags);
+}
+
+extern "C" int or_rfi_run_guided(or_rfi* r, float* data, float* weights, int nt, int nsub, int npol,
+                                 int nchan, const uint8_t* hint, double eps_chan, double eps_spec,
+                                 uint8_t* flags, double* report12) {
+    Rfi* g = static_cast<Rfi*>(r->impl);
+    g->hint = hint;
+    g->eps_c = eps_chan;
+    g->eps_s = eps_spec;
+    g->guide_reset();
+    const int rc = g->run(data, weights, nt, nsub, npol, nchan, flags);
+    g->hint = nullptr;
+    for (int i = 0; i < 12; ++i) report12[i] = g->rep[i];
+    return rc;
 }
 
 extern "C" void or_rfi_state(const or_rfi* r, double* out10) { r->impl->state(out10); }

@@ -120,6 +120,23 @@ void or_rfi_destroy(or_rfi*);
  * bit0 channel clipped, bit1 spectrum clipped. */
 int or_rfi_run(or_rfi*, float* data, float* weights, int nt, int nsub, int npol,
                int nchan, uint8_t* flags);
+/* or_rfi_run with another implementation's flags as a guide (hint
+ * [t][nbins], the layout of `flags`).  Where this run's channel or spectrum
+ * decision differs from the hint and its decision statistic lies within eps
+ * of the threshold (channel: |(I - dataModel - bp) - margin| <= eps_chan *
+ * rmsRunAve; spectrum: |(mean - meanRunAve) - tolerance| <= eps_spec *
+ * bandpass rms / sqrt(nBins)), the hint's decision is taken; every other
+ * difference is a mismatch, after which the hint is followed as well so the
+ * two runs keep one state.  report12: [channel decisions, channel
+ * differences within eps, channel mismatches, largest |statistic| of a
+ * channel difference within eps, spectrum decisions, spectrum differences
+ * within eps, spectrum mismatches, largest |statistic| of those, smallest
+ * |statistic| of any channel decision, smallest |statistic| of any spectrum
+ * rejection test, first spectrum with a difference (-1: none), 0]
+ * (statistics in their eps units). */
+int or_rfi_run_guided(or_rfi*, float* data, float* weights, int nt, int nsub, int npol, int nchan,
+                      const uint8_t* hint, double eps_chan, double eps_spec, uint8_t* flags,
+                      double* report12);
 /* Scalar state after the last run: [meanRunAve, rmsRunAve, bp_mean, bp_rms,
  * params0, num, badSpectra, meanBufferSize, rmsBufferSize, remainingZeros]. */
 void or_rfi_state(const or_rfi*, double* out10);

@@ -63,6 +63,8 @@ def lib():
             "or_rfi_create": (vp, [C.c_char_p, f, f, i, i, i, i, i, i, C.c_char_p, i]),
             "or_rfi_destroy": (None, [vp]),
             "or_rfi_run": (i, [vp, P(C.c_float), P(C.c_float), i, i, i, i, vp]),
+            "or_rfi_run_guided": (i, [vp, P(C.c_float), P(C.c_float), i, i, i, i, vp, C.c_double,
+                                      C.c_double, vp, P(C.c_double)]),
             "or_rfi_state": (None, [vp, P(C.c_double)]),
             "or_rfi_bandpass": (i, [vp, P(C.c_float), i]),
             "or_sum_canonical": (d, [P(C.c_float), i, i]),
@@ -234,6 +236,25 @@ class RFI:
         if rc != 0:
             raise RuntimeError("or_rfi_run failed %d" % rc)
         return fl
+
+    def run_guided(self, data, hint, eps_chan, eps_spec):
+        """run() following another implementation's flags where this run's
+        decision statistic lies within eps of its threshold (or_rfi_run_guided).
+        Returns (flags, report) with report a dict of counts and statistics."""
+        assert data.dtype == np.float32 and data.flags.c_contiguous
+        nt, nsub, npol, nchan = data.shape
+        hint = np.ascontiguousarray(hint, dtype=np.uint8).reshape(nt, nsub * nchan)
+        weights = np.ones_like(data)
+        fl = np.zeros((nt, nsub * nchan), np.uint8)
+        rep = np.zeros(12, np.float64)
+        rc = lib().or_rfi_run_guided(self.h, _f32p(data), _f32p(weights), nt, nsub, npol, nchan,
+                                     hint.ctypes.data, eps_chan, eps_spec, fl.ctypes.data, _f64p(rep))
+        if rc != 0:
+            raise RuntimeError("or_rfi_run_guided failed %d" % rc)
+        keys = ("chan_decisions", "chan_near", "chan_mismatch", "chan_near_max", "spec_decisions",
+                "spec_near", "spec_mismatch", "spec_near_max", "chan_closest", "spec_closest",
+                "first_difference")
+        return fl, {k: float(v) for k, v in zip(keys, rep)}
 
     def state(self):
         out = np.zeros(10, np.float64)

@@ -63,6 +63,7 @@ struct DedispArgs {
     int nchan, nout, tdms;
     float start, step;
     int slot;  // floats per channel slot in shared memory
+    unsigned long long wait_ns;  // limit of each pipeline wait
 };
 
 template <int DMS, int R, int CS>
@@ -217,7 +218,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
         ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-constexpr unsigned long long kWaitLimitNs = 500000000ull;  // 0.5 s per wait
 
 template <int DMS, int R, int CS, int ST>
 __global__ void __launch_bounds__((DMS + 1) * 32, 1)
@@ -261,7 +261,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         for (int st = 0; st < nstages && ok; ++st) {
             const int b = st % ST;
             const unsigned round = (unsigned)(st / ST);
-            if (!mbar_wait_warp(&empty[b], (round & 1u) ^ 1u, kWaitLimitNs)) {
+            if (!mbar_wait_warp(&empty[b], (round & 1u) ^ 1u, a.wait_ns)) {
                 if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                 ok = false;
                 break;
@@ -302,7 +302,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
         // the CTA's shared memory is released.
         if (!ok) {
             for (int st = max(0, issued - ST); st < issued; ++st)
-                mbar_wait_warp(&full[st % ST], (unsigned)(st / ST) & 1u, kWaitLimitNs);
+                mbar_wait_warp(&full[st % ST], (unsigned)(st / ST) & 1u, pv::kDrainWaitNs);
         }
         return;
     }
@@ -317,7 +317,7 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
     bool ok = true;
     for (int st = 0; st < nstages; ++st) {
         const int b = st % ST;
-        if (!mbar_wait_warp(&full[b], (unsigned)(st / ST) & 1u, kWaitLimitNs)) {
+        if (!mbar_wait_warp(&full[b], (unsigned)(st / ST) & 1u, a.wait_ns)) {
             if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
             ok = false;
             break;
@@ -405,7 +405,8 @@ template <int R, int CS, int ST, int STORE>
 __global__ void __launch_bounds__(17 * 32, 1)
 dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles,
                         int ntiles, int slot, int* __restrict__ counter,
-                        const pv::BeamStep* __restrict__ bs, int* __restrict__ status) {
+                        const pv::BeamStep* __restrict__ bs, int* __restrict__ status,
+                        unsigned long long wait_ns) {
     constexpr int DMS = 16;
     constexpr int TT = 32 * R;
     constexpr int E = Store<STORE>::E, AU = Store<STORE>::AU;
@@ -450,7 +451,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
                 }
             }
             const int b_first = gs % ST;
-            if (!mbar_wait_warp(&empty[b_first], ((gs / ST) & 1u) ^ 1u, kWaitLimitNs)) {
+            if (!mbar_wait_warp(&empty[b_first], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
                 if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                 ok = false;
                 break;
@@ -473,7 +474,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             const unsigned char* ring = reinterpret_cast<const unsigned char*>(J.ring);
             for (int st = 0; st < nst; ++st) {
                 const int b = gs % ST;
-                if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, kWaitLimitNs)) {
+                if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
                     if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                     ok = false;
                     break;
@@ -517,7 +518,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
         if (!ok) {
             // wait (bounded) for the copies still in flight
             for (unsigned g = gs > (unsigned)ST ? gs - ST : 0; g < gs; ++g)
-                mbar_wait_warp(&full[g % ST], (g / ST) & 1u, kWaitLimitNs);
+                mbar_wait_warp(&full[g % ST], (g / ST) & 1u, pv::kDrainWaitNs);
         }
         return;
     }
@@ -537,7 +538,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     unsigned gs = 0;
     for (;;) {
         const int b0 = gs % ST;
-        if (!mbar_wait_warp(&full[b0], (gs / ST) & 1u, kWaitLimitNs)) {
+        if (!mbar_wait_warp(&full[b0], (gs / ST) & 1u, wait_ns)) {
             if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
             return;
         }
@@ -571,7 +572,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             };
             for (int st = 0; st < nst; ++st) {
                 const int b = gs % ST;
-                if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, kWaitLimitNs)) {
+                if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, wait_ns)) {
                     if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                     return;
                 }
@@ -625,7 +626,7 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
         for (int r = 0; r < R / 2; ++r) acc2[r] = 0ull;
         for (int st = 0; st < nst; ++st) {
             const int b = gs % ST;
-            if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, kWaitLimitNs)) {
+            if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, wait_ns)) {
                 if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
                 return;
             }
@@ -793,7 +794,7 @@ int dedisperse_device(float* out, long long out_stride, const float* in, long lo
         return PV_ERR_ARG;
     }
     DedispArgs a{out, out_stride, in, row_stride, row_len, ring_len, t_base % std::max(ring_len, 1LL),
-                 d_dmshift, nchan, nout, tdms, start, step, 0};
+                 d_dmshift, nchan, nout, tdms, start, step, 0, wait_ns()};
     // Ring rows with 16-byte aligned spans go through the TMA pipeline.
     if (status && ring_len > 0 && ring_len % 4 == 0 && row_stride % 4 == 0 &&
         (reinterpret_cast<uintptr_t>(in) & 15) == 0 && getenv("PV_DEDISP_V1") == nullptr) {
@@ -861,7 +862,7 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
     } else {
         PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
     }
-    kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status);
+    kern<<<grid, 17 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status, pv::wait_ns());
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
@@ -1310,6 +1311,12 @@ int plan_tables(const pv_dedisp_plan* p, const float** d_dmshift, const float** 
     return PV_OK;
 }
 }  // namespace pv
+
+extern "C" int pv_dedisp_plan_clear_status(pv_dedisp_plan* p, void* stream) {
+    if (!p) return PV_ERR_ARG;
+    PV_CUDA(cudaMemsetAsync(p->d_status, 0, sizeof(int), pv::as_stream(stream)), "clear plan status");
+    return PV_OK;
+}
 
 extern "C" int pv_dedisp_plan_max_shift(const pv_dedisp_plan* p) { return p ? p->max_shift : -1; }
 

@@ -20,6 +20,14 @@ const char* last_error();
 
 // Kernels launched by this library since load (pv_kernel_launches()).
 extern std::atomic<long long> g_launches;
+
+// Limit of a pipelined kernel's bounded device-side waits (ns), passed to
+// each launch (pv_set_wait_limit).  The drain of a kernel's own copies in
+// flight after a give-up always waits up to kDrainWaitNs.
+constexpr unsigned long long kDefaultWaitNs = 500000000ull;  // 0.5 s
+constexpr unsigned long long kDrainWaitNs = 500000000ull;
+extern std::atomic<unsigned long long> g_wait_ns;
+inline unsigned long long wait_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
 inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 inline int cuda_status(cudaError_t e, const char* what) {

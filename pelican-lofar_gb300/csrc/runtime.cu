@@ -16,6 +16,7 @@ std::vector<int> g_sm_counts;
 }  // namespace
 
 std::atomic<long long> g_launches{0};
+std::atomic<unsigned long long> g_wait_ns{kDefaultWaitNs};
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -68,6 +69,12 @@ void scratch_free(void* p, cudaStream_t s) {
 extern "C" const char* pv_last_error(void) { return pv::last_error(); }
 extern "C" int pv_version(void) { return 100; }
 extern "C" long long pv_kernel_launches(void) { return pv::g_launches.load(); }
+
+extern "C" long long pv_set_wait_limit(long long ns) {
+    const unsigned long long prev = pv::g_wait_ns.load();
+    pv::g_wait_ns.store(ns > 0 ? (unsigned long long)ns : pv::kDefaultWaitNs);
+    return (long long)prev;
+}
 
 // ---------------------------------------------------------------------------
 // Host-side delay table (DedispersionModule::resize, DedispersionModule.cpp:151-162)

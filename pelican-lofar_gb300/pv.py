@@ -126,6 +126,8 @@ def _declare(L):
         "pv_ddmod_pop": (i, [vp, vp, ll, P(i), P(ll), vp]),
         "pv_ddmod_params": (i, [vp, P(i)]),
         "pv_dedisp_plan_status": (i, [vp, P(i)]),
+        "pv_dedisp_plan_clear_status": (i, [vp, vp]),
+        "pv_set_wait_limit": (ll, [ll]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
@@ -209,6 +211,53 @@ def dedisperse(d_in, nout, tdms, d_dmshift, start_over_tsamp, step_over_tsamp, o
                                   _ptr(d_dmshift), start_over_tsamp, step_over_tsamp,
                                   _stream(stream)))
     return out
+
+
+class DedispPlan:
+    """A dedispersion plan (pv_dedisp_plan_*): delay constants and tile choice
+    for one channel set and trial grid; runs on linear or ring rows."""
+
+    def __init__(self, dmshift, tdms, start_over_tsamp, step_over_tsamp):
+        k = np.ascontiguousarray(dmshift, np.float32)
+        self.nchan, self.tdms = len(k), tdms
+        self.h = C.c_void_p()
+        check(load().pv_dedisp_plan_create(C.byref(self.h), k.ctypes.data_as(C.POINTER(C.c_float)),
+                                           len(k), tdms, start_over_tsamp, step_over_tsamp))
+
+    def max_shift(self):
+        return load().pv_dedisp_plan_max_shift(self.h)
+
+    def run(self, d_in, nout, out=None, ring_len=0, t_base=0, row_len=None, stream=None):
+        """d_in: float32 [nchan][row_stride] -> out [tdms][nout] (ring rows
+        when ring_len > 0: output t reads column (t_base + t + shift) mod ring_len)."""
+        import torch
+        assert d_in.dtype == torch.float32 and d_in.is_contiguous() and d_in.shape[0] == self.nchan
+        stride = d_in.shape[1]
+        if out is None:
+            out = torch.empty((self.tdms, nout), dtype=torch.float32, device=d_in.device)
+        check(load().pv_dedisp_plan_run(self.h, _ptr(out), out.stride(0), _ptr(d_in), stride,
+                                        stride if row_len is None else row_len, ring_len, t_base, nout,
+                                        _stream(stream)))
+        return out
+
+    def status(self):
+        st = C.c_int()
+        check(load().pv_dedisp_plan_status(self.h, C.byref(st)))
+        return st.value
+
+    def clear_status(self, stream=None):
+        check(load().pv_dedisp_plan_clear_status(self.h, _stream(stream)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.pv_dedisp_plan_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def set_wait_limit(ns):
+    """Limit (ns) of the pipelined kernels' bounded device waits from now on
+    (<= 0: the default 0.5 s); returns the previous limit."""
+    return load().pv_set_wait_limit(int(ns))
 
 
 def dedisperse_ref_api(d_out, d_in, start_over_tsamp, step_over_tsamp, tdms, num_samples,

@@ -88,11 +88,13 @@ def inject_dispersed_pulse(vc, sub_freq0, sub_bw, tsamp_raw, dm, t0, width, snr_
                            f_ref=None):
     """Adds a dispersed broadband burst to complex voltages vc [sub][pol][n]
     (in place, complex64).  The burst is complex Gaussian noise under a
-    Gaussian envelope of FWHM `width` seconds centred at t0 (seconds, at
-    f_ref); each subband is dispersed coherently by applying the group delay
-    k*DM*(f^-2 - f_ref^-2) per frequency (k = 4148.741601) in the Fourier
-    domain.  snr_scale is the burst's voltage variance relative to the noise
-    at the envelope peak."""
+    Gaussian envelope of FWHM `width` seconds arriving at t0 (seconds) at
+    frequency f_ref and at t0 + k*DM*(f^-2 - f_ref^-2) at frequency f
+    (k = 4148.741601).  In each subband the envelope is centred at the delay
+    of the subband centre fc, and the rest of the delay,
+    k*DM*(f^-2 - fc^-2), is applied in the Fourier domain as the group delay
+    of a phase over the subband's baseband frequencies.  snr_scale is the
+    burst's voltage variance relative to the noise at the envelope peak."""
     nsub, npol, n = vc.shape
     sigma_env = width / 2.3548
     if f_ref is None:
@@ -101,22 +103,22 @@ def inject_dispersed_pulse(vc, sub_freq0, sub_bw, tsamp_raw, dm, t0, width, snr_
     noise_var = float(np.mean(np.abs(vc[:, :, : min(n, 4096)]) ** 2)) / 2.0
     for s in range(nsub):
         fc = sub_freq0 + s * sub_bw
-        f_lo, f_hi = fc - sub_bw / 2, fc + sub_bw / 2
-        d_lo = k_dm * dm * (1 / f_lo ** 2 - 1 / f_ref ** 2)
-        d_hi = k_dm * dm * (1 / f_hi ** 2 - 1 / f_ref ** 2)
-        a = t0 + min(d_lo, d_hi) - 6 * sigma_env
-        b = t0 + max(d_lo, d_hi) + 6 * sigma_env
-        i0, i1 = int(a / tsamp_raw), int(np.ceil(b / tsamp_raw))
-        if i1 <= 0 or i0 >= n:
+        tc = t0 + k_dm * dm * (1 / fc ** 2 - 1 / f_ref ** 2)
+        # in-subband delays relative to the centre: positive below fc, negative above
+        lo_d = k_dm * dm * (1 / (fc + sub_bw / 2) ** 2 - 1 / fc ** 2)
+        hi_d = k_dm * dm * (1 / (fc - sub_bw / 2) ** 2 - 1 / fc ** 2)
+        a = tc + lo_d - 6 * sigma_env
+        b = tc + hi_d + 6 * sigma_env
+        if b / tsamp_raw <= 0 or a / tsamp_raw >= n:
             continue
-        L = 1 << int(np.ceil(np.log2(max(i1 - i0, 16) * 2)))
-        start = i0 - L // 4
+        L = 1 << int(np.ceil(np.log2(max((b - a) / tsamp_raw, 16) * 2)))
+        start = int(np.floor(a / tsamp_raw)) - L // 4
         t = (start + np.arange(L)) * tsamp_raw
-        env = np.exp(-0.5 * ((t - t0) / sigma_env) ** 2)
+        env = np.exp(-0.5 * ((t - tc) / sigma_env) ** 2)
         nu = np.fft.fftfreq(L, d=tsamp_raw) / 1e6  # MHz, baseband
         order = np.argsort(nu)
         f = fc + nu[order]
-        delay = k_dm * dm * (1 / f ** 2 - 1 / f_ref ** 2)  # seconds
+        delay = k_dm * dm * (1 / f ** 2 - 1 / fc ** 2)  # seconds, relative to the centre
         # phase whose frequency derivative gives the group delay
         dnu = (nu[1] - nu[0]) * 1e6
         phase = np.empty(L)
@@ -125,7 +127,8 @@ def inject_dispersed_pulse(vc, sub_freq0, sub_bw, tsamp_raw, dm, t0, width, snr_
             burst = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * np.sqrt(snr_scale * noise_var) * env
             disp = np.fft.ifft(np.fft.fft(burst) * np.exp(1j * phase))
             lo, hi = max(start, 0), min(start + L, n)
-            vc[s, p, lo:hi] += disp[lo - start:hi - start].astype(np.complex64)
+            if hi > lo:
+                vc[s, p, lo:hi] += disp[lo - start:hi - start].astype(np.complex64)
     return vc
 
 
@@ -152,3 +155,56 @@ def ab_emulator_packets(npackets, channels, counter0=0, quarter0=0, beam=0, reco
         if quarter == 0:
             counter += 1
     return np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)
+
+
+def lofar_band(f_sub0, nsub, nchan_sub, sub_bw=0.1953125):
+    """Filterbank channel 0 frequency and channel width (MHz) of nsub LOFAR
+    subbands from centre frequency f_sub0, channelised into nchan_sub
+    channels each (the PPF puts the subband centre at channel nchan_sub/2)."""
+    foff = sub_bw / nchan_sub
+    return f_sub0 - (nchan_sub // 2) * foff, foff
+
+
+def top_channel_freq(f_sub0, nsub, nchan_sub, sub_bw=0.1953125):
+    """Frequency of the highest filterbank channel: the reference frequency
+    of the dedispersion delays (the band is handled highest channel first)."""
+    fch1, foff = lofar_band(f_sub0, nsub, nchan_sub, sub_bw)
+    return fch1 + foff * (nsub * nchan_sub - 1)
+
+
+def lofar_stream(rng, nsub, nsamp, f_sub0, nchan_sub, pulses=(), rfi_channels=(), rfi_amp=0.0,
+                 bursts=(), burst_gain=0.0, burst_len=0, sigma=16.0, sub_bw=0.1953125,
+                 tsamp_raw=5.12e-6, t_offset=0.0):
+    """Dual-polarisation complex int16 station voltages [sub][pol][nsamp][2]:
+    Gaussian noise (sigma per component), persistent narrowband sinusoids at
+    the centre of the filterbank channels listed in rfi_channels (global
+    channel index sub*nchan_sub + c, amplitude rfi_amp * sigma), broadband
+    bursts (noise power raised by burst_gain over burst_len raw samples from
+    each start in bursts) and dispersed pulses (dm, t0 at the top channel in
+    seconds, FWHM width in seconds, snr_scale; see inject_dispersed_pulse),
+    rounded and saturated to int16.  t_offset (seconds) is the stream time of
+    sample 0: the sinusoids keep their phase across consecutive chunks."""
+    v = rng.standard_normal((nsub, 2, nsamp, 2), dtype=np.float32) * np.float32(sigma)
+    vc = (v[..., 0] + 1j * v[..., 1]).astype(np.complex64)
+    del v
+    f_ref = top_channel_freq(f_sub0, nsub, nchan_sub, sub_bw)
+    for dm, t0, width, scale in pulses:  # before the RFI, which would raise the noise estimate
+        inject_dispersed_pulse(vc, f_sub0, sub_bw, tsamp_raw, dm, t0, width, scale, rng, f_ref=f_ref)
+    if len(rfi_channels):
+        t = t_offset + np.arange(nsamp) * tsamp_raw
+        for g in rfi_channels:
+            s, c = divmod(int(g), nchan_sub)
+            nu = (c - nchan_sub // 2) * (sub_bw / nchan_sub) * 1e6  # Hz from the subband centre
+            phase = (int(g) * 0.7548776662 % 1.0) * 2 * np.pi + np.array([0.0, 1.0])  # fixed per channel
+            for p in range(2):
+                vc[s, p] += (rfi_amp * sigma * np.exp(1j * (2 * np.pi * nu * t + phase[p]))).astype(np.complex64)
+    for b in bursts:
+        lo, hi = int(b), min(int(b) + burst_len, nsamp)
+        if hi > lo:
+            extra = rng.standard_normal((nsub, 2, hi - lo, 2), dtype=np.float32) * np.float32(
+                sigma * np.sqrt(burst_gain))
+            vc[:, :, lo:hi] += (extra[..., 0] + 1j * extra[..., 1]).astype(np.complex64)
+    out = np.empty((nsub, 2, nsamp, 2), np.int16)
+    out[..., 0] = np.clip(np.rint(vc.real), -32768, 32767)
+    out[..., 1] = np.clip(np.rint(vc.imag), -32768, 32767)
+    return out
