@@ -486,7 +486,7 @@ def run_batch(args, cfgs, workload):
     bhosts = []  # the batch's staging, allocated after the batch (see the plain arm's)
     for i, c in enumerate(cfgs):
         v = chunk_input(i, c)
-        batch.set_input(i, v, stream=stream)
+        batch.set_input(i, v, stream=stream, both=True)  # the same chunk at every step
         bhosts.append(pv.HostBuffer(v.numel() * v.element_size()))
         bhosts[-1].fill_from(v, stream=stream)
         stream.synchronize()

@@ -47,6 +47,13 @@ long long pv_kernel_launches(void);
  * Returns the previous limit.  No counterpart in the reference, whose
  * GPU_Job reports failures as GPU_Job::Failed (lib/src/GPU_Manager.cpp). */
 long long pv_set_wait_limit(long long ns);
+/* Failure-path test hook: the next n pipelined dedispersion launches (single
+ * beam, plan or pv_dedisperse on ring rows) withhold the copies of their
+ * first channel stage in every CTA, so the consumers' wait on that stage
+ * can only end at the wait limit.  Nothing faults or hangs: the kernel
+ * records PV_ERR_TIMEOUT and returns, as for a copy that never lands.
+ * Returns the previous count. */
+int pv_stall_next_launches(int n);
 /* cudaMemcpyAsync with cudaMemcpyDefault (host or device pointers). */
 int pv_device_copy(void* dst, const void* src, long long bytes, void* stream);
 /* Page-locked host memory for input staging (cudaHostAlloc, portable).
@@ -292,6 +299,11 @@ int pv_rfi_run(pv_rfi* rfi, float* d_data, int nt, int nsub, int npol, int nchan
 int pv_rfi_state(pv_rfi* rfi, double* h_out10);
 /* The rebinned bandpass model the first run used (host copy). */
 int pv_rfi_bandpass(pv_rfi* rfi, float* h_out, int nbins);
+/* The bandpass as RFI_Clipper::bandPass() holds it after the last spectrum
+ * (lib/src/RFI_Clipper.cpp:562-563 setMean/setRMS, lib/BandPass.h:43-70):
+ * h_out[nbins] its currentSet() (NULL: skipped), h_stats4 [mean, rms,
+ * median, params()[0]].  Synchronous. */
+int pv_rfi_bandpass_current(pv_rfi* rfi, float* h_out, int nbins, float* h_stats4);
 /* Threads of the clipper's CTA for a band of nbins channels; also the number
  * of FP32 partial sums of its channel reductions (256, 512 or 1024). */
 int pv_rfi_parts(int nbins);
@@ -365,6 +377,23 @@ int pv_beam_info(const pv_beam* beam, long long* h_info8);
 /* Device time (ms) of the last dedispersed chunk's stages: channelise, RFI,
  * ring write, dedisperse, analyse (needs timing = 1; synchronises). */
 int pv_beam_stage_ms(pv_beam* beam, float* h_ms5);
+/* Saved state.  A beam's stream state is the PPF tap history per subband and
+ * polarisation (the FIR buffer of PPFChanneliser, lib/PPFChanneliser.h:
+ * 115-121), the clipper's running averages, history buffers and last good
+ * spectrum (lib/RFI_Clipper.h:51-64) and the delay ring.  No reference
+ * function saves it: the reference's modules keep it in memory for the life
+ * of the pipeline.  Saving it lets a stream move to another process or GPU,
+ * or restart, and continue bit for bit: a beam of the same configuration
+ * that loads the state of a beam after chunk k and then processes chunk k+1
+ * gives the windows and events the first beam gives.  The state is host
+ * memory of pv_beam_state_size bytes (the ring dominates: channels x ring
+ * samples x 4 bytes).  Save synchronises the stream; load synchronises too,
+ * rejects a state of another configuration with PV_ERR_CONFIG, and leaves the
+ * beam with no window read yet (pv_beam_events reports first sample -1
+ * until the next window). */
+long long pv_beam_state_size(const pv_beam* beam);
+int pv_beam_state_save(pv_beam* beam, void* h_state, long long cap, void* stream);
+int pv_beam_state_load(pv_beam* beam, const void* h_state, long long bytes, void* stream);
 /* Device views of the last chunk's filterbank (after RFI), its pre-RFI copy
  * (debug_taps), the dedispersed window [tdms][chunk] and the ring. */
 int pv_beam_buffers(const pv_beam* beam, float** d_filterbank, float** d_filterbank_raw,
@@ -405,6 +434,10 @@ void pv_batch_destroy(pv_batch* batch);
  * (pv_beam_input_bytes(.., 1) bytes, [sub][pol][sample] complex int16).
  * Steps alternate between two buffer sets, so ask again before every step. */
 int pv_batch_input(pv_batch* batch, int beam, void** d_voltages, long long* bytes);
+/* The input buffer of a beam's chunks of one parity (0: its 1st, 3rd, ...
+ * chunk; 1: its 2nd, 4th, ...): a caller that feeds the same chunk every
+ * step fills both once. */
+int pv_batch_input_parity(pv_batch* batch, int beam, int parity, void** d_voltages, long long* bytes);
 /* One step from the input buffers, asynchronously.  h_active[beam] != 0
  * (h_active NULL: every beam) marks the beams that have a chunk this step;
  * the others keep their state and skip every stage (a serving loop's

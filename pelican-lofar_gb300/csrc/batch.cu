@@ -585,6 +585,13 @@ extern "C" int pv_batch_input(pv_batch* b, int beam, void** d_voltages, long lon
     return PV_OK;
 }
 
+extern "C" int pv_batch_input_parity(pv_batch* b, int beam, int parity, void** d_voltages, long long* bytes) {
+    if (!b || beam < 0 || beam >= b->n || (parity != 0 && parity != 1)) return PV_ERR_ARG;
+    if (d_voltages) *d_voltages = b->d_in[(size_t)parity * b->n + beam];
+    if (bytes) *bytes = b->in_bytes[beam];
+    return PV_OK;
+}
+
 namespace {
 
 // Sets this step's mask (all beams when h_active is null) in its host-mapped

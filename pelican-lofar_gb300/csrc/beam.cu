@@ -250,6 +250,119 @@ extern "C" int pv_beam_events(pv_beam* b, pv_event* h_events, long long cap, lon
     return PV_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Saved state: a header naming the configuration and the stream position,
+// then the PPF tap history, the clipper's running state and the ring's
+// ring_len columns of every channel row.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct BeamStateHeader {
+    char magic[8];
+    long long version, bytes;
+    long long nbins, nsub, nchan_sub, ntaps, int_time, int_chan, chunk, tdms, history, lag, ring_len;
+    long long chunks;  // chunks in the ring (prefilled silence included)
+    long long ppf_bytes, rfi_bytes, ring_bytes;
+    double fch1, foff, tsamp, dm_low, dm_step;
+};
+constexpr char kStateMagic[8] = {'P', 'V', 'B', 'E', 'A', 'M', 'S', '1'};
+
+BeamStateHeader state_header(const pv_beam* b) {
+    const pv_beam_config& c = b->cfg;
+    BeamStateHeader h{};
+    std::memcpy(h.magic, kStateMagic, 8);
+    h.version = 1;
+    h.nbins = b->nbins;
+    h.nsub = c.nsub;
+    h.nchan_sub = c.nchan_sub;
+    h.ntaps = c.ntaps;
+    h.int_time = c.int_time;
+    h.int_chan = c.int_chan;
+    h.chunk = c.chunk;
+    h.tdms = c.tdms;
+    h.history = c.history;
+    h.lag = b->lag;
+    h.ring_len = b->ring_len;
+    h.chunks = b->chunks;
+    h.ppf_bytes = pv::ppf_state_bytes(b->ppf, c.nsub, 2);
+    h.rfi_bytes = pv::rfi_state_bytes(b->rfi, b->nbins);
+    h.ring_bytes = (long long)b->nbins * b->ring_len * (long long)sizeof(float);
+    h.fch1 = c.fch1;
+    h.foff = c.foff;
+    h.tsamp = c.tsamp;
+    h.dm_low = c.dm_low;
+    h.dm_step = c.dm_step;
+    h.bytes = (long long)sizeof(BeamStateHeader) + h.ppf_bytes + h.rfi_bytes + h.ring_bytes;
+    return h;
+}
+
+}  // namespace
+
+extern "C" long long pv_beam_state_size(const pv_beam* b) {
+    if (!b) return -1;
+    return state_header(b).bytes;
+}
+
+extern "C" int pv_beam_state_save(pv_beam* b, void* h_buf, long long cap, void* stream) {
+    if (!b || !h_buf) return PV_ERR_ARG;
+    const BeamStateHeader h = state_header(b);
+    if (cap < h.bytes) {
+        pv::set_error("pv_beam_state_save: %lld bytes needed, %lld given", h.bytes, cap);
+        return PV_ERR_ARG;
+    }
+    cudaStream_t s = pv::as_stream(stream);
+    char* p = static_cast<char*>(h_buf);
+    std::memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    PV_TRY(pv::ppf_state_io(b->ppf, b->cfg.nsub, 2, p, true, s));
+    p += h.ppf_bytes;
+    PV_TRY(pv::rfi_state_io(b->rfi, b->nbins, p, true, s));
+    p += h.rfi_bytes;
+    PV_CUDA(cudaMemcpy2DAsync(p, sizeof(float) * (size_t)b->ring_len, b->d_ring, sizeof(float) * (size_t)b->row_stride,
+                              sizeof(float) * (size_t)b->ring_len, (size_t)b->nbins, cudaMemcpyDeviceToHost, s),
+            "save ring");
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise state save");
+    return PV_OK;
+}
+
+extern "C" int pv_beam_state_load(pv_beam* b, const void* h_buf, long long bytes, void* stream) {
+    if (!b || !h_buf) return PV_ERR_ARG;
+    const BeamStateHeader want = state_header(b);
+    BeamStateHeader h{};
+    if (bytes < (long long)sizeof(h)) {
+        pv::set_error("pv_beam_state_load: %lld bytes are not a beam state", bytes);
+        return PV_ERR_ARG;
+    }
+    std::memcpy(&h, h_buf, sizeof(h));
+    if (std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1) {
+        pv::set_error("pv_beam_state_load: not a beam state of this library version");
+        return PV_ERR_ARG;
+    }
+    if (h.bytes != bytes || h.nbins != want.nbins || h.nsub != want.nsub || h.nchan_sub != want.nchan_sub ||
+        h.ntaps != want.ntaps || h.int_time != want.int_time || h.int_chan != want.int_chan ||
+        h.chunk != want.chunk || h.tdms != want.tdms || h.history != want.history || h.lag != want.lag ||
+        h.ring_len != want.ring_len || h.ppf_bytes != want.ppf_bytes || h.rfi_bytes != want.rfi_bytes ||
+        h.ring_bytes != want.ring_bytes || h.fch1 != want.fch1 || h.foff != want.foff || h.tsamp != want.tsamp ||
+        h.dm_low != want.dm_low || h.dm_step != want.dm_step) {
+        pv::set_error("pv_beam_state_load: the state was saved from a beam of another configuration");
+        return PV_ERR_CONFIG;
+    }
+    cudaStream_t s = pv::as_stream(stream);
+    const char* p = static_cast<const char*>(h_buf) + sizeof(h);
+    PV_TRY(pv::ppf_state_io(b->ppf, b->cfg.nsub, 2, const_cast<char*>(p), false, s));
+    p += h.ppf_bytes;
+    PV_TRY(pv::rfi_state_io(b->rfi, b->nbins, const_cast<char*>(p), false, s));
+    p += h.rfi_bytes;
+    PV_CUDA(cudaMemcpy2DAsync(b->d_ring, sizeof(float) * (size_t)b->row_stride, p, sizeof(float) * (size_t)b->ring_len,
+                              sizeof(float) * (size_t)b->ring_len, (size_t)b->nbins, cudaMemcpyHostToDevice, s),
+            "load ring");
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise state load");
+    b->chunks = h.chunks;
+    b->window = -1;  // no window of this stream has been dedispersed since the load
+    b->timed = false;
+    return PV_OK;
+}
+
 extern "C" int pv_beam_buffers(const pv_beam* b, float** d_filterbank, float** d_filterbank_raw,
                                float** d_dedispersed, float** d_ring) {
     if (!b) return PV_ERR_ARG;

@@ -17,6 +17,7 @@
 // HBM.  Raw int16 station samples are accepted directly (the conversion to
 // float is exact).
 #include <algorithm>
+#include <cstring>
 #include <cstdlib>
 #include <vector>
 
@@ -773,6 +774,30 @@ extern "C" int pv_ppf_run(pv_ppf* h, const float* d_in, int nsub, int npol, int 
                           float* d_out, void* stream) {
     return run_channelise(h, d_in, 0, nsub, npol, nblocks, 0, reinterpret_cast<float2*>(d_out),
                           nullptr, 1, 1, 1, nullptr, pv::as_stream(stream));
+}
+
+long long pv::ppf_state_bytes(const pv_ppf* h, int nsub, int npol) {
+    return (long long)nsub * npol * (h->ntaps - 1) * h->nchan * (long long)sizeof(float2);
+}
+
+// Copies the tap history [sub][pol][T-1][N] (complex float) to or from host
+// memory.  A channeliser that has run no block yet has an all-zero history.
+int pv::ppf_state_io(pv_ppf* h, int nsub, int npol, void* h_buf, bool save, cudaStream_t s) {
+    PV_TRY(prepare_history(h, nsub, npol, s));
+    const size_t bytes = (size_t)ppf_state_bytes(h, nsub, npol);
+    if (bytes == 0) return PV_OK;
+    if (save) {
+        if (!h->have_hist) {
+            PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+            std::memset(h_buf, 0, bytes);
+            return PV_OK;
+        }
+        PV_CUDA(cudaMemcpyAsync(h_buf, h->d_hist[h->cur], bytes, cudaMemcpyDeviceToHost, s), "save PPF history");
+        return PV_OK;
+    }
+    PV_CUDA(cudaMemcpyAsync(h->d_hist[h->cur], h_buf, bytes, cudaMemcpyHostToDevice, s), "load PPF history");
+    h->have_hist = true;
+    return PV_OK;
 }
 
 int pv::channelise_stokes_i(pv_ppf* h, const void* d_in, int nsub, int nblocks, int window, int bin, float* d_stokes,

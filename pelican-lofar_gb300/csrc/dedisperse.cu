@@ -64,6 +64,7 @@ struct DedispArgs {
     float start, step;
     int slot;  // floats per channel slot in shared memory
     unsigned long long wait_ns;  // limit of each pipeline wait
+    int stall;                   // failure-path test: the first stage's copies are withheld
 };
 
 template <int DMS, int R, int CS>
@@ -266,6 +267,10 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
                 ok = false;
                 break;
             }
+            if (a.stall && st == 0) {  // nothing completes this stage: its consumers' wait runs out
+                issued = st + 1;
+                continue;
+            }
             const int c = st * CS + lane;
             unsigned bytes = 0, piece1 = 0, piece2 = 0;
             long long g_al = 0;
@@ -298,12 +303,13 @@ dedisperse_tma_kernel(const DedispArgs a, int* __restrict__ status) {
             }
             issued = st + 1;
         }
-        // On a give-up, wait (bounded) for the copies still in flight before
-        // the CTA's shared memory is released.
-        if (!ok) {
-            for (int st = max(0, issued - ST); st < issued; ++st)
+        // Before the producer leaves, its last copies have landed (bounded):
+        // consumers that give up return at once, and the CTA's shared memory
+        // must not be released under copies in flight.
+        (void)ok;
+        for (int st = max(0, issued - ST); st < issued; ++st)
+            if (!(a.stall && st == 0))  // the withheld stage has no copies in flight
                 mbar_wait_warp(&full[st % ST], (unsigned)(st / ST) & 1u, pv::kDrainWaitNs);
-        }
         return;
     }
 
@@ -515,11 +521,10 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
             }
             if (!ok) break;
         }
-        if (!ok) {
-            // wait (bounded) for the copies still in flight
-            for (unsigned g = gs > (unsigned)ST ? gs - ST : 0; g < gs; ++g)
-                mbar_wait_warp(&full[g % ST], (g / ST) & 1u, pv::kDrainWaitNs);
-        }
+        // the last copies have landed (bounded) before the producer leaves
+        (void)ok;
+        for (unsigned g = gs > (unsigned)ST ? gs - ST : 0; g < gs; ++g)
+            mbar_wait_warp(&full[g % ST], (g / ST) & 1u, pv::kDrainWaitNs);
         return;
     }
 
@@ -794,10 +799,11 @@ int dedisperse_device(float* out, long long out_stride, const float* in, long lo
         return PV_ERR_ARG;
     }
     DedispArgs a{out, out_stride, in, row_stride, row_len, ring_len, t_base % std::max(ring_len, 1LL),
-                 d_dmshift, nchan, nout, tdms, start, step, 0, wait_ns()};
+                 d_dmshift, nchan, nout, tdms, start, step, 0, wait_ns(), 0};
     // Ring rows with 16-byte aligned spans go through the TMA pipeline.
     if (status && ring_len > 0 && ring_len % 4 == 0 && row_stride % 4 == 0 &&
         (reinterpret_cast<uintptr_t>(in) & 15) == 0 && getenv("PV_DEDISP_V1") == nullptr) {
+        a.stall = take_stall();
         const int spread16 = delay_spread(h_dmshift, tdms, 16, start, step);
         const int slot = (1024 + spread16 + 8 + 3) & ~3;
         // every copy (span + 16-byte rounding) must fit in one ring turn

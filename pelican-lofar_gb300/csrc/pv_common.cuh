@@ -28,6 +28,15 @@ constexpr unsigned long long kDefaultWaitNs = 500000000ull;  // 0.5 s
 constexpr unsigned long long kDrainWaitNs = 500000000ull;
 extern std::atomic<unsigned long long> g_wait_ns;
 inline unsigned long long wait_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
+// Failure-path test hook (pv_stall_next_launches): the next n pipelined
+// dedispersion launches withhold the copies of their first stage.
+extern std::atomic<int> g_stall_launches;
+inline int take_stall() {
+    int n = g_stall_launches.load();
+    while (n > 0 && !g_stall_launches.compare_exchange_weak(n, n - 1)) {
+    }
+    return n > 0 ? 1 : 0;
+}
 inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 inline int cuda_status(cudaError_t e, const char* what) {

@@ -51,6 +51,12 @@ int chan_job_warps(ChanJob& job);  // sets nranges, returns the job's warp count
 // input: 0 complex float voltages, 1 int16 voltages, 2 int16 LOFAR packets (pkt_bytes of every job)
 int launch_chan_fast(int nchan, int input, const ChanJob* d_jobs, const ChanJob& one, int njobs,
                      long long nwarps, const BeamStep* bs, cudaStream_t s);
+// Saved state of one beam (pv_beam_state_*): the PPF tap history and the
+// clipper's running state, as bytes in host memory.
+long long ppf_state_bytes(const pv_ppf* h, int nsub, int npol);
+int ppf_state_io(pv_ppf* h, int nsub, int npol, void* h_buf, bool save, cudaStream_t s);
+long long rfi_state_bytes(const pv_rfi* h, int nbins);
+int rfi_state_io(pv_rfi* h, int nbins, void* h_buf, bool save, cudaStream_t s);
 // coefficient [T][N] and twiddle [N/2] tables of a PPF handle
 int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
                int* ntaps);

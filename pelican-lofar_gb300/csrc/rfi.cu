@@ -757,6 +757,8 @@ struct pv_rfi {
     float* d_terms = nullptr;
     unsigned char* d_killed = nullptr;
     std::vector<float> h_bp;  // bandpass after rebinning (host copy)
+    std::vector<float> h_terms;          // host copy of the device terms [deg][nbins]
+    std::vector<unsigned char> h_killed; // [nbins]
 };
 
 namespace {
@@ -832,6 +834,8 @@ int setup(pv_rfi* h, int nbins, cudaStream_t s) {
     PV_CUDA(cudaMemsetAsync(h->dev.last_good, 0, sizeof(float) * nbins, s), "clear last good spectrum");
     PV_CUDA(cudaMemsetAsync(h->dev.mean_buf, 0, sizeof(double) * h->history, s), "clear history");
     PV_CUDA(cudaMemsetAsync(h->dev.rms_buf, 0, sizeof(double) * h->history, s), "clear history");
+    h->h_terms = terms;
+    h->h_killed = killed;
     if (!terms.empty()) {
         PV_CUDA(cudaMalloc(&h->d_terms, sizeof(float) * terms.size()), "allocate bandpass terms");
         PV_CUDA(cudaMemcpyAsync(h->d_terms, terms.data(), sizeof(float) * terms.size(),
@@ -913,6 +917,31 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     return rfi_launch(threads, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
+long long pv::rfi_state_bytes(const pv_rfi* h, int nbins) {
+    return (long long)sizeof(RfiState) + 2LL * h->history * (long long)sizeof(double) +
+           (long long)nbins * (long long)sizeof(float);
+}
+
+// Copies the running state (RfiState, both history buffers and the last good
+// spectrum) to or from host memory, in that order.  A clipper that has run
+// no spectrum yet is set up first, so its initial state is what is saved.
+int pv::rfi_state_io(pv_rfi* h, int nbins, void* h_buf, bool save, cudaStream_t s) {
+    PV_TRY(setup(h, nbins, s));
+    char* p = static_cast<char*>(h_buf);
+    const size_t hist = sizeof(double) * (size_t)h->history;
+    struct Part { void* dev; size_t bytes; };
+    const Part parts[4] = {{h->dev.state, sizeof(RfiState)}, {h->dev.mean_buf, hist}, {h->dev.rms_buf, hist},
+                           {h->dev.last_good, sizeof(float) * (size_t)nbins}};
+    for (const Part& q : parts) {
+        if (save)
+            PV_CUDA(cudaMemcpyAsync(p, q.dev, q.bytes, cudaMemcpyDeviceToHost, s), "save RFI state");
+        else
+            PV_CUDA(cudaMemcpyAsync(q.dev, p, q.bytes, cudaMemcpyHostToDevice, s), "load RFI state");
+        p += q.bytes;
+    }
+    return PV_OK;
+}
+
 extern "C" int pv_rfi_parts(int nbins) { return nbins <= 1024 ? 256 : (nbins <= 4096 ? 512 : 1024); }
 
 extern "C" int pv_rfi_state(pv_rfi* h, double* out10) {
@@ -933,6 +962,35 @@ extern "C" int pv_rfi_state(pv_rfi* h, double* out10) {
     out10[7] = st.mean_size;
     out10[8] = st.rms_size;
     out10[9] = st.remaining_zeros;
+    return PV_OK;
+}
+
+extern "C" int pv_rfi_bandpass_current(pv_rfi* h, float* h_out, int nbins, float* h_stats4) {
+    if (!h || nbins != h->nbins || !h->dev.state) {
+        pv::set_error("pv_rfi_bandpass_current: run the clipper on %d channels first", nbins);
+        return PV_ERR_STATE;
+    }
+    RfiState st{};
+    PV_CUDA(cudaMemcpy(&st, h->dev.state, sizeof(st), cudaMemcpyDeviceToHost), "read RFI state");
+    const int deg = h->cfg.deg;
+    if (h_out) {
+        // the device's bp_value: params[0] + the k >= 1 terms in order, times the rebin scale
+        for (int i = 0; i < nbins; ++i) {
+            if (!h->h_killed.empty() && h->h_killed[i] && !h->bp.killed.empty()) {
+                h_out[i] = 0.0f;
+                continue;
+            }
+            float tot = st.params0;
+            for (int k = 0; k < deg; ++k) tot = tot + h->h_terms[(size_t)k * nbins + i];
+            h_out[i] = h->cfg.scale * tot;
+        }
+    }
+    if (h_stats4) {
+        h_stats4[0] = st.bp_mean;
+        h_stats4[1] = st.bp_rms;
+        h_stats4[2] = Bandpass::at(h->bp.median, h->bp.current.key());
+        h_stats4[3] = st.params0;
+    }
     return PV_OK;
 }
 

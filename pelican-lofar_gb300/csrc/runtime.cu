@@ -17,6 +17,7 @@ std::vector<int> g_sm_counts;
 
 std::atomic<long long> g_launches{0};
 std::atomic<unsigned long long> g_wait_ns{kDefaultWaitNs};
+std::atomic<int> g_stall_launches{0};
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -69,6 +70,12 @@ void scratch_free(void* p, cudaStream_t s) {
 extern "C" const char* pv_last_error(void) { return pv::last_error(); }
 extern "C" int pv_version(void) { return 100; }
 extern "C" long long pv_kernel_launches(void) { return pv::g_launches.load(); }
+
+extern "C" int pv_stall_next_launches(int n) {
+    const int prev = pv::g_stall_launches.load();
+    pv::g_stall_launches.store(n > 0 ? n : 0);
+    return prev;
+}
 
 extern "C" long long pv_set_wait_limit(long long ns) {
     const unsigned long long prev = pv::g_wait_ns.load();

@@ -80,6 +80,7 @@ def _declare(L):
         "pv_rfi_run": (i, [vp, vp, i, i, i, i, vp, vp]),
         "pv_rfi_state": (i, [vp, P(C.c_double)]),
         "pv_rfi_bandpass": (i, [vp, P(C.c_float), i]),
+        "pv_rfi_bandpass_current": (i, [vp, P(C.c_float), i, P(C.c_float)]),
         "pv_rfi_parts": (i, [i]),
         "pv_beam_create": (i, [P(vp), vp]),
         "pv_beam_destroy": (None, [vp]),
@@ -90,11 +91,15 @@ def _declare(L):
         "pv_beam_info": (i, [vp, P(ll)]),
         "pv_beam_buffers": (i, [vp, P(vp), P(vp), P(vp), P(vp)]),
         "pv_beam_stage_ms": (i, [vp, P(C.c_float)]),
+        "pv_beam_state_size": (ll, [vp]),
+        "pv_beam_state_save": (i, [vp, vp, ll, vp]),
+        "pv_beam_state_load": (i, [vp, vp, ll, vp]),
         "pv_host_alloc": (i, [P(vp), ll, i]),
         "pv_host_free": (None, [vp]),
         "pv_batch_create": (i, [P(vp), vp, i, i]),
         "pv_batch_destroy": (None, [vp]),
         "pv_batch_input": (i, [vp, i, P(vp), P(ll)]),
+        "pv_batch_input_parity": (i, [vp, i, i, P(vp), P(ll)]),
         "pv_batch_run": (i, [vp, vp, vp]),
         "pv_batch_run_host": (i, [vp, P(vp), vp, vp]),
         "pv_batch_events": (i, [vp, i, ll, vp, ll, P(ll), P(ll)]),
@@ -128,6 +133,7 @@ def _declare(L):
         "pv_dedisp_plan_status": (i, [vp, P(i)]),
         "pv_dedisp_plan_clear_status": (i, [vp, vp]),
         "pv_set_wait_limit": (ll, [ll]),
+        "pv_stall_next_launches": (i, [i]),
         "pv_analyser_thresholds": (i, [f, f, i, P(C.c_float)]),
         "pv_analyse": (i, [vp, ll, i, i, f, f, i, vp, ll, P(ll), vp]),
     }
@@ -252,6 +258,12 @@ class DedispPlan:
         if getattr(self, "h", None) and self.h.value and _lib is not None:
             _lib.pv_dedisp_plan_destroy(self.h)
             self.h = C.c_void_p()
+
+
+def stall_next_launches(n):
+    """Failure-path test hook: the next n pipelined dedispersion launches
+    withhold their first stage's copies, so a wait there runs out."""
+    return load().pv_stall_next_launches(int(n))
 
 
 def set_wait_limit(ns):
@@ -477,6 +489,17 @@ class Beam:
         p = [C.c_void_p() for _ in range(4)]
         check(load().pv_beam_buffers(self.h, *[C.byref(x) for x in p]))
         return [x.value for x in p]
+
+    def save_state(self, stream=None):
+        """The stream state (tap history, clipper state, ring) as bytes."""
+        n = load().pv_beam_state_size(self.h)
+        buf = np.empty(n, np.uint8)
+        check(load().pv_beam_state_save(self.h, C.c_void_p(buf.ctypes.data), n, _stream(stream)))
+        return buf
+
+    def load_state(self, state, stream=None):
+        state = np.ascontiguousarray(state, np.uint8)
+        check(load().pv_beam_state_load(self.h, C.c_void_p(state.ctypes.data), state.nbytes, _stream(stream)))
 
     def __del__(self):
         if getattr(self, "h", None) and self.h.value and _lib is not None:
@@ -784,11 +807,21 @@ class Batch:
         check(load().pv_batch_input(self.h, beam, C.byref(p), C.byref(n)))
         return p.value, n.value
 
-    def set_input(self, beam, d_voltages, stream=None):
-        """Device-to-device copy of one beam's int16 voltages into its input buffer."""
-        p, n = self.input(beam)
-        assert d_voltages.numel() * d_voltages.element_size() == n
-        check(load().pv_device_copy(C.c_void_p(p), _ptr(d_voltages), n, _stream(stream)))
+    def set_input(self, beam, d_voltages, stream=None, both=False):
+        """Device-to-device copy of one beam's int16 voltages into the input
+        buffer of its next chunk, or (both) of its chunks of either parity:
+        the same chunk at every step."""
+        bufs = []
+        if both:
+            for par in (0, 1):
+                p, n = C.c_void_p(), C.c_longlong()
+                check(load().pv_batch_input_parity(self.h, beam, par, C.byref(p), C.byref(n)))
+                bufs.append((p.value, n.value))
+        else:
+            bufs.append(self.input(beam))
+        for p, n in bufs:
+            assert d_voltages.numel() * d_voltages.element_size() == n
+            check(load().pv_device_copy(C.c_void_p(p), _ptr(d_voltages), n, _stream(stream)))
 
     def _mask(self, active):
         if active is None:

@@ -99,3 +99,42 @@ def test_beam_host_input_equals_device_input(pv, oracle, cuda):
         oa = pv.device_array(a.buffers()[2], (kw["tdms"], 256)).cpu().numpy()
         ob = pv.device_array(b.buffers()[2], (kw["tdms"], 256)).cpu().numpy()
         assert np.array_equal(oa, ob)
+
+
+def test_beam_state_saved_and_loaded_continues_bit_for_bit(pv, oracle, cuda):
+    """A beam that loads another beam's state after chunk k gives, from chunk
+    k+1 on, the same filterbanks, windows and events as the beam that ran
+    continuously; the state of the loaded beam saves back to the same bytes;
+    a beam of another configuration refuses it."""
+    import torch
+    a, kw, _ = _setup(pv, oracle, chunk=256, history=1000)
+    nsub, nch, chunk, tdms = kw["nsub"], kw["nchan_sub"], kw["chunk"], kw["tdms"]
+    rng = np.random.default_rng(31)
+    chunks = [torch.from_numpy(voltages(rng, nsub, 2, chunk * 4 * nch)[0].reshape(nsub, 2, -1)).to(cuda)
+              for _ in range(12)]
+    fresh = pv.Beam(pv.beam_config(**kw))
+    s0 = fresh.save_state()
+    k = 8  # past the clipper's 1000-spectrum warm-up and the ring's lag
+    assert a.info()["lag"] < k
+    for c in chunks[:k]:
+        a.process(c)
+    state = a.save_state()
+    assert state.nbytes == pv.load().pv_beam_state_size(a.h) > s0.nbytes // 2
+    assert not np.array_equal(state, s0)
+    b = pv.Beam(pv.beam_config(**kw))
+    b.load_state(state)
+    assert np.array_equal(b.save_state(), state)
+    assert b.events()[2] == -1  # no window since the load
+    for c in chunks[k:]:
+        a.process(c)
+        b.process(c)
+        ea, na, fa = a.events()
+        eb, nb, fb = b.events()
+        assert na == nb and fa == fb >= 0 and np.array_equal(ea, eb)
+        for i in (0, 2):
+            shape = (chunk, nsub, 1, nch) if i == 0 else (tdms, chunk)
+            assert np.array_equal(pv.device_array(a.buffers()[i], shape).cpu().numpy(),
+                                  pv.device_array(b.buffers()[i], shape).cpu().numpy())
+    other = pv.Beam(pv.beam_config(**dict(kw, tdms=tdms + 1)))
+    with pytest.raises(pv.PvError, match="another configuration"):
+        other.load_state(state)

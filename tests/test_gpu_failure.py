@@ -1,7 +1,8 @@
 """Failure detection without a GPU fault.  The pipelined dedispersion kernels
-bound every device-side wait; a limit short enough for the waits on copies in
-flight to run out makes the kernel record PV_ERR_TIMEOUT, wait for its own
-copies and return.  The error reaches the caller through the plan status and
+bound every device-side wait.  A launch whose first stage's copies are
+withheld (pv_stall_next_launches: a barrier that nothing completes) waits
+there until a short limit runs out, records PV_ERR_TIMEOUT, waits for its
+own copies in flight and returns.  The error reaches the caller through the plan status and
 pv_beam_events, and the context stays usable: the next launch with the
 default limit is bit-exact.  (The reference reports a failed GPU job as
 GPU_Job::Failed and cancels its export, lib/src/DedispersionModule.cpp:299-311.)"""
@@ -32,17 +33,20 @@ def test_plan_wait_runs_out_then_recovers(pv, oracle, cuda):
     plan, lin, ring_len, want = _ring_case(pv, oracle, rng)
     d_ring = torch.from_numpy(lin).to(cuda)
     nout = want.shape[1]
-    prev = pv.set_wait_limit(1)  # 1 ns: a wait on copies still in flight gives up at once
+    prev = pv.set_wait_limit(1000000)  # 1 ms
     try:
+        pv.stall_next_launches(1)
         plan.run(d_ring, nout, ring_len=ring_len, t_base=0)
         torch.cuda.synchronize()
         assert plan.status() == PV_ERR_TIMEOUT
+        assert pv.stall_next_launches(0) == 0  # the hook was used by that launch
         # later launches stop at their start while the status holds the error
         plan.run(d_ring, nout, ring_len=ring_len, t_base=0)
         torch.cuda.synchronize()
         assert plan.status() == PV_ERR_TIMEOUT
     finally:
-        assert pv.set_wait_limit(prev) == 1
+        pv.stall_next_launches(0)
+        assert pv.set_wait_limit(prev) == 1000000
     plan.clear_status()
     out = plan.run(d_ring, nout, ring_len=ring_len, t_base=0)
     torch.cuda.synchronize()
@@ -61,14 +65,16 @@ def test_beam_reports_timeout_and_other_beams_run(pv, oracle, cuda):
     rng = np.random.default_rng(7)
     v16, _ = voltages(rng, nsub, 2, chunk * 4 * nch)
     d_v = torch.from_numpy(v16.reshape(nsub, 2, -1)).to(cuda)
-    prev = pv.set_wait_limit(1)
+    prev = pv.set_wait_limit(1000000)
     try:
         bad = pv.Beam(pv.beam_config(**kw))
+        pv.stall_next_launches(1)
         bad.process(d_v)
         with pytest.raises(pv.PvError) as e:
             bad.events()
         assert "gave up" in str(e.value)
     finally:
+        pv.stall_next_launches(0)
         pv.set_wait_limit(prev)
     good = pv.Beam(pv.beam_config(**kw))
     ref = pv.Beam(pv.beam_config(**kw))
