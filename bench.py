@@ -221,27 +221,48 @@ def device_voltages(cfg, dev, seed):
     nb = max(1, n // 10000)
     for b0 in rng.integers(0, n - 16, size=nb):
         v[:, :, int(b0):int(b0) + 16, :] *= 3.0
-    # dispersed pulses (dm, width s, position as a fraction of the chunk):
-    # Gaussian amplitude envelopes delayed per subband by the cold-plasma
-    # delay at the subband centre frequency.  Every step feeds the same
-    # chunk, so the stream is periodic in the chunk duration and each
-    # subband's envelope sits at its delay modulo the chunk: the whole
-    # dispersed track is in the stream, a pulse once per chunk.  The peak
-    # raises a channel's power by 49 %, about 1.4 sigma of one integrated
-    # sample, under the 5-sigma channel clip; dedispersed over ~1000
-    # channels and a few samples the pulse stands far above 6 sigma.
-    f_top = cfg["f_sub0"] + (nsub - 1) * SUB_BW
+    # dispersed pulses (dm, width s, position as a fraction of the chunk): in
+    # every subband, complex noise of PULSE_SCALE x the noise variance under a
+    # Gaussian envelope centred at the cold-plasma delay of the subband
+    # centre, dispersed across the subband in the Fourier domain (the group
+    # delay k*DM*(f^-2 - fc^-2) as a phase), so each channel holds the pulse
+    # at its own delay.  Every step feeds the same chunk, so the stream is
+    # periodic in the chunk duration and the burst is added modulo the chunk:
+    # the whole dispersed track is in the stream, a pulse once per chunk.
+    # Each channel's power rises by about 0.6 sigma of one integrated sample
+    # at the peak, well under the 5-sigma channel clip; dedispersed over
+    # hundreds to thousands of channels the pulse stands far above 6 sigma.
+    k_dm, tsr = 4148.741601, RAW_TSAMP
+    nch = cfg["nchan_sub"]
+    f_top = cfg["f_sub0"] + (nsub - 1) * SUB_BW + (nch // 2 - 1) * SUB_BW / nch  # highest channel
+    gp = torch.Generator(device=dev)
+    gp.manual_seed(seed + 1)
     for dm, width, pos in cfg.get("pulses", []):
-        sig = max(width / 2.355 / RAW_TSAMP, 1.0)
+        sig = width / 2.3548
         for s in range(nsub):
-            f = cfg["f_sub0"] + s * SUB_BW
-            delay = 4148.741601 * dm * (1.0 / f ** 2 - 1.0 / f_top ** 2) / RAW_TSAMP
-            c0 = (pos * n + delay) % n
-            lo, hi = int(c0 - 4 * sig), int(c0 + 4 * sig) + 1
-            tt = torch.arange(lo, hi, device=dev, dtype=torch.float32)
-            env = 1.0 + 0.22 * torch.exp(-0.5 * ((tt - c0) / sig) ** 2)
-            idx = torch.remainder(torch.arange(lo, hi, device=dev), n)
-            v[s, :, idx, :] *= env[None, :, None]
+            fc = cfg["f_sub0"] + s * SUB_BW
+            tc = pos * n * tsr + k_dm * dm * (1 / fc ** 2 - 1 / f_top ** 2)
+            lo_d = k_dm * dm * (1 / (fc + SUB_BW / 2) ** 2 - 1 / fc ** 2)
+            hi_d = k_dm * dm * (1 / (fc - SUB_BW / 2) ** 2 - 1 / fc ** 2)
+            L = 1 << int(np.ceil(np.log2(max((hi_d - lo_d + 12 * sig) / tsr, 32) * 2)))
+            start = int(np.floor((tc + lo_d - 6 * sig) / tsr)) - L // 4
+            t = (start + torch.arange(L, device=dev, dtype=torch.float64)) * tsr
+            env = torch.exp(-0.5 * ((t - tc) / sig) ** 2)
+            nu = torch.fft.fftfreq(L, d=tsr, device=dev, dtype=torch.float64)
+            order = torch.argsort(nu)
+            f = fc + nu[order] / 1e6
+            delay = k_dm * dm * (1 / f ** 2 - 1 / fc ** 2)
+            phase = torch.empty(L, device=dev, dtype=torch.float64)
+            phase[order] = -2 * np.pi * torch.cumsum(delay, 0) * (1.0 / (L * tsr))
+            rot = torch.polar(torch.ones_like(phase), phase).to(torch.complex64)
+            idx = torch.remainder(start + torch.arange(L, device=dev), n)
+            envf = (env * float(np.sqrt(PULSE_SCALE * 256.0))).float()
+            for p in range(2):
+                burst = torch.complex(torch.randn(L, generator=gp, device=dev),
+                                      torch.randn(L, generator=gp, device=dev)) * envf
+                disp = torch.fft.ifft(torch.fft.fft(burst) * rot)
+                v[s, p, :, 0].index_add_(0, idx, disp.real.float())
+                v[s, p, :, 1].index_add_(0, idx, disp.imag.float())
     return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
 
 
@@ -689,6 +710,8 @@ def run_batch(args, cfgs, workload):
 
 
 PRECISION_BEAMS = 6
+# Voltage variance of an injected pulse relative to the noise at its peak.
+PULSE_SCALE = 0.2
 # Untimed steps of both arms whose windows and events are compared bit for bit.
 PARITY_STEPS = 8
 

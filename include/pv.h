@@ -425,8 +425,9 @@ typedef struct pv_batch pv_batch;
                                  the median and sigma the median absolute deviation x 1.4826 of
                                  the first chunk in which the channel varies (until then the
                                  channel's samples are stored as its offset) */
-#define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..3 */
-#define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % 4)
+#define PV_BATCH_VARIANTS 6            /* dedispersion tile variants (4 and 5: FP32 rings only) */
+#define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..5 */
+#define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % PV_BATCH_VARIANTS)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
 void pv_batch_destroy(pv_batch* batch);
 #define PV_BATCH_HOST_EVENTS 65536 /* events per beam per step kept in host memory */
@@ -465,9 +466,12 @@ int pv_batch_events(pv_batch* batch, int beam, long long step, pv_event* h_event
 int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
 /* Dedispersion tiling: [variant, time tile, channels per stage, stages,
  * slot floats, tiles, CTAs, shared bytes], the DM tile height of every beam,
- * the autotuner's time (ms) of each variant (-1: not timed or not usable) and
- * the kernels one graph replay launches (0 without a graph).  Any may be NULL. */
-int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tune_ms4,
+ * the autotuner's time (ms) of each of the PV_BATCH_VARIANTS variants (-1:
+ * not timed or not usable) and the kernels one graph replay launches (0
+ * without a graph).  Any may be NULL.  Variants 0-3 give each trial of a
+ * DM tile one warp (one shared-memory word per add); variants 4 and 5 give
+ * each warp two adjacent trials that share the words they both read. */
+int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tune_ms,
                    long long* h_graph_kernels);
 /* Device time (ms) of the last step's stages (PV_BATCH_TIMING): channelise,
  * RFI, ring write, dedisperse, analyse (pipelined: the last two run

@@ -12,7 +12,9 @@
 //   RFI_Clipper::run(WeightedSpectrumDataSet*), bandPass()                    lib/RFI_Clipper.h:37-38
 //   DedispersionModule::dedisperse(WeightedSpectrumDataSet*), connect(),
 //       unlockCallback(), onChainCompletion(), waitForJobCompletion(),
-//       maxshift(), numberOfSamples()                                          lib/DedispersionModule.h:76-104
+//       lockNumber(), maxshift(), numberOfSamples()                            lib/DedispersionModule.h:76-104,
+//                                                                              lib/AsyncronousModule.h:40-53
+//   LockingPtrContainer::next(), unlock()                                     lib/LockingPtrContainer.hpp
 //   DedispersionAnalyser::analyse(DedispersionSpectra*, DedispersionDataAnalysis*) lib/DedispersionAnalyser.h:31
 //   SigprocStokesWriter::sendStream(), DedispersionDataAnalysisOutput::sendStream()
 //                                                                              lib/SigprocStokesWriter.h,
@@ -22,9 +24,12 @@
 // and defaults.  Errors the reference throws as QString (or reports with
 // exit()) are thrown here as std::runtime_error with the same text.  Data
 // sets live in host memory as in the reference; each run() moves its data
-// through device memory.  The DedispersionModule calls its connected
-// functors synchronously, on the thread that completes a buffer, and
-// releases input blobs at once (their samples are copied when added).
+// through device memory.  The DedispersionModule is asynchronous as the
+// reference's: dedisperse() returns once the samples are in the device
+// ring, a worker thread calls the connected functors, and input blobs stay
+// locked (lockNumber) until the buffers holding their samples are
+// exported.  DedispersionPipeline keeps a chunk on the device from the
+// voltages to the dedispersion when it computes Stokes I only.
 //
 // Qt and the pelican core are absent: ConfigNode here is a small XML reader
 // of one module element, and blobs are plain classes.
@@ -38,8 +43,11 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <ctime>
 #include <iostream>
 #include <complex>
@@ -49,9 +57,12 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 namespace pelican {
@@ -269,6 +280,11 @@ class SpectrumDataSet : public DataBlob {
         nb_ = nBlocks; ns_ = nSubbands; np_ = nPols; nc_ = nChannels;
         d_.assign((size_t)nb_ * ns_ * np_ * nc_, T());
     }
+    // The shape without clearing the data (kept where the size does not change).
+    void reshape(unsigned nBlocks, unsigned nSubbands, unsigned nPols, unsigned nChannels) {
+        nb_ = nBlocks; ns_ = nSubbands; np_ = nPols; nc_ = nChannels;
+        d_.resize((size_t)nb_ * ns_ * np_ * nc_);
+    }
     unsigned nTimeBlocks() const { return nb_; }
     unsigned nSubbands() const { return ns_; }
     unsigned nPolarisations() const { return np_; }
@@ -298,8 +314,9 @@ class WeightedSpectrumDataSet : public DataBlob {
     void reset(SpectrumDataSetStokes* d) {
         data_ = d;
         if (d) {
-            w_.resize(d->nTimeBlocks(), d->nSubbands(), d->nPolarisations(), d->nChannels());
-            std::fill(w_.data(), w_.data() + w_.size(), 1.0f);
+            const size_t before = w_.size();
+            w_.reshape(d->nTimeBlocks(), d->nSubbands(), d->nPolarisations(), d->nChannels());
+            if (w_.size() > before) std::fill(w_.data() + before, w_.data() + w_.size(), 1.0f);
         }
     }
     SpectrumDataSetStokes* stats() const { return data_; }
@@ -514,6 +531,23 @@ class PPFChanneliser {
     PPFChanneliser(const PPFChanneliser&) = delete;
     PPFChanneliser& operator=(const PPFChanneliser&) = delete;
 
+    // run() followed by StokesGenerator's Stokes I, fused in one device pass
+    // into d_stokes [block][subband][1][channel] (the fused pipeline); the
+    // values equal run() then StokesGenerator::run with numberOfStokes 1.
+    void runStokesIDevice(const TimeSeriesDataSetC32* in, float* d_stokes, void* stream) {
+        if (!in || in->nTimeBlocks() == 0 || in->nSubbands() == 0)
+            throw std::runtime_error("PPFChanneliser: Empty time data blob");
+        if (in->nTimesPerBlock() != nchan_)
+            throw std::runtime_error("PPFChanneliser: Data blob has incorrect number of channels");
+        if (in->nPolarisations() != 2) throw std::runtime_error("StokesGenerator: needs 2 polarisations");
+        const unsigned ns = in->nSubbands(), nb = in->nTimeBlocks();
+        const size_t n = (size_t)ns * 2 * nb * nchan_;
+        float* d_in = din_.as<float>(2 * n);
+        pv_check(pv_device_copy(d_in, in->data(), (long long)(8 * n), stream));
+        int nu = 0;
+        pv_check(pv_channelise(h_, d_in, 0, (int)ns, (int)nb, 1, 1, 1, d_stokes, &nu, stream));
+    }
+
     void run(const TimeSeriesDataSetC32* in, SpectrumDataSetC32* out) {
         if (!in || in->nTimeBlocks() == 0 || in->nSubbands() == 0)
             throw std::runtime_error("PPFChanneliser: Empty time data blob");
@@ -532,6 +566,8 @@ class PPFChanneliser {
         out->setLofarTimestamp(in->getLofarTimestamp());
     }
 
+    unsigned channels() const { return nchan_; }
+
   private:
     pv_ppf* h_ = nullptr;
     unsigned nchan_ = 0;
@@ -546,6 +582,7 @@ class StokesGenerator {
         if (nstokes_ != 1 && nstokes_ != 4)
             throw std::runtime_error("StokesGenerator: You can either generate 1 or 4 Stokes parameters.");
     }
+    unsigned numberOfStokes() const { return nstokes_; }
     void run(const SpectrumDataSetC32* in, SpectrumDataSetStokes* out) {
         const unsigned nt = in->nTimeBlocks(), ns = in->nSubbands(), nc = in->nChannels();
         if (in->nPolarisations() != 2) throw std::runtime_error("StokesGenerator: needs 2 polarisations");
@@ -595,6 +632,29 @@ class StokesIntegrator {
     DeviceBuffer din_, dout_;
 };
 
+// The clipper's bandpass model as RFI_Clipper::bandPass() returns it
+// (lib/BandPass.h:34-80): the rebinned model the next spectrum is compared
+// with, its mean and RMS (setMean/setRMS after every spectrum,
+// RFI_Clipper.cpp:562-563), the median and the polynomial.  A snapshot,
+// refreshed by each bandPass() call.
+class BandPass {
+  public:
+    const std::vector<float>& currentSet() const { return set_; }
+    float intensityOfBin(unsigned i) const { return set_[i]; }
+    float mean() const { return mean_; }
+    float rms() const { return rms_; }
+    float median() const { return median_; }
+    // the polynomial's constant term as setMean leaves it (the other
+    // coefficients are the file's, scaled by the rebinning)
+    float params0() const { return params0_; }
+    unsigned nBins() const { return (unsigned)set_.size(); }
+
+  private:
+    friend class RFI_Clipper;
+    std::vector<float> set_;
+    float mean_ = 0.0f, rms_ = 0.0f, median_ = 0.0f, params0_ = 0.0f;
+};
+
 // lib/src/RFI_Clipper.cpp:22-573 (the BandPassData file is read here and
 // parsed by the library, BandPassAdapter.cpp:30-108)
 class RFI_Clipper {
@@ -637,26 +697,103 @@ class RFI_Clipper {
         const size_t n = d->size();
         float* dd = dbuf_.as<float>(n);
         pv_check(pv_device_copy(dd, d->data(), (long long)(4 * n), nullptr));
-        pv_check(pv_rfi_run(h_, dd, (int)d->nTimeBlocks(), (int)d->nSubbands(), (int)d->nPolarisations(),
-                            (int)d->nChannels(), nullptr, nullptr));
+        runDevice(dd, d->nTimeBlocks(), d->nSubbands(), d->nPolarisations(), d->nChannels(), nullptr);
         pv_check(pv_device_copy(d->data(), dd, (long long)(4 * n), nullptr));
         pv_check(pv_synchronize(nullptr));
-        nbins_ = d->nSubbands() * d->nChannels();
     }
-    // The rebinned bandpass model in use (BandPass::currentSet).
-    std::vector<float> bandPass() {
-        std::vector<float> bp(nbins_);
-        if (nbins_) pv_check(pv_rfi_bandpass(h_, bp.data(), (int)nbins_));
-        return bp;
+    // run() on Stokes data already in device memory, asynchronously on stream.
+    void runDevice(float* d_stokes, unsigned nt, unsigned nsub, unsigned npol, unsigned nchan, void* stream) {
+        pv_check(pv_rfi_run(h_, d_stokes, (int)nt, (int)nsub, (int)npol, (int)nchan, nullptr, stream));
+        nbins_ = nsub * nchan;
+    }
+    // The bandpass in use (lib/RFI_Clipper.h:38); empty before the first run.
+    const BandPass& bandPass() const {
+        if (nbins_) {
+            bp_.set_.resize(nbins_);
+            float st[4];
+            pv_check(pv_rfi_bandpass_current(h_, bp_.set_.data(), (int)nbins_, st));
+            bp_.mean_ = st[0];
+            bp_.rms_ = st[1];
+            bp_.median_ = st[2];
+            bp_.params0_ = st[3];
+        }
+        return bp_;
     }
 
   private:
     pv_rfi* h_ = nullptr;
     unsigned nbins_ = 0;
     DeviceBuffer dbuf_;
+    mutable BandPass bp_;
 };
 
-// lib/src/DedispersionModule.cpp:45-325 with the reference's buffering
+// lib/LockingPtrContainer.hpp: a pool of blobs handed out by next() and
+// given back by unlock() (a pipeline's ring of Stokes blobs that the
+// DedispersionModule holds until their buffers are exported).
+template <typename T>
+class LockingPtrContainer {
+  public:
+    explicit LockingPtrContainer(std::vector<T*>* data = nullptr) {
+        if (data) reset(data);
+    }
+    void reset(std::vector<T*>* data) {
+        std::lock_guard<std::mutex> l(m_);
+        data_ = data;
+        available_.assign(data->begin(), data->end());
+    }
+    // The next free blob.  The reference waits without limit
+    // (LockingPtrContainer.hpp:37-43); here a wait longer than wait_s seconds
+    // throws, since only a history too small for the module's buffers can
+    // make it.
+    T* next(double wait_s = 60.0) {
+        std::unique_lock<std::mutex> l(m_);
+        if (!cv_.wait_for(l, std::chrono::duration<double>(wait_s), [&] { return !available_.empty(); }))
+            throw std::runtime_error("LockingPtrContainer: no free data blob (the pipeline's <history> is "
+                                     "smaller than the blobs its DedispersionModule buffers hold)");
+        T* p = available_.front();
+        available_.pop_front();
+        return p;
+    }
+    void unlock(const T* d) {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            available_.push_back(const_cast<T*>(d));
+        }
+        cv_.notify_one();
+    }
+    int numberAvailable() const {
+        std::lock_guard<std::mutex> l(m_);
+        return (int)available_.size();
+    }
+    bool allAvailable() const {
+        std::lock_guard<std::mutex> l(m_);
+        return !data_ || available_.size() == data_->size();
+    }
+
+  private:
+    std::vector<T*>* data_ = nullptr;
+    std::deque<T*> available_;
+    mutable std::mutex m_;
+    std::condition_variable cv_;
+};
+
+// lib/src/DedispersionModule.cpp:45-325 with the reference's buffering and
+// the asynchronous contract of lib/AsyncronousModule.h:40-53.  dedisperse()
+// moves the blob's samples into the device ring and, when a buffer fills,
+// launches its dedispersion, then returns.  A worker thread takes each
+// filled buffer in order, copies its DedispersionSpectra back, calls the
+// connect() functors, unlocks the buffer's input blobs (unlockCallback gets
+// those whose lock count reaches 0) and then the onChainCompletion()
+// callbacks.  A buffer whose GPU job fails is not delivered: its blobs are
+// unlocked and the error is printed, as GPU_Job::Failed is
+// (DedispersionModule.cpp:299-311).  Lock counts follow the reference
+// (:216-246, AsyncronousModule.cpp:113-131): the blobs added since the last
+// fill are locked once when a buffer fills, the blobs whose samples the
+// next buffer's overlap holds once more, and the blob being added once more
+// when it continues past the buffer outside that overlap; exporting a
+// buffer unlocks each of its input blobs once.  Input blobs must stay alive
+// and unchanged until unlocked.  The functors of one module run one after
+// another on its worker thread.
 class DedispersionModule {
   public:
     using Functor = std::function<void(DedispersionSpectra*)>;
@@ -672,84 +809,197 @@ class DedispersionModule {
         foff_ = std::stod(config.getOption("channelBandwidth", "MHz", "1.0"));
         pv_check(pv_ddmod_create(&h_, (int)samples_, (int)tdms_, dm_low_, dm_step_, fch1_, foff_));
     }
-    ~DedispersionModule() { pv_ddmod_destroy(h_); }
+    ~DedispersionModule() {
+        waitForJobCompletion();
+        {
+            std::lock_guard<std::mutex> l(q_mu_);
+            stop_ = true;
+        }
+        q_cv_.notify_all();
+        if (worker_.joinable()) worker_.join();
+        pv_ddmod_destroy(h_);
+    }
     DedispersionModule(const DedispersionModule&) = delete;
     DedispersionModule& operator=(const DedispersionModule&) = delete;
 
     void connect(const Functor& f) { functors_.push_back(f); }
-    void unlockCallback(const UnlockCallback& f) { unlock_ = f; }
+    void unlockCallback(const UnlockCallback& f) { unlock_.push_back(f); }
     void onChainCompletion(const std::function<void()>& f) { chain_.push_back(f); }
-    void waitForJobCompletion() {}
+    // Blocks until every filled buffer has been exported (AsyncronousModule.cpp:49-51).
+    void waitForJobCompletion() const {
+        std::unique_lock<std::mutex> l(q_mu_);
+        idle_cv_.wait(l, [&] { return jobs_.empty() && !busy_; });
+    }
+    // Locks this module holds on a blob (AsyncronousModule.cpp:113-119).
+    int lockNumber(const DataBlob* d) const {
+        std::lock_guard<std::mutex> l(locks_mu_);
+        auto it = locks_.find(d);
+        return it == locks_.end() ? 0 : it->second;
+    }
     unsigned numberOfSamples() const { return samples_; }
     int maxshift() const {
         int p[6] = {0};
+        std::lock_guard<std::mutex> l(dd_mu_);
         pv_check(pv_ddmod_params(h_, p));
         return p[0];
     }
 
-    void dedisperse(WeightedSpectrumDataSet* weighted) { dedisperse_blob(weighted->stats(), weighted); }
+    void dedisperse(WeightedSpectrumDataSet* weighted) {
+        add(weighted->dataSet(), weighted->dataSet()->data(), nullptr);
+    }
     void dedisperse(DataBlob* blob) {
         auto* w = dynamic_cast<WeightedSpectrumDataSet*>(blob);
         if (!w) throw std::runtime_error("DedispersionModule: expecting a WeightedSpectrumDataSet");
         dedisperse(w);
     }
+    // dedisperse() of a blob whose Stokes data (the blob's layout) are
+    // already in device memory at d_stokes, ordered on stream: the fused
+    // pipeline's path, with no host copy of the samples.
+    void dedisperseDevice(WeightedSpectrumDataSet* weighted, const float* d_stokes, void* stream) {
+        add(weighted->dataSet(), d_stokes, stream);
+    }
 
   private:
-    void dedisperse_blob(SpectrumDataSetStokes* d, DataBlob* blob) {
-        int done = 0;
-        nch_ = d->nChannels();
-        nsub_ = d->nSubbands();
-        pv_check(pv_ddmod_add(h_, d->data(), (int)d->nTimeBlocks(), (int)d->nSubbands(),
-                              (int)d->nPolarisations(), (int)d->nChannels(), d->getBlockRate(), &done,
-                              nullptr));
-        if (unlock_) unlock_(std::vector<DataBlob*>{blob});  // samples are copied on add
+    struct Span {
+        const SpectrumDataSetStokes* blob;
+        long long start, end;  // the blob's samples in the stream
+    };
+    struct Job {
+        std::vector<const SpectrumDataSetStokes*> inputs;
+        unsigned nch, nsub;
+        double rate, t0;
+    };
+
+    void add(SpectrumDataSetStokes* d, const float* data, void* stream) {
         if (!have_t0_) {  // sample 0 of the stream: times are t0 + (t + firstSample) * rate
             t0_ = d->getLofarTimestamp();
             have_t0_ = true;
         }
-        // a copy of the blob for the buffers that will hold its samples
-        held_.push_back(Held{received_, std::make_shared<SpectrumDataSetStokes>(*d)});
-        received_ += d->nTimeBlocks();
-        for (int i = 0; i < done; ++i) {
+        const long long nt = d->nTimeBlocks();
+        spans_.push_back(Span{d, received_, received_ + nt});
+        received_ += nt;
+        pending_.push_back(d);
+        int done = 0, p[6] = {0};
+        {
+            std::lock_guard<std::mutex> l(dd_mu_);
+            pv_check(pv_ddmod_add(h_, data, (int)nt, (int)d->nSubbands(), (int)d->nPolarisations(),
+                                  (int)d->nChannels(), d->getBlockRate(), &done, stream));
+            pv_check(pv_ddmod_params(h_, p));
+        }
+        if (done == 0) return;
+        const long long nout = p[2], B = samples_;
+        std::vector<Job> jobs;
+        {
+            std::lock_guard<std::mutex> l(locks_mu_);
+            for (int i = 0; i < done; ++i) {
+                const long long first = filled_ * nout, end = first + B, next = first + nout;
+                Job job{{}, d->nChannels(), d->nSubbands(), d->getBlockRate(), t0_};
+                for (const Span& sp : spans_)
+                    if (sp.start < end && sp.end > first) job.inputs.push_back(sp.blob);
+                for (const DataBlob* b : pending_) ++locks_[b];  // lockAllUnprotected(_blobs)
+                pending_.clear();
+                bool in_next = false;
+                for (const Span& sp : spans_)
+                    if (sp.start < end && sp.end > next) {  // the overlap copied to the next buffer
+                        ++locks_[sp.blob];
+                        in_next = in_next || sp.blob == d;
+                    }
+                if (received_ > end && !in_next) ++locks_[d];
+                ++filled_;
+                jobs.push_back(std::move(job));
+            }
+            // blobs wholly before the next buffer are in no later buffer
+            while (!spans_.empty() && spans_.front().end <= filled_ * nout) spans_.pop_front();
+        }
+        {
+            std::lock_guard<std::mutex> l(q_mu_);
+            for (Job& j : jobs) jobs_.push_back(std::move(j));
+            if (!worker_.joinable()) worker_ = std::thread([this] { work(); });
+        }
+        q_cv_.notify_one();
+    }
+
+    void work() {
+        for (;;) {
+            Job job;
+            {
+                std::unique_lock<std::mutex> l(q_mu_);
+                q_cv_.wait(l, [&] { return stop_ || !jobs_.empty(); });
+                if (jobs_.empty()) return;
+                job = std::move(jobs_.front());
+                jobs_.pop_front();
+                busy_ = true;
+            }
+            export_job(job);
+            {
+                std::lock_guard<std::mutex> l(q_mu_);
+                busy_ = false;
+            }
+            idle_cv_.notify_all();
+        }
+    }
+
+    void export_job(const Job& job) {
+        DedispersionSpectra out;
+        bool ok = true;
+        try {
+            std::lock_guard<std::mutex> l(dd_mu_);
             int p[6] = {0};
             pv_check(pv_ddmod_params(h_, p));
-            DedispersionSpectra out;
             out.resize((unsigned)p[2], tdms_, dm_low_ < 0.0f ? 0.0f : dm_low_, dm_step_);
             int nout = 0;
             long long first = 0;
             pv_check(pv_ddmod_pop(h_, out.data().data(), (long long)out.data().size(), &nout, &first, nullptr));
             out.setFirstSample((unsigned)first);
-            out.setInputShape(nch_, nsub_);
-            out.setBlockRate(d->getBlockRate());
-            out.setLofarTimestamp(t0_);
-            std::vector<const SpectrumDataSetStokes*> inputs;
-            for (const Held& h : held_)
-                if (h.start < first + (long long)samples_ && h.start + h.blob->nTimeBlocks() > first)
-                    inputs.push_back(h.blob.get());
-            out.setInputDataBlobs(inputs);
-            for (auto& f : functors_) f(&out);
-            for (auto& f : chain_) f();
-            // later buffers start after this one: blobs wholly before it are not needed again
-            while (!held_.empty() && held_.front().start + held_.front().blob->nTimeBlocks() <= first)
-                held_.pop_front();
+        } catch (const std::exception& e) {
+            std::cerr << "DedispersionModule: " << e.what() << std::endl;
+            ok = false;
         }
+        if (ok) {
+            out.setInputShape(job.nch, job.nsub);
+            out.setBlockRate(job.rate);
+            out.setLofarTimestamp(job.t0);
+            out.setInputDataBlobs(job.inputs);
+            for (auto& f : functors_) f(&out);
+        }
+        // exportComplete (DedispersionModule.cpp:317-325) and the unlock triggers
+        std::vector<DataBlob*> freed;
+        {
+            std::lock_guard<std::mutex> l(locks_mu_);
+            for (const SpectrumDataSetStokes* b : job.inputs) {
+                auto it = locks_.find(b);
+                if (it != locks_.end() && --it->second == 0) {
+                    freed.push_back(const_cast<SpectrumDataSetStokes*>(b));
+                    locks_.erase(it);
+                }
+            }
+        }
+        for (auto& f : unlock_) f(freed);
+        if (ok)
+            for (auto& f : chain_) f();
     }
-    struct Held {
-        long long start;  // the blob's first sample in the stream
-        std::shared_ptr<SpectrumDataSetStokes> blob;
-    };
-    std::deque<Held> held_;
-    long long received_ = 0;
 
     pv_ddmod* h_ = nullptr;
     double t0_ = 0.0;
     bool have_t0_ = false;
-    unsigned samples_ = 0, tdms_ = 0, nch_ = 0, nsub_ = 0;
+    unsigned samples_ = 0, tdms_ = 0;
     float dm_step_ = 0.0f, dm_low_ = 0.0f;
     double fch1_ = 0.0, foff_ = 0.0;
     std::vector<Functor> functors_;
     std::vector<std::function<void()>> chain_;
-    UnlockCallback unlock_;
+    std::vector<UnlockCallback> unlock_;
+    // caller-thread bookkeeping
+    std::deque<Span> spans_;
+    std::vector<const DataBlob*> pending_;  // added since the last fill (the reference's _blobs)
+    long long received_ = 0, filled_ = 0;
+    // shared with the worker
+    mutable std::mutex dd_mu_, locks_mu_, q_mu_;
+    std::unordered_map<const DataBlob*, int> locks_;
+    std::deque<Job> jobs_;
+    bool busy_ = false, stop_ = false;
+    mutable std::condition_variable idle_cv_;
+    std::condition_variable q_cv_;
+    std::thread worker_;
 };
 
 // lib/src/DedispersionAnalyser.cpp:30-203
@@ -790,24 +1040,23 @@ class DedispersionAnalyser {
 // Pipeline driver
 // ---------------------------------------------------------------------------
 
-// pipelines/udpstream/src/DedispersionPipeline.cpp:48-155: per chunk of
-// voltages, PPFChanneliser -> StokesGenerator -> RFI_Clipper ->
-// DedispersionModule (no StokesIntegrator in this pipeline: :101-104); each
-// completed buffer is analysed and goes to the "TriggerInput" output, and
-// to "DedispersionDataAnalysis" when its event count is at least <events
-// min> (min >= max) or within [min, max].  Modules and limits come from one
-// XML file with the reference's element names.  Outputs are callbacks in
-// place of the pelican output manager; input spectra are not kept, so
-// "SignalFoundSpectrum" has no data to send.
 // What both pipeline drivers do with a dedispersed buffer
 // (DedispersionPipeline.cpp:111-150, ABPipeline.cpp:142-170): analyse it,
 // send the result to the "TriggerInput" outputs, and to the
 // "DedispersionDataAnalysis" outputs when the event count lies in
-// <events min max> (at least min when min >= max).
+// <events min max> (at least min when min >= max), with each of the
+// buffer's input blobs to the "SignalFoundSpectrum" outputs.  The analysis
+// runs on the DedispersionModule's worker thread, beside the next run().
+// The Stokes blobs the module reads come from a ring of <history> blobs
+// (createBlobs + LockingPtrContainer, DedispersionPipeline.cpp:83-90) that
+// the module's unlock callback refills (updateBufferLock, :209-217).
 class PipelineAnalysis {
   public:
     using Output = std::function<void(const DedispersionDataAnalysis&)>;
     using SpectrumOutput = std::function<void(const SpectrumDataSetStokes&)>;
+    virtual ~PipelineAnalysis() {
+        if (dd_) dd_->waitForJobCompletion();
+    }
     // AbstractPipeline::dataOutput: "TriggerInput" or "DedispersionDataAnalysis"
     void connectOutput(const std::string& stream, const Output& f) { outputs_.emplace_back(stream, f); }
     // "SignalFoundSpectrum": each input blob of a buffer that reaches the
@@ -815,15 +1064,27 @@ class PipelineAnalysis {
     void connectSpectrumOutput(const std::string& stream, const SpectrumOutput& f) {
         spectrum_outputs_.emplace_back(stream, f);
     }
-    unsigned buffers() const { return buffers_; }
+    // Buffers analysed so far (complete after waitForJobCompletion()).
+    unsigned buffers() const { return buffers_.load(); }
+    // Waits until every filled buffer has been analysed and sent.
+    void waitForJobCompletion() const { dd_->waitForJobCompletion(); }
+    const DedispersionModule& dedispersionModule() const { return *dd_; }
+    unsigned history() const { return (unsigned)ring_.size(); }
 
   protected:
     // the modules after the first stages: RFI_Clipper, DedispersionModule, DedispersionAnalyser
-    void setup(const std::string& config_file) {
+    void setup(const std::string& config_file, unsigned history) {
         rfi_.reset(new RFI_Clipper(ConfigNode::fromFile(config_file, "RFI_Clipper")));
         dd_.reset(new DedispersionModule(ConfigNode::fromFile(config_file, "DedispersionModule")));
         an_.reset(new DedispersionAnalyser(ConfigNode::fromFile(config_file, "DedispersionAnalyser")));
         dd_->connect([this](DedispersionSpectra* d) { analysis(d); });
+        dd_->unlockCallback([this](const std::vector<DataBlob*>& blobs) {
+            for (DataBlob* b : blobs) stokes_buffer_.unlock(static_cast<SpectrumDataSetStokes*>(b));
+        });
+        history = std::max(history, 1u);
+        for (unsigned k = 0; k < history; ++k) ring_.emplace_back(new SpectrumDataSetStokes);
+        for (auto& b : ring_) ring_ptrs_.push_back(b.get());
+        stokes_buffer_.reset(&ring_ptrs_);
     }
     void emit(const std::string& stream, const DedispersionDataAnalysis& r) {
         for (auto& o : outputs_)
@@ -843,28 +1104,64 @@ class PipelineAnalysis {
         }
     }
 
-    unsigned min_ = 5, max_ = 0, buffers_ = 0;
+    unsigned min_ = 5, max_ = 0;
+    std::atomic<unsigned> buffers_{0};
     std::unique_ptr<RFI_Clipper> rfi_;
     std::unique_ptr<DedispersionModule> dd_;
     std::unique_ptr<DedispersionAnalyser> an_;
     std::vector<std::pair<std::string, Output>> outputs_;
     std::vector<std::pair<std::string, SpectrumOutput>> spectrum_outputs_;
+    std::vector<std::unique_ptr<SpectrumDataSetStokes>> ring_;
+    std::vector<SpectrumDataSetStokes*> ring_ptrs_;
+    LockingPtrContainer<SpectrumDataSetStokes> stokes_buffer_;
 };
 
+// pipelines/udpstream/src/DedispersionPipeline.cpp:48-155: per chunk of
+// voltages, PPFChanneliser -> StokesGenerator -> RFI_Clipper ->
+// DedispersionModule (no StokesIntegrator in this pipeline: :101-104).
+// Modules and limits come from one XML file with the reference's element
+// names; outputs are callbacks in place of the pelican output manager.
+// With numberOfStokes 1 (and <fused value="true"/>, the default) the chunk
+// stays in device memory from the voltages to the dedispersion ring: one
+// fused PPF + Stokes-I pass, the clipper on the device and the module
+// reading the clipped spectra there, where the module chain copies each
+// stage's data set to the host and back.  The results are identical; the
+// Stokes blobs receive the clipped spectra only when a
+// "SignalFoundSpectrum" output is connected.
 class DedispersionPipeline : public PipelineAnalysis {
   public:
     explicit DedispersionPipeline(const std::string& config_file) {
         const ConfigNode c = ConfigNode::fromFile(config_file, "DedispersionPipeline");
         min_ = to_uint(c.getOption("events", "min", "5"));
         max_ = to_uint(c.getOption("events", "max", "0"));
+        const unsigned history = to_uint(c.getOption("history", "value", "10"));
         ppf_.reset(new PPFChanneliser(ConfigNode::fromFile(config_file, "PPFChanneliser")));
         stokes_.reset(new StokesGenerator(ConfigNode::fromFile(config_file, "StokesGenerator")));
-        setup(config_file);
+        fused_ = stokes_->numberOfStokes() == 1 && lower(c.getOption("fused", "value", "true")) == "true";
+        setup(config_file, history);
     }
+    bool fused() const { return fused_; }
     void run(TimeSeriesDataSetC32* timeSeries) {
+        SpectrumDataSetStokes* stokes = stokes_buffer_.next();
+        if (fused_) {
+            const unsigned nb = timeSeries->nTimeBlocks(), ns = timeSeries->nSubbands(), nc = ppf_->channels();
+            float* d = dstokes_.as<float>((size_t)nb * ns * nc);
+            ppf_->runStokesIDevice(timeSeries, d, nullptr);
+            stokes->reshape(nb, ns, 1, nc);
+            stokes->setBlockRate(timeSeries->getBlockRate() * nc);  // PPFChanneliser.cpp:99
+            stokes->setLofarTimestamp(timeSeries->getLofarTimestamp());
+            WeightedSpectrumDataSet w(stokes);
+            rfi_->runDevice(d, nb, ns, 1, nc, nullptr);
+            if (!spectrum_outputs_.empty()) {
+                pv_check(pv_device_copy(stokes->data(), d, (long long)(4 * stokes->size()), nullptr));
+                pv_check(pv_synchronize(nullptr));
+            }
+            dd_->dedisperseDevice(&w, d, nullptr);
+            return;
+        }
         ppf_->run(timeSeries, &spectra_);
-        stokes_->run(&spectra_, &stokes_data_);
-        WeightedSpectrumDataSet w(&stokes_data_);
+        stokes_->run(&spectra_, stokes);
+        WeightedSpectrumDataSet w(stokes);
         rfi_->run(&w);
         dd_->dedisperse(&w);
     }
@@ -873,20 +1170,21 @@ class DedispersionPipeline : public PipelineAnalysis {
     std::unique_ptr<PPFChanneliser> ppf_;
     std::unique_ptr<StokesGenerator> stokes_;
     SpectrumDataSetC32 spectra_;
-    SpectrumDataSetStokes stokes_data_;
+    DeviceBuffer dstokes_;
+    bool fused_ = false;
 };
 
 // pipelines/udpstream/src/ABPipeline.cpp:56-140: the ALFABURST driver.  Each
 // chunk's spectra (ABDataAdapter) go through the StokesIntegrator (its
-// element is optional: 1 and 1 when absent, as createModule gives), the
+// element is optional: 1 and 1 when absent, as createModule gives), are
+// copied to the next blob of the ring (:83-87), then go through the
 // RFI_Clipper, the DedispersionModule and the analyser; <events min max>
-// default to 5 and 5.  <history> sizes the reference's lock ring of input
-// blobs, which the module here does not need: it copies the data it keeps.
+// default to 5 and 5.
 class ABPipeline : public PipelineAnalysis {
   public:
     explicit ABPipeline(const std::string& config_file) {
         const ConfigNode c = ConfigNode::fromFile(config_file, "ABPipeline");
-        history_ = to_uint(c.getOption("history", "value", "10"));
+        const unsigned history = to_uint(c.getOption("history", "value", "10"));
         min_ = to_uint(c.getOption("events", "min", "5"));
         max_ = to_uint(c.getOption("events", "max", "5"));
         ConfigNode integ;
@@ -895,19 +1193,19 @@ class ABPipeline : public PipelineAnalysis {
         } catch (const std::runtime_error&) {
         }
         integrator_.reset(new StokesIntegrator(integ));
-        setup(config_file);
+        setup(config_file, history);
     }
     void run(SpectrumDataSetStokes* stokes) {
         if (!stokes) throw std::runtime_error("No stokes!");
+        SpectrumDataSetStokes* buf = stokes_buffer_.next();
         integrator_->run(stokes, &integrated_);
-        WeightedSpectrumDataSet w(&integrated_);
+        *buf = integrated_;
+        WeightedSpectrumDataSet w(buf);
         rfi_->run(&w);
         dd_->dedisperse(&w);
     }
-    unsigned history() const { return history_; }
 
   private:
-    unsigned history_ = 10;
     std::unique_ptr<StokesIntegrator> integrator_;
     SpectrumDataSetStokes integrated_;
 };

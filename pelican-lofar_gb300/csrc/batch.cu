@@ -711,7 +711,7 @@ extern "C" int pv_batch_info(const pv_batch* b, int beam, long long* h_info8) {
     return PV_OK;
 }
 
-extern "C" int pv_batch_tiles(const pv_batch* b, int* h_shape8, int* h_dms, float* h_tune_ms4,
+extern "C" int pv_batch_tiles(const pv_batch* b, int* h_shape8, int* h_dms, float* h_tune_ms,
                               long long* h_graph_kernels) {
     if (!b) return PV_ERR_ARG;
     if (h_shape8) PV_TRY(pv::dd_batch_shape(b->dd, h_shape8));
@@ -719,9 +719,9 @@ extern "C" int pv_batch_tiles(const pv_batch* b, int* h_shape8, int* h_dms, floa
         const auto& d = pv::dd_batch_dms(b->dd);
         std::copy(d.begin(), d.end(), h_dms);
     }
-    if (h_tune_ms4) {
+    if (h_tune_ms) {
         const auto& t = pv::dd_batch_tune_ms(b->dd);
-        for (int i = 0; i < 4; ++i) h_tune_ms4[i] = i < (int)t.size() ? t[i] : -1.0f;
+        for (int i = 0; i < PV_BATCH_VARIANTS; ++i) h_tune_ms[i] = i < (int)t.size() ? t[i] : -1.0f;
     }
     if (h_graph_kernels) *h_graph_kernels = b->exec ? b->graph_kernels : 0;
     return PV_OK;

@@ -407,6 +407,112 @@ struct Store {
     static constexpr int AU = 16 / E;  // elements per 16 bytes
 };
 
+// The producer warp of the batched kernels: takes (beam, DM tile, time tile)
+// tiles of beams that dedisperse a window this step from the global counter,
+// records each tile beside its first stage and streams the tile's channel
+// spans (TT samples plus the tile's delay spread) into the stage slots with
+// bulk copies, CS channels per stage, ST stages in flight.  Waits are
+// bounded; the last copies have landed before it returns.
+template <int TT, int CS, int ST, int STORE>
+__device__ __forceinline__ void batch_producer(const pv::DdJob* __restrict__ jobs,
+                                               const pv::DdTile* __restrict__ tiles, int ntiles, int slot,
+                                               int* __restrict__ counter, const pv::BeamStep* __restrict__ bs,
+                                               int* __restrict__ status, unsigned long long wait_ns,
+                                               unsigned char* slots, int* meta_off, float* meta_k,
+                                               float* meta_sc, int* s_first, uint64_t* full, uint64_t* empty,
+                                               int lane) {
+    constexpr int E = Store<STORE>::E, AU = Store<STORE>::AU;
+    unsigned gs = 0;
+    bool ok = true, sentinel = false;
+    for (;;) {
+        int tile = -1;  // next tile of a beam that has a window at this step
+        for (;;) {
+            int t = 0;
+            if (lane == 0) t = atomicAdd(counter, 1);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if (t >= ntiles) break;
+            if (bs[jobs[tiles[t].job].beam].sel) {
+                tile = t;
+                break;
+            }
+        }
+        const int b_first = gs % ST;
+        if (!mbar_wait_warp(&empty[b_first], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
+            if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+            ok = false;
+            break;
+        }
+        if (tile < 0) {  // no work left: release the consumers
+            if (lane == 0) {
+                s_first[b_first] = -1;
+                mbar_arrive(&full[b_first]);
+            }
+            sentinel = true;
+            break;
+        }
+        const pv::DdTile tt = tiles[tile];
+        const pv::DdJob& J = jobs[tt.job];
+        const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
+        const float dv0 = pv_trial_value(tt.d0, J.start, J.step);
+        const float dv_last = pv_trial_value(d_last, J.start, J.step);
+        const int valid = min(TT, J.nout - tt.t0);
+        const long long t_base = (bs[J.beam].window * J.chunk) % J.ring_len;
+        const int nst = (J.nchan + CS - 1) / CS;
+        const unsigned char* ring = reinterpret_cast<const unsigned char*>(J.ring);
+        for (int st = 0; st < nst; ++st) {
+            const int b = gs % ST;
+            if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
+                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                ok = false;
+                break;
+            }
+            if (st == 0 && lane == 0) s_first[b] = tile;
+            const int c = st * CS + lane;
+            unsigned bytes = 0, piece1 = 0, piece2 = 0;
+            long long g_al = 0;
+            if (lane < CS && c < J.nchan) {
+                const float k = J.dmshift[c];
+                const int s0 = pv_shift(k, dv0);
+                const int span = valid + pv_shift(k, dv_last) - s0;
+                const long long g0 = (t_base + tt.t0 + s0) % J.ring_len;
+                g_al = g0 & ~(long long)(AU - 1);
+                const int base = (int)(g0 - g_al);
+                const unsigned n = (unsigned)((base + span + AU - 1) & ~(AU - 1));
+                piece1 = (unsigned)min((long long)n, J.ring_len - g_al);
+                piece2 = n - piece1;
+                bytes = n * (unsigned)E;
+                meta_off[b * CS + lane] = s0 - base;
+                meta_k[b * CS + lane] = k;
+                if (STORE == PV_STORE_U8) meta_sc[b * CS + lane] = J.scale[c];
+            }
+            __threadfence_block();
+            unsigned total = bytes;
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&full[b], total);
+            __syncwarp();
+            if (bytes) {
+                const unsigned char* src = ring + (long long)c * J.row_stride * E;
+                unsigned char* dst = slots + (size_t)(b * CS + lane) * slot * E;
+                bulk_g2s(dst, src + g_al * E, piece1 * (unsigned)E, &full[b]);
+                if (piece2) bulk_g2s(dst + (size_t)piece1 * E, src, piece2 * (unsigned)E, &full[b]);
+            }
+            ++gs;
+        }
+        if (!ok) break;
+    }
+    // The last copies have landed (bounded) before the producer leaves.  The
+    // end-of-work record re-armed the slot of stage gs - ST, whose copies had
+    // landed before its consumers released the slot: that stage is skipped
+    // (its barrier's parity now names the newer phase).
+    (void)ok;
+    unsigned g0 = gs > (unsigned)ST ? gs - ST : 0;
+    if (sentinel && gs >= (unsigned)ST) g0 = gs - ST + 1;
+    for (unsigned g = g0; g < gs; ++g)
+        mbar_wait_warp(&full[g % ST], (g / ST) & 1u, pv::kDrainWaitNs);
+}
+
 template <int R, int CS, int ST, int STORE>
 __global__ void __launch_bounds__(17 * 32, 1)
 dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles,
@@ -441,90 +547,8 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     if (s_abort != 0) return;
 
     if (warp == DMS) {
-        // ---------------- producer ----------------
-        unsigned gs = 0;
-        bool ok = true;
-        for (;;) {
-            int tile = -1;  // next tile of a beam that has a window at this step
-            for (;;) {
-                int t = 0;
-                if (lane == 0) t = atomicAdd(counter, 1);
-                t = __shfl_sync(0xffffffffu, t, 0);
-                if (t >= ntiles) break;
-                if (bs[jobs[tiles[t].job].beam].sel) {
-                    tile = t;
-                    break;
-                }
-            }
-            const int b_first = gs % ST;
-            if (!mbar_wait_warp(&empty[b_first], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
-                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
-                ok = false;
-                break;
-            }
-            if (tile < 0) {  // no work left: release the consumers
-                if (lane == 0) {
-                    s_first[b_first] = -1;
-                    mbar_arrive(&full[b_first]);
-                }
-                break;
-            }
-            const pv::DdTile tt = tiles[tile];
-            const pv::DdJob& J = jobs[tt.job];
-            const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
-            const float dv0 = pv_trial_value(tt.d0, J.start, J.step);
-            const float dv_last = pv_trial_value(d_last, J.start, J.step);
-            const int valid = min(TT, J.nout - tt.t0);
-            const long long t_base = (bs[J.beam].window * J.chunk) % J.ring_len;
-            const int nst = (J.nchan + CS - 1) / CS;
-            const unsigned char* ring = reinterpret_cast<const unsigned char*>(J.ring);
-            for (int st = 0; st < nst; ++st) {
-                const int b = gs % ST;
-                if (st > 0 && !mbar_wait_warp(&empty[b], ((gs / ST) & 1u) ^ 1u, wait_ns)) {
-                    if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
-                    ok = false;
-                    break;
-                }
-                if (st == 0 && lane == 0) s_first[b] = tile;
-                const int c = st * CS + lane;
-                unsigned bytes = 0, piece1 = 0, piece2 = 0;
-                long long g_al = 0;
-                if (lane < CS && c < J.nchan) {
-                    const float k = J.dmshift[c];
-                    const int s0 = pv_shift(k, dv0);
-                    const int span = valid + pv_shift(k, dv_last) - s0;
-                    const long long g0 = (t_base + tt.t0 + s0) % J.ring_len;
-                    g_al = g0 & ~(long long)(AU - 1);
-                    const int base = (int)(g0 - g_al);
-                    const unsigned n = (unsigned)((base + span + AU - 1) & ~(AU - 1));
-                    piece1 = (unsigned)min((long long)n, J.ring_len - g_al);
-                    piece2 = n - piece1;
-                    bytes = n * (unsigned)E;
-                    meta_off[b * CS + lane] = s0 - base;
-                    meta_k[b * CS + lane] = k;
-                    if (STORE == PV_STORE_U8) meta_sc[b * CS + lane] = J.scale[c];
-                }
-                __threadfence_block();
-                unsigned total = bytes;
-#pragma unroll
-                for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
-                __syncwarp();
-                if (lane == 0) mbar_arrive_expect_tx(&full[b], total);
-                __syncwarp();
-                if (bytes) {
-                    const unsigned char* src = ring + (long long)c * J.row_stride * E;
-                    unsigned char* dst = slots + (size_t)(b * CS + lane) * slot * E;
-                    bulk_g2s(dst, src + g_al * E, piece1 * (unsigned)E, &full[b]);
-                    if (piece2) bulk_g2s(dst + (size_t)piece1 * E, src, piece2 * (unsigned)E, &full[b]);
-                }
-                ++gs;
-            }
-            if (!ok) break;
-        }
-        // the last copies have landed (bounded) before the producer leaves
-        (void)ok;
-        for (unsigned g = gs > (unsigned)ST ? gs - ST : 0; g < gs; ++g)
-            mbar_wait_warp(&full[g % ST], (g / ST) & 1u, pv::kDrainWaitNs);
+        batch_producer<TT, CS, ST, STORE>(jobs, tiles, ntiles, slot, counter, bs, status, wait_ns, slots,
+                                         meta_off, meta_k, meta_sc, s_first, full, empty, lane);
         return;
     }
 
@@ -722,6 +746,152 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
     }
 }
 
+// ---------------------------------------------------------------------------
+// K4 batched, FP32 rows, trial pairs.  The batched producer fills the same
+// stage slots; eight consumer warps each take two adjacent trials of the
+// tile (d, d+1) and lane l the 33 consecutive output samples 33l..33l+32 of
+// a 1056-sample time tile.  For each channel the lane reads the 33 + delta
+// words row[o_d + 33l + j], delta = o_(d+1) - o_d the channel's shift
+// difference between the two trials, once into registers and adds word j
+// to trial d's sample j and to trial d+1's sample j - delta: up to
+// delta = 32, 33 + delta shared-memory words feed 66 adds (the one-trial
+// consumers read one word per add).  delta selects a fully unrolled variant
+// (a warp-uniform jump), larger shifts take two separate 33-word reads.
+// Lanes 33 words apart read distinct banks, so every read is one
+// conflict-free wavefront.  Each output still adds its channels 0..nchan-1
+// in order with FP32 adds: the results are bit-identical to the other
+// kernels.
+// ---------------------------------------------------------------------------
+constexpr int kPairS = 33;  // output samples per lane
+
+template <int D>
+__device__ __forceinline__ void pair_add(const float* __restrict__ row, float (&a0)[kPairS],
+                                         float (&a1)[kPairS]) {
+#pragma unroll
+    for (int j = 0; j < kPairS + D; ++j) {
+        const float w = row[j];
+        if (j < kPairS) a0[j] = __fadd_rn(a0[j], w);
+        if (j >= D) a1[j - D] = __fadd_rn(a1[j - D], w);
+    }
+}
+
+__device__ __forceinline__ void pair_add_far(const float* __restrict__ row, int dl, float (&a0)[kPairS],
+                                             float (&a1)[kPairS]) {
+#pragma unroll
+    for (int j = 0; j < kPairS; ++j) a0[j] = __fadd_rn(a0[j], row[j]);
+    const float* rb = row + dl;
+#pragma unroll
+    for (int j = 0; j < kPairS; ++j) a1[j] = __fadd_rn(a1[j], rb[j]);
+}
+
+template <int CS, int ST>
+__global__ void __launch_bounds__(9 * 32, 1)
+dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles, int ntiles,
+                       int slot, int* __restrict__ counter, const pv::BeamStep* __restrict__ bs,
+                       int* __restrict__ status, unsigned long long wait_ns) {
+    constexpr int NW = 8;  // consumer warps, two trials each: 16 trials per tile
+    constexpr int TT = 32 * kPairS;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* slots = smem_raw;  // [ST*CS][slot] floats
+    int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * slot * 4);
+    float* meta_k = reinterpret_cast<float*>(meta_off + ST * CS);
+    float* meta_sc = meta_k + ST * CS;
+    int* s_first = reinterpret_cast<int*>(meta_sc + ST * CS);
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_first + 2 * ST);
+    uint64_t* empty = full + ST;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) {
+        s_abort = *(volatile int*)status;
+        for (int b = 0; b < ST; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], NW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (s_abort != 0) return;
+    if (warp == NW) {
+        batch_producer<TT, CS, ST, PV_STORE_F32>(jobs, tiles, ntiles, slot, counter, bs, status, wait_ns, slots,
+                                                 meta_off, meta_k, meta_sc, s_first, full, empty, lane);
+        return;
+    }
+    const float* slotf = reinterpret_cast<const float*>(slots);
+    unsigned gs = 0;
+    for (;;) {
+        const int b0 = gs % ST;
+        if (!mbar_wait_warp(&full[b0], (gs / ST) & 1u, wait_ns)) {
+            if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+            return;
+        }
+        const int tile = *(volatile int*)&s_first[b0];
+        if (tile < 0) return;
+        const pv::DdTile tt = tiles[tile];
+        const pv::DdJob& J = jobs[tt.job];
+        const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
+        const int da = tt.d0 + 2 * warp;
+        const bool act_a = 2 * warp < J.dms && da <= d_last;
+        const bool act_b = 2 * warp + 1 < J.dms && da + 1 <= d_last;
+        const float dva = pv_trial_value(min(da, d_last), J.start, J.step);
+        const float dvb = pv_trial_value(min(da + 1, d_last), J.start, J.step);
+        const int nst = (J.nchan + CS - 1) / CS;
+        float a0[kPairS], a1[kPairS];
+#pragma unroll
+        for (int j = 0; j < kPairS; ++j) a0[j] = a1[j] = 0.0f;
+        for (int st = 0; st < nst; ++st) {
+            const int b = gs % ST;
+            if (st > 0 && !mbar_wait_warp(&full[b], (gs / ST) & 1u, wait_ns)) {
+                if (lane == 0) atomicExch(status, PV_ERR_TIMEOUT);
+                return;
+            }
+            if (act_a) {
+                const int c_end = min(CS, J.nchan - st * CS);
+                // lane j computes channel j's two row offsets; the warp takes them by shuffle
+                int my_oa = 0, my_dl = 0;
+                if (lane < c_end) {
+                    const float k = meta_k[b * CS + lane];
+                    const int mo = meta_off[b * CS + lane];
+                    my_oa = min(pv_shift(k, dva) - mo, slot - TT - 16);
+                    my_dl = min(pv_shift(k, dvb) - mo, slot - TT - 16) - my_oa;
+                }
+                for (int j = 0; j < c_end; ++j) {
+                    const int oa = __shfl_sync(0xffffffffu, my_oa, j);
+                    const int dl = __shfl_sync(0xffffffffu, my_dl, j);
+                    const float* row = slotf + (size_t)(b * CS + j) * slot + oa + kPairS * lane;
+                    switch (dl) {
+#define PV_PAIR(D) \
+    case D:        \
+        pair_add<D>(row, a0, a1); \
+        break;
+                        PV_PAIR(0) PV_PAIR(1) PV_PAIR(2) PV_PAIR(3) PV_PAIR(4) PV_PAIR(5) PV_PAIR(6)
+                        PV_PAIR(7) PV_PAIR(8) PV_PAIR(9) PV_PAIR(10) PV_PAIR(11) PV_PAIR(12) PV_PAIR(13)
+                        PV_PAIR(14) PV_PAIR(15) PV_PAIR(16) PV_PAIR(17) PV_PAIR(18) PV_PAIR(19) PV_PAIR(20)
+                        PV_PAIR(21) PV_PAIR(22) PV_PAIR(23) PV_PAIR(24) PV_PAIR(25) PV_PAIR(26) PV_PAIR(27)
+                        PV_PAIR(28) PV_PAIR(29) PV_PAIR(30) PV_PAIR(31) PV_PAIR(32)
+#undef PV_PAIR
+                        default:
+                            pair_add_far(row, dl, a0, a1);
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[b]);
+            ++gs;
+        }
+        float* oa_p = J.out + (long long)da * J.out_stride;
+#pragma unroll
+        for (int j = 0; j < kPairS; ++j) {
+            const long long t = tt.t0 + kPairS * lane + j;
+            if (t < J.nout) {
+                if (act_a) oa_p[t] = a0[j];
+                if (act_b) oa_p[J.out_stride + t] = a1[j];
+            }
+        }
+    }
+}
+
 // Largest delay spread s(c, d0+DMS-1) - s(c, d0) over channels and DM tiles,
 // evaluated with the kernel's own float arithmetic on the host.
 int delay_spread(const std::vector<float>& dmshift, int tdms, int dms, float start, float step) {
@@ -835,10 +1005,13 @@ namespace {
 
 struct Variant {
     int R, CS, ST;
+    bool pair;  // FP32 trial-pair consumers (dedisperse_pair_kernel, R = 33)
 };
 // Time tile 32R samples, CS channels per pipeline stage, ST stages in flight.
-constexpr Variant kVariants[] = {{32, 4, 4}, {32, 2, 4}, {16, 4, 4}, {32, 8, 2}};
-constexpr int kNumVariants = 4;
+constexpr Variant kVariants[] = {{32, 4, 4, false}, {32, 2, 4, false}, {16, 4, 4, false},
+                                 {32, 8, 2, false}, {33, 8, 2, true},  {33, 4, 4, true}};
+constexpr int kNumVariants = 6;
+static_assert(kNumVariants == PV_BATCH_VARIANTS, "variant count of the C ABI");
 constexpr size_t kBatchSmemBudget = 220 * 1024;
 
 int store_bytes(int store) { return store == PV_STORE_F32 ? 4 : (store == PV_STORE_F16 ? 2 : 1); }
@@ -872,9 +1045,35 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
+template <int CS, int ST>
+int launch_pair_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem, int grid,
+                  int* counter, const pv::BeamStep* bs, int* status, cudaStream_t s, bool set_attr) {
+    auto kern = dedisperse_pair_kernel<CS, ST>;
+    if (set_attr) {
+        size_t limit = 0;
+        PV_CUDA(pv::allow_max_dynamic_smem(kern, &limit), "cudaFuncSetAttribute(dedisperse_pair)");
+        if (smem > limit) {
+            pv::set_error("dedisperse_pair: %zu bytes of shared memory exceed one CTA's %zu", smem, limit);
+            return PV_ERR_ARG;
+        }
+        return PV_OK;
+    }
+    if (grid < 0) {
+        grid = -grid;
+    } else {
+        PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
+    }
+    kern<<<grid, 9 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status, pv::wait_ns());
+    return pv::check_launch("dedisperse_pair_kernel");
+}
+
 int launch_batch(int variant, int store, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles,
                  int slot, size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
                  cudaStream_t s, bool set_attr) {
+    if (variant == 4 && store == PV_STORE_F32)
+        return launch_pair_t<8, 2>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
+    if (variant == 5 && store == PV_STORE_F32)
+        return launch_pair_t<4, 4>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
     switch (variant * 3 + store) {
 #define PV_VAR(I, R, CS, ST, SS)                                                                 \
     case I * 3 + SS:                                                                            \
@@ -944,6 +1143,7 @@ struct Shape {
 // front of it and 16 more elements for the reduced-precision readers.
 bool build_shape(const Variant& v, int store, const DdBeam* beams, int n,
                  std::vector<std::map<int, int>>& exact, Shape& out) {
+    if (v.pair && store != PV_STORE_F32) return false;
     const int TT = 32 * v.R;
     const size_t fixed = batch_smem(v, 0, store);
     const int E = store_bytes(store);

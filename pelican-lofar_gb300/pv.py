@@ -865,7 +865,7 @@ class Batch:
 
     def tiles(self):
         shape, dms = (C.c_int * 8)(), (C.c_int * len(self.cfgs))()
-        tune, nk = (C.c_float * 4)(), C.c_longlong()
+        tune, nk = (C.c_float * 6)(), C.c_longlong()
         check(load().pv_batch_tiles(self.h, shape, dms, tune, C.byref(nk)))
         keys = ["variant", "time_tile", "chan_per_stage", "stages", "slot", "tiles", "ctas", "smem"]
         d = dict(zip(keys, list(shape)))

@@ -27,6 +27,10 @@
 //   test_ampp udp DIR           AdapterTimeSeriesDataSet on DIR/chunk.bin with DIR/config.xml;
 //                               writes DIR/ts.bin, prints "SHAPE nb ns np nt" and "TIME ts rate"
 #include <pv/ampp.hpp>
+#include <thread>
+#include <mutex>
+#include <chrono>
+#include <atomic>
 
 #include <cstdio>
 #include <cstdlib>
@@ -149,6 +153,12 @@ int chain_mode(const std::string& dir) {
     return 0;
 }
 
+// DedispersionModuleTest (lib/test/src/DedispersionModuleTest.cpp:109-275):
+// nblobs blobs go through the module; prints the lock count of every blob
+// after each dedisperse() call, what the functor saw (the known answer, the
+// events, whether dedisperse() had returned and on which thread it ran),
+// and after waitForJobCompletion() the lock counts and the blobs the unlock
+// callback released, in order.
 int ddmod_mode(const std::string& dir, int nblobs) {
     const ConfigNode dd_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionModule");
     const ConfigNode an_cfg = ConfigNode::fromFile(dir + "/config.xml", "DedispersionAnalyser");
@@ -156,27 +166,61 @@ int ddmod_mode(const std::string& dir, int nblobs) {
     unsigned nt, nsub, nchan;
     double tsamp;
     shape >> nt >> nsub >> nchan >> tsamp;
-    const auto blob = read_file<float>(dir + "/blob.bin");
+    const auto data = read_file<float>(dir + "/blob.bin");
+    std::vector<std::unique_ptr<SpectrumDataSetStokes>> blobs;
+    for (int b = 0; b < nblobs; ++b) {
+        blobs.emplace_back(new SpectrumDataSetStokes);
+        SpectrumDataSetStokes& st = *blobs.back();
+        st.resize(nt, nsub, 1, nchan);
+        std::memcpy(st.data(), data.data() + (size_t)b * st.size(), st.size() * sizeof(float));
+        st.setBlockRate(tsamp);
+    }
+    auto index_of = [&](const DataBlob* d) {
+        for (size_t k = 0; k < blobs.size(); ++k)
+            if (blobs[k].get() == d) return (int)k;
+        return -1;
+    };
     DedispersionModule dd(dd_cfg);
     DedispersionAnalyser an(an_cfg);
-    int unlocked = 0, completed = 0;
-    dd.unlockCallback([&](const std::vector<DataBlob*>& blobs) { unlocked += (int)blobs.size(); });
+    std::vector<int> unlocked;
+    std::mutex mu;
+    int completed = 0;
+    std::atomic<int> started{0}, returned{0};
+    std::atomic<int> async_ok{1}, other_thread{1};
+    const std::thread::id main_id = std::this_thread::get_id();
+    dd.unlockCallback([&](const std::vector<DataBlob*>& freed) {
+        std::lock_guard<std::mutex> l(mu);
+        for (const DataBlob* b : freed) unlocked.push_back(index_of(b));
+    });
     dd.onChainCompletion([&]() { ++completed; });
     dd.connect([&](DedispersionSpectra* s) {
+        if (std::this_thread::get_id() == main_id) other_thread = 0;
+        // the dedisperse() call that filled this buffer returns first
+        const auto t_end = std::chrono::steady_clock::now() + std::chrono::seconds(10);
+        while (returned.load() < started.load() && std::chrono::steady_clock::now() < t_end)
+            std::this_thread::sleep_for(std::chrono::milliseconds(1));
+        if (returned.load() < started.load()) async_ok = 0;
         DedispersionDataAnalysis result;
         const int n = an.analyse(s, &result);
-        std::printf("AMP %g\nEVENTS %d\nFIRST %u\n", s->dmAmplitude(0u, 10.0f), n, s->firstSample());
+        std::printf("AMP %g\nEVENTS %d\nFIRST %u\nINPUTS %zu\n", s->dmAmplitude(0u, 10.0f), n, s->firstSample(),
+                    s->inputDataBlobs().size());
     });
     for (int b = 0; b < nblobs; ++b) {
-        SpectrumDataSetStokes st;
-        st.resize(nt, nsub, 1, nchan);
-        std::memcpy(st.data(), blob.data() + (size_t)b * st.size(), st.size() * sizeof(float));
-        st.setBlockRate(tsamp);
-        WeightedSpectrumDataSet w(&st);
+        WeightedSpectrumDataSet w(blobs[b].get());
+        ++started;
         dd.dedisperse(&w);
+        ++returned;
+        std::printf("LOCKS_ADD%d", b);
+        for (auto& x : blobs) std::printf(" %d", dd.lockNumber(x.get()));
+        std::printf("\n");
     }
     dd.waitForJobCompletion();
-    std::printf("MAXSHIFT %d\nUNLOCKED %d\nCOMPLETED %d\n", dd.maxshift(), unlocked, completed);
+    std::printf("LOCKS_END");
+    for (auto& x : blobs) std::printf(" %d", dd.lockNumber(x.get()));
+    std::printf("\nUNLOCKED");
+    for (int k : unlocked) std::printf(" %d", k);
+    std::printf("\nASYNC %d\nTHREAD %d\n", async_ok.load(), other_thread.load());
+    std::printf("MAXSHIFT %d\nCOMPLETED %d\n", dd.maxshift(), completed);
     return 0;
 }
 
@@ -213,8 +257,10 @@ int ddout_mode(const std::string& dir, int nblobs) {
         std::printf("META %.17g %.17g %u %.17g %.17g %.9g %d\n", s->getLofarTimestamp(), s->getBlockRate(),
                     s->firstSample(), s->dmLow(), s->dmStep(), result.getRMS(), result.eventsFound());
     });
+    std::vector<std::unique_ptr<SpectrumDataSetStokes>> held;  // locked until their buffers are exported
     for (int b = 0; b < nblobs; ++b) {
-        SpectrumDataSetStokes st;
+        held.emplace_back(new SpectrumDataSetStokes);
+        SpectrumDataSetStokes& st = *held.back();
         st.resize(nt, nsub, 1, nchan);
         std::memcpy(st.data(), blob.data() + (size_t)b * st.size(), st.size() * sizeof(float));
         st.setBlockRate(tsamp);
@@ -260,7 +306,8 @@ int pipeline_mode(const std::string& dir, int nchunks) {
         adapter.deserialise(all.data() + (size_t)k * chunk);
         pipeline.run(&ts);
     }
-    std::printf("BUFFERS %u\n", pipeline.buffers());
+    pipeline.waitForJobCompletion();
+    std::printf("BUFFERS %u\nFUSED %d\n", pipeline.buffers(), pipeline.fused() ? 1 : 0);
     return 0;
 }
 
@@ -315,6 +362,7 @@ int ab_mode(const std::string& dir, int nchunks) {
         std::printf("TIME %.17g %.17g\n", stokes.getLofarTimestamp(), stokes.getBlockRate());
         pipeline.run(&stokes);
     }
+    pipeline.waitForJobCompletion();
     std::printf("BUFFERS %u\nGAPS %lld\n", pipeline.buffers(), adapter.gaps());
     return 0;
 }

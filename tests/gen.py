@@ -208,3 +208,25 @@ def lofar_stream(rng, nsub, nsamp, f_sub0, nchan_sub, pulses=(), rfi_channels=()
     out[..., 0] = np.clip(np.rint(vc.real), -32768, 32767)
     out[..., 1] = np.clip(np.rint(vc.imag), -32768, 32767)
     return out
+
+
+def lofar_packets(v16, ts0=1300000000, seq0=1000, spp=16, packet_bytes=8148):
+    """Station voltages [sub][2][n][2] int16 as fixed-size 16-bit LOFAR UDP
+    packets (16-byte header, data [subband][time][pol] complex int16,
+    padding to packet_bytes; lib/LofarUdpHeader.h:25-35): n/spp packets."""
+    nsub, npol, n, _ = v16.shape
+    npk = n // spp
+    data = np.ascontiguousarray(v16[:, :, :npk * spp].reshape(nsub, npol, npk, spp, 2).transpose(2, 0, 3, 1, 4))
+    useful = nsub * spp * npol * 4
+    chunk = np.zeros((npk, packet_bytes), np.uint8)
+    hdr = np.zeros(npk, dtype=[("version", "u1"), ("source", "u1"), ("config", "<u2"), ("station", "<u2"),
+                               ("beamlets", "u1"), ("blocks", "u1"), ("ts", "<u4"), ("seq", "<u4")])
+    hdr["version"] = 3
+    hdr["config"] = 16
+    hdr["beamlets"] = nsub
+    hdr["blocks"] = spp
+    hdr["ts"] = ts0
+    hdr["seq"] = seq0 + spp * np.arange(npk)
+    chunk[:, :16] = hdr.view(np.uint8).reshape(npk, 16)
+    chunk[:, 16:16 + useful] = data.reshape(npk, -1).view(np.uint8)
+    return chunk.reshape(-1)

@@ -118,14 +118,41 @@ def test_shim_dedispersion_module_known_answer(pv, cuda, shim_exe, tmp_path):
     (tmp_path / "shape.txt").write_text("%d %d %d %r\n" % (8192, GEN_NSUB, GEN_NCHAN, GEN_TSAMP))
     foff = -6.0 / (GEN_NSUB * GEN_NCHAN)
     (tmp_path / "config.xml").write_text(DD_XML.format(fch1=repr(GEN_FCH1), foff=repr(foff)))
-    out = _run(shim_exe, "ddmod", tmp_path, 1).split()
-    vals = dict(zip(out[::2], out[1::2]))
-    assert float(vals["AMP"]) == 2048.0
-    assert int(vals["EVENTS"]) > 200  # more events than DM bins (DedispersionAnalyserTest)
-    assert vals["FIRST"] == "0" and vals["UNLOCKED"] == "1" and vals["COMPLETED"] == "1"
+    lines = _run(shim_exe, "ddmod", tmp_path, 1).splitlines()
+    vals = {ln.split()[0]: ln.split()[1:] for ln in lines}
+    assert float(vals["AMP"][0]) == 2048.0
+    assert int(vals["EVENTS"][0]) > 200  # more events than DM bins (DedispersionAnalyserTest)
+    assert vals["FIRST"] == ["0"] and vals["COMPLETED"] == ["1"]
+    # the blob fills the buffer: locked for it and for the next buffer's overlap, so one lock
+    # remains after the export and the unlock callback releases nothing yet
+    assert int(vals["LOCKS_ADD0"][0]) == 2 and vals["LOCKS_END"] == ["1"] and vals["UNLOCKED"] == []
+    assert vals["ASYNC"] == ["1"] and vals["THREAD"] == ["1"]
     o = pv.DedispersionModule(8192, 200, 0.0, 0.1, GEN_FCH1, foff)
     o.add(blob, GEN_TSAMP)
-    assert int(vals["MAXSHIFT"]) == o.params()["maxshift"]
+    assert int(vals["MAXSHIFT"][0]) == o.params()["maxshift"]
+
+
+@pytest.mark.gpu
+def test_shim_dedispersion_module_locks_and_returns_before_the_functors(pv, cuda, shim_exe, tmp_path):
+    """DedispersionModuleTest::test_multipleBlobsPerBuffer (lib/test/src/
+    DedispersionModuleTest.cpp:201-270): two blobs of half a buffer.  The
+    first only buffers (no locks, no functor call); the second fills the
+    buffer, dedisperse() returns before the functor runs (on another
+    thread), the second blob holds more than one lock (it is also in the
+    next buffer's overlap); after the chain the first blob is free and was
+    passed to the unlock callback, the second keeps one lock."""
+    blobs = generator_pulse(4096, 10.0, nblocks=2)
+    np.concatenate(blobs).tofile(tmp_path / "blob.bin")
+    (tmp_path / "shape.txt").write_text("%d %d %d %r\n" % (4096, GEN_NSUB, GEN_NCHAN, GEN_TSAMP))
+    foff = -6.0 / (GEN_NSUB * GEN_NCHAN)
+    (tmp_path / "config.xml").write_text(DD_XML.format(fch1=repr(GEN_FCH1), foff=repr(foff)))
+    lines = _run(shim_exe, "ddmod", tmp_path, 2).splitlines()
+    vals = {ln.split()[0]: ln.split()[1:] for ln in lines}
+    assert vals["LOCKS_ADD0"] == ["0", "0"]
+    assert int(vals["LOCKS_ADD1"][1]) > 1
+    assert float(vals["AMP"][0]) == 2048.0 and vals["INPUTS"] == ["2"] and vals["COMPLETED"] == ["1"]
+    assert vals["LOCKS_END"] == ["0", "1"] and vals["UNLOCKED"] == ["0"]
+    assert vals["ASYNC"] == ["1"] and vals["THREAD"] == ["1"]
 
 
 UDP_XML = """<configuration>
@@ -469,8 +496,9 @@ PIPELINE_XML = """<configuration>
     <nRawPolarisations value="2"/>
   </AdapterTimeSeriesDataSet>
   <DedispersionPipeline>
-    <history value="10"/>
+    <history value="{history}"/>
     <events min="{emin}" max="{emax}"/>
+    <fused value="{fused}"/>
   </DedispersionPipeline>
   <PPFChanneliser>
     <outputChannelsPerSubband value="{nchan}"/>
@@ -480,11 +508,11 @@ PIPELINE_XML = """<configuration>
   <RFI_Clipper active="true" channelRejectionRMS="5.0" spectrumRejectionRMS="4.0">
     <BandPassData file="band.bp"/>
     <Band matching="true"/>
-    <History maximum="1000"/>
+    <History maximum="{rfi_history}"/>
     <zeroDMing active="true"/>
   </RFI_Clipper>
   <DedispersionModule>
-    <timeBinsPerBufferPow2 value="12"/>
+    <timeBinsPerBufferPow2 value="{pow2}"/>
     <dedispersionSamples value="{tdms}"/>
     <dedispersionStepSize value="{dm_step}"/>
     <dedispersionMinimum value="0"/>
@@ -532,8 +560,10 @@ def test_shim_pipeline_from_packets_to_event_file(pv, oracle, cuda, shim_exe, tm
                                                    float(fb0.mean()), float(fb0.std())))
     (tmp_path / "config.xml").write_text(PIPELINE_XML.format(
         npk=npk, nchan=nchan, nsub=nsub, emin=emin, emax=emax, tdms=tdms, dm_step=dm_step, fch1=repr(fch1),
-        foff=repr(foff), thr=thr, path=str(tmp_path / "ev")))
+        foff=repr(foff), thr=thr, path=str(tmp_path / "ev"), history=10, fused="true", rfi_history=1000,
+        pow2=12))
     out = _run(shim_exe, "pipeline", tmp_path, nchunks)
+    assert "FUSED 1" in out
     nbuf = int(out.split("BUFFERS")[1].split()[0])
     # the same chain through the binding
     rfi = pv.RFI((tmp_path / "band.bp").read_text(), cr=5.0, sr=4.0, history=1000, zero_dming=True)
@@ -556,3 +586,72 @@ def test_shim_pipeline_from_packets_to_event_file(pv, oracle, cuda, shim_exe, tm
     assert files[0].read_text() == pv.EVENTS_TEXT_HEADER + text
     if emin > 1000:
         assert text == ""  # no buffer has a million events
+
+
+@pytest.mark.gpu
+def test_shim_pipeline_plain_single_beam_full_size(pv, oracle, cuda, shim_exe, tmp_path):
+    """The plain single-beam workload through the reference's pipeline
+    structure (DedispersionPipeline has no integrator): 32 subbands from
+    140 MHz in 16-bit station packets, 65536 samples per subband per chunk,
+    16 channels per subband (81.92 us), RFI_Clipper at 5 sigma with a
+    10000-spectrum history, 512 trials over DM 0-100 in buffers of 2^15
+    spectra, events at 6 sigma; the DM 56.8 pulse 0.5 s into the stream.
+    The fused device chain and the module chain write the same event file,
+    which equals the chain composed through the Python binding, and the
+    strongest event is the pulse."""
+    import torch
+    from gen import lofar_band, lofar_packets, lofar_stream
+    nsub, nchan, per_chunk, nchunks, tdms, thr = 32, 16, 65536, 9, 512, 6.0
+    dm_step = np.float32(100.0 / 511)
+    fch1, foff = lofar_band(140.0, nsub, nchan)
+    rng = np.random.default_rng(56)
+    v = lofar_stream(rng, nsub, per_chunk * nchunks, 140.0, nchan, pulses=[(56.8, 0.5, 1e-3, 0.52)])
+    npk = per_chunk // 16
+    chunks = [lofar_packets(np.ascontiguousarray(v[:, :, k * per_chunk:(k + 1) * per_chunk]), seq0=1000 + k * per_chunk)
+              for k in range(nchunks)]
+    np.concatenate(chunks).tofile(tmp_path / "chunks.bin")
+    ad = pv.UdpAdapter(True, 16, npk, 16, nchan, nsub, 2)
+    ppf = pv.PPF(nchan, 8, window="kaiser")
+    st = []
+    for c in chunks:
+        ts = ad.deserialise(torch.from_numpy(c).to(cuda))
+        st.append(pv.stokes(ppf.run(ts.reshape(nsub, 2, -1)), 1))
+    fb0 = st[0].cpu().numpy()
+    (tmp_path / "band.bp").write_text(make_bp_text(nsub * nchan, fch1, foff, float(fb0.mean()),
+                                                   float(fb0.std())))
+    texts = {}
+    for fused in ("true", "false"):
+        d = tmp_path / fused
+        d.mkdir()
+        (d / "band.bp").write_text((tmp_path / "band.bp").read_text())
+        os.symlink(tmp_path / "chunks.bin", d / "chunks.bin")
+        (d / "config.xml").write_text(PIPELINE_XML.format(
+            npk=npk, nchan=nchan, nsub=nsub, emin=1, emax=0, tdms=tdms, dm_step=repr(float(dm_step)),
+            fch1=repr(fch1), foff=repr(foff), thr=thr, path=str(d / "ev"), history=32, fused=fused,
+            rfi_history=10000, pow2=15))
+        out = _run(shim_exe, "pipeline", d, nchunks)
+        assert ("FUSED 1" in out) == (fused == "true")
+        assert int(out.split("BUFFERS")[1].split()[0]) == 1
+        files = list(d.glob("ev_D*.dat"))
+        assert len(files) == 1
+        texts[fused] = files[0].read_text()
+    assert texts["true"] == texts["false"]
+    # the same chain through the binding
+    rfi = pv.RFI((tmp_path / "band.bp").read_text(), cr=5.0, sr=4.0, history=10000, zero_dming=True)
+    dd = pv.DedispersionModule(1 << 15, tdms, 0.0, float(dm_step), fch1, foff)
+    tsamp = ad.block_rate * nchan
+    rms = float(np.sqrt(np.float32(nchan) * np.float32(nsub)))
+    t_start = 1300000000 + 1000 / 195313
+    text, dump, best = "", 0, None
+    for x in st:
+        rfi.run(x)
+        for buf, first in dd.add(x.cpu().numpy(), tsamp):
+            ev, n = pv.analyse(torch.from_numpy(buf).to(cuda), thr, rms, 4)
+            dump += 1
+            text += pv.events_text(ev, t_start, tsamp, first, 0.0, float(dm_step), np.float32(rms), dump)
+            snr = ev["value"][1:] / (rms * np.sqrt(ev["bin_factor"][1:]))
+            k = int(np.argmax(snr)) + 1
+            best = (float(snr[k - 1]), int(ev["dm"][k]), first + int(ev["t"][k]))
+    assert texts["true"] == pv.EVENTS_TEXT_HEADER + text
+    snr, d_best, t_best = best
+    assert abs(d_best - 56.8 / float(dm_step)) <= 2 and abs(t_best - 0.5 / tsamp) <= 32 and snr >= 10, best

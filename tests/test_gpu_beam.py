@@ -96,6 +96,8 @@ def test_beam_host_input_equals_device_input(pv, oracle, cuda):
         ea, na, fa = a.events()
         eb, nb, fb = b.events()
         assert na == nb and fa == fb and np.array_equal(ea, eb)
+        if fa < 0:
+            continue  # no window yet: the output buffers hold nothing
         oa = pv.device_array(a.buffers()[2], (kw["tdms"], 256)).cpu().numpy()
         ob = pv.device_array(b.buffers()[2], (kw["tdms"], 256)).cpu().numpy()
         assert np.array_equal(oa, ob)
