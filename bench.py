@@ -502,7 +502,8 @@ def run_batch(args, cfgs, workload):
     torch.cuda.empty_cache()
 
     # ---------------- batched engine ----------------
-    batch = pv.Batch([beam_cfg(c) for c in cfgs], tune=True, graph=True, timing=True,
+    batch = pv.Batch([beam_cfg(c) for c in cfgs], tune=args.variant is None, graph=True, timing=True,
+                     variant=args.variant or 0,
                      pipelined=not args.unpipelined, store=args.store)
     bhosts = []  # the batch's staging, allocated after the batch (see the plain arm's)
     for i, c in enumerate(cfgs):
@@ -1203,6 +1204,8 @@ def main():
     ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
                     help="batch64, serve128: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="dedispersion tile variant (0-5) instead of the autotuner's choice (profiling)")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
     args = ap.parse_args()

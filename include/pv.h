@@ -216,7 +216,11 @@ int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp, float thr
  * cudaFree or allocating library routine.
  *
  * The first call on each device looks up the array's device address with
- * that device current; make that first call before any stream capture.
+ * that device current; make that first call before any stream capture.  The
+ * address is kept for the life of the process: the entry point assumes the
+ * device's primary context (the one the CUDA runtime uses) and no
+ * cudaDeviceReset between calls, after which the array would live at
+ * another address.
  * Every call on a device shares the one array, so calls that overlap on the
  * GPU (other streams, other host threads) race and corrupt each other's
  * results; serialise them.  Nothing in the array needs clearing between
@@ -479,12 +483,104 @@ int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tu
 int pv_batch_stage_ms(pv_batch* batch, float* h_ms5);
 int pv_batch_buffers(const pv_batch* batch, int beam, float** d_filterbank, float** d_dedispersed,
                      float** d_ring);
+/* Starts a new stream in slot `beam` of the batch: the slot's ring (prefilled
+ * silence again when configured so), PPF history, clipper state and window
+ * go back to those of a new beam of the same configuration, so a serving
+ * loop gives a drained stream's slot, and its device memory, to the next
+ * stream of that configuration without rebuilding the batch or its graph.
+ * Waits for the issued steps; the slot's next step is the new stream's
+ * first chunk.  (A pelican pipeline gets the same by creating its modules
+ * again.) */
+int pv_batch_reset_beam(pv_batch* batch, int beam, void* stream);
 /* 1 if step `step` (one of the steps issued) has finished on the device, 0 if not. */
 int pv_batch_step_done(const pv_batch* batch, long long step);
 /* Device bytes one beam of this configuration takes in a batch created with
  * `flags` (ring, input buffers, filterbank, window, events, scratch): the
  * admission cost of a serving loop under an HBM budget. */
 long long pv_batch_footprint(const pv_beam_config* config, int flags);
+
+/* ---- Serving loop ---------------------------------------------------------
+ * No counterpart in the reference, whose pipelines run one beam per process
+ * (pipelines/udpstream/src/DedispersionPipeline.cpp:96-174).  pv_serve runs
+ * streams of chunks from many beams through the batched engine in real time:
+ * a chunk is queued as sub-chunks of one step (the configuration's chunk)
+ * each; streams are admitted under an HBM budget (pv_batch_footprint); a
+ * stream that arrives takes at once the slot of a drained stream of the same
+ * configuration in a running cohort (pv_batch_reset_beam), the others are
+ * admitted first fit every admit_every seconds as a new cohort (one batch on
+ * its own CUDA stream: the steps of all cohorts overlap); every step of a
+ * cohort takes one sub-chunk of each beam with one queued (continuous
+ * batching), at most max_inflight steps in flight; a cohort whose streams
+ * have drained is released, its memory returned, once a waiting stream needs
+ * the memory or after it has lingered idle `linger` seconds.  A chunk's latency runs from its arrival to the end of
+ * the step that processed its last sub-chunk.  PV_SERVE_FIFO1 is the plain
+ * per-chunk path: one pv_beam per stream, the oldest queued sub-chunk alone,
+ * its events read back before the next. */
+#define PV_SERVE_BATCH 0
+#define PV_SERVE_FIFO1 1
+typedef struct {
+    double budget_bytes;  /* device memory the admitted beams may take */
+    int policy;           /* PV_SERVE_BATCH or PV_SERVE_FIFO1 */
+    int batch_flags;      /* pv_batch_create flags of every cohort (PV_BATCH_GRAPH, PIPELINED, STORE_*) */
+    int max_inflight;     /* steps in flight per cohort, 1 or 2 (0: 2) */
+    double admit_every;   /* seconds between admission rounds of new cohorts */
+    double horizon;       /* stop after this many seconds (0: when every chunk is served) */
+    int reuse_slots;      /* give a drained stream's slot to a waiting stream of the same configuration */
+    double linger;        /* seconds a drained cohort is kept for a stream of its configuration when no
+                             waiting stream needs its memory */
+} pv_serve_config;
+typedef struct {
+    int nchunks;               /* chunks of the stream */
+    const double* arrivals;    /* their arrival times, seconds from the start, ascending */
+    const int* sizes;          /* their sizes in spectra, multiples of the configuration's chunk */
+    const void* h_voltages;    /* page-locked int16 voltages of one sub-chunk (pv_beam_input_bytes),
+                                  the stream's receive buffer, copied in for every sub-chunk */
+    double units_per_spectrum; /* DM trials x channels: the work one spectrum brings */
+} pv_serve_stream;
+typedef struct {
+    long long chunks, chunks_done, cohorts, slot_reuses, steps;
+    int max_concurrent_beams;
+    double wall_s, units, throughput; /* DM-trial*chan*samples per second of wall time */
+    double latency_p50, latency_p99, latency_max;             /* seconds from arrival to processed */
+    double latency_admitted_p50, latency_admitted_p99;        /* chunks arriving after admission */
+    double latency_over_duration_p50, latency_over_duration_p99; /* latency / the chunk's duration */
+    double within_real_time;                                  /* share of chunks with latency < duration */
+    double admission_wait_p50, admission_wait_p99;            /* first arrival to admission */
+    double peak_footprint_bytes;
+} pv_serve_stats;
+/* Hooks that replace the GPU engine and the wall clock (tests drive the loop
+ * on the CPU with them).  open returns a cohort handle for n streams (NULL:
+ * failure); step returns a step id (< 0: failure); done: 1 once that step
+ * has finished; reset_slot: PV_OK once slot `slot` serves stream `stream`. */
+typedef struct {
+    void* ctx;
+    long long (*footprint)(void* ctx, const pv_beam_config* config);
+    void* (*open)(void* ctx, const pv_beam_config* configs, const int* streams, int n);
+    long long (*step)(void* ctx, void* cohort, const unsigned char* active, int n);
+    int (*done)(void* ctx, void* cohort, long long step);
+    int (*reset_slot)(void* ctx, void* cohort, int slot, int stream);
+    void (*close)(void* ctx, void* cohort);
+    double (*clock)(void* ctx);           /* seconds (NULL: the wall clock) */
+    void (*sleep)(void* ctx, double seconds);
+    /* events of a finished step's slot: the total count, *first the window's first
+       sample (-1: none this step), up to cap events copied to out (NULL: no output) */
+    long long (*events)(void* ctx, void* cohort, long long step, int slot, pv_event* out, long long cap,
+                        long long* first);
+} pv_serve_engine;
+/* Where the events of every dedispersed window go (the pipeline's
+ * "DedispersionDataAnalysis" stream): called from pv_serve's thread for each
+ * window of each stream, in order, with the window's first sample in the
+ * stream, up to PV_BATCH_HOST_EVENTS events and their total (dummy first). */
+typedef struct {
+    void* ctx;
+    void (*events)(void* ctx, int stream, long long first_sample, const pv_event* events, long long n,
+                   long long total);
+} pv_serve_output;
+/* Serves the streams (configs[i] is stream i's beam) until every chunk is
+ * processed or the horizon passes, then fills *stats.  engine NULL: the
+ * library's batched engine (or pv_beam per stream for PV_SERVE_FIFO1). */
+int pv_serve(const pv_serve_config* config, const pv_beam_config* configs, const pv_serve_stream* streams,
+             int nstreams, const pv_serve_engine* engine, const pv_serve_output* output, pv_serve_stats* stats);
 
 /* ---- LOFAR UDP ingest (AdapterTimeSeriesDataSet) -------------------------
  * Replaces AdapterTimeSeriesDataSet::deserialise/_checkData/_readData

@@ -156,14 +156,18 @@ __global__ void analyse_total(const int* __restrict__ counts, const long long* _
     *total = npairs > 0 ? 1 + offsets[npairs - 1] + counts[npairs - 1] : 1;
 }
 
-long long scan_workspace(long long n) {
-    long long total = 0;
-    while (n > 1) {
-        const long long nb = pv::ceil_div<long long>(n, kScanBlock);
-        total += 2 * nb;  // block sums + their scan
-        n = nb;
-    }
-    return total;
+// Block sums and their scans of every level of the scan of n values.
+constexpr long long scan_workspace(long long n) {
+    return n > 1 ? 2 * ((n + kScanBlock - 1) / kScanBlock) + scan_workspace((n + kScanBlock - 1) / kScanBlock)
+                 : 0;
+}
+
+// Scratch bytes of the analyser for npairs (trial, block) pairs: per-pair
+// counts and offsets, the scan workspace and two totals, rounded to 256.
+constexpr size_t scratch_bytes_for(long long npairs) {
+    return (((size_t)(npairs > 1 ? npairs : 1) * (sizeof(int) + sizeof(long long)) +
+             (size_t)(scan_workspace(npairs > 1 ? npairs : 1) + 2) * sizeof(long long) + 256) + 255) /
+           256 * 256;
 }
 
 // Exclusive scan of in[0..n) into out; ws holds scan_workspace(n) values.
@@ -212,11 +216,8 @@ namespace pv {
 
 // Scratch bytes the analyser needs for tdms x nsamp at 2^bin_pow2 blocks.
 size_t analyse_scratch_bytes(int tdms, int nsamp, int bin_pow2) {
-    const long long npairs = (long long)tdms * (nsamp >> bin_pow2);
-    const long long n = std::max<long long>(npairs, 1);
-    const size_t bytes = (size_t)n * sizeof(int) + (size_t)n * sizeof(long long) +
-                         (size_t)(scan_workspace(n) + 2) * sizeof(long long) + 256;
-    return (bytes + 255) / 256 * 256;  // keeps anything placed after it aligned
+    // rounded to 256 bytes: keeps anything placed after it aligned
+    return scratch_bytes_for((long long)tdms * (nsamp >> bin_pow2));
 }
 
 // Analyser with caller-provided scratch (analyse_scratch_bytes bytes);
@@ -294,16 +295,12 @@ extern "C" int pv_analyse(const float* d_data, long long ld, int tdms, int nsamp
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr long long noalloc_scan_workspace(long long n) {
-    return n > 1 ? 2 * ((n + kScanBlock - 1) / kScanBlock) +
-                       noalloc_scan_workspace((n + kScanBlock - 1) / kScanBlock)
-                 : 0;
-}
 constexpr size_t kNoAllocPairs = PV_ANALYSE_NOALLOC_MAX_PAIRS;
-constexpr size_t kNoAllocScratch =
-    ((kNoAllocPairs * (sizeof(int) + sizeof(long long)) +
-      (size_t)(noalloc_scan_workspace((long long)kNoAllocPairs) + 2) * sizeof(long long) + 256 +
-      255) / 256) * 256;
+// the same formula as pv_analyse's scratch at the largest pair count: a call
+// within the pair limit always fits
+constexpr size_t kNoAllocScratch = scratch_bytes_for((long long)kNoAllocPairs);
+static_assert(scratch_bytes_for((long long)kNoAllocPairs) >= scratch_bytes_for((long long)kNoAllocPairs - 1),
+              "scratch grows with the pair count");
 // Scratch (counts, offsets, scan workspace) followed by the event total.
 // Every GPU that loads the library keeps this array until the process exits.
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch + 256];
@@ -351,8 +348,7 @@ extern "C" int pv_analyse_noalloc(const float* d_data, long long ld, int tdms, i
         return PV_ERR_ARG;
     }
     const long long pairs = (long long)tdms * (nsamp >> bin_pow2);
-    const size_t need = pv::analyse_scratch_bytes(tdms, nsamp, bin_pow2);
-    if (pairs > (long long)kNoAllocPairs || need > kNoAllocScratch) {
+    if (pairs > (long long)kNoAllocPairs) {
         pv::set_error("pv_analyse_noalloc: %d trials x %d blocks of 2^%d samples = %lld pairs "
                       "exceeds the fixed scratch limit of %lld pairs; use pv_analyse",
                       tdms, nsamp >> bin_pow2, bin_pow2, pairs, (long long)kNoAllocPairs);

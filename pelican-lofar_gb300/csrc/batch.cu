@@ -632,6 +632,40 @@ int launch_step(pv_batch* b, cudaStream_t s) {
 
 }  // namespace
 
+extern "C" int pv_batch_reset_beam(pv_batch* b, int beam, void* stream) {
+    if (!b || beam < 0 || beam >= b->n) return PV_ERR_ARG;
+    cudaStream_t s = pv::as_stream(stream);
+    // every issued step has finished with this beam's buffers
+    for (int i = 0; i < 2; ++i)
+        if (b->done_valid[i]) PV_CUDA(cudaEventSynchronize(b->done[i]), "wait for the issued steps");
+    pv_beam* x = b->beams[beam];
+    const int elem = b->store == PV_STORE_F32 ? 4 : (b->store == PV_STORE_F16 ? 2 : 1);
+    PV_CUDA(cudaMemsetAsync(x->d_ring, elem == 1 ? 0x80 : 0, (size_t)elem * x->nbins * (size_t)x->row_stride, s),
+            "clear ring");
+    const size_t hist = sizeof(float2) * (size_t)x->cfg.nsub * 2 * 7 * x->cfg.nchan_sub;
+    for (int h = 0; h < 2; ++h) PV_CUDA(cudaMemsetAsync(b->d_hist[2 * beam + h], 0, hist, s), "clear PPF history");
+    PV_CUDA(cudaMemsetAsync(x->d_out, 0, sizeof(float) * (size_t)x->cfg.tdms * x->cfg.chunk, s), "clear window");
+    PV_TRY(pv::rfi_reset(x->rfi, s));
+    if (b->store == PV_STORE_U8 && b->d_scale[beam]) {
+        std::vector<float> so(2 * (size_t)x->nbins + 1, 0.0f);
+        if (x->cfg.rfi_active && x->cfg.zero_dming) std::fill(so.begin(), so.begin() + x->nbins, 6.0f / 127.0f);
+        PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+        PV_CUDA(cudaMemcpy(b->d_scale[beam], so.data(), sizeof(float) * so.size(), cudaMemcpyHostToDevice),
+                "reset ring calibration");
+    }
+    pv::BeamStep& m = b->mirror[beam];
+    const long long base = m.base;
+    const int lag = m.lag;
+    m = pv::BeamStep{};
+    m.base = base;
+    m.written = base;
+    m.lag = lag;
+    b->processed[beam] = 0;
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+    PV_CUDA(cudaMemcpy(b->d_bs + beam, &m, sizeof(m), cudaMemcpyHostToDevice), "reset beam progress");
+    return PV_OK;
+}
+
 extern "C" int pv_batch_run(pv_batch* b, const unsigned char* h_active, void* stream) {
     if (!b) return PV_ERR_ARG;
     PV_TRY(set_mask(b, h_active));

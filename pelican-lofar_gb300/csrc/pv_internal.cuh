@@ -57,6 +57,7 @@ long long ppf_state_bytes(const pv_ppf* h, int nsub, int npol);
 int ppf_state_io(pv_ppf* h, int nsub, int npol, void* h_buf, bool save, cudaStream_t s);
 long long rfi_state_bytes(const pv_rfi* h, int nbins);
 int rfi_state_io(pv_rfi* h, int nbins, void* h_buf, bool save, cudaStream_t s);
+int rfi_reset(pv_rfi* h, cudaStream_t s);
 // coefficient [T][N] and twiddle [N/2] tables of a PPF handle
 int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle, int* nchan,
                int* ntaps);

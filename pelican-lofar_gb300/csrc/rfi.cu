@@ -917,6 +917,24 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     return rfi_launch(threads, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
+// Back to the state of a clipper that has seen no spectrum (the running
+// averages, histories and last good spectrum of setup()), asynchronously.
+int pv::rfi_reset(pv_rfi* h, cudaStream_t s) {
+    if (!h || !h->dev.state) return PV_OK;
+    RfiState st{};
+    st.remaining_zeros = h->nbins;
+    st.params0 = h->bp.params[0];
+    st.bp_mean = Bandpass::at(h->bp.mean, h->bp.current.key());
+    st.bp_rms = Bandpass::at(h->bp.rms, h->bp.current.key());
+    // st is a stack value: copy synchronously with respect to the host
+    PV_CUDA(cudaStreamSynchronize(s), "synchronise");
+    PV_CUDA(cudaMemcpy(h->dev.state, &st, sizeof(st), cudaMemcpyHostToDevice), "reset RFI state");
+    PV_CUDA(cudaMemsetAsync(h->dev.last_good, 0, sizeof(float) * h->nbins, s), "clear last good spectrum");
+    PV_CUDA(cudaMemsetAsync(h->dev.mean_buf, 0, sizeof(double) * h->history, s), "clear history");
+    PV_CUDA(cudaMemsetAsync(h->dev.rms_buf, 0, sizeof(double) * h->history, s), "clear history");
+    return PV_OK;
+}
+
 long long pv::rfi_state_bytes(const pv_rfi* h, int nbins) {
     return (long long)sizeof(RfiState) + 2LL * h->history * (long long)sizeof(double) +
            (long long)nbins * (long long)sizeof(float);

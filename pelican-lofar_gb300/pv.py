@@ -109,6 +109,8 @@ def _declare(L):
         "pv_batch_buffers": (i, [vp, i, P(vp), P(vp), P(vp)]),
         "pv_batch_step_done": (i, [vp, ll]),
         "pv_batch_footprint": (ll, [vp, i]),
+        "pv_batch_reset_beam": (i, [vp, i, vp]),
+        "pv_serve": (i, [vp, vp, vp, i, vp, vp, vp]),
         "pv_udp_check": (i, [vp, ll, P(ll), P(i)]),
         "pv_udp_unpack": (i, [vp, vp, ll, vp, i, vp]),
         "pv_udp_time": (i, [vp, vp, P(d), P(d)]),
@@ -971,3 +973,125 @@ class DedispersionModule:
         if getattr(self, "h", None) and self.h.value and _lib is not None:
             _lib.pv_ddmod_destroy(self.h)
             self.h = C.c_void_p()
+
+
+# ---------------------------------------------------------------------------
+# serving loop (pv_serve)
+# ---------------------------------------------------------------------------
+
+SERVE_BATCH, SERVE_FIFO1 = 0, 1
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_double), ("policy", C.c_int), ("batch_flags", C.c_int),
+                ("max_inflight", C.c_int), ("admit_every", C.c_double), ("horizon", C.c_double),
+                ("reuse_slots", C.c_int), ("linger", C.c_double)]
+
+
+class ServeStream(C.Structure):
+    _fields_ = [("nchunks", C.c_int), ("arrivals", C.POINTER(C.c_double)), ("sizes", C.POINTER(C.c_int)),
+                ("h_voltages", C.c_void_p), ("units_per_spectrum", C.c_double)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("chunks", "chunks_done", "cohorts", "slot_reuses", "steps")] + \
+               [("max_concurrent_beams", C.c_int)] + \
+               [(n, C.c_double) for n in ("wall_s", "units", "throughput", "latency_p50", "latency_p99",
+                                          "latency_max", "latency_admitted_p50", "latency_admitted_p99",
+                                          "latency_over_duration_p50", "latency_over_duration_p99",
+                                          "within_real_time", "admission_wait_p50", "admission_wait_p99",
+                                          "peak_footprint_bytes")]
+
+
+_FOOT = C.CFUNCTYPE(C.c_longlong, C.c_void_p, C.c_void_p)
+_OPEN = C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int)
+_STEP = C.CFUNCTYPE(C.c_longlong, C.c_void_p, C.c_void_p, C.POINTER(C.c_ubyte), C.c_int)
+_DONE = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_longlong)
+_RESET = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int)
+_CLOSE = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)
+_CLOCK = C.CFUNCTYPE(C.c_double, C.c_void_p)
+_SLEEP = C.CFUNCTYPE(None, C.c_void_p, C.c_double)
+_EVENTS = C.CFUNCTYPE(C.c_longlong, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p, C.c_longlong,
+                      C.POINTER(C.c_longlong))
+_OUTPUT = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_longlong, C.c_void_p, C.c_longlong, C.c_longlong)
+
+
+class ServeEngine(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("footprint", _FOOT), ("open", _OPEN), ("step", _STEP), ("done", _DONE),
+                ("reset_slot", _RESET), ("close", _CLOSE), ("clock", _CLOCK), ("sleep", _SLEEP),
+                ("events", _EVENTS)]
+
+
+class ServeOutput(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("events", _OUTPUT)]
+
+
+def _engine_hooks(eng):
+    """C hooks over a Python engine with footprint(cfg), open(cfgs, ids) ->
+    cohort, step(cohort, active) -> id, done(cohort, id), reset_slot(cohort,
+    slot, stream), close(cohort), clock() and sleep(s); cohorts are kept by
+    handle number."""
+    cohorts, nxt = {}, [1]
+
+    def foot(ctx, cfg):
+        return int(eng.footprint(C.cast(cfg, C.POINTER(BeamConfig)).contents))
+
+    def open_(ctx, cfgs, ids, n):
+        arr = C.cast(cfgs, C.POINTER(BeamConfig))
+        c = eng.open([arr[k] for k in range(n)], [ids[k] for k in range(n)])
+        if c is None:
+            return None
+        h = nxt[0]
+        nxt[0] += 1
+        cohorts[h] = c
+        return h
+
+    def step(ctx, h, active, n):
+        return int(eng.step(cohorts[h], np.ctypeslib.as_array(active, (n,)).copy()))
+
+    def done(ctx, h, i):
+        return 1 if eng.done(cohorts[h], i) else 0
+
+    def reset(ctx, h, slot, stream):
+        return int(eng.reset_slot(cohorts[h], slot, stream))
+
+    def close(ctx, h):
+        eng.close(cohorts.pop(h))
+
+    hooks = ServeEngine(None, _FOOT(foot), _OPEN(open_), _STEP(step), _DONE(done), _RESET(reset), _CLOSE(close),
+                        _CLOCK(lambda ctx: float(eng.clock())), _SLEEP(lambda ctx, dt: eng.sleep(dt)), _EVENTS(0))
+    return hooks
+
+
+def serve(configs, streams, budget_bytes, policy="batch", batch_flags=None, max_inflight=2, admit_every=0.5,
+          horizon=0.0, reuse_slots=True, linger=2.0, engine=None, on_events=None):
+    """pv_serve: configs[i] (BeamConfig) is stream i's beam; streams[i] a dict
+    with arrivals (s), sizes (spectra), voltages (a HostBuffer with one
+    sub-chunk, or None with an engine) and units_per_spectrum.  engine (for
+    tests) replaces the GPU and the clock.  Returns the statistics as a dict."""
+    n = len(configs)
+    cfg_arr = (BeamConfig * n)(*configs)
+    keep = []
+    st_arr = (ServeStream * n)()
+    for i, s in enumerate(streams):
+        a = np.ascontiguousarray(s["arrivals"], np.float64)
+        z = np.ascontiguousarray(s["sizes"], np.int32)
+        keep += [a, z]
+        v = s.get("voltages")
+        st_arr[i] = ServeStream(len(a), a.ctypes.data_as(C.POINTER(C.c_double)), z.ctypes.data_as(C.POINTER(C.c_int)),
+                                C.c_void_p(v.ptr) if v is not None else None, float(s["units_per_spectrum"]))
+    if batch_flags is None:
+        batch_flags = BATCH_GRAPH | BATCH_PIPELINED
+    sc = ServeConfig(float(budget_bytes), SERVE_BATCH if policy == "batch" else SERVE_FIFO1, int(batch_flags),
+                     int(max_inflight), float(admit_every), float(horizon), int(bool(reuse_slots)), float(linger))
+    out = ServeStats()
+    hooks = _engine_hooks(engine) if engine is not None else None
+    output = None
+    if on_events is not None:  # on_events(stream, first_sample, events array, total)
+        def _out(ctx, stream, first, ev, nev, total):
+            arr = np.ctypeslib.as_array(C.cast(ev, C.POINTER(C.c_int32)), (int(nev) * 4,)).view(EVENT_DTYPE).copy()
+            on_events(int(stream), int(first), arr, int(total))
+        output = ServeOutput(None, _OUTPUT(_out))
+    check(load().pv_serve(C.byref(sc), cfg_arr, st_arr, n, C.byref(hooks) if hooks is not None else None,
+                          C.byref(output) if output is not None else None, C.byref(out)))
+    return {f: getattr(out, f) for f, _ in ServeStats._fields_}

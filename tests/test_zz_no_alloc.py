@@ -49,6 +49,31 @@ def test_no_alloc_matches_pv_analyse_on_two_calls(pv, cuda, tdms, nsamp, bin_pow
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("tdms,nsamp,bin_pow2,cap", [(200, 4096, 6, 5), (8, 40, 6, 16), (0, 256, 6, 4),
+                                                     (37, 64 * 20 + 13, 3, 1)])
+def test_no_alloc_matches_pv_analyse_when_truncated_or_empty(pv, cuda, tdms, nsamp, bin_pow2, cap):
+    """Fewer event slots than events (the total still counts them all), and
+    calls with no (trial, block) pair (no trials, or fewer samples than one
+    2^bin_pow2 block: only the dummy event)."""
+    import torch
+    L = pv.load()
+    for name in ("pv_analyse", "pv_analyse_noalloc"):
+        getattr(L, name).restype = C.c_int
+        getattr(L, name).argtypes = ARGS
+    rng = np.random.default_rng(tdms + nsamp + cap)
+    data = (rng.standard_normal((tdms, nsamp)) * 2.0).astype(np.float32)
+    d = torch.from_numpy(data).to(cuda)
+    want, n_want = _run(pv, L.pv_analyse, d, 2.5, 1.0, bin_pow2, cap)
+    if tdms == 0 or nsamp < (1 << bin_pow2):
+        assert n_want == 1
+    else:
+        assert n_want > cap
+    for _ in range(2):
+        got, n_got = _run(pv, L.pv_analyse_noalloc, d, 2.5, 1.0, bin_pow2, cap)
+        assert n_got == n_want
+        assert np.array_equal(got, want)
+
+
 def test_no_alloc_rejects_calls_beyond_its_limit(pv, cuda):
     import torch
     L = pv.load()
