@@ -261,8 +261,11 @@ def device_voltages(cfg, dev, seed):
                 burst = torch.complex(torch.randn(L, generator=gp, device=dev),
                                       torch.randn(L, generator=gp, device=dev)) * envf
                 disp = torch.fft.ifft(torch.fft.fft(burst) * rot)
-                v[s, p, :, 0].index_add_(0, idx, disp.real.float())
-                v[s, p, :, 1].index_add_(0, idx, disp.imag.float())
+                # pieces of at most n samples have distinct wrapped indices: the sums are
+                # deterministic (index_add_ adds repeated indices atomically, in any order)
+                for q in range(0, L, n):
+                    v[s, p, :, 0].index_add_(0, idx[q:q + n], disp.real[q:q + n].float())
+                    v[s, p, :, 1].index_add_(0, idx[q:q + n], disp.imag[q:q + n].float())
     return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
 
 
@@ -608,11 +611,19 @@ def run_batch(args, cfgs, workload):
     precision = None
     if args.store != "f32" and args.chunk is None:  # reduced profiling cases start in the clipper's warm-up
         del batch
+        batch = None
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
         few = sorted(range(nb), key=lambda i: cfgs[i]["dm_max"] * cfgs[i]["nsub"])[:PRECISION_BEAMS]
         precision = precision_check(pv, [cfgs[i] for i in few], args.store, dev, seed(0))
 
+    served = None
+    if args.serve and args.chunk is None and world == 1:
+        del batch, bhosts
+        batch = None
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        served = short_serve(pv, cfgs, args.store)
     ms, e2e_ms, plain_ms, plain_e2e_ms = max_over_ranks([ms, e2e_ms, plain_ms, plain_e2e_ms], dev, world)
     value = job_rate(units_step, args.steps, world, ms)
     e2e_value = job_rate(units_step, e2e_steps, world, e2e_ms)
@@ -704,10 +715,51 @@ def run_batch(args, cfgs, workload):
             "cpu_baseline": cpu}
     if precision is not None:
         line["precision"] = precision
+    if served is not None:
+        line["serve"] = served
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+# The short serving run of the default line: the 64 beams of the mix as
+# Poisson streams over SERVE_SECONDS under a 160 GB budget, through pv_serve.
+SERVE_SECONDS = 20.0
+
+
+def short_serve(pv, cfgs, store, seed=64):
+    """p50/p99 chunk latency of the serving loop (pv_serve) over the batch mix."""
+    import torch
+    import serve
+    dev = torch.device("cuda", 0)
+    pcfgs = [pv_config(pv, c) for c in cfgs]
+    spec = [{"cfg": pc, "tsamp": c["tsamp"], "tdms": c["tdms"], "nchan": c["nsub"] * c["nchan_sub"]}
+            for pc, c in zip(pcfgs, cfgs)]
+    streams = serve.poisson_streams(spec, SERVE_SECONDS, seed=seed)
+    trace = []
+    for i, (pc, st) in enumerate(zip(pcfgs, streams)):
+        v = device_voltages(cfgs[i], dev, 7000 + i)
+        hb = pv.HostBuffer(v.numel() * v.element_size())
+        hb.fill_from(v)
+        del v
+        trace.append({"arrivals": st.arrivals, "sizes": st.sizes, "voltages": hb,
+                      "units_per_spectrum": st.units_per_spectrum})
+    flags = pv.BATCH_GRAPH | pv.BATCH_PIPELINED | {"f32": 0, "f16": 16, "u8": 32}[store] | (3 << 8)
+    rep = pv.serve(pcfgs, trace, 160e9, policy="batch", batch_flags=flags, admit_every=0.5, linger=2.0,
+                   horizon=SERVE_SECONDS + 20.0)
+    durations = [s.sizes[0] * c["tsamp"] for s, c in zip(streams, cfgs)]
+    return {"streams": len(streams), "seconds": SERVE_SECONDS, "chunks": rep["chunks"],
+            "chunks_done": rep["chunks_done"], "latency_p50_ms": rep["latency_p50"] * 1e3,
+            "latency_p99_ms": rep["latency_p99"] * 1e3,
+            "latency_p99_over_chunk_duration": rep["latency_over_duration_p99"],
+            "chunks_within_real_time": rep["within_real_time"],
+            "admission_wait_p99_s": rep["admission_wait_p99"], "cohorts": rep["cohorts"],
+            "slot_reuses": rep["slot_reuses"], "throughput": rep["throughput"],
+            "chunk_duration_s": [min(durations), max(durations)],
+            "what": "pv_serve (C++ loop): the mix's 64 beams as Poisson chunk streams (one chunk of 1-8 "
+                    "steps per chunk duration), continuous batching under a 160 GB budget; latency from a "
+                    "chunk's arrival to the end of the step that processed it"}
 
 
 PRECISION_BEAMS = 6
@@ -964,7 +1016,9 @@ def serve_beams(nbeams=128, seed=128):
 
 
 def run_serve(args, workload):
-    """The serving loop over 128 streaming beams, batched and plain."""
+    """The serving loop (pv_serve, C++ in the library) over 128 streaming
+    beams: the batched engine, then the plain per-chunk path, on the same
+    Poisson trace."""
     import torch
     import pv
     import serve
@@ -978,23 +1032,27 @@ def run_serve(args, workload):
     streams = serve.poisson_streams(spec, args.duration, seed=7)
     budget = int(args.budget_gb * 1e9)
 
-    def voltages(cfg):
+    def staging(cfg):  # one sub-chunk of seeded voltages in page-locked memory: the stream's receive buffer
         g = torch.Generator(device=dev)
         g.manual_seed(int(cfg.nsub) * 1000 + int(cfg.nchan_sub))
         n = serve.SUB_CHUNK * cfg.int_time * cfg.nchan_sub
         v = torch.randn((cfg.nsub, 2, n, 2), generator=g, device=dev) * 16.0
-        return torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
+        v = torch.clamp(torch.round(v), -32768, 32767).to(torch.int16)
+        hb = pv.HostBuffer(v.numel() * v.element_size())
+        hb.fill_from(v)
+        return hb
 
-    def new_stream():
-        return torch.cuda.Stream(device=dev)
-
+    bufs = [staging(c) for c in cfgs]
+    trace = [{"arrivals": s.arrivals, "sizes": s.sizes, "voltages": bufs[i], "units_per_spectrum": s.units_per_spectrum}
+             for i, s in enumerate(streams)]
+    flags = pv.BATCH_GRAPH | pv.BATCH_PIPELINED | {"f32": 0, "f16": 16, "u8": 32}[args.store] | (3 << 8)
     reports = {}
     clocks = ClockSampler(0)
     clocks.start()
-    for name, eng, policy in (("batched", serve.BatchEngine(pv, voltages, new_stream, store=args.store), "batch"),
-                              ("plain", serve.PlainEngine(pv, voltages, new_stream), "fifo1")):
+    for name, policy in (("batched", "batch"), ("plain", "fifo1")):
         launches0 = pv.launches()
-        rep = serve.Server(eng, streams, budget, policy=policy).run(horizon=args.duration + args.grace)
+        rep = pv.serve(cfgs, trace, budget, policy=policy, batch_flags=flags, admit_every=0.5, linger=2.0,
+                       horizon=args.duration + args.grace)
         rep["gpu_launches"] = pv.launches() - launches0
         reports[name] = rep
         torch.cuda.synchronize()
@@ -1002,28 +1060,31 @@ def run_serve(args, workload):
     clk = clocks.stop()
     b, p = reports["batched"], reports["plain"]
     rt_units = sum(s.units_per_spectrum * sum(s.sizes) for s in streams)
+    sub_bytes = [h.nbytes for h in bufs]
     line = {"metric": "DM-trial*chan*samples/s", "value": b["throughput"],
-            "unit": "DM-trial*chan*samples/s", "n_gpus": 1, "steps": b["chunks_done"],
+            "unit": "DM-trial*chan*samples/s", "n_gpus": 1, "steps": b["steps"],
             "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded Gaussian int16 voltages, Poisson chunk arrivals",
             "config": {"workload": workload, "beams": len(streams), "duration_s": args.duration,
-                       "ring_storage": args.store,
+                       "ring_storage": args.store, "loop": "pv_serve (C++)",
                        "budget_gb": args.budget_gb,
                        "chunks": b["chunks"], "offered_units": rt_units,
                        "chunk_spectra": "4096-32768 per beam, Poisson, one chunk per chunk duration",
                        "nchan_range": [min(x["nchan"] for x in spec), max(x["nchan"] for x in spec)]},
             "e2e": {"value": b["throughput"], "unit": "DM-trial*chan*samples/s",
                     "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
-                    "what": "voltages copied from page-locked host memory every step"},
+                    "sub_chunk_bytes_mean": float(np.mean(sub_bytes)),
+                    "what": "every sub-chunk's voltages copied from its stream's page-locked receive buffer, "
+                            "wall time of the whole trace"},
             "serve": b, "plain": p,
-            "latency_ms": {"p50": b["latency_s"]["p50"] * 1e3, "p99": b["latency_s"]["p99"] * 1e3,
-                           "p99_after_admission": b["latency_after_admission_s"]["p99"] * 1e3,
-                           "p99_over_chunk_duration": b["latency_over_chunk_duration"]["p99"],
-                           "plain_p50": p["latency_s"]["p50"] * 1e3,
-                           "plain_p99": p["latency_s"]["p99"] * 1e3,
-                           "plain_p99_over_chunk_duration": p["latency_over_chunk_duration"]["p99"]},
-            "batched_over_plain_latency_p99": p["latency_s"]["p99"] / b["latency_s"]["p99"],
+            "latency_ms": {"p50": b["latency_p50"] * 1e3, "p99": b["latency_p99"] * 1e3,
+                           "p99_after_admission": b["latency_admitted_p99"] * 1e3,
+                           "p99_over_chunk_duration": b["latency_over_duration_p99"],
+                           "plain_p50": p["latency_p50"] * 1e3,
+                           "plain_p99": p["latency_p99"] * 1e3,
+                           "plain_p99_over_chunk_duration": p["latency_over_duration_p99"]},
+            "batched_over_plain_latency_p99": p["latency_p99"] / max(b["latency_p99"], 1e-9),
             "gpu_launches": b["gpu_launches"], "clocks": clk, "cpu_baseline": None}
     print(json.dumps(line))
 
@@ -1204,6 +1265,8 @@ def main():
     ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
                     help="batch64, serve128: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
+    ap.add_argument("--no-serve", dest="serve", action="store_false",
+                    help="batch64: skip the short serving run")
     ap.add_argument("--variant", type=int, default=None,
                     help="dedispersion tile variant (0-5) instead of the autotuner's choice (profiling)")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")

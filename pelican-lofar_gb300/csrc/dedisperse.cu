@@ -764,21 +764,23 @@ dedisperse_batch_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __
 // ---------------------------------------------------------------------------
 constexpr int kPairS = 33;  // output samples per lane
 
+// w holds row[0..32], read before the jump: every delta needs them.
 template <int D>
-__device__ __forceinline__ void pair_add(const float* __restrict__ row, float (&a0)[kPairS],
-                                         float (&a1)[kPairS]) {
+__device__ __forceinline__ void pair_add(const float* __restrict__ row, const float (&w)[kPairS],
+                                         float (&a0)[kPairS], float (&a1)[kPairS]) {
 #pragma unroll
-    for (int j = 0; j < kPairS + D; ++j) {
-        const float w = row[j];
-        if (j < kPairS) a0[j] = __fadd_rn(a0[j], w);
-        if (j >= D) a1[j - D] = __fadd_rn(a1[j - D], w);
+    for (int j = 0; j < kPairS; ++j) {
+        a0[j] = __fadd_rn(a0[j], w[j]);
+        if (j >= D) a1[j - D] = __fadd_rn(a1[j - D], w[j]);
     }
+#pragma unroll
+    for (int j = kPairS; j < kPairS + D; ++j) a1[j - D] = __fadd_rn(a1[j - D], row[j]);
 }
 
-__device__ __forceinline__ void pair_add_far(const float* __restrict__ row, int dl, float (&a0)[kPairS],
-                                             float (&a1)[kPairS]) {
+__device__ __forceinline__ void pair_add_far(const float* __restrict__ row, int dl, const float (&w)[kPairS],
+                                             float (&a0)[kPairS], float (&a1)[kPairS]) {
 #pragma unroll
-    for (int j = 0; j < kPairS; ++j) a0[j] = __fadd_rn(a0[j], row[j]);
+    for (int j = 0; j < kPairS; ++j) a0[j] = __fadd_rn(a0[j], w[j]);
     const float* rb = row + dl;
 #pragma unroll
     for (int j = 0; j < kPairS; ++j) a1[j] = __fadd_rn(a1[j], rb[j]);
@@ -856,14 +858,20 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
                     my_oa = min(pv_shift(k, dva) - mo, slot - TT - 16);
                     my_dl = min(pv_shift(k, dvb) - mo, slot - TT - 16) - my_oa;
                 }
+                // channel j+1's offsets are taken while channel j is added
+                int oa = __shfl_sync(0xffffffffu, my_oa, 0);
+                int dl = __shfl_sync(0xffffffffu, my_dl, 0);
                 for (int j = 0; j < c_end; ++j) {
-                    const int oa = __shfl_sync(0xffffffffu, my_oa, j);
-                    const int dl = __shfl_sync(0xffffffffu, my_dl, j);
+                    const int oa_n = __shfl_sync(0xffffffffu, my_oa, (j + 1) & 31);
+                    const int dl_n = __shfl_sync(0xffffffffu, my_dl, (j + 1) & 31);
                     const float* row = slotf + (size_t)(b * CS + j) * slot + oa + kPairS * lane;
+                    float w[kPairS];
+#pragma unroll
+                    for (int q = 0; q < kPairS; ++q) w[q] = row[q];
                     switch (dl) {
 #define PV_PAIR(D) \
     case D:        \
-        pair_add<D>(row, a0, a1); \
+        pair_add<D>(row, w, a0, a1); \
         break;
                         PV_PAIR(0) PV_PAIR(1) PV_PAIR(2) PV_PAIR(3) PV_PAIR(4) PV_PAIR(5) PV_PAIR(6)
                         PV_PAIR(7) PV_PAIR(8) PV_PAIR(9) PV_PAIR(10) PV_PAIR(11) PV_PAIR(12) PV_PAIR(13)
@@ -872,8 +880,10 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
                         PV_PAIR(28) PV_PAIR(29) PV_PAIR(30) PV_PAIR(31) PV_PAIR(32)
 #undef PV_PAIR
                         default:
-                            pair_add_far(row, dl, a0, a1);
+                            pair_add_far(row, dl, w, a0, a1);
                     }
+                    oa = oa_n;
+                    dl = dl_n;
                 }
             }
             __syncwarp();
