@@ -1146,6 +1146,7 @@ class CpuChain:
         po.analyse(out, cfg["threshold"], self.rms, cfg["bin_pow2"])
         t4 = time.perf_counter()
         del st
+        self.last_wall = (t1 - t0) + (t3 - t2) + (t4 - t3)  # what was actually run
         return (t1 - t0) * self.sub_scale + (t3 - t2) + (t4 - t3) * self.trial_scale
 
 
@@ -1225,12 +1226,18 @@ def run_reference(args, cfgs, workload):
                   % (len(chains), len(cfgs)) + "; ".join(ch.sample for ch in chains))
     for _ in range(args.warmup):
         step_secs()
-    secs = [step_secs() for _ in range(args.steps)]
+    secs, walls = [], []
+    for _ in range(args.steps):
+        secs.append(step_secs())
+        walls.append(sum(ch.last_wall for ch in chains))
     units = sum(c["tdms"] * c["nsub"] * c["nchan_sub"] * c["chunk"] for c in cfgs)
     value = units * len(secs) / float(np.sum(secs))
     line = {"impl": "reference", "metric": "DM-trial*chan*samples/s", "value": value,
             "unit": "DM-trial*chan*samples/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
+            "ms_per_step_what": "host time of the bounded sample each step runs; value is the whole step's "
+                                "work over the step's time extrapolated from the sample's stage times",
+            "ms_per_step_extrapolated": float(np.mean(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded Gaussian voltages and filterbank",
             "config": {"workload": workload, "beams": len(cfgs),

@@ -786,13 +786,18 @@ __device__ __forceinline__ void pair_add_far(const float* __restrict__ row, int 
     for (int j = 0; j < kPairS; ++j) a1[j] = __fadd_rn(a1[j], rb[j]);
 }
 
-template <int CS, int ST>
-__global__ void __launch_bounds__(9 * 32, 1)
+// PAIRS trial pairs per tile (2 * PAIRS trials) and HALVES parts of the
+// time tile (HALVES x 1056 samples): consumer warp w takes pair w % PAIRS in
+// part w / PAIRS.  8 x 1: 8 consumer warps; 6 x 2: 12, more warps to hide
+// each channel's offset shuffle, jump and first reads within the register
+// file's share of one SM sub-partition (13 warps: up to 128 registers).
+template <int CS, int ST, int PAIRS, int HALVES>
+__global__ void __launch_bounds__((PAIRS * HALVES + 1) * 32, 1)
 dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles, int ntiles,
                        int slot, int* __restrict__ counter, const pv::BeamStep* __restrict__ bs,
                        int* __restrict__ status, unsigned long long wait_ns) {
-    constexpr int NW = 8;  // consumer warps, two trials each: 16 trials per tile
-    constexpr int TT = 32 * kPairS;
+    constexpr int NW = PAIRS * HALVES;
+    constexpr int TT = 32 * kPairS * HALVES;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* slots = smem_raw;  // [ST*CS][slot] floats
     int* meta_off = reinterpret_cast<int*>(slots + (size_t)ST * CS * slot * 4);
@@ -833,9 +838,11 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
         const pv::DdTile tt = tiles[tile];
         const pv::DdJob& J = jobs[tt.job];
         const int d_last = min(tt.d0 + J.dms, J.tdms) - 1;
-        const int da = tt.d0 + 2 * warp;
-        const bool act_a = 2 * warp < J.dms && da <= d_last;
-        const bool act_b = 2 * warp + 1 < J.dms && da + 1 <= d_last;
+        const int pair = warp % PAIRS, half = warp / PAIRS;
+        const int da = tt.d0 + 2 * pair;
+        const bool act_a = 2 * pair < J.dms && da <= d_last;
+        const bool act_b = 2 * pair + 1 < J.dms && da + 1 <= d_last;
+        const int lane_t = half * 32 * kPairS + kPairS * lane;  // the lane's first sample in the tile
         const float dva = pv_trial_value(min(da, d_last), J.start, J.step);
         const float dvb = pv_trial_value(min(da + 1, d_last), J.start, J.step);
         const int nst = (J.nchan + CS - 1) / CS;
@@ -864,7 +871,7 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
                 for (int j = 0; j < c_end; ++j) {
                     const int oa_n = __shfl_sync(0xffffffffu, my_oa, (j + 1) & 31);
                     const int dl_n = __shfl_sync(0xffffffffu, my_dl, (j + 1) & 31);
-                    const float* row = slotf + (size_t)(b * CS + j) * slot + oa + kPairS * lane;
+                    const float* row = slotf + (size_t)(b * CS + j) * slot + oa + lane_t;
                     float w[kPairS];
 #pragma unroll
                     for (int q = 0; q < kPairS; ++q) w[q] = row[q];
@@ -893,7 +900,7 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
         float* oa_p = J.out + (long long)da * J.out_stride;
 #pragma unroll
         for (int j = 0; j < kPairS; ++j) {
-            const long long t = tt.t0 + kPairS * lane + j;
+            const long long t = tt.t0 + lane_t + j;
             if (t < J.nout) {
                 if (act_a) oa_p[t] = a0[j];
                 if (act_b) oa_p[J.out_stride + t] = a1[j];
@@ -1015,11 +1022,12 @@ namespace {
 
 struct Variant {
     int R, CS, ST;
-    bool pair;  // FP32 trial-pair consumers (dedisperse_pair_kernel, R = 33)
+    bool pair;  // FP32 trial-pair consumers (dedisperse_pair_kernel, R = 33 per part of the time tile)
+    int dmax;   // trials per tile at most
 };
 // Time tile 32R samples, CS channels per pipeline stage, ST stages in flight.
-constexpr Variant kVariants[] = {{32, 4, 4, false}, {32, 2, 4, false}, {16, 4, 4, false},
-                                 {32, 8, 2, false}, {33, 8, 2, true},  {33, 4, 4, true}};
+constexpr Variant kVariants[] = {{32, 4, 4, false, 16}, {32, 2, 4, false, 16}, {16, 4, 4, false, 16},
+                                 {32, 8, 2, false, 16}, {33, 8, 2, true, 16},  {66, 8, 2, true, 12}};
 constexpr int kNumVariants = 6;
 static_assert(kNumVariants == PV_BATCH_VARIANTS, "variant count of the C ABI");
 constexpr size_t kBatchSmemBudget = 220 * 1024;
@@ -1055,10 +1063,11 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
-template <int CS, int ST>
+template <int CS, int ST, int PAIRS, int HALVES>
 int launch_pair_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem, int grid,
                   int* counter, const pv::BeamStep* bs, int* status, cudaStream_t s, bool set_attr) {
-    auto kern = dedisperse_pair_kernel<CS, ST>;
+    constexpr int NW = PAIRS * HALVES;
+    auto kern = dedisperse_pair_kernel<CS, ST, PAIRS, HALVES>;
     if (set_attr) {
         size_t limit = 0;
         PV_CUDA(pv::allow_max_dynamic_smem(kern, &limit), "cudaFuncSetAttribute(dedisperse_pair)");
@@ -1073,7 +1082,7 @@ int launch_pair_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, in
     } else {
         PV_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), s), "reset tile counter");
     }
-    kern<<<grid, 9 * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status, pv::wait_ns());
+    kern<<<grid, (NW + 1) * 32, smem, s>>>(jobs, tiles, ntiles, slot, counter, bs, status, pv::wait_ns());
     return pv::check_launch("dedisperse_pair_kernel");
 }
 
@@ -1081,9 +1090,9 @@ int launch_batch(int variant, int store, const pv::DdJob* jobs, const pv::DdTile
                  int slot, size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
                  cudaStream_t s, bool set_attr) {
     if (variant == 4 && store == PV_STORE_F32)
-        return launch_pair_t<8, 2>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
+        return launch_pair_t<8, 2, 8, 1>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
     if (variant == 5 && store == PV_STORE_F32)
-        return launch_pair_t<4, 4>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
+        return launch_pair_t<8, 2, 6, 2>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
     switch (variant * 3 + store) {
 #define PV_VAR(I, R, CS, ST, SS)                                                                 \
     case I * 3 + SS:                                                                            \
@@ -1167,7 +1176,7 @@ bool build_shape(const Variant& v, int store, const DdBeam* beams, int n,
         const DdBeam& B = beams[i];
         float kmax = 0.0f;
         for (int c = 0; c < B.nchan; ++c) kmax = std::max(kmax, B.h_dmshift[c]);
-        int dms = 16, sp = 0;
+        int dms = v.dmax, sp = 0;
         for (; dms >= 1; --dms) {
             if (TT + spread_bound(kmax, B.tdms, dms, B.start, B.step) + pad > slot_cap) continue;
             auto it = exact[i].find(dms);

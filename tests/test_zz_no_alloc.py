@@ -23,7 +23,8 @@ def _run(pv, fn, d_data, threshold, rms, bin_pow2, cap):
     ev = torch.zeros(cap * 4, dtype=torch.int32, device=d_data.device)
     n = C.c_longlong(-1)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    pv.check(fn(C.c_void_p(d_data.data_ptr()), d_data.stride(0), tdms, nsamp, threshold, rms,
+    ld = d_data.stride(0) if tdms > 0 else nsamp  # an empty tensor reports stride 0
+    pv.check(fn(C.c_void_p(d_data.data_ptr()), ld, tdms, nsamp, threshold, rms,
                 bin_pow2, C.c_void_p(ev.data_ptr()), cap, C.byref(n), stream))
     k = min(n.value, cap)
     return ev[: 4 * k].cpu().numpy().view(pv.EVENT_DTYPE).copy(), n.value
