@@ -508,14 +508,20 @@ def run_batch(args, cfgs, workload):
     batch = pv.Batch([beam_cfg(c) for c in cfgs], tune=args.variant is None, graph=True, timing=True,
                      variant=args.variant or 0,
                      pipelined=not args.unpipelined, store=args.store)
-    bhosts = []  # the batch's staging, allocated after the batch (see the plain arm's)
+    # the batch's staging, allocated after the batch (see the plain arm's), holds the plain arm's
+    # very bytes: both arms take identical voltages
+    bhosts = []
+    L = pv.load()
     for i, c in enumerate(cfgs):
-        v = chunk_input(i, c)
-        batch.set_input(i, v, stream=stream, both=True)  # the same chunk at every step
-        bhosts.append(pv.HostBuffer(v.numel() * v.element_size()))
-        bhosts[-1].fill_from(v, stream=stream)
+        bhosts.append(pv.HostBuffer(hosts[i].nbytes))
+        pv.check(L.pv_device_copy(pv.C.c_void_p(bhosts[i].ptr), pv.C.c_void_p(hosts[i].ptr), hosts[i].nbytes,
+                                  pv._stream(stream)))
+        for par in (0, 1):  # the same chunk at every step: both input buffers
+            p, nbytes = pv.C.c_void_p(), pv.C.c_longlong()
+            pv.check(L.pv_batch_input_parity(batch.h, i, par, pv.C.byref(p), pv.C.byref(nbytes)))
+            assert nbytes.value == bhosts[i].nbytes
+            pv.check(L.pv_device_copy(p, pv.C.c_void_p(bhosts[i].ptr), nbytes.value, pv._stream(stream)))
         stream.synchronize()
-        del v
     del hosts
     torch.cuda.empty_cache()
     infos = [batch.info(i) for i in range(nb)]
