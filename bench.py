@@ -60,6 +60,47 @@ RAW_TSAMP = 5.12e-6  # s
 DD_BATCH_BYTES_PER_ADD = 1.776e9 / 5.1204063232e10
 
 
+def dd_kernel_name(variant):
+    """The batched dedispersion kernel of a tile variant."""
+    return "dedisperse_batch_kernel" if variant < 4 else "dedisperse_pair_kernel"
+
+
+PAIR_S = 33       # output samples per lane of the trial-pair kernels
+PAIR_LIM = {4: 32, 5: 32, 6: 15, 7: 15, 8: 15}  # largest shift difference read from registers
+
+
+def shared_words_per_add(cfgs, variant, dms, samples=64):
+    """Shared-memory words the batched kernel reads per FP32 add on these
+    beams: 1 for the one-trial variants; for the trial-pair variants a lane
+    reads 33 + delta words for its 66 adds (delta = the channel's shift
+    difference between the pair's trials, up to the variant's limit) or 66
+    beyond it.  Evaluated over every channel and a sample of the trial pairs
+    of each DM tile, weighted by adds."""
+    if variant < 4:
+        return 1.0
+    lim = PAIR_LIM[variant]
+    words = adds = 0.0
+    for c, h in zip(cfgs, dms):
+        nb = c["nsub"] * c["nchan_sub"]
+        f = c["fch1"] + np.arange(nb) * c["foff"]
+        k = (4148.741601 * (1.0 / f ** 2 - 1.0 / f.max() ** 2)).astype(np.float32)
+        step = np.float32(c["dm_step"]) / np.float32(c["tsamp"])
+        ds = np.unique(np.linspace(0, c["tdms"] - 2, samples).astype(np.int64))
+        ds = ds[(ds % h) % 2 == 0]  # first trial of a pair within its tile
+        if len(ds) == 0:
+            continue
+        va = ds.astype(np.float32)[:, None] * step
+        vb = (ds + 1).astype(np.float32)[:, None] * step
+        sa = np.trunc(k[None, :] * va).astype(np.int64)
+        sb = np.trunc(k[None, :] * vb).astype(np.int64)
+        dl = sb - sa
+        w = np.where(dl <= lim, PAIR_S + dl, 2 * PAIR_S).astype(np.float64)
+        wt = c["tdms"] * c["chunk"] / len(ds)
+        words += w.sum() * wt
+        adds += 2 * PAIR_S * dl.size * wt
+    return words / adds if adds else 1.0
+
+
 def beam_dict(nsub, nchan_sub, dm_max, tdms, chunk, **kw):
     int_time = 4
     foff = SUB_BW / nchan_sub
@@ -644,11 +685,15 @@ def run_batch(args, cfgs, workload):
     achieved = units_step / (st["dedisperse"] / 1e3)
     fb_bytes = sum(c["chunk"] * c["nsub"] * c["nchan_sub"] * 4 for c in cfgs)
     chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
-    roofline = {"kernel": "dedisperse_batch_kernel", "bound": "fp32",
+    variant = tiles["variant"]
+    words = shared_words_per_add(cfgs, variant, tiles["dms"])
+    roofline = {"kernel": dd_kernel_name(variant), "bound": "fp32",
                 "achieved": achieved / 1e12, "peak": fadd_peak / 1e12, "unit": "Tadd/s",
                 "frac": achieved / fadd_peak,
-                "smem_bound_frac": achieved / (fadd_peak / 4),
-                "smem_bound": "one 4-byte shared-memory read per add: 32 of 128 lanes per clock",
+                "smem_bound_frac": achieved * words / (fadd_peak / 4),
+                "smem_words_per_add": words,
+                "smem_bound": "32 four-byte shared-memory words per clock per SM (one 128-byte wavefront); "
+                              "the kernel reads smem_words_per_add words per add on this workload",
                 "traffic": DD_BATCH_BYTES_PER_ADD * units_step,
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
                                   "on the 3-beam, 1024-sample case, scaled by adds",
@@ -1281,7 +1326,7 @@ def main():
     ap.add_argument("--no-serve", dest="serve", action="store_false",
                     help="batch64: skip the short serving run")
     ap.add_argument("--variant", type=int, default=None,
-                    help="dedispersion tile variant (0-5) instead of the autotuner's choice (profiling)")
+                    help="dedispersion tile variant (0-8) instead of the autotuner's choice (profiling)")
     ap.add_argument("--chunk", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--nsub", type=int, default=None, help="reduced case for profiling")
     args = ap.parse_args()

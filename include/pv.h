@@ -429,8 +429,8 @@ typedef struct pv_batch pv_batch;
                                  the median and sigma the median absolute deviation x 1.4826 of
                                  the first chunk in which the channel varies (until then the
                                  channel's samples are stored as its offset) */
-#define PV_BATCH_VARIANTS 6            /* dedispersion tile variants (4 and 5: FP32 rings only) */
-#define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..5 */
+#define PV_BATCH_VARIANTS 9            /* dedispersion tile variants (4 to 8: FP32 rings only) */
+#define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..8 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % PV_BATCH_VARIANTS)
 int pv_batch_create(pv_batch** batch, const pv_beam_config* configs, int nbeams, int flags);
 void pv_batch_destroy(pv_batch* batch);
@@ -473,8 +473,10 @@ int pv_batch_info(const pv_batch* batch, int beam, long long* h_info8);
  * the autotuner's time (ms) of each of the PV_BATCH_VARIANTS variants (-1:
  * not timed or not usable) and the kernels one graph replay launches (0
  * without a graph).  Any may be NULL.  Variants 0-3 give each trial of a
- * DM tile one warp (one shared-memory word per add); variants 4 and 5 give
- * each warp two adjacent trials that share the words they both read. */
+ * DM tile one warp (one shared-memory word per add); variants 4 to 8 give
+ * each warp two adjacent trials that share the words they both read
+ * (6 to 8 read from registers shift differences up to 15 instead of 32,
+ * 7 and 8 with 14 adding warps instead of 12). */
 int pv_batch_tiles(const pv_batch* batch, int* h_shape8, int* h_dms, float* h_tune_ms,
                    long long* h_graph_kernels);
 /* Device time (ms) of the last step's stages (PV_BATCH_TIMING): channelise,

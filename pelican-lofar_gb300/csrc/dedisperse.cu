@@ -192,12 +192,16 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                  "r"(bytes) : "memory");
 }
+// A waiting thread sleeps until the phase completes or for up to 100 us
+// (the suspend-time hint) instead of polling: a warp that waits for a stage
+// or a free slot issues no instructions meanwhile.
+constexpr unsigned kSuspendHintNs = 100000u;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+        : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity), "n"(kSuspendHintNs) : "memory");
     return ok != 0;
 }
 // Whole-warp wait for the phase of the given parity.  Every lane observes the
@@ -786,12 +790,44 @@ __device__ __forceinline__ void pair_add_far(const float* __restrict__ row, int 
     for (int j = 0; j < kPairS; ++j) a1[j] = __fadd_rn(a1[j], rb[j]);
 }
 
+// The jump over the shift difference dl: 0..LIM from registers, larger
+// differences read trial b's 33 words separately.  LIM 15 halves the jump's
+// code, which the instruction cache of a sub-partition then holds.
+template <int LIM>
+__device__ __forceinline__ void pair_dispatch(const float* __restrict__ row, int dl, const float (&w)[kPairS],
+                                              float (&a0)[kPairS], float (&a1)[kPairS]) {
+#define PV_PAIR(D) \
+    case D:        \
+        pair_add<D>(row, w, a0, a1); \
+        break;
+    if constexpr (LIM == 32) {
+        switch (dl) {
+            PV_PAIR(0) PV_PAIR(1) PV_PAIR(2) PV_PAIR(3) PV_PAIR(4) PV_PAIR(5) PV_PAIR(6) PV_PAIR(7) PV_PAIR(8)
+            PV_PAIR(9) PV_PAIR(10) PV_PAIR(11) PV_PAIR(12) PV_PAIR(13) PV_PAIR(14) PV_PAIR(15) PV_PAIR(16)
+            PV_PAIR(17) PV_PAIR(18) PV_PAIR(19) PV_PAIR(20) PV_PAIR(21) PV_PAIR(22) PV_PAIR(23) PV_PAIR(24)
+            PV_PAIR(25) PV_PAIR(26) PV_PAIR(27) PV_PAIR(28) PV_PAIR(29) PV_PAIR(30) PV_PAIR(31) PV_PAIR(32)
+            default:
+                pair_add_far(row, dl, w, a0, a1);
+        }
+    } else {
+        static_assert(LIM == 15, "shift-difference limits 15 and 32");
+        switch (dl) {
+            PV_PAIR(0) PV_PAIR(1) PV_PAIR(2) PV_PAIR(3) PV_PAIR(4) PV_PAIR(5) PV_PAIR(6) PV_PAIR(7) PV_PAIR(8)
+            PV_PAIR(9) PV_PAIR(10) PV_PAIR(11) PV_PAIR(12) PV_PAIR(13) PV_PAIR(14) PV_PAIR(15)
+            default:
+                pair_add_far(row, dl, w, a0, a1);
+        }
+    }
+#undef PV_PAIR
+}
+
 // PAIRS trial pairs per tile (2 * PAIRS trials) and HALVES parts of the
 // time tile (HALVES x 1056 samples): consumer warp w takes pair w % PAIRS in
-// part w / PAIRS.  8 x 1: 8 consumer warps; 6 x 2: 12, more warps to hide
-// each channel's offset shuffle, jump and first reads within the register
-// file's share of one SM sub-partition (13 warps: up to 128 registers).
-template <int CS, int ST, int PAIRS, int HALVES>
+// part w / PAIRS.  8 x 1: 8 consumer warps; 6 x 2: 12; 7 x 2: 14, more warps
+// to hide each channel's offset shuffle, jump and first reads within the
+// register file's share of one SM sub-partition (13 to 16 warps: up to 128
+// registers).
+template <int CS, int ST, int PAIRS, int HALVES, int LIM>
 __global__ void __launch_bounds__((PAIRS * HALVES + 1) * 32, 1)
 dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __restrict__ tiles, int ntiles,
                        int slot, int* __restrict__ counter, const pv::BeamStep* __restrict__ bs,
@@ -875,20 +911,7 @@ dedisperse_pair_kernel(const pv::DdJob* __restrict__ jobs, const pv::DdTile* __r
                     float w[kPairS];
 #pragma unroll
                     for (int q = 0; q < kPairS; ++q) w[q] = row[q];
-                    switch (dl) {
-#define PV_PAIR(D) \
-    case D:        \
-        pair_add<D>(row, w, a0, a1); \
-        break;
-                        PV_PAIR(0) PV_PAIR(1) PV_PAIR(2) PV_PAIR(3) PV_PAIR(4) PV_PAIR(5) PV_PAIR(6)
-                        PV_PAIR(7) PV_PAIR(8) PV_PAIR(9) PV_PAIR(10) PV_PAIR(11) PV_PAIR(12) PV_PAIR(13)
-                        PV_PAIR(14) PV_PAIR(15) PV_PAIR(16) PV_PAIR(17) PV_PAIR(18) PV_PAIR(19) PV_PAIR(20)
-                        PV_PAIR(21) PV_PAIR(22) PV_PAIR(23) PV_PAIR(24) PV_PAIR(25) PV_PAIR(26) PV_PAIR(27)
-                        PV_PAIR(28) PV_PAIR(29) PV_PAIR(30) PV_PAIR(31) PV_PAIR(32)
-#undef PV_PAIR
-                        default:
-                            pair_add_far(row, dl, w, a0, a1);
-                    }
+                    pair_dispatch<LIM>(row, dl, w, a0, a1);
                     oa = oa_n;
                     dl = dl_n;
                 }
@@ -1022,13 +1045,14 @@ namespace {
 
 struct Variant {
     int R, CS, ST;
-    bool pair;  // FP32 trial-pair consumers (dedisperse_pair_kernel, R = 33 per part of the time tile)
-    int dmax;   // trials per tile at most
+    bool pair; // FP32 trial-pair consumers (dedisperse_pair_kernel, R = 33 per part of the time tile)
+    int dmax;  // trials per tile at most
 };
 // Time tile 32R samples, CS channels per pipeline stage, ST stages in flight.
 constexpr Variant kVariants[] = {{32, 4, 4, false, 16}, {32, 2, 4, false, 16}, {16, 4, 4, false, 16},
-                                 {32, 8, 2, false, 16}, {33, 8, 2, true, 16},  {66, 8, 2, true, 12}};
-constexpr int kNumVariants = 6;
+                                 {32, 8, 2, false, 16}, {33, 8, 2, true, 16},  {66, 8, 2, true, 12},
+                                 {66, 8, 2, true, 12},  {66, 8, 2, true, 14},  {66, 4, 4, true, 14}};
+constexpr int kNumVariants = 9;
 static_assert(kNumVariants == PV_BATCH_VARIANTS, "variant count of the C ABI");
 constexpr size_t kBatchSmemBudget = 220 * 1024;
 
@@ -1063,11 +1087,11 @@ int launch_batch_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, i
     return pv::check_launch("dedisperse_batch_kernel");
 }
 
-template <int CS, int ST, int PAIRS, int HALVES>
+template <int CS, int ST, int PAIRS, int HALVES, int LIM>
 int launch_pair_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, int slot, size_t smem, int grid,
                   int* counter, const pv::BeamStep* bs, int* status, cudaStream_t s, bool set_attr) {
     constexpr int NW = PAIRS * HALVES;
-    auto kern = dedisperse_pair_kernel<CS, ST, PAIRS, HALVES>;
+    auto kern = dedisperse_pair_kernel<CS, ST, PAIRS, HALVES, LIM>;
     if (set_attr) {
         size_t limit = 0;
         PV_CUDA(pv::allow_max_dynamic_smem(kern, &limit), "cudaFuncSetAttribute(dedisperse_pair)");
@@ -1089,10 +1113,18 @@ int launch_pair_t(const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles, in
 int launch_batch(int variant, int store, const pv::DdJob* jobs, const pv::DdTile* tiles, int ntiles,
                  int slot, size_t smem, int grid, int* counter, const pv::BeamStep* bs, int* status,
                  cudaStream_t s, bool set_attr) {
-    if (variant == 4 && store == PV_STORE_F32)
-        return launch_pair_t<8, 2, 8, 1>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
-    if (variant == 5 && store == PV_STORE_F32)
-        return launch_pair_t<8, 2, 6, 2>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, set_attr);
+    if (store == PV_STORE_F32 && variant >= 4 && variant <= 8) {
+#define PV_PAIRV(I, CS, ST, P, H, L)                                                                   \
+    if (variant == I)                                                                                 \
+        return launch_pair_t<CS, ST, P, H, L>(jobs, tiles, ntiles, slot, smem, grid, counter, bs, status, s, \
+                                              set_attr);
+        PV_PAIRV(4, 8, 2, 8, 1, 32)
+        PV_PAIRV(5, 8, 2, 6, 2, 32)
+        PV_PAIRV(6, 8, 2, 6, 2, 15)
+        PV_PAIRV(7, 8, 2, 7, 2, 15)
+        PV_PAIRV(8, 4, 4, 7, 2, 15)
+#undef PV_PAIRV
+    }
     switch (variant * 3 + store) {
 #define PV_VAR(I, R, CS, ST, SS)                                                                 \
     case I * 3 + SS:                                                                            \

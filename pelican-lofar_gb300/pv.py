@@ -510,6 +510,8 @@ class Beam:
 
 
 BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
+BATCH_VARIANTS = 9  # PV_BATCH_VARIANTS: dedispersion tile variants
+
 class UdpConfig(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("fixed_size_packets", "sample_bits", "packets_per_chunk",
                                        "samples_per_packet", "nchan", "nsub", "npol", "clock_mhz")]
@@ -867,7 +869,7 @@ class Batch:
 
     def tiles(self):
         shape, dms = (C.c_int * 8)(), (C.c_int * len(self.cfgs))()
-        tune, nk = (C.c_float * 6)(), C.c_longlong()
+        tune, nk = (C.c_float * BATCH_VARIANTS)(), C.c_longlong()
         check(load().pv_batch_tiles(self.h, shape, dms, tune, C.byref(nk)))
         keys = ["variant", "time_tile", "chan_per_stage", "stages", "slot", "tiles", "ctas", "smem"]
         d = dict(zip(keys, list(shape)))

@@ -59,7 +59,9 @@ def mix_configs(pv, cuda):
                          [(True, True, 0, False, False), (False, False, 1, False, False),
                           (False, True, 3, True, False), (False, True, 0, False, True),
                           (True, True, 0, True, True), (False, True, 4, True, False),
-                          (False, False, 5, False, True), (False, True, 4, False, True)])
+                          (False, False, 5, False, True), (False, True, 4, False, True),
+                          (False, True, 6, True, False), (False, False, 7, False, True),
+                          (False, True, 8, False, False), (False, True, 6, False, True)])
 def test_batch_equals_beams_alone(pv, cuda, mix_configs, tune, graph, variant, prefilled, pipelined):
     """Filterbank, event list and dedispersed window of every beam equal the
     single-beam chain's; pipelined, a window arrives one step later."""
