@@ -548,7 +548,8 @@ def run_batch(args, cfgs, workload):
     # ---------------- batched engine ----------------
     batch = pv.Batch([beam_cfg(c) for c in cfgs], tune=args.variant is None, graph=True, timing=True,
                      variant=args.variant or 0,
-                     pipelined=not args.unpipelined, store=args.store)
+                     pipelined=not args.unpipelined, store=args.store, rfi_one_cta=args.rfi_one_cta,
+                     rfi_cluster8=args.rfi_cluster8, rfi_cluster4=args.rfi_cluster4)
     # the batch's staging, allocated after the batch (see the plain arm's), holds the plain arm's
     # very bytes: both arms take identical voltages
     bhosts = []
@@ -728,6 +729,11 @@ def run_batch(args, cfgs, workload):
                                 "one launch after the clippers" if args.unpipelined else
                                 "pipelined: window k-lag-1 dedispersed while chunk k is channelised "
                                 "and clipped"),
+                       "clippers": "one CTA per beam" if args.rfi_one_cta else (
+                                   "beams of more than 1024 channels on clusters of 128-thread CTAs"
+                                   if args.rfi_cluster8 else (
+                                       "one CTA per beam up to 4096 channels, else a cluster of 4 CTAs"
+                                       if args.rfi_cluster4 or args.unpipelined else "one CTA per beam")),
                        "parallelism": "replicas" if world > 1 else "one GPU, all beams batched"},
             "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
@@ -1322,6 +1328,13 @@ def main():
                     help="batch64: one dedispersion launch per step after the clippers (the same work)")
     ap.add_argument("--store", default="f32", choices=["f32", "f16", "u8"],
                     help="batch64, serve128: delay-ring storage (FP32, FP16, or uint8 with per-channel scale)")
+    ap.add_argument("--rfi-one-cta", action="store_true",
+                    help="batch64: every beam's clipper on one CTA (default: beams of more than 1024 "
+                         "channels on a cluster of 2 or 4 CTAs)")
+    ap.add_argument("--rfi-cluster4", action="store_true",
+                    help="batch64: clippers of beams of more than 4096 channels on clusters of 4 CTAs")
+    ap.add_argument("--rfi-cluster8", action="store_true",
+                    help="batch64: clippers of beams of more than 1024 channels on clusters of 128-thread CTAs")
     ap.add_argument("--tdms", type=int, default=None, help="reduced case for profiling")
     ap.add_argument("--no-serve", dest="serve", action="store_false",
                     help="batch64: skip the short serving run")

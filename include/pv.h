@@ -308,9 +308,17 @@ int pv_rfi_bandpass(pv_rfi* rfi, float* h_out, int nbins);
  * h_out[nbins] its currentSet() (NULL: skipped), h_stats4 [mean, rms,
  * median, params()[0]].  Synchronous. */
 int pv_rfi_bandpass_current(pv_rfi* rfi, float* h_out, int nbins, float* h_stats4);
-/* Threads of the clipper's CTA for a band of nbins channels; also the number
- * of FP32 partial sums of its channel reductions (256, 512 or 1024). */
+/* The number of FP32 partial sums of the clipper's channel reductions for a
+ * band of nbins channels (256, 512 or 1024): partial p sums channels p,
+ * p + parts, ... in order. */
 int pv_rfi_parts(int nbins);
+/* How pv_rfi_run spreads a band over the GPU (no counterpart in the
+ * reference, whose clipper is one CPU thread): 0 one CTA of `parts`
+ * threads; 1 (the default) bands of 1024 partials over a cluster of 4 CTAs
+ * of 256 threads; 2 bands of 512 or 1024 partials over clusters of 128-thread
+ * CTAs.  Every choice computes the same partial sums, so flags and outputs
+ * are identical. */
+int pv_rfi_set_split(pv_rfi* rfi, int split);
 
 /* ------------------------------------------------------------------------
  * One beam's device-resident chain, in the order of DedispersionPipeline::run
@@ -429,6 +437,15 @@ typedef struct pv_batch pv_batch;
                                  the median and sigma the median absolute deviation x 1.4826 of
                                  the first chunk in which the channel varies (until then the
                                  channel's samples are stored as its offset) */
+/* How the clippers spread over the GPU.  Every choice computes the same
+ * partial sums, so the flags and outputs are identical.  By default a
+ * pipelined batch gives each beam's clipper one CTA (the clippers share the
+ * GPU with the dedispersion) and an unpipelined batch spreads beams of more
+ * than 4096 channels over a cluster of 4 CTAs (the clippers run alone). */
+#define PV_BATCH_RFI_ONE_CTA 64   /* one CTA per beam */
+#define PV_BATCH_RFI_CLUSTER8 128 /* beams of more than 1024 channels on clusters of 128-thread CTAs
+                                     (4 CTAs up to 4096 channels, 8 beyond) */
+#define PV_BATCH_RFI_CLUSTER4 0x10000 /* beams of more than 4096 channels on a cluster of 4 CTAs */
 #define PV_BATCH_VARIANTS 9            /* dedispersion tile variants (4 to 8: FP32 rings only) */
 #define PV_BATCH_VARIANT(v) ((v) << 8) /* without PV_BATCH_TUNE: tile variant 0..8 */
 #define PV_BATCH_VARIANT_OF(flags) ((((flags) >> 8) & 0xff) % PV_BATCH_VARIANTS)

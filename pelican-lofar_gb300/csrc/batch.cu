@@ -307,6 +307,18 @@ int capture(pv_batch* b) {
 
 }  // namespace
 
+// How the clippers of wide beams spread over the GPU (rfi_batch_create's
+// split).  Pipelined, the clippers share the GPU with the dedispersion,
+// whose time is what a cluster's extra SMs take: one CTA per beam.
+// Unpipelined, the clippers run alone and their longest beam sets the
+// stage's time: beams of 1024 partial sums over a cluster of 4 CTAs.
+static int rfi_split(int flags) {
+    if (flags & PV_BATCH_RFI_ONE_CTA) return 0;
+    if (flags & PV_BATCH_RFI_CLUSTER8) return 2;
+    if (flags & PV_BATCH_RFI_CLUSTER4) return 1;
+    return (flags & PV_BATCH_PIPELINED) ? 0 : 1;
+}
+
 extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, int nbeams, int flags) {
     if (!out || !configs || nbeams <= 0) {
         pv::set_error("pv_batch_create: no beams");
@@ -447,7 +459,7 @@ extern "C" int pv_batch_create(pv_batch** out, const pv_beam_config* configs, in
             nch[i] = b->beams[i]->nchan_fb;
         }
         rc = pv::rfi_batch_create(&b->rfi, hs.data(), data.data(), nsub.data(), nch.data(), nbeams,
-                                  chunk, b->d_bs, s0);
+                                  chunk, b->d_bs, rfi_split(flags), s0);
         if (rc != PV_OK) return fail(rc);
     }
     // A8: ring writes

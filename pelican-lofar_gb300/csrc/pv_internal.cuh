@@ -112,12 +112,14 @@ void dd_batch_destroy(DdBatch* b);
 
 // Batched RFI clippers (rfi.cu).
 struct RfiBatch;
-// handles[i] null: beam i has no clipper; bs: the batch's BeamStep array (inactive beams skip)
+// handles[i] null: beam i has no clipper; bs: the batch's BeamStep array (inactive beams skip);
+// split: 0 one CTA per beam; 1 beams of more than 4096 channels on a cluster of 4 CTAs;
+// 2 beams of more than 1024 channels on clusters of 128-thread CTAs
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
-                     const int* nchan, int n, int nt, const BeamStep* bs, cudaStream_t s);
+                     const int* nchan, int n, int nt, const BeamStep* bs, int split, cudaStream_t s);
 int rfi_batch_launches(const RfiBatch* b);  // number of classes (beams with one channel count), largest first
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s);
-int rfi_batch_ctas(const RfiBatch* b, int k);  // CTAs (beams) of class k
+int rfi_batch_ctas(const RfiBatch* b, int k);  // CTAs of class k (beams x CTAs per beam)
 void rfi_batch_destroy(RfiBatch* b);
 
 // Batched ring writes (buffer.cu): stokes [nt][nsub][1][nchan] of one beam.

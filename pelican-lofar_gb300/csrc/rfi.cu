@@ -3,18 +3,19 @@
 //
 // The clipper is a sequential state machine over spectra: every spectrum's
 // channel-clip margin, bandpass level and rejection test depend on running
-// averages updated by the previous spectrum.  One CTA of 256 threads walks a
-// beam's spectra in order; thread p owns channels p, p+256, ... of each
-// spectrum.  The state (running mean/RMS, their history rings, the last good
-// spectrum, the bandpass offset) lives in device memory between calls, so a
-// stream of chunks gives the same result as one long chunk.
+// averages updated by the previous spectrum.  One CTA, or for a wide beam a
+// cluster of CTAs, walks a beam's spectra in order; partial p (P = 256, 512
+// or 1024 by channel count) owns channels p, p+P, ... of each spectrum.  The
+// state (running mean/RMS, their history rings, the last good spectrum, the
+// bandpass offset) lives in device memory between calls, so a stream of
+// chunks gives the same result as one long chunk.
 //
 // Arithmetic.  This is the FP64 variant of the reference: per-spectrum
 // statistics and running averages are double, channel values and the
 // bandpass are float as in the reference.  Channel sums use a fixed order
-// (thread p's sequential partial, a halving tree of offsets 16..1 inside each
-// warp, then offsets 4, 2, 1 over the 8 warp sums) so results are
-// deterministic.  Clip flags therefore match the reference's FP32 arithmetic
+// (partial p's sequential sum, a halving tree of offsets 16..1 inside each
+// warp, then offsets P/64..1 over the P/32 warp sums) so results are
+// deterministic and independent of how the partials are spread over CTAs.  Clip flags therefore match the reference's FP32 arithmetic
 // except for channels or spectra within rounding distance of a threshold.
 #include <algorithm>
 #include <cmath>
@@ -24,6 +25,8 @@
 #include <string>
 #include <tuple>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "pv_internal.cuh"
 
@@ -224,8 +227,7 @@ struct RfiBuffers {
 // Block reductions.  Every thread holds one FP32 partial per quantity (thread
 // p sums channels p, p+P, ... in order).  The canonical order reduces each
 // warp's 32 partials by the halving tree of offsets 16..1 and the NW warp
-// sums by offsets NW/2..1; thread 0 finishes the second stage and is the only
-// thread that sees the result.
+// sums by offsets NW/2..1 (warp 0, lane_tree below).
 // ---------------------------------------------------------------------------
 template <int K>
 __device__ __forceinline__ void warp_tree(float (&v)[K], float* red /*[32][K]*/) {
@@ -242,24 +244,6 @@ __device__ __forceinline__ void warp_tree(float (&v)[K], float* red /*[32][K]*/)
 #pragma unroll
         for (int k = 0; k < K; ++k) red[warp * K + k] = v[k];
 }
-// second stage, thread 0 only (after a barrier)
-template <int K>
-__device__ __forceinline__ void block_tree_finish(const float* red, float (&out)[K]) {
-    const int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        float w[32];
-        for (int g = 0; g < nw; ++g) w[g] = red[g * K + k];
-        for (int off = nw / 2; off >= 1; off >>= 1)
-            for (int l = 0; l < off; ++l) w[l] = __fadd_rn(w[l], w[l + off]);
-        out[k] = w[0];
-    }
-}
-
-__device__ __forceinline__ long long elem(int t, int bin, int p, int nsub, int npol, int nchan) {
-    const int s = bin / nchan, c = bin - s * nchan;
-    return (((long long)t * nsub + s) * npol + p) * nchan + c;
-}
 
 __device__ __forceinline__ float bp_value(const RfiConfig& cfg, const RfiBuffers& b, float params0, int i) {
     if (b.killed && b.killed[i]) return 0.0f;
@@ -271,13 +255,6 @@ __device__ __forceinline__ float bp_value(const RfiConfig& cfg, const RfiBuffers
 __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src) {
     const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem_src) : "memory");
-}
-
-// Stages spectrum t (pol 0) into buf with cp.async.
-__device__ __forceinline__ void prefetch_spectrum(float* buf, const float* data, int t, int nbins,
-                                                  int nsub, int npol, int nchan) {
-    for (int i = threadIdx.x; i < nbins; i += blockDim.x) cp_async4(buf + i, data + elem(t, i, 0, nsub, npol, nchan));
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
 // Values warp 0 derives from the scalar state and broadcasts.
@@ -306,28 +283,60 @@ struct Geo {
     }
 };
 
-// Warp-0 tree over the NW warp partials red[g*K + k] (canonical second stage);
-// every lane of warp 0 returns the total.
-__device__ __forceinline__ float warp0_tree(const float* red, int K, int k, int nw) {
+// A beam's clipper may span a cluster of C CTAs of T threads: partial p =
+// rank * T + thread, so the P = C * T partials, their channels and the
+// canonical sums are those of one CTA of P threads.  Warp 0 of every CTA
+// reads the NW = P / 32 warp partials of the whole cluster (distributed
+// shared memory) and runs the same scalar chain on them, so every CTA holds
+// the same state without a broadcast.
+template <int C, typename V>
+__device__ __forceinline__ const V* cta_buf(const V* p, int rank) {
+    if constexpr (C == 1) return p;
+    else return cooperative_groups::this_cluster().map_shared_rank(p, (unsigned)rank);
+}
+// Barrier after the warp partials are written: the whole cluster's.
+template <int C>
+__device__ __forceinline__ void partials_barrier() {
+    if constexpr (C == 1) __syncthreads();
+    else cooperative_groups::this_cluster().sync();
+}
+// Warp 0: lane g < NW takes the K partials of warp g of the cluster (the
+// loads are independent: one round trip to the other CTAs for all of them);
+// lanes from NW on take `fill`.
+template <int C, int WPC, int K, typename V>
+__device__ __forceinline__ void lane_partials(const V* buf, V (&out)[K], V fill) {
+    constexpr int NW = C * WPC;
     const int lane = threadIdx.x & 31;
-    float w = lane < nw ? red[lane * K + k] : 0.0f;
-    for (int off = nw / 2; off >= 1; off >>= 1) {
+    if (lane < NW) {
+        const V* src = cta_buf<C>(buf, lane / WPC) + (lane % WPC) * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = src[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = fill;
+    }
+}
+// The canonical second stage over the lanes' warp sums (offsets NW/2..1);
+// every lane returns the total.
+template <int NW>
+__device__ __forceinline__ float lane_tree(float w) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = NW / 2; off >= 1; off >>= 1) {
         const float o = __shfl_down_sync(0xffffffffu, w, off);
         if (lane < off) w = __fadd_rn(w, o);
     }
     return __shfl_sync(0xffffffffu, w, 0);
 }
-__device__ __forceinline__ int warp0_isum(const int* redi, int K, int k, int nw) {
-    const int lane = threadIdx.x & 31;
-    return __reduce_add_sync(0xffffffffu, lane < nw ? redi[lane * K + k] : 0);
-}
-__device__ __forceinline__ float warp0_min(const float* redm, int K, int k, int nw) {
-    const int lane = threadIdx.x & 31;
-    float m = lane < nw ? redm[lane * K + k] : 1e30f;
+__device__ __forceinline__ float lane_min(float m) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, off));
     return m;
 }
+// Shared words of the reduction buffers (one set per phase: a CTA rewrites a
+// phase's buffer only after a later cluster barrier, which every reader of
+// the previous contents has passed).
+constexpr int kRedWords = 32 * 16 * 2 + 32 + 32 * 8 + 32 * 2 + 32;
 
 // History rings of the running averages as warp 0 sees them: the newest two
 // entries and the prefetched oldest entry stay in registers.
@@ -362,20 +371,25 @@ __device__ __forceinline__ void steady_start(RfiState& st, Hist& hr, const RfiCo
 // (the spectrum, the bandpass, the last good value) never crosses threads and
 // the passes of consecutive spectra need barriers only around the block
 // reductions and warp 0's scalar work.
+template <int T, int C>
 __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers& bufs,
                                          float* __restrict__ data, int nt, const Geo& geo,
-                                         unsigned char* __restrict__ flags) {
+                                         unsigned char* __restrict__ flags, int rank) {
     extern __shared__ float sh[];
     __shared__ Bcast bc;
+    constexpr int P = T * C, WPC = T / 32;
     const int nbins = cfg.nbins, H = cfg.history;
-    const int P = blockDim.x;
-    float* bp = sh;                                      // [nbins]
-    float* specs = sh + nbins;                           // [2][nbins]
-    float* red = sh + 3 * nbins;                         // [32][16]
-    float* redm = red + 32 * 16;                         // [32][16]
-    int* redi = reinterpret_cast<int*>(redm + 32 * 16);  // [32][9]
+    const int nloc = (nbins + P - 1) / P * T;  // this CTA's channels: m * P + rank * T + tid -> m * T + tid
+    float* bp = sh;                                         // [nloc]
+    float* specs = sh + nloc;                               // [2][nloc]
+    float* red_a = sh + 3 * nloc;                           // [32][16] adaptive band sums
+    float* redm = red_a + 32 * 16;                          // [32][16] adaptive band minima
+    float* red_c = redm + 32 * 16;                          // [32] clip pass: good sum
+    int* redi_c = reinterpret_cast<int*>(red_c + 32);       // [32][8] clip pass: good per band
+    float* red_f = reinterpret_cast<float*>(redi_c + 32 * 8);  // [32][2] fill pass: sums
+    int* redi_f = reinterpret_cast<int*>(red_f + 32 * 2);   // [32] fill pass: filled
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nw = P >> 5;
+    const int tg = rank * T + tid;  // the thread's partial
     const double inv_h = 1.0 / (double)H;
     const long long spec_elems = (long long)geo.nsub * geo.npol * geo.nchan;
 
@@ -399,17 +413,17 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         }
     }
     __syncthreads();
-    for (int i = tid; i < nbins; i += P) bp[i] = bp_value(cfg, bufs, bc.params0, i);
+    for (int i = tg, li = tid; i < nbins; i += P, li += T) bp[li] = bp_value(cfg, bufs, bc.params0, i);
     auto prefetch = [&](int t) {
-        float* buf = specs + (t & 1) * nbins;
+        float* buf = specs + (t & 1) * nloc;
         const float* src = data + (long long)t * spec_elems;
-        for (int i = tid; i < nbins; i += P) cp_async4(buf + i, src + geo.off(i));
+        for (int i = tg, li = tid; i < nbins; i += P, li += T) cp_async4(buf + li, src + geo.off(i));
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
     if (nt > 0) prefetch(0);
 
     for (int t = 0; t < nt; ++t) {
-        float* spec = specs + (t & 1) * nbins;
+        float* spec = specs + (t & 1) * nloc;
         float* dst = data + (long long)t * spec_elems;
         // the spectrum's channels are this thread's own copies: no barrier needed
         if (t + 1 < nt) {
@@ -423,14 +437,14 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             float mins[16], part[16];
 #pragma unroll
             for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
-            for (int i = tid; i < nbins; i += P) {
+            for (int i = tg, li = tid; i < nbins; i += P, li += T) {
                 const int band = geo.band(i);
-                const float v = spec[i];
+                const float v = spec[li];
 #pragma unroll
                 for (int b = 0; b < 8; ++b) {
                     if (b == band) {
                         mins[b] = fminf(mins[b], v);
-                        mins[8 + b] = fminf(mins[8 + b], bp[i]);
+                        mins[8 + b] = fminf(mins[8 + b], bp[li]);
                         part[b] = __fadd_rn(part[b], v);
                         part[8 + b] = __fadd_rn(part[8 + b], __fmul_rn(v, v));
                     }
@@ -440,18 +454,21 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             for (int k = 0; k < 16; ++k)
 #pragma unroll
                 for (int off = 16; off >= 1; off >>= 1) mins[k] = fminf(mins[k], __shfl_xor_sync(0xffffffffu, mins[k], off));
-            warp_tree<16>(part, red);
+            warp_tree<16>(part, red_a);
             if (lane == 0)
 #pragma unroll
                 for (int k = 0; k < 16; ++k) redm[warp * 16 + k] = mins[k];
-            __syncthreads();
+            partials_barrier<C>();
             if (warp == 0) {
-                float dmm[8], srms = 0.0f;
+                float dmm[8], srms = 0.0f, pa[16], pm[16];
+                lane_partials<C, WPC>(red_a, pa, 0.0f);
+                lane_partials<C, WPC>(redm, pm, 1e30f);
+#pragma unroll
                 for (int b = 0; b < 8; ++b) {
-                    const float s1 = warp0_tree(red, 16, b, nw);
-                    const float s2 = warp0_tree(red, 16, 8 + b, nw);
-                    const float md = warp0_min(redm, 16, b, nw);
-                    const float mm = warp0_min(redm, 16, 8 + b, nw);
+                    const float s1 = lane_tree<C * WPC>(pa[b]);
+                    const float s2 = lane_tree<C * WPC>(pa[8 + b]);
+                    const float md = lane_min(pm[b]);
+                    const float mm = lane_min(pm[8 + b]);
                     dmm[b] = __fsub_rn(md, mm);
                     const float a = __fdiv_rn(s2, (float)geo.cpb);
                     const float m = __fdiv_rn(s1, (float)geo.cpb);
@@ -488,14 +505,14 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         int good[8];
 #pragma unroll
         for (int b = 0; b < 8; ++b) good[b] = 0;
-        for (int i = tid; i < nbins; i += P) {
-            const float v = spec[i];
-            const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[i]) > margin_f;
+        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+            const float v = spec[li];
+            const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[li]) > margin_f;
             if (clip) {
                 const float lg = bufs.last_good[i];
                 const long long o = geo.off(i);
                 for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = lg;
-                spec[i] = lg;
+                spec[li] = lg;
             } else {
                 gpart[0] = __fadd_rn(gpart[0], v);
                 const int band = geo.band(i);
@@ -504,20 +521,24 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             }
             if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
         }
-        warp_tree<1>(gpart, red);
+        warp_tree<1>(gpart, red_c);
 #pragma unroll
         for (int k = 0; k < 8; ++k) good[k] = __reduce_add_sync(0xffffffffu, good[k]);
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < 8; ++k) redi[warp * 9 + k] = good[k];
-        __syncthreads();
+            for (int k = 0; k < 8; ++k) redi_c[warp * 8 + k] = good[k];
+        partials_barrier<C>();
         // ---- warp 0: spectrum mean, history, rejection (RFI_Clipper.cpp:343-470) ----
         if (warp == 0) {
-            const float gsum = warp0_tree(red, 1, 0, nw);
+            float pc[1];
+            int pi[8];
+            lane_partials<C, WPC>(red_c, pc, 0.0f);
+            lane_partials<C, WPC>(redi_c, pi, 0);
+            const float gsum = lane_tree<C * WPC>(pc[0]);
             int gb[8], total_good = 0;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                gb[k] = warp0_isum(redi, 9, k, nw);
+                gb[k] = __reduce_add_sync(0xffffffffu, pi[k]);
                 total_good += gb[k];
             }
             st.frac_bad_channels = __fadd_rn(st.frac_bad_channels,
@@ -578,8 +599,8 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         // ---- last good spectrum, clipSample, flatten (RFI_Clipper.cpp:441-494) ----
         int filled = 0;
         float s12[2] = {0.0f, 0.0f};
-        for (int i = tid; i < nbins; i += P) {
-            float v = spec[i];
+        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+            float v = spec[li];
             if (do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
                 bufs.last_good[i] = v;
                 ++filled;
@@ -590,20 +611,24 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 v = -0.2f;
                 if (flags) flags[(long long)t * nbins + i] |= 2;
             }
-            v = __fsub_rn(v, __fadd_rn(bp[i], dm_f));
-            spec[i] = v;
+            v = __fsub_rn(v, __fadd_rn(bp[li], dm_f));
+            spec[li] = v;
             s12[0] = __fadd_rn(s12[0], v);
             s12[1] = __fadd_rn(s12[1], __fmul_rn(v, v));
         }
-        warp_tree<2>(s12, red);
+        warp_tree<2>(s12, red_f);
         filled = __reduce_add_sync(0xffffffffu, filled);
-        if (lane == 0) redi[warp * 9 + 8] = filled;
-        __syncthreads();
+        if (lane == 0) redi_f[warp] = filled;
+        partials_barrier<C>();
         // ---- warp 0: normalisation constants, statistics, bandpass, next start ----
         if (warp == 0) {
-            const float s1 = warp0_tree(red, 2, 0, nw);
-            const float s2 = warp0_tree(red, 2, 1, nw);
-            st.remaining_zeros -= warp0_isum(redi, 9, 8, nw);
+            float pf[2];
+            int pz[1];
+            lane_partials<C, WPC>(red_f, pf, 0.0f);
+            lane_partials<C, WPC>(redi_f, pz, 0);
+            const float s1 = lane_tree<C * WPC>(pf[0]);
+            const float s2 = lane_tree<C * WPC>(pf[1]);
+            st.remaining_zeros -= __reduce_add_sync(0xffffffffu, pz[0]);
             const float m = __fdiv_rn(s1, (float)nbins);
             const float ms = __fdiv_rn(s2, (float)nbins);
             float srms = __fsqrt_rn(__fsub_rn(ms, __fmul_rn(m, m)));
@@ -654,25 +679,27 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         const float sub_f = bc.sub_f, rms_f = bc.rms_f;
         const bool rebuild = bc.rebuild_bp != 0;
         const float p0 = bc.params0;
-        for (int i = tid; i < nbins; i += P) {
-            float v = spec[i];
+        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+            float v = spec[li];
             if (!spectrum_clip) {
                 v = __fdiv_rn(__fsub_rn(v, sub_f), rms_f);
                 if (v > cfg.cr) v = 0.0f;
             }
             dst[geo.off(i)] = v;
-            if (rebuild) bp[i] = bp_value(cfg, bufs, p0, i);
+            if (rebuild) bp[li] = bp_value(cfg, bufs, p0, i);
         }
     }
-    if (tid == 0) *bufs.state = st;
+    if (tid == 0) *bufs.state = st;  // every CTA of a cluster holds the same state
+    if constexpr (C > 1) cooperative_groups::this_cluster().sync();  // no CTA leaves while others read it
 }
 
-// MAXT is the block size (the partial count), which sets the register budget.
-template <int MAXT>
-__global__ void __launch_bounds__(MAXT, 1)
+// T threads per CTA (which sets the register budget), C CTAs per beam (a
+// cluster); T * C is the partial count.
+template <int T, int C>
+__global__ void __launch_bounds__(T, 1)
 rfi_kernel(RfiConfig cfg, RfiBuffers bufs, float* __restrict__ data, int nt, Geo geo,
            unsigned char* __restrict__ flags) {
-    rfi_body(cfg, bufs, data, nt, geo, flags);
+    rfi_body<T, C>(cfg, bufs, data, nt, geo, flags, C > 1 ? (int)cooperative_groups::this_cluster().block_rank() : 0);
 }
 
 // One beam's clipper in a batched launch.
@@ -686,59 +713,104 @@ struct RfiJob {
     int beam;  // index into the batch's BeamStep array
 };
 
-// The clippers of many beams at once: CTA b runs job b (every job of a launch
-// has the same partial count, the block size); beams without a chunk this
-// step return at once.
-template <int MAXT>
-__global__ void __launch_bounds__(MAXT, 1) rfi_batch_kernel(const RfiJob* __restrict__ jobs,
-                                                            const pv::BeamStep* __restrict__ bs) {
-    if (bs && !bs[jobs[blockIdx.x].beam].active) return;
-    const RfiConfig cfg = jobs[blockIdx.x].cfg;
-    const RfiBuffers bufs = jobs[blockIdx.x].bufs;
-    const Geo geo = jobs[blockIdx.x].geo;
-    rfi_body(cfg, bufs, jobs[blockIdx.x].data, jobs[blockIdx.x].nt, geo, jobs[blockIdx.x].flags);
+// The clippers of many beams at once: cluster b (CTAs b*C .. b*C+C-1) runs
+// job b (every job of a launch has the same partial count); beams without a
+// chunk this step return at once.
+template <int T, int C>
+__global__ void __launch_bounds__(T, 1) rfi_batch_kernel(const RfiJob* __restrict__ jobs,
+                                                         const pv::BeamStep* __restrict__ bs) {
+    const int job = blockIdx.x / C;
+    if (bs && !bs[jobs[job].beam].active) return;  // the whole cluster returns
+    const RfiConfig cfg = jobs[job].cfg;
+    const RfiBuffers bufs = jobs[job].bufs;
+    const Geo geo = jobs[job].geo;
+    rfi_body<T, C>(cfg, bufs, jobs[job].data, jobs[job].nt, geo, jobs[job].flags, (int)(blockIdx.x % C));
 }
 
-size_t rfi_smem_bytes(int nbins) {
-    return sizeof(float) * (3 * (size_t)nbins) + sizeof(float) * 32 * 16 * 2 + sizeof(int) * 32 * 9;
+// Threads per CTA and CTAs per beam for a partial count.  split 0: one CTA
+// of `parts` threads; 1: beams of 1024 partials on a cluster of 4 CTAs of
+// 256 threads; 2: beams of 512 or 1024 partials on clusters of 128-thread
+// CTAs (4 or 8).  The partials, and so every sum, are the same.
+void rfi_shape(int parts, int split, int* threads, int* ctas) {
+    *threads = parts;
+    *ctas = 1;
+    if (split == 1 && parts == 1024) {
+        *threads = 256;
+        *ctas = 4;
+    } else if (split == 2 && parts >= 512) {
+        *threads = 128;
+        *ctas = parts / 128;
+    }
 }
 
-// Sets the shared-memory attribute of both kernels of a block size and
-// launches one of them: jobs != null selects the batched kernel.
-template <int MAXT>
+size_t rfi_smem_bytes(int nbins, int parts, int threads) {
+    const size_t nloc = (size_t)((nbins + parts - 1) / parts) * threads;
+    return sizeof(float) * (3 * nloc + kRedWords);
+}
+
+template <typename K>
+int rfi_set_smem(K kern, size_t smem) {
+    size_t limit = 0;
+    PV_CUDA(pv::allow_max_dynamic_smem(kern, &limit), "cudaFuncSetAttribute(rfi)");
+    if (smem > limit) {
+        pv::set_error("RFI_Clipper: %zu bytes of shared memory exceed one CTA's %zu", smem, limit);
+        return PV_ERR_ARG;
+    }
+    return PV_OK;
+}
+
+template <typename K, typename... Args>
+int rfi_launch_ex(K kern, int clusters, int C, int T, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)(clusters * C));
+    lc.blockDim = dim3((unsigned)T);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.attrs = at;
+    lc.numAttrs = C > 1 ? 1 : 0;
+    PV_CUDA(cudaLaunchKernelEx(&lc, kern, args...), "launch RFI clipper");
+    return PV_OK;
+}
+
+// Sets the shared-memory attribute of both kernels of a shape and launches
+// one of them: jobs != null selects the batched kernel (nblocks jobs;
+// nblocks == 0: the attribute only, before any stream capture).
+template <int T, int C>
 int rfi_launch_t(size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamStep* bs,
                  const RfiConfig& cfg, const RfiBuffers& bufs, float* data, int nt, const Geo& geo,
                  unsigned char* flags, cudaStream_t s) {
     if (jobs) {
-        if (nblocks == 0) {  // set-up call: the attribute only, before any stream capture
-            size_t limit = 0;
-            PV_CUDA(pv::allow_max_dynamic_smem(rfi_batch_kernel<MAXT>, &limit), "cudaFuncSetAttribute(rfi batch)");
-            if (smem > limit) {
-                pv::set_error("RFI_Clipper: %zu bytes of shared memory exceed one CTA's %zu", smem, limit);
-                return PV_ERR_ARG;
-            }
-            return PV_OK;
-        }
-        rfi_batch_kernel<MAXT><<<nblocks, MAXT, smem, s>>>(jobs, bs);
+        if (nblocks == 0) return rfi_set_smem(rfi_batch_kernel<T, C>, smem);
+        PV_TRY(rfi_launch_ex(rfi_batch_kernel<T, C>, nblocks, C, T, smem, s, jobs, bs));
         return pv::check_launch("rfi_batch_kernel");
     }
-    PV_CUDA(cudaFuncSetAttribute(rfi_kernel<MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem), "cudaFuncSetAttribute(rfi)");
-    rfi_kernel<MAXT><<<1, MAXT, smem, s>>>(cfg, bufs, data, nt, geo, flags);
+    PV_TRY(rfi_set_smem(rfi_kernel<T, C>, smem));
+    PV_TRY(rfi_launch_ex(rfi_kernel<T, C>, 1, C, T, smem, s, cfg, bufs, data, nt, geo, flags));
     return pv::check_launch("rfi_kernel");
 }
 
-int rfi_launch(int parts, size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamStep* bs,
+int rfi_launch(int parts, int split, size_t smem, int nblocks, const RfiJob* jobs, const pv::BeamStep* bs,
                const RfiConfig& cfg, const RfiBuffers& bufs, float* data, int nt, const Geo& geo,
                unsigned char* flags, cudaStream_t s) {
-    switch (parts) {
-        case 256: return rfi_launch_t<256>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
-        case 512: return rfi_launch_t<512>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
-        case 1024: return rfi_launch_t<1024>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
-        default:
-            pv::set_error("RFI_Clipper: no kernel for %d partial sums", parts);
-            return PV_ERR_ARG;
-    }
+    int T = 0, C = 0;
+    rfi_shape(parts, split, &T, &C);
+#define PV_RFI_SHAPE(TT, CC)                                                                          \
+    if (T == TT && C == CC)                                                                          \
+        return rfi_launch_t<TT, CC>(smem, nblocks, jobs, bs, cfg, bufs, data, nt, geo, flags, s);
+    PV_RFI_SHAPE(256, 1)
+    PV_RFI_SHAPE(512, 1)
+    PV_RFI_SHAPE(1024, 1)
+    PV_RFI_SHAPE(256, 4)
+    PV_RFI_SHAPE(128, 4)
+    PV_RFI_SHAPE(128, 8)
+#undef PV_RFI_SHAPE
+    pv::set_error("RFI_Clipper: no kernel for %d partial sums", parts);
+    return PV_ERR_ARG;
 }
 
 }  // namespace
@@ -750,6 +822,7 @@ struct pv_rfi {
     Bandpass bp;
     float cr = 10.0f, sr = 4.0f;
     int history = 10, zero_dming = 0, use_mor = 1, band_matching = 0, active = 1;
+    int split = 1;  // rfi_shape's split of a wide beam over a cluster
     float start_freq = 0.0f, end_freq = 0.0f;
     int nbins = 0;
     RfiConfig cfg{};
@@ -906,15 +979,18 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
     const int nbins = nsub * nchan;
     PV_TRY(setup(h, nbins, s));
     if (nt == 0) return PV_OK;
-    const int threads = pv_rfi_parts(nbins);
-    const size_t smem = rfi_smem_bytes(nbins);
+    // A wide beam alone spreads its channels over a cluster of CTAs.
+    const int parts = pv_rfi_parts(nbins);
+    int T = 0, C = 0;
+    rfi_shape(parts, h->split, &T, &C);
+    const size_t smem = rfi_smem_bytes(nbins, parts, T);
     if (smem > 227 * 1024) {
-        pv::set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
+        pv::set_error("RFI_Clipper: %d channels exceed the shared memory of %d CTAs", nbins, C);
         return PV_ERR_ARG;
     }
     Geo geo{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1,
             nbins / 8};
-    return rfi_launch(threads, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
+    return rfi_launch(parts, h->split, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
 // Back to the state of a clipper that has seen no spectrum (the running
@@ -957,6 +1033,15 @@ int pv::rfi_state_io(pv_rfi* h, int nbins, void* h_buf, bool save, cudaStream_t 
             PV_CUDA(cudaMemcpyAsync(q.dev, p, q.bytes, cudaMemcpyHostToDevice, s), "load RFI state");
         p += q.bytes;
     }
+    return PV_OK;
+}
+
+extern "C" int pv_rfi_set_split(pv_rfi* h, int split) {
+    if (!h || split < 0 || split > 2) {
+        pv::set_error("pv_rfi_set_split: split must be 0, 1 or 2");
+        return PV_ERR_ARG;
+    }
+    h->split = split;
     return PV_OK;
 }
 
@@ -1032,13 +1117,14 @@ namespace pv {
 
 struct RfiBatch {
     struct Class {
-        int parts = 0, nbins = 0;
+        int parts = 0, nbins = 0, threads = 0, ctas = 1;  // ctas: CTAs (a cluster) per beam
         size_t smem = 0;
         RfiJob* d_jobs = nullptr;
         int njobs = 0;
     };
     std::vector<Class> classes;
     const BeamStep* bs = nullptr;
+    int split = 1;
 };
 
 void rfi_batch_destroy(RfiBatch* b) {
@@ -1049,31 +1135,36 @@ void rfi_batch_destroy(RfiBatch* b) {
 }
 
 int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data, const int* nsub,
-                     const int* nchan, int n, int nt, const BeamStep* bs, cudaStream_t s) {
+                     const int* nchan, int n, int nt, const BeamStep* bs, int split, cudaStream_t s) {
     auto* b = new RfiBatch;
     b->bs = bs;
+    b->split = split;
     std::vector<std::vector<RfiJob>> jobs;
     for (int i = 0; i < n; ++i) {
         pv_rfi* h = handles[i];
         if (!h || !h->active) continue;
         const int nbins = nsub[i] * nchan[i];
         int rc = setup(h, nbins, s);
-        const size_t smem = rfi_smem_bytes(nbins);
+        const int parts = pv_rfi_parts(nbins);
+        int T = 0, C = 0;
+        rfi_shape(parts, split, &T, &C);
+        const size_t smem = rfi_smem_bytes(nbins, parts, T);
         if (rc == PV_OK && smem > 227 * 1024) {
-            set_error("RFI_Clipper: %d channels exceed one CTA's shared memory", nbins);
+            set_error("RFI_Clipper: %d channels exceed the shared memory of %d CTAs", nbins, C);
             rc = PV_ERR_ARG;
         }
         if (rc != PV_OK) {
             rfi_batch_destroy(b);
             return rc;
         }
-        const int parts = pv_rfi_parts(nbins);
         size_t k = 0;
         while (k < b->classes.size() && b->classes[k].nbins != nbins) ++k;
         if (k == b->classes.size()) {
             b->classes.emplace_back();
             b->classes[k].parts = parts;
             b->classes[k].nbins = nbins;
+            b->classes[k].threads = T;
+            b->classes[k].ctas = C;
             jobs.emplace_back();
         }
         b->classes[k].smem = std::max(b->classes[k].smem, smem);
@@ -1112,7 +1203,7 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         int rc = e == cudaSuccess ? PV_OK : cuda_status(e, "RFI batch jobs");
         // set the kernel attribute now, outside any stream capture
         if (rc == PV_OK)
-            rc = rfi_launch(c.parts, c.smem, 0, c.d_jobs, nullptr, RfiConfig{}, RfiBuffers{}, nullptr, 0,
+            rc = rfi_launch(c.parts, b->split, c.smem, 0, c.d_jobs, nullptr, RfiConfig{}, RfiBuffers{}, nullptr, 0,
                             Geo{}, nullptr, s);
         if (rc != PV_OK) {
             rfi_batch_destroy(b);
@@ -1125,12 +1216,12 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
 
 int rfi_batch_launches(const RfiBatch* b) { return (int)b->classes.size(); }
 
-int rfi_batch_ctas(const RfiBatch* b, int k) { return b->classes[k].njobs; }
+int rfi_batch_ctas(const RfiBatch* b, int k) { return b->classes[k].njobs * b->classes[k].ctas; }
 
 int rfi_batch_launch_one(RfiBatch* b, int k, cudaStream_t s) {
     auto& c = b->classes[k];
     if (c.njobs == 0) return PV_OK;
-    return rfi_launch(c.parts, c.smem, c.njobs, c.d_jobs, b->bs, RfiConfig{}, RfiBuffers{}, nullptr, 0,
+    return rfi_launch(c.parts, b->split, c.smem, c.njobs, c.d_jobs, b->bs, RfiConfig{}, RfiBuffers{}, nullptr, 0,
                       Geo{}, nullptr, s);
 }
 

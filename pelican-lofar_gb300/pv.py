@@ -384,11 +384,13 @@ class RFI:
     """Device RFI_Clipper."""
 
     def __init__(self, bp_text, cr=10.0, sr=4.0, history=10, zero_dming=False, mean_over_rms=True,
-                 band_matching=True, active=True):
+                 band_matching=True, active=True, split=None):
         self.h = C.c_void_p()
         check(load().pv_rfi_create(C.byref(self.h), bp_text.encode() if bp_text else None, cr, sr,
                                    history, int(zero_dming), int(mean_over_rms), int(band_matching),
                                    int(active)))
+        if split is not None:  # 0 one CTA, 1 wide bands over 4 CTAs, 2 over clusters of 128-thread CTAs
+            check(load().pv_rfi_set_split(self.h, int(split)))
 
     def run(self, d_data, flags=False, stream=None):
         import torch
@@ -511,6 +513,9 @@ class Beam:
 
 BATCH_TUNE, BATCH_GRAPH, BATCH_TIMING, BATCH_PIPELINED = 1, 2, 4, 8
 BATCH_VARIANTS = 9  # PV_BATCH_VARIANTS: dedispersion tile variants
+BATCH_RFI_ONE_CTA = 64  # PV_BATCH_RFI_ONE_CTA: every clipper on one CTA
+BATCH_RFI_CLUSTER8 = 128  # PV_BATCH_RFI_CLUSTER8: clusters of 128-thread CTAs
+BATCH_RFI_CLUSTER4 = 0x10000  # PV_BATCH_RFI_CLUSTER4: beams of 1024 partials on 4 CTAs
 
 class UdpConfig(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("fixed_size_packets", "sample_bits", "packets_per_chunk",
@@ -793,13 +798,16 @@ def batch_footprint(cfg, pipelined=True, store="f32"):
 class Batch:
     """Many beams advanced one chunk per step by batched launches (pv_batch)."""
 
-    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0, pipelined=False, store="f32"):
+    def __init__(self, cfgs, tune=True, graph=True, timing=False, variant=0, pipelined=False, store="f32",
+                 rfi_one_cta=False, rfi_cluster8=False, rfi_cluster4=False):
         self.cfgs = list(cfgs)
         self.pipelined = pipelined
         self.store = store
         self._arr = (BeamConfig * len(self.cfgs))(*self.cfgs)
         flags = (BATCH_TUNE if tune else (variant << 8)) | (BATCH_GRAPH if graph else 0) | \
-            (BATCH_TIMING if timing else 0) | (BATCH_PIPELINED if pipelined else 0) | BATCH_STORE[store]
+            (BATCH_TIMING if timing else 0) | (BATCH_PIPELINED if pipelined else 0) | BATCH_STORE[store] | \
+            (BATCH_RFI_ONE_CTA if rfi_one_cta else 0) | (BATCH_RFI_CLUSTER8 if rfi_cluster8 else 0) | \
+            (BATCH_RFI_CLUSTER4 if rfi_cluster4 else 0)
         self.h = C.c_void_p()
         check(load().pv_batch_create(C.byref(self.h), self._arr, len(self.cfgs), flags))
 

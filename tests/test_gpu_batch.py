@@ -80,14 +80,16 @@ def test_batch_with_two_clipper_classes_equals_beams_alone(pv, cuda, mix_configs
     _compare_with_beams_alone(pv, cuda, mix_configs[:2] + [big], False, True, 0, False, pipelined)
 
 
-def _compare_with_beams_alone(pv, cuda, mix, tune, graph, variant, prefilled, pipelined, wide_spread=False):
+def _compare_with_beams_alone(pv, cuda, mix, tune, graph, variant, prefilled, pipelined, wide_spread=False,
+                              rfi_one_cta=False, rfi_cluster8=False, rfi_cluster4=False):
     import torch
     cfgs = mix
     if prefilled:  # rings start as lag chunks of silence: windows from the first chunk on
         cfgs = [type(c).from_buffer_copy(c) for c in cfgs]
         for c, o in zip(cfgs, mix):
             c._bp, c.bp_text, c.prefilled = o._bp, o._bp, 1
-    batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant, pipelined=pipelined)
+    batch = pv.Batch(cfgs, tune=tune, graph=graph, variant=variant, pipelined=pipelined, rfi_one_cta=rfi_one_cta,
+                     rfi_cluster8=rfi_cluster8, rfi_cluster4=rfi_cluster4)
     alone = [pv.Beam(c) for c in cfgs]
     lags = [batch.info(i)["lag"] for i in range(len(cfgs))]
     assert lags == [b.info()["lag"] for b in alone]
@@ -137,6 +139,24 @@ def _compare_with_beams_alone(pv, cuda, mix, tune, graph, variant, prefilled, pi
     if prefilled:
         assert compared == len(cfgs) * (max(lags) + 3)
     assert events_seen > 0
+
+
+@pytest.mark.parametrize("pipelined,one_cta,cluster8,cluster4", [(False, True, False, False),
+                                                                (True, False, True, False),
+                                                                (False, False, False, False),
+                                                                (True, False, False, True)])
+def test_batch_clipper_shapes_equal_beams_alone(pv, cuda, mix_configs, pipelined, one_cta, cluster8, cluster4):
+    """Beams of 1280 and 5120 channels (512 and 1024 partial sums): their
+    batched clippers on one CTA each, on clusters of 128-thread CTAs, or the
+    5120-channel beam on 4 CTAs give the same filterbanks, windows and events
+    as the beams alone (the same partial sums in the same order whatever the
+    CTAs)."""
+    rng = np.random.default_rng(98)
+    big = calibrated(pv, cuda, beam_kw(40, 32, 24, 0.05), rng)    # 1280 channels
+    wide = calibrated(pv, cuda, beam_kw(80, 64, 16, 0.02), rng)   # 5120 channels
+    assert pv.load().pv_rfi_parts(5120) == 1024 and pv.load().pv_rfi_parts(1280) == 512
+    _compare_with_beams_alone(pv, cuda, mix_configs[:1] + [big, wide], False, True, 0, False, pipelined,
+                              rfi_one_cta=one_cta, rfi_cluster8=cluster8, rfi_cluster4=cluster4)
 
 
 def test_batch_autotuner_times_the_variants(pv, cuda, mix_configs):

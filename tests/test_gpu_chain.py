@@ -153,9 +153,12 @@ def test_rfi_four_stokes_clips_all_polarisations(pv, oracle, cuda):
 
 
 
+@pytest.mark.parametrize("split", [0, 1, 2])
 @pytest.mark.parametrize("nsub,nchan", [(128, 16), (96, 64)])
-def test_rfi_wide_bands_bit_exact(pv, oracle, cuda, nsub, nchan):
-    """2048 and 6144 channels: 512 and 1024 partial sums per reduction."""
+def test_rfi_wide_bands_bit_exact(pv, oracle, cuda, nsub, nchan, split):
+    """2048 and 6144 channels: 512 and 1024 partial sums per reduction, on
+    one CTA (split 0) or spread over a cluster of CTAs (1: 4 x 256 threads
+    for 1024 partials; 2: 4 or 8 x 128 threads)."""
     import torch
     rng = np.random.default_rng(nsub)
     nt = 1250
@@ -164,10 +167,28 @@ def test_rfi_wide_bands_bit_exact(pv, oracle, cuda, nsub, nchan):
     bp = make_bp_text(nbins, BP_START, BP_WIDTH, 1000.0, 50.0)
     parts = pv.load().pv_rfi_parts(nbins)
     assert parts == (512 if nbins <= 4096 else 1024)
-    g = pv.RFI(bp, cr=5.0, history=1100)
+    g = pv.RFI(bp, cr=5.0, history=1100, split=split)
     o = oracle.RFI(bp, cr=5.0, history=1100, mode=1, parts=parts)
     dd = torch.from_numpy(np.ascontiguousarray(data)).to(cuda)
     gf = g.run(dd, flags=True).cpu().numpy()
     d = np.ascontiguousarray(data)
     of = o.run(d, flags=True)
     assert np.array_equal(gf, of) and np.array_equal(dd.cpu().numpy(), d)
+
+
+def test_rfi_cluster_four_stokes_bit_exact(pv, oracle, cuda):
+    """6144 channels of four Stokes parameters over a cluster of 8 CTAs: every
+    polarisation of a clipped channel and spectrum is replaced."""
+    import torch
+    rng = np.random.default_rng(5)
+    nt, nsub, nchan = 1100, 96, 64
+    I = stokes_filterbank(rng, nt, nsub, nchan)
+    data = np.ascontiguousarray(np.concatenate([I, I * 0.1, I * 0.2, I * -0.3], axis=2))
+    bp = make_bp_text(nsub * nchan, BP_START, BP_WIDTH, 1000.0, 50.0)
+    parts = pv.load().pv_rfi_parts(nsub * nchan)
+    g = pv.RFI(bp, cr=5.0, history=1050, split=2)
+    o = oracle.RFI(bp, cr=5.0, history=1050, mode=1, parts=parts)
+    dd = torch.from_numpy(data).to(cuda)
+    gf = g.run(dd, flags=True).cpu().numpy()
+    of = o.run(data, flags=True)
+    assert np.array_equal(gf, of) and np.array_equal(dd.cpu().numpy(), data)
