@@ -257,6 +257,9 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem_src) : "memory");
 }
 
+// Ring index x in [0, 2H) reduced to [0, H).
+__device__ __forceinline__ int wrap_h(int x, int H) { return x >= H ? x - H : x; }
+
 // Values warp 0 derives from the scalar state and broadcasts.
 struct Bcast {
     float dm_f, margin_f;        // for the next clip pass
@@ -269,6 +272,10 @@ struct Bcast {
 struct Geo {
     int nsub, npol, nchan, lg_nchan;  // lg_nchan < 0: nchan is not a power of two
     int cpb;
+    // RFI_Clipper.cpp:383-394 compares good-channel counts with 0.8 * cpb and
+    // 0.8 * nbins in double: for an integer count n, n < x exactly when
+    // n < ceil(x), so the thresholds are these integers.
+    int band_good_min, good_min;
     __device__ __forceinline__ long long off(int bin) const {
         int sb, c;
         if (lg_nchan >= 0) { sb = bin >> lg_nchan; c = bin & (nchan - 1); }
@@ -282,6 +289,14 @@ struct Geo {
         return b;
     }
 };
+
+Geo make_geo(int nsub, int npol, int nchan) {
+    const int nbins = nsub * nchan;
+    Geo g{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1, nbins / 8, 0, 0};
+    g.band_good_min = (int)std::ceil(0.8 * g.cpb);
+    g.good_min = (int)std::ceil(0.8 * nbins);
+    return g;
+}
 
 // A beam's clipper may span a cluster of C CTAs of T threads: partial p =
 // rank * T + thread, so the P = C * T partials, their channels and the
@@ -355,7 +370,7 @@ __device__ __forceinline__ void steady_start(RfiState& st, Hist& hr, const RfiCo
     st.rms_run = st.rms_run + hr.last * inv_h;
     const double spectrum_rms = cfg.use_mor ? fabs(st.mean_run * st.inv_mor) : st.rms_carry;
     if (lane == 0) bufs.rms_buf[st.rms_head] = spectrum_rms;  // full: overwrite the oldest
-    st.rms_head = (st.rms_head + 1) % H;
+    st.rms_head = wrap_h(st.rms_head + 1, H);
     hr.prev = hr.last;
     hr.last = spectrum_rms;
     hr.front = bufs.rms_buf[st.rms_head];  // oldest entry for the spectrum after next
@@ -378,6 +393,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
     extern __shared__ float sh[];
     __shared__ Bcast bc;
     constexpr int P = T * C, WPC = T / 32;
+    constexpr int UR = T >= 1024 ? 1 : 4;  // channel loops unrolled where registers allow
     const int nbins = cfg.nbins, H = cfg.history;
     const int nloc = (nbins + P - 1) / P * T;  // this CTA's channels: m * P + rank * T + tid -> m * T + tid
     float* bp = sh;                                         // [nloc]
@@ -437,6 +453,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             float mins[16], part[16];
 #pragma unroll
             for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
+#pragma unroll UR
             for (int i = tg, li = tid; i < nbins; i += P, li += T) {
                 const int band = geo.band(i);
                 const float v = spec[li];
@@ -479,7 +496,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                     for (int j = i; j > 0 && dmm[j - 1] > dmm[j]; --j) {
                         const float x = dmm[j]; dmm[j] = dmm[j - 1]; dmm[j - 1] = x;
                     }
-                const int pos = (st.rms_head + st.rms_size) % H;
+                const int pos = wrap_h(st.rms_head + st.rms_size, H);
                 if (lane == 0) bufs.rms_buf[pos] = (double)srms;
                 st.rms_acc_prev = st.rms_acc;
                 st.rms_acc = st.rms_acc + (double)srms;
@@ -505,6 +522,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         int good[8];
 #pragma unroll
         for (int b = 0; b < 8; ++b) good[b] = 0;
+#pragma unroll UR
         for (int i = tg, li = tid; i < nbins; i += P, li += T) {
             const float v = spec[li];
             const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[li]) > margin_f;
@@ -547,12 +565,12 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             int bad_bands = 0;
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                if ((double)gb[b] < 0.8 * geo.cpb) ++bad_bands;
+                if (gb[b] < geo.band_good_min) ++bad_bands;
                 if (gb[b] == 0) bad_bands += 4;
             }
-            if ((double)total_good < 0.8 * nbins) bad_bands += 4;
+            if (total_good < geo.good_min) bad_bands += 4;
             if (st.mean_size < H) {
-                const int pos = (st.mean_head + st.mean_size) % H;
+                const int pos = wrap_h(st.mean_head + st.mean_size, H);
                 if (lane == 0) bufs.mean_buf[pos] = (double)spectrum_sum;
                 st.mean_acc_prev = st.mean_acc;
                 st.mean_acc = st.mean_acc + (double)spectrum_sum;
@@ -562,7 +580,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 st.mean_run = st.mean_run - hm.front * inv_h;
                 st.mean_run = st.mean_run + hm.last * inv_h;
                 if (lane == 0) bufs.mean_buf[st.mean_head] = (double)spectrum_sum;
-                st.mean_head = (st.mean_head + 1) % H;
+                st.mean_head = wrap_h(st.mean_head + 1, H);
             }
             hm.prev = hm.last;
             hm.last = (double)spectrum_sum;
@@ -574,8 +592,8 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 sclip = 1;
                 st.bad_spectra += 1;
                 // pop_back + push_back(back()): the newest entry takes the previous one's value
-                const int mlast = (st.mean_head + st.mean_size - 1) % H;
-                const int rlast = (st.rms_head + st.rms_size - 1) % H;
+                const int mlast = wrap_h(st.mean_head + st.mean_size - 1, H);
+                const int rlast = wrap_h(st.rms_head + st.rms_size - 1, H);
                 if (lane == 0) {
                     bufs.mean_buf[mlast] = hm.prev;
                     bufs.rms_buf[rlast] = hr.prev;
@@ -599,6 +617,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         // ---- last good spectrum, clipSample, flatten (RFI_Clipper.cpp:441-494) ----
         int filled = 0;
         float s12[2] = {0.0f, 0.0f};
+#pragma unroll UR
         for (int i = tg, li = tid; i < nbins; i += P, li += T) {
             float v = spec[li];
             if (do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
@@ -679,6 +698,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         const float sub_f = bc.sub_f, rms_f = bc.rms_f;
         const bool rebuild = bc.rebuild_bp != 0;
         const float p0 = bc.params0;
+#pragma unroll UR
         for (int i = tg, li = tid; i < nbins; i += P, li += T) {
             float v = spec[li];
             if (!spectrum_clip) {
@@ -988,8 +1008,7 @@ extern "C" int pv_rfi_run(pv_rfi* h, float* d_data, int nt, int nsub, int npol, 
         pv::set_error("RFI_Clipper: %d channels exceed the shared memory of %d CTAs", nbins, C);
         return PV_ERR_ARG;
     }
-    Geo geo{nsub, npol, nchan, (nchan & (nchan - 1)) == 0 ? __builtin_ctz((unsigned)nchan) : -1,
-            nbins / 8};
+    const Geo geo = make_geo(nsub, npol, nchan);
     return rfi_launch(parts, h->split, smem, 1, nullptr, nullptr, h->cfg, h->dev, d_data, nt, geo, d_flags, s);
 }
 
@@ -1173,8 +1192,7 @@ int rfi_batch_create(RfiBatch** out, pv_rfi* const* handles, float* const* data,
         j.bufs = h->dev;
         j.data = data[i];
         j.flags = nullptr;
-        j.geo = Geo{nsub[i], 1, nchan[i],
-                    (nchan[i] & (nchan[i] - 1)) == 0 ? __builtin_ctz((unsigned)nchan[i]) : -1, nbins / 8};
+        j.geo = make_geo(nsub[i], 1, nchan[i]);
         j.nt = nt;
         j.beam = i;
         jobs[k].push_back(j);
