@@ -439,11 +439,8 @@ def run_pv(args, cfg):
             "e2e": {"value": e2e_value, "unit": "DM-trial*chan*samples/s",
                     "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms / args.steps,
-                    "h2d_alone_gbs": h2d_alone_gbs,
-                    "h2d_alone_ms_per_step": in_bytes / h2d_alone_gbs / 1e6,
-                    "what": "voltages copied from page-locked host buffers on the "
-                            "batch's copy stream while the previous step computes; events of the "
-                            "previous step read meanwhile"},
+                    "what": "pv_beam_process_host: each chunk's voltages copied from a page-locked "
+                            "host buffer, then its events read back to the host"},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline,
             "roofline_channeliser": roofline_chan,
             "stage_ms": st,
