@@ -55,9 +55,10 @@ import numpy as np
 
 SUB_BW = 0.1953125  # MHz
 RAW_TSAMP = 5.12e-6  # s
-# DRAM bytes per FP32 add of dedisperse_batch_kernel: 1.776 GB for 5.12e10 adds, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) on the first 3 beams with 1024-sample chunks
-DD_BATCH_BYTES_PER_ADD = 1.776e9 / 5.1204063232e10
+# DRAM bytes per FP32 add of the batched dedispersion (dedisperse_pair_kernel, tile variant 7):
+# 4.364 GB for 2.048e11 adds, measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
+# first 3 beams of the mix with 4096-sample chunks
+DD_BATCH_BYTES_PER_ADD = 4.3636e9 / 2.04816252928e11
 
 
 def dd_kernel_name(variant):
@@ -694,7 +695,8 @@ def run_batch(args, cfgs, workload):
                               "the kernel reads smem_words_per_add words per add on this workload",
                 "traffic": DD_BATCH_BYTES_PER_ADD * units_step,
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
-                                  "on the 3-beam, 1024-sample case, scaled by adds",
+                                  "of tile variant 7 on the mix's first 3 beams with 4096-sample "
+                                  "chunks, scaled by adds",
                 "peak_source": "%d SMs x 128 FP32 lanes x sm_max_mhz of MEASURED_PEAKS.json (%s)"
                                % (nsm, peak_src),
                 "per_unit": "one FP32 add per DM-trial*channel*sample (%d per launch)" % units_step,
