@@ -248,9 +248,12 @@ int pv_window_from_name(const char* name);
 int pv_fir_coefficients(int ntaps, int nchan, int window, double* h_coeffs);
 
 /* A channeliser with its per-(subband, polarisation) tap history on the
- * device.  nchan (outputChannelsPerSubband) must be a power of two in
- * 2..1024.  h_coeffs [ntaps][nchan] float, or NULL to design them for
- * `window` as the reference does (then converted to float). */
+ * device.  nchan (outputChannelsPerSubband) is 1 or even, up to 1024
+ * (PPFChanneliser.cpp:42-44): powers of two take a radix-2 FFT, other even
+ * counts a direct DFT, and one channel passes the time series through
+ * unfiltered (PPFChanneliser.cpp:108-131).  h_coeffs [ntaps][nchan] float,
+ * or NULL to design them for `window` as the reference does (then converted
+ * to float). */
 typedef struct pv_ppf pv_ppf;
 int pv_ppf_create(pv_ppf** ppf, int nchan, int ntaps, int window, const float* h_coeffs);
 void pv_ppf_destroy(pv_ppf* ppf);

@@ -35,8 +35,8 @@ struct ChanArgs {
     const float2* hist_in;   // [sub][pol][T-1][N] previous blocks (may be null: zeros)
     float2* hist_out;        // [sub][pol][T-1][N] blocks carried to the next call
     const float* coeffs;     // [T][N]
-    const float2* twiddle;   // [N/2] exp(-2 pi i k / N)
-    int nsub, npol, nblocks, N, T, log2n, BT;
+    const float2* twiddle;   // [N/2] exp(-2 pi i k / N) ([N] when N is not a power of two)
+    int nsub, npol, nblocks, N, T, log2n, BT;  // log2n < 0: N is not a power of two (direct DFT)
     // output
     int mode;                // 0: complex spectra, 1: Stokes + integration
     float2* spectra;         // mode 0: [block][sub][pol][N]
@@ -76,11 +76,12 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
     const int rows = nb + H;                 // staged blocks per polarisation
     float2* x = sm;                          // [P][BT+H][N]
     float2* y = sm + (size_t)P * (BT + H) * N;    // [P][BT][N]
-    float2* tw = y + (size_t)P * BT * N;          // [N/2]
-    float* cf = reinterpret_cast<float*>(tw + N / 2);  // [T][N]
+    float2* tw = y + (size_t)P * BT * N;          // [N/2], or [N] for the direct DFT
+    const int ntw = a.log2n < 0 ? N : N / 2;
+    float* cf = reinterpret_cast<float*>(tw + N);  // [T][N]
     const int tid = threadIdx.x, nt = blockDim.x;
 
-    for (int i = tid; i < N / 2; i += nt) tw[i] = a.twiddle[i];
+    for (int i = tid; i < ntw; i += nt) tw[i] = a.twiddle[i];
     for (int i = tid; i < T * N; i += nt) cf[i] = a.coeffs[i];
     // stage blocks b0-H .. b0+nb-1; negative blocks come from the history
     for (int p = 0; p < P; ++p) {
@@ -114,6 +115,10 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
         const int c = i % N, pb = i / N;
         const int p = pb / nb, b = pb - p * nb;
         const float2* xs = x + ((size_t)p * (BT + H) + b) * N + c;
+        if (N == 1) {  // PPFChanneliser.cpp:108-131: one channel is the time series itself
+            y[(size_t)p * BT + b] = xs[(size_t)H * N];
+            continue;
+        }
         float re = 0.0f, im = 0.0f;
         for (int t = 0; t < T; ++t) {
             const float k = cf[t * N + c];
@@ -124,11 +129,31 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
         y[((size_t)p * BT + b) * N + c] = make_float2(re, im);
     }
     __syncthreads();
+    if (a.log2n < 0) {
+        // N not a power of two: the forward DFT sum_j y[j] exp(-2 pi i j k / N) of every row
+        // into x (no longer needed), in natural channel order
+        for (int i = tid; i < P * nb * N; i += nt) {
+            const int k = i % N, pb = i / N;
+            const int p = pb / nb, b = pb - p * nb;
+            const float2* r = y + ((size_t)p * BT + b) * N;
+            float re = 0.0f, im = 0.0f;
+            int m = 0;  // j * k mod N
+            for (int j = 0; j < N; ++j) {
+                const float2 v = r[j], w = tw[m];
+                re = __fadd_rn(re, __fsub_rn(__fmul_rn(v.x, w.x), __fmul_rn(v.y, w.y)));
+                im = __fadd_rn(im, __fadd_rn(__fmul_rn(v.x, w.y), __fmul_rn(v.y, w.x)));
+                m += k;
+                if (m >= N) m -= N;
+            }
+            x[((size_t)p * BT + b) * N + k] = make_float2(re, im);
+        }
+        __syncthreads();
+    }
     // In-place radix-2 decimation-in-frequency FFT of every (pol, block) row
     // of y (dif_upper gives the butterfly arithmetic); row position i then
     // holds channel bitrev(i).
     const int half = N / 2, lg = a.log2n;
-    for (int lh = lg - 1; lh >= 0; --lh) {
+    for (int lh = lg - 1; lh >= 0; --lh) {  // no stage when lg <= 0
         const int h = 1 << lh;
         for (int i = tid; i < P * nb * half; i += nt) {
             const int j = i & (half - 1), row = i >> (lg - 1);
@@ -144,15 +169,16 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
         }
         __syncthreads();
     }
-    const float2* src = y;
-    const int rev = 32 - lg;
+    const float2* src = lg < 0 ? x : y;
+    // row position of channel c: bit-reversed after the radix-2 FFT, natural after the DFT
+    auto pos = [lg](int c) { return lg > 0 ? (int)(__brev((unsigned)c) >> (32 - lg)) : c; };
     // src holds the spectra, rows of stride N with pol stride BT*N
     if (a.mode == 0) {
         for (int i = tid; i < P * nb * N; i += nt) {
             const int c = i % N, pb = i / N;
             const int b = pb % nb, p = pb / nb;
             a.spectra[(((long long)(b0 + b) * a.nsub + s) * P + p) * N + c] =
-                src[((size_t)p * BT + b) * N + (__brev(c) >> rev)];
+                src[((size_t)p * BT + b) * N + pos(c)];
         }
         return;
     }
@@ -172,7 +198,7 @@ __global__ void __launch_bounds__(256) channelise_kernel(const ChanArgs a) {
             const float2* X = src + (size_t)b * N;
             const float2* Y = src + ((size_t)BT + b) * N;
             for (int c = nc * a.bin; c < (nc + 1) * a.bin; ++c) {
-                const int i = __brev(c) >> rev;
+                const int i = pos(c);
                 const float xr = X[i].x, xi = X[i].y, yr = Y[i].x, yi = Y[i].y;
                 const float px = __fadd_rn(__fmul_rn(xr, xr), __fmul_rn(xi, xi));
                 const float py = __fadd_rn(__fmul_rn(yr, yr), __fmul_rn(yi, yi));
@@ -543,7 +569,7 @@ int tile_blocks(int N, int T, int P, int window, size_t* smem_out) {
     // fits in shared memory
     for (int bt = 128; bt >= 1; bt /= 2) {
         if (window > 0 && bt % window != 0) continue;
-        const size_t smem = ((size_t)P * (bt + T - 1) * N + (size_t)P * bt * N + N / 2) * sizeof(float2) +
+        const size_t smem = ((size_t)P * (bt + T - 1) * N + (size_t)P * bt * N + N) * sizeof(float2) +
                             (size_t)T * N * sizeof(float);
         if (smem <= 200 * 1024 && (size_t)P * bt * N <= 256 * 256) {
             *smem_out = smem;
@@ -706,15 +732,22 @@ int ppf_tables(const pv_ppf* h, const float** d_coeffs, const float2** d_twiddle
 
 extern "C" int pv_ppf_create(pv_ppf** out, int nchan, int ntaps, int window,
                              const float* h_coeffs) {
-    if (!out || nchan < 2 || ntaps < 1 || (nchan & (nchan - 1)) != 0 || nchan > 1024) {
-        pv::set_error("PPFChanneliser: channels must be a power of two in 2..1024 (got %d)", nchan);
+    // PPFChanneliser.cpp:42-44: one channel or an even number of them
+    if (!out || nchan < 1 || (nchan != 1 && nchan % 2 != 0) || ntaps < 1 || nchan > 1024) {
+        pv::set_error("PPFChanneliser: Number of channels needs to be even (1 or 2..1024, got %d)", nchan);
         return PV_ERR_CONFIG;
     }
     auto* h = new pv_ppf;
     h->nchan = nchan;
     h->ntaps = ntaps;
+    const bool pow2 = (nchan & (nchan - 1)) == 0;
     while ((1 << h->log2n) < nchan) ++h->log2n;
-    if (h_coeffs) {
+    if (!pow2) h->log2n = -1;  // direct DFT
+    if (nchan == 1) {
+        // The time series is the spectrum (PPFChanneliser.cpp:108-131): no filter, no history.
+        h->ntaps = 1;
+        h->h_coeffs.assign(1, 1.0f);
+    } else if (h_coeffs) {
         h->h_coeffs.assign(h_coeffs, h_coeffs + (size_t)nchan * ntaps);
     } else {
         std::vector<double> c;
@@ -723,12 +756,12 @@ extern "C" int pv_ppf_create(pv_ppf** out, int nchan, int ntaps, int window,
         h->h_coeffs.resize(c.size());
         for (size_t i = 0; i < c.size(); ++i) h->h_coeffs[i] = (float)c[i];  // PPFChanneliser.cpp:212-217
     }
-    std::vector<float2> tw(nchan / 2);
-    for (int k = 0; k < nchan / 2; ++k) {
+    std::vector<float2> tw(std::max(1, pow2 ? nchan / 2 : nchan));
+    for (int k = 0; k < (int)tw.size(); ++k) {
         const double ang = -2.0 * M_PI * k / nchan;
         tw[k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
-    if (nchan >= 4) tw[nchan / 4] = make_float2(0.0f, -1.0f);  // exactly -i (cos(pi/2) is not 0 in FP64)
+    if (nchan % 4 == 0) tw[nchan / 4] = make_float2(0.0f, -1.0f);  // exactly -i (cos(pi/2) is not 0 in FP64)
     cudaError_t e = cudaMalloc(&h->d_coeffs, sizeof(float) * h->h_coeffs.size());
     if (e == cudaSuccess) e = cudaMalloc(&h->d_twiddle, sizeof(float2) * tw.size());
     if (e == cudaSuccess)

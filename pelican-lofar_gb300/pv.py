@@ -317,7 +317,7 @@ class PPF:
     """Device channeliser with its tap history (PPFChanneliser)."""
 
     def __init__(self, nchan, ntaps=8, window="kaiser", coeffs=None):
-        self.nchan, self.ntaps = nchan, ntaps
+        self.nchan, self.ntaps = nchan, (1 if nchan == 1 else ntaps)  # one channel: no filter
         self.h = C.c_void_p()
         c = None
         if coeffs is not None:

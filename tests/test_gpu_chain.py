@@ -30,6 +30,37 @@ def test_ppf_matches_oracle(pv, oracle, cuda, nchan, ntaps, window):
     assert np.max(np.abs(got - want)) <= 2e-5 * np.sqrt(p_want.mean())
 
 
+@pytest.mark.parametrize("nchan,ntaps,window", [(24, 8, "kaiser"), (6, 4, "hamming"), (96, 8, "blackman")])
+def test_ppf_even_channel_counts_match_oracle(pv, oracle, cuda, nchan, ntaps, window):
+    """Even channel counts that are not powers of two (PPFChanneliser.cpp:42-44):
+    the FIR as for the others, the transform a direct FP32 DFT against the
+    oracle's FP64 one; spectra and Stokes I over two chunks (the tap history
+    carried on the device)."""
+    import torch
+    rng = np.random.default_rng(nchan)
+    nsub, npol, nblk = 3, 2, 40
+    g, o, _ = _ppf_pair(pv, oracle, nchan, ntaps, window)
+    for _ in range(2):
+        _, x = voltages(rng, nsub, npol, nblk * nchan)
+        got = g.run(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        want = o.run(x.reshape(nsub, npol, nblk, nchan))
+        p_want = np.abs(want.astype(np.complex128)) ** 2
+        assert np.max(np.abs(np.abs(got) ** 2 - p_want)) <= 2e-5 * p_want.mean()
+        assert np.max(np.abs(got - want)) <= 2e-5 * np.sqrt(p_want.mean())
+
+
+def test_ppf_single_channel_is_the_time_series(pv, oracle, cuda):
+    """One channel: the spectra are the time samples, bit for bit."""
+    import torch
+    rng = np.random.default_rng(3)
+    nsub, npol, nblk = 4, 2, 33
+    _, x = voltages(rng, nsub, npol, nblk)
+    g = pv.PPF(1, 8)
+    got = g.run(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    want = oracle.PPF(1, 8, np.ones((8, 1), np.float32)).run(x.reshape(nsub, npol, nblk, 1))
+    assert np.array_equal(got, want)
+
+
 def test_ppf_history_is_continuous(pv, oracle, cuda):
     """Two calls carry the tap history: identical to one call over both."""
     import torch

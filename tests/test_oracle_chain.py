@@ -6,7 +6,7 @@ from gen import make_bp_text, stokes_filterbank
 
 
 @pytest.mark.parametrize("window", ["kaiser", "hamming", "blackman", "gaussian"])
-@pytest.mark.parametrize("nchan,ntaps", [(16, 8), (64, 8), (512, 8), (32, 4)])
+@pytest.mark.parametrize("nchan,ntaps", [(16, 8), (64, 8), (512, 8), (32, 4), (24, 8), (6, 4)])
 def test_fir_coefficients_product_vs_oracle(pv, oracle, window, nchan, ntaps):
     """The library's host coefficient design against the oracle's
     (PolyphaseCoefficients.cpp:308-364), two independent restatements."""
@@ -87,3 +87,28 @@ def test_guided_run_counts_a_planted_difference(oracle):
     f0, rep = r0.run_guided(data.copy(), hint, 1e-3, 1e-2)
     assert rep["chan_mismatch"] == 1 and rep["chan_near"] == 0 and rep["first_difference"] == 1300
     assert np.array_equal(f0, hint)
+
+
+@pytest.mark.parametrize("N", [24, 6])
+def test_ppf_oracle_dft_against_numpy(oracle, N):
+    """Channel counts that are not powers of two (the reference takes any even
+    count, PPFChanneliser.cpp:42-44): the oracle's DFT as numpy.fft."""
+    rng = np.random.default_rng(N)
+    T, nsub, npol, nblk = 8, 2, 2, 20
+    coeffs = oracle.fir_coefficients(T, N, "kaiser").astype(np.float32)
+    x = (rng.standard_normal((nsub, npol, nblk, N)) + 1j * rng.standard_normal((nsub, npol, nblk, N))).astype(np.complex64)
+    got = oracle.PPF(N, T, coeffs).run(x)
+    pad = np.concatenate([np.zeros((nsub, npol, T - 1, N), np.complex64), x], axis=2)
+    y = np.zeros((nsub, npol, nblk, N), np.complex128)
+    for t in range(T):
+        y += pad[:, :, t:t + nblk, :].astype(np.complex128) * coeffs[t][None, None, None, :]
+    want = np.fft.fft(y, axis=-1).transpose(2, 0, 1, 3)
+    assert np.max(np.abs(got - want)) <= 1e-4 * np.sqrt(np.mean(np.abs(want) ** 2))
+
+
+def test_ppf_oracle_single_channel_is_the_time_series(oracle):
+    """One channel: the spectra are the time samples (PPFChanneliser.cpp:108-131)."""
+    rng = np.random.default_rng(1)
+    x = (rng.standard_normal((3, 2, 17, 1)) + 1j * rng.standard_normal((3, 2, 17, 1))).astype(np.complex64)
+    got = oracle.PPF(1, 8, np.ones((8, 1), np.float32)).run(x)
+    assert np.array_equal(got, x.transpose(2, 0, 1, 3))
