@@ -298,6 +298,19 @@ Geo make_geo(int nsub, int npol, int nchan) {
     return g;
 }
 
+// The band of a thread's current channel as its channels rise: band b holds
+// channels [b*cpb, (b+1)*cpb), band 7 the rest (Geo::band).
+struct BandRun {
+    int band, end;  // end: first channel of the next band (INT_MAX for band 7)
+    __device__ __forceinline__ BandRun(const Geo& g, int i) { set(g, g.band(i)); }
+    __device__ __forceinline__ void set(const Geo& g, int b) {
+        band = b;
+        end = b < 7 ? (b + 1) * g.cpb : 0x7fffffff;
+    }
+    __device__ __forceinline__ bool ends_before(int i) const { return i >= end; }
+    __device__ __forceinline__ void advance(const Geo& g, int i) { set(g, g.band(i)); }
+};
+
 // A beam's clipper may span a cluster of C CTAs of T threads: partial p =
 // rank * T + thread, so the P = C * T partials, their channels and the
 // canonical sums are those of one CTA of P threads.  Warp 0 of every CTA
@@ -453,20 +466,36 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
             float mins[16], part[16];
 #pragma unroll
             for (int b = 0; b < 8; ++b) { mins[b] = 1e6f; mins[8 + b] = 1e6f; part[b] = 0.0f; part[8 + b] = 0.0f; }
+            // A thread's channels rise, so each band's are consecutive in its loop: the band's
+            // statistics accumulate in registers (sums from +0, minima from 1e6, in channel
+            // order) and go to their band's slot when the band ends.
+            BandRun run(geo, tg);
+            float s1 = 0.0f, s2 = 0.0f, m1 = 1e6f, m2 = 1e6f;
+            auto flush = [&]() {
+#pragma unroll
+                for (int b = 0; b < 8; ++b)
+                    if (b == run.band) {
+                        part[b] = s1;
+                        part[8 + b] = s2;
+                        mins[b] = m1;
+                        mins[8 + b] = m2;
+                    }
+                s1 = s2 = 0.0f;
+                m1 = m2 = 1e6f;
+            };
 #pragma unroll UR
             for (int i = tg, li = tid; i < nbins; i += P, li += T) {
-                const int band = geo.band(i);
-                const float v = spec[li];
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    if (b == band) {
-                        mins[b] = fminf(mins[b], v);
-                        mins[8 + b] = fminf(mins[8 + b], bp[li]);
-                        part[b] = __fadd_rn(part[b], v);
-                        part[8 + b] = __fadd_rn(part[8 + b], __fmul_rn(v, v));
-                    }
+                if (run.ends_before(i)) {
+                    flush();
+                    run.advance(geo, i);
                 }
+                const float v = spec[li];
+                m1 = fminf(m1, v);
+                m2 = fminf(m2, bp[li]);
+                s1 = __fadd_rn(s1, v);
+                s2 = __fadd_rn(s2, __fmul_rn(v, v));
             }
+            if (tg < nbins) flush();
 #pragma unroll
             for (int k = 0; k < 16; ++k)
 #pragma unroll
@@ -522,22 +551,35 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         int good[8];
 #pragma unroll
         for (int b = 0; b < 8; ++b) good[b] = 0;
-#pragma unroll UR
-        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
-            const float v = spec[li];
-            const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[li]) > margin_f;
-            if (clip) {
-                const float lg = bufs.last_good[i];
-                const long long o = geo.off(i);
-                for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = lg;
-                spec[li] = lg;
-            } else {
-                gpart[0] = __fadd_rn(gpart[0], v);
-                const int band = geo.band(i);
+        {
+            // good channels per band: counted for the current band, stored when it ends
+            BandRun run(geo, tg);
+            int g = 0;
+            auto flush = [&]() {
 #pragma unroll
-                for (int b = 0; b < 8; ++b) good[b] += (b == band);
+                for (int b = 0; b < 8; ++b) good[b] += b == run.band ? g : 0;
+                g = 0;
+            };
+#pragma unroll UR
+            for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+                if (run.ends_before(i)) {
+                    flush();
+                    run.advance(geo, i);
+                }
+                const float v = spec[li];
+                const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[li]) > margin_f;
+                if (clip) {
+                    const float lg = bufs.last_good[i];
+                    const long long o = geo.off(i);
+                    for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = lg;
+                    spec[li] = lg;
+                } else {
+                    gpart[0] = __fadd_rn(gpart[0], v);
+                    ++g;
+                }
+                if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
             }
-            if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
+            flush();
         }
         warp_tree<1>(gpart, red_c);
 #pragma unroll
