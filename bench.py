@@ -55,10 +55,15 @@ import numpy as np
 
 SUB_BW = 0.1953125  # MHz
 RAW_TSAMP = 5.12e-6  # s
-# DRAM bytes per FP32 add of the batched dedispersion (dedisperse_pair_kernel, tile variant 7):
-# 4.364 GB for 2.048e11 adds, measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) on the
-# first 3 beams of the mix with 4096-sample chunks
-DD_BATCH_BYTES_PER_ADD = 4.3636e9 / 2.04816252928e11
+# DRAM bytes per add of the batched dedispersion, measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on the mix's first 3 beams: (bytes, adds, the capture)
+DD_BATCH_TRAFFIC = {
+    ("f32", "pair"): (4.3636e9, 2.04816252928e11, "dedisperse_pair_kernel, tile variant 7, 4096-sample chunks"),
+    ("f32", "one"): (1.776e9, 5.1204063232e10, "dedisperse_batch_kernel, FP32 rings, 1024-sample chunks"),
+    ("f16", "one"): (0.907e9, 5.1204063232e10, "dedisperse_batch_kernel, FP16 rings, 1024-sample chunks"),
+    ("u8", "one"): (0.457e9, 5.1204063232e10, "dedisperse_batch_kernel, u8 rings, 1024-sample chunks"),
+}
+RING_SAMPLES_PER_WORD = {"f32": 1, "f16": 2, "u8": 4}
 
 
 def dd_kernel_name(variant):
@@ -70,15 +75,16 @@ PAIR_S = 33       # output samples per lane of the trial-pair kernels
 PAIR_LIM = {4: 32, 5: 32, 6: 15, 7: 15, 8: 15}  # largest shift difference read from registers
 
 
-def shared_words_per_add(cfgs, variant, dms, samples=64):
-    """Shared-memory words the batched kernel reads per FP32 add on these
-    beams: 1 for the one-trial variants; for the trial-pair variants a lane
-    reads 33 + delta words for its 66 adds (delta = the channel's shift
-    difference between the pair's trials, up to the variant's limit) or 66
-    beyond it.  Evaluated over every channel and a sample of the trial pairs
-    of each DM tile, weighted by adds."""
+def shared_words_per_add(cfgs, variant, dms, store="f32", samples=64):
+    """Shared-memory words the batched kernel reads per add on these beams:
+    for the one-trial variants one sample per add (a 32-bit word holds 1, 2
+    or 4 samples of an FP32, FP16 or u8 ring); for the trial-pair variants
+    (FP32 rings) a lane reads 33 + delta words for its 66 adds (delta = the
+    channel's shift difference between the pair's trials, up to the
+    variant's limit) or 66 beyond it.  Evaluated over every channel and a
+    sample of the trial pairs of each DM tile, weighted by adds."""
     if variant < 4:
-        return 1.0
+        return 1.0 / RING_SAMPLES_PER_WORD[store]
     lim = PAIR_LIM[variant]
     words = adds = 0.0
     for c, h in zip(cfgs, dms):
@@ -685,7 +691,8 @@ def run_batch(args, cfgs, workload):
     fb_bytes = sum(c["chunk"] * c["nsub"] * c["nchan_sub"] * 4 for c in cfgs)
     chan_gbs = (in_bytes + fb_bytes) / (st["channelise"] / 1e3) / 1e9
     variant = tiles["variant"]
-    words = shared_words_per_add(cfgs, variant, tiles["dms"])
+    words = shared_words_per_add(cfgs, variant, tiles["dms"], args.store)
+    t_bytes, t_adds, t_what = DD_BATCH_TRAFFIC[(args.store, "pair" if variant >= 4 else "one")]
     roofline = {"kernel": dd_kernel_name(variant), "bound": "fp32",
                 "achieved": achieved / 1e12, "peak": fadd_peak / 1e12, "unit": "Tadd/s",
                 "frac": achieved / fadd_peak,
@@ -693,10 +700,9 @@ def run_batch(args, cfgs, workload):
                 "smem_words_per_add": words,
                 "smem_bound": "32 four-byte shared-memory words per clock per SM (one 128-byte wavefront); "
                               "the kernel reads smem_words_per_add words per add on this workload",
-                "traffic": DD_BATCH_BYTES_PER_ADD * units_step,
+                "traffic": t_bytes / t_adds * units_step,
                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture "
-                                  "of tile variant 7 on the mix's first 3 beams with 4096-sample "
-                                  "chunks, scaled by adds",
+                                  "(%s) on the mix's first 3 beams, scaled by adds" % t_what,
                 "peak_source": "%d SMs x 128 FP32 lanes x sm_max_mhz of MEASURED_PEAKS.json (%s)"
                                % (nsm, peak_src),
                 "per_unit": "one FP32 add per DM-trial*channel*sample (%d per launch)" % units_step,
