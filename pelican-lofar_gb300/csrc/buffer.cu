@@ -33,6 +33,12 @@ __device__ __forceinline__ void ring_store(float* ring, long long i, float v, co
     }
 }
 
+// One CTA of 32 x 8 threads moves a strip of 32 bins x kStrip samples:
+// coalesced 128-byte reads of each sample's 32 bins into shared memory (rows
+// padded to kStrip + 1 words: both phases are free of bank conflicts), then
+// coalesced 128-byte writes of each bin's samples into its ring row.
+constexpr int kStrip = 128;
+
 template <int STORE = PV_STORE_F32>
 __device__ __forceinline__ void ring_write_tile(float* __restrict__ ring, long long row_stride,
                                                 long long ring_len, long long pos,
@@ -40,26 +46,35 @@ __device__ __forceinline__ void ring_write_tile(float* __restrict__ ring, long l
                                                 int npol, int nchan, int inverted, int t0, int b0,
                                                 const float* scale = nullptr,
                                                 const float* offset = nullptr) {
-    __shared__ float tile[kTile][kTile + 1];
+    __shared__ float tile[kTile][kStrip + 1];
     const int nbins = nsub * nchan;
-    // read: rows of the tile are samples, columns are bins (coalesced in bins)
-    for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
-        const int t = t0 + i, b = b0 + threadIdx.x;
-        if (t < nt && b < nbins) {
-            const int s = b / nchan, c = b - s * nchan;
-            tile[i][threadIdx.x] = stokes[(long long)nchan * (npol * ((long long)nsub * t + s)) + c];
+    const int b = b0 + threadIdx.x;
+    if (b < nbins) {
+        const int s = b / nchan, c = b - s * nchan;
+        const long long base = (long long)nchan * npol * s + c;
+        const long long tstride = (long long)nchan * npol * nsub;  // one spectrum
+#pragma unroll 4
+        for (int i = threadIdx.y; i < kStrip; i += blockDim.y) {
+            const int t = t0 + i;
+            if (t < nt) tile[threadIdx.x][i] = stokes[tstride * t + base];
         }
     }
     __syncthreads();
-    // write: rows of the ring are bins, columns samples (coalesced in samples)
-    for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
-        const int b = b0 + i, t = t0 + threadIdx.x;
-        if (t < nt && b < nbins) {
-            const int row = inverted ? nbins - 1 - b : b;
-            long long col = pos + t;
-            if (ring_len > 0) col %= ring_len;
-            ring_store<STORE>(ring, (long long)row * row_stride + col, tile[threadIdx.x][i], scale, offset,
-                              row);
+    long long col0 = pos + t0;
+    if (ring_len > 0) col0 %= ring_len;
+    for (int j = threadIdx.y; j < kTile; j += blockDim.y) {
+        const int bb = b0 + j;
+        if (bb >= nbins) break;
+        const int row = inverted ? nbins - 1 - bb : bb;
+        const long long rbase = (long long)row * row_stride;
+#pragma unroll
+        for (int k = 0; k < kStrip / 32; ++k) {
+            const int i = threadIdx.x + 32 * k;
+            if (t0 + i < nt) {
+                long long col = col0 + i;
+                if (ring_len > 0 && col >= ring_len) col = ring_len >= kStrip ? col - ring_len : col % ring_len;
+                ring_store<STORE>(ring, rbase + col, tile[j][i], scale, offset, row);
+            }
         }
     }
 }
@@ -68,7 +83,7 @@ __global__ void ring_write_kernel(float* __restrict__ ring, long long row_stride
                                   long long pos, const float* __restrict__ stokes, int nt, int nsub,
                                   int npol, int nchan, int inverted) {
     ring_write_tile(ring, row_stride, ring_len, pos, stokes, nt, nsub, npol, nchan, inverted,
-                    blockIdx.x * kTile, blockIdx.y * kTile);
+                    blockIdx.x * kStrip, blockIdx.y * kTile);
 }
 
 // The rings of many beams: CTAs are laid out job after job; an active beam's
@@ -86,10 +101,10 @@ __global__ void ring_write_batch_kernel(const pv::RingJob* __restrict__ jobs, in
     const pv::BeamStep& B = bs[J.beam];
     if (!B.active) return;
     const int local = (int)(blockIdx.x - J.block_begin);
-    const int tiles_t = (J.nt + kTile - 1) / kTile;
+    const int tiles_t = (J.nt + kStrip - 1) / kStrip;
     const int bt = local / tiles_t, tt = local - bt * tiles_t;
     ring_write_tile<STORE>(J.ring, J.row_stride, J.ring_len, B.written * J.nt, J.stokes, J.nt, J.nsub,
-                           1, J.nchan, J.inverted, tt * kTile, bt * kTile, J.scale, J.offset);
+                           1, J.nchan, J.inverted, tt * kStrip, bt * kTile, J.scale, J.offset);
 }
 
 // u8 rings of beams without a clipper: each row's offset (the median of its
@@ -180,14 +195,14 @@ int ring_write_device(float* ring, long long row_stride, long long ring_len, lon
                       const float* stokes, int nt, int nsub, int npol, int nchan, int inverted,
                       cudaStream_t s) {
     if (nt <= 0) return PV_OK;
-    dim3 grid((unsigned)ceil_div(nt, kTile), (unsigned)ceil_div(nsub * nchan, kTile));
+    dim3 grid((unsigned)ceil_div(nt, kStrip), (unsigned)ceil_div(nsub * nchan, kTile));
     ring_write_kernel<<<grid, dim3(kTile, 8), 0, s>>>(ring, row_stride, ring_len, pos, stokes, nt,
                                                      nsub, npol, nchan, inverted);
     return check_launch("ring_write_kernel");
 }
 
 int ring_job_blocks(const RingJob& j) {
-    return ceil_div(j.nt, kTile) * ceil_div(j.nsub * j.nchan, kTile);
+    return ceil_div(j.nt, kStrip) * ceil_div(j.nsub * j.nchan, kTile);
 }
 
 int ring_cal_blocks(const RingJob& j) { return j.nsub * j.nchan; }
