@@ -433,12 +433,15 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         hr.prev = st.rms_size > 1 ? bufs.rms_buf[(st.rms_head + st.rms_size - 2) % H] : 0.0;
         hr.front = bufs.rms_buf[st.rms_head];
         if (lane == 0) bc.params0 = st.params0;
-        if (nt > 0) {
-            if (st.rms_size < H) {
-                if (lane == 0) bc.adapt = 1;
-            } else {
-                steady_start(st, hr, cfg, bufs, inv_h, bc);
-            }
+    }
+    // Every CTA of a cluster reads the oldest rms entry before any CTA's
+    // steady_start overwrites it.
+    if constexpr (C > 1) cooperative_groups::this_cluster().sync();
+    if (warp == 0 && nt > 0) {
+        if (st.rms_size < H) {
+            if (lane == 0) bc.adapt = 1;
+        } else {
+            steady_start(st, hr, cfg, bufs, inv_h, bc);
         }
     }
     __syncthreads();
