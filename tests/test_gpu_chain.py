@@ -223,3 +223,25 @@ def test_rfi_cluster_four_stokes_bit_exact(pv, oracle, cuda):
     gf = g.run(dd, flags=True).cpu().numpy()
     of = o.run(data, flags=True)
     assert np.array_equal(gf, of) and np.array_equal(dd.cpu().numpy(), data)
+
+
+@pytest.mark.parametrize("split", [1, 2])
+def test_rfi_cluster_chunks_in_steady_state_bit_exact(pv, oracle, cuda, split):
+    """6144 channels over a cluster, four chunks with a 300-spectrum history:
+    from the second chunk on a launch starts in the steady state, whose first
+    update overwrites the oldest history entry every CTA has just read."""
+    import torch
+    rng = np.random.default_rng(17)
+    nsub, nchan, per = 96, 64, 400
+    data = stokes_filterbank(rng, 4 * per, nsub, nchan)
+    bp = make_bp_text(nsub * nchan, BP_START, BP_WIDTH, 1000.0, 50.0)
+    parts = pv.load().pv_rfi_parts(nsub * nchan)
+    g = pv.RFI(bp, cr=5.0, history=300, split=split)
+    o = oracle.RFI(bp, cr=5.0, history=300, mode=1, parts=parts)
+    for k in range(4):
+        d = np.ascontiguousarray(data[k * per:(k + 1) * per])
+        dd = torch.from_numpy(d).to(cuda)
+        gf = g.run(dd, flags=True).cpu().numpy()
+        of = o.run(d, flags=True)
+        assert np.array_equal(gf, of) and np.array_equal(dd.cpu().numpy(), d), k
+    assert np.array_equal(g.state()[[0, 1, 5, 6, 7, 8, 9]], o.state()[[0, 1, 5, 6, 7, 8, 9]])
