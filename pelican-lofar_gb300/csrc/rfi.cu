@@ -417,9 +417,26 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
     int* redi_c = reinterpret_cast<int*>(red_c + 32);       // [32][8] clip pass: good per band
     float* red_f = reinterpret_cast<float*>(redi_c + 32 * 8);  // [32][2] fill pass: sums
     int* redi_f = reinterpret_cast<int*>(red_f + 32 * 2);   // [32] fill pass: filled
+    // The last good spectrum of this CTA's channels, staged in shared memory
+    // when the launch gave room for it (rfi_smem_bytes): a clipped channel
+    // then costs no global load in the clip pass.
+    unsigned dsm;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsm));
+    float* lgood = dsm >= sizeof(float) * (4 * (size_t)nloc + kRedWords) ? sh + 3 * nloc + kRedWords : nullptr;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tg = rank * T + tid;  // the thread's partial
     const double inv_h = 1.0 / (double)H;
+    // A flat bandpass (no polynomial terms, no killed channels) has one value
+    // for every channel, scale * params[0] (bp_value): the passes then use
+    // that scalar instead of a per-channel array.
+    const bool flat = cfg.deg == 0 && bufs.killed == nullptr;
+    const float bp_scale = cfg.scale;
+    // pol-0 element offset of the thread's channels: geo.off(i), which rises
+    // by P * npol from one of its channels to the next when nchan divides P
+    const int npol = geo.npol, nchan_g = geo.nchan;
+    const bool off_step = geo.lg_nchan >= 0 && P % geo.nchan == 0;
+    const long long off0 = tg < nbins ? geo.off(tg) : 0;
+    const long long off_inc = (long long)P * npol;
     const long long spec_elems = (long long)geo.nsub * geo.npol * geo.nchan;
 
     RfiState st;   // warp 0 only (every lane the same)
@@ -445,7 +462,11 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         }
     }
     __syncthreads();
-    for (int i = tg, li = tid; i < nbins; i += P, li += T) bp[li] = bp_value(cfg, bufs, bc.params0, i);
+    float bp_flat = __fmul_rn(bp_scale, bc.params0);  // the flat bandpass's value
+    for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+        if (!flat) bp[li] = bp_value(cfg, bufs, bc.params0, i);
+        if (lgood) lgood[li] = bufs.last_good[i];
+    }
     auto prefetch = [&](int t) {
         float* buf = specs + (t & 1) * nloc;
         const float* src = data + (long long)t * spec_elems;
@@ -494,7 +515,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 }
                 const float v = spec[li];
                 m1 = fminf(m1, v);
-                m2 = fminf(m2, bp[li]);
+                m2 = fminf(m2, flat ? bp_flat : bp[li]);
                 s1 = __fadd_rn(s1, v);
                 s2 = __fadd_rn(s2, __fmul_rn(v, v));
             }
@@ -563,24 +584,29 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 for (int b = 0; b < 8; ++b) good[b] += b == run.band ? g : 0;
                 g = 0;
             };
+            const float bpf = bp_flat;
+            unsigned char* fl = flags ? flags + (long long)t * nbins : nullptr;
+            long long o = off0;
 #pragma unroll UR
-            for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+            for (int i = tg, li = tid; i < nbins; i += P, li += T, o += off_inc) {
                 if (run.ends_before(i)) {
                     flush();
                     run.advance(geo, i);
                 }
                 const float v = spec[li];
-                const bool clip = __fsub_rn(__fsub_rn(v, dm_f), bp[li]) > margin_f;
-                if (clip) {
-                    const float lg = bufs.last_good[i];
-                    const long long o = geo.off(i);
-                    for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = lg;
+                const bool clip = __fsub_rn(__fsub_rn(v, dm_f), flat ? bpf : bp[li]) > margin_f;
+                if (clip) {  // the channel takes its last good value, every polarisation
+                    const float lg = lgood ? lgood[li] : bufs.last_good[i];
+                    if (npol > 1) {
+                        const long long oo = off_step ? o : geo.off(i);
+                        for (int p = 1; p < npol; ++p) dst[oo + (long long)p * nchan_g] = lg;
+                    }
                     spec[li] = lg;
                 } else {
                     gpart[0] = __fadd_rn(gpart[0], v);
                     ++g;
                 }
-                if (flags) flags[(long long)t * nbins + i] = clip ? 1 : 0;
+                if (fl) fl[i] = clip ? 1 : 0;
             }
             flush();
         }
@@ -662,20 +688,23 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         // ---- last good spectrum, clipSample, flatten (RFI_Clipper.cpp:441-494) ----
         int filled = 0;
         float s12[2] = {0.0f, 0.0f};
+        const float bpd = __fadd_rn(bp_flat, dm_f);  // bandpass + dataModel of a flat bandpass
+        long long of = off0;
 #pragma unroll UR
-        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+        for (int i = tg, li = tid; i < nbins; i += P, li += T, of += off_inc) {
             float v = spec[li];
-            if (do_fill && bufs.last_good[i] == 0.0f && v != 0.0f) {
+            if (do_fill && (lgood ? lgood[li] : bufs.last_good[i]) == 0.0f && v != 0.0f) {
                 bufs.last_good[i] = v;
+                if (lgood) lgood[li] = v;
                 ++filled;
             }
             if (spectrum_clip) {
-                const long long o = geo.off(i);
-                for (int p = 1; p < geo.npol; ++p) dst[o + (long long)p * geo.nchan] = -0.2f;
+                const long long o = off_step ? of : geo.off(i);
+                for (int p = 1; p < npol; ++p) dst[o + (long long)p * nchan_g] = -0.2f;
                 v = -0.2f;
                 if (flags) flags[(long long)t * nbins + i] |= 2;
             }
-            v = __fsub_rn(v, __fadd_rn(bp[li], dm_f));
+            v = __fsub_rn(v, flat ? bpd : __fadd_rn(bp[li], dm_f));
             spec[li] = v;
             s12[0] = __fadd_rn(s12[0], v);
             s12[1] = __fadd_rn(s12[1], __fmul_rn(v, v));
@@ -743,16 +772,19 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
         const float sub_f = bc.sub_f, rms_f = bc.rms_f;
         const bool rebuild = bc.rebuild_bp != 0;
         const float p0 = bc.params0;
+        const float cr = cfg.cr;
+        long long on = off0;
 #pragma unroll UR
-        for (int i = tg, li = tid; i < nbins; i += P, li += T) {
+        for (int i = tg, li = tid; i < nbins; i += P, li += T, on += off_inc) {
             float v = spec[li];
             if (!spectrum_clip) {
                 v = __fdiv_rn(__fsub_rn(v, sub_f), rms_f);
-                if (v > cfg.cr) v = 0.0f;
+                if (v > cr) v = 0.0f;
             }
-            dst[geo.off(i)] = v;
-            if (rebuild) bp[li] = bp_value(cfg, bufs, p0, i);
+            dst[off_step ? on : geo.off(i)] = v;
+            if (rebuild && !flat) bp[li] = bp_value(cfg, bufs, p0, i);
         }
+        if (rebuild && flat) bp_flat = __fmul_rn(bp_scale, p0);  // bp_value of a flat bandpass
     }
     if (tid == 0) *bufs.state = st;  // every CTA of a cluster holds the same state
     if constexpr (C > 1) cooperative_groups::this_cluster().sync();  // no CTA leaves while others read it
@@ -808,9 +840,12 @@ void rfi_shape(int parts, int split, int* threads, int* ctas) {
     }
 }
 
+// Shared bytes of a clipper CTA: bandpass, two spectra and the reduction
+// buffers, plus the last good spectrum's copy when that still fits.
 size_t rfi_smem_bytes(int nbins, int parts, int threads) {
     const size_t nloc = (size_t)((nbins + parts - 1) / parts) * threads;
-    return sizeof(float) * (3 * nloc + kRedWords);
+    const size_t staged = sizeof(float) * (4 * nloc + kRedWords);
+    return staged <= 227 * 1024 ? staged : sizeof(float) * (3 * nloc + kRedWords);
 }
 
 template <typename K>
