@@ -256,6 +256,11 @@ __device__ __forceinline__ void cp_async4(float* smem_dst, const float* gmem_src
     const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(gmem_src) : "memory");
 }
+// both addresses 16-byte aligned
+__device__ __forceinline__ void cp_async16(float* smem_dst, const float* gmem_src) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem_src) : "memory");
+}
 
 // Ring index x in [0, 2H) reduced to [0, H).
 __device__ __forceinline__ int wrap_h(int x, int H) { return x >= H ? x - H : x; }
@@ -403,7 +408,7 @@ template <int T, int C>
 __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers& bufs,
                                          float* __restrict__ data, int nt, const Geo& geo,
                                          unsigned char* __restrict__ flags, int rank) {
-    extern __shared__ float sh[];
+    extern __shared__ __align__(16) float sh[];
     __shared__ Bcast bc;
     constexpr int P = T * C, WPC = T / 32;
     constexpr int UR = T >= 1024 ? 1 : 4;  // channel loops unrolled where registers allow
@@ -463,28 +468,38 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
     }
     __syncthreads();
     float bp_flat = __fmul_rn(bp_scale, bc.params0);  // the flat bandpass's value
+    // Spectrum t's channels are copied into specs[t & 1] by cp.async, in
+    // units of 4 channels (16 bytes) where a subband's channels come in
+    // fours: channels i..i+3 (i a multiple of 4) are then adjacent both in
+    // the spectrum and in the CTA's slots (li = m * T + k for i = m * P +
+    // rank * T + k).  Any thread may copy any unit; the copies are completed
+    // by their issuers and published by a barrier before the passes read them.
+    const bool vec4 = (nchan_g & 3) == 0 && (reinterpret_cast<unsigned long long>(data) & 15) == 0;
+    const int unit = vec4 ? 4 : 1;
+    const int nunits = nloc / unit;
+    auto stage = [&](int t, int first, int stride) {
+        float* buf = specs + (t & 1) * nloc;
+        const float* src = data + (long long)t * spec_elems;
+        for (int u = first; u < nunits; u += stride) {
+            const int li = u * unit, m = li / T, k = li - m * T;
+            const int i = m * P + rank * T + k;  // rises with u
+            if (i >= nbins) break;
+            if (vec4) cp_async16(buf + li, src + geo.off(i));
+            else cp_async4(buf + li, src + geo.off(i));
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    if (nt > 0) stage(0, tid, T);
     for (int i = tg, li = tid; i < nbins; i += P, li += T) {
         if (!flat) bp[li] = bp_value(cfg, bufs, bc.params0, i);
         if (lgood) lgood[li] = bufs.last_good[i];
     }
-    auto prefetch = [&](int t) {
-        float* buf = specs + (t & 1) * nloc;
-        const float* src = data + (long long)t * spec_elems;
-        for (int i = tg, li = tid; i < nbins; i += P, li += T) cp_async4(buf + li, src + geo.off(i));
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-    if (nt > 0) prefetch(0);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
 
     for (int t = 0; t < nt; ++t) {
         float* spec = specs + (t & 1) * nloc;
         float* dst = data + (long long)t * spec_elems;
-        // the spectrum's channels are this thread's own copies: no barrier needed
-        if (t + 1 < nt) {
-            prefetch(t + 1);
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        }
         // ---- adaptive phase start, RFI_Clipper.cpp:214-278 ----
         if (bc.adapt) {
             float mins[16], part[16];
@@ -617,6 +632,10 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
 #pragma unroll
             for (int k = 0; k < 8; ++k) redi_c[warp * 8 + k] = good[k];
         partials_barrier<C>();
+        // Every thread has finished spectrum t-1, whose slots spectrum t+1
+        // takes: the other warps copy it in while warp 0 runs its chain, and
+        // complete their copies before the barrier ahead of the normalise pass.
+        if (warp != 0 && t + 1 < nt) stage(t + 1, tid - 32, T - 32);
         // ---- warp 0: spectrum mean, history, rejection (RFI_Clipper.cpp:343-470) ----
         if (warp == 0) {
             float pc[1];
@@ -767,6 +786,7 @@ __device__ __forceinline__ void rfi_body(const RfiConfig& cfg, const RfiBuffers&
                 }
             }
         }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // spectrum t+1 in its slots
         __syncthreads();
         // ---- normalise and store (RFI_Clipper.cpp:507-532); rebuild the bandpass ----
         const float sub_f = bc.sub_f, rms_f = bc.rms_f;
